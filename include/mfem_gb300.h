@@ -1,0 +1,220 @@
+/*
+ * mfem_gb300 — C ABI of the GB300 mixed-FEM Newton timestep.
+ *
+ * The library owns every device allocation it makes; host buffers passed in
+ * are caller-owned and copied.  Every entry point returns an int status
+ * (MFEM_OK = 0).  Calls on distinct scenes/batches are thread-safe; calls on
+ * one object are not re-entrant (the reference optimizer is not either).
+ *
+ * The entry points replace these reference interfaces (tytrusty/mfem):
+ *   scene create/destroy  <- SimState<3>::load(json)  src/simulation_state.cpp:92-341
+ *                            + NewtonOptimizer<3>::reset()  src/optimizers/newton_optimizer.cpp:127-140
+ *   scene step            <- NewtonOptimizer<3>::step()  src/optimizers/newton_optimizer.cpp:11-89
+ *   batch step            <- (no counterpart: many independent NewtonOptimizer::step calls)
+ *   get/set state         <- Displacement::value(), MixedStretch::value()
+ *                            src/variables/displacement.h:93-95, mixed_stretch.h:47-49
+ *   elem_update           <- MixedStretch::update_rotations + update_derivatives
+ *                            src/variables/mixed_stretch.cpp:133-204
+ *   assemble              <- Assembler<double,3,-1>::update_matrix  src/utils/sparse_utils.cpp:141-203
+ *   pcg solve             <- EigenIterativeSolver<ConjugateGradient<..,Lower|Upper>> ("eigen-pcg-diag")
+ *                            src/linear_solvers/eigen_iterative_solver.h:20-29
+ */
+#ifndef MFEM_GB300_H
+#define MFEM_GB300_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define MFEM_ABI_VERSION 1
+
+/* ---- status codes ---------------------------------------------------- */
+enum {
+  MFEM_OK = 0,
+  MFEM_ERR_INVALID = 1,      /* bad argument or descriptor                    */
+  MFEM_ERR_OOM = 2,          /* device allocation failed                      */
+  MFEM_ERR_CUDA = 3,         /* CUDA runtime error                            */
+  MFEM_ERR_NONFINITE = 4,    /* NaN/Inf in the state or a reduction           */
+  MFEM_ERR_CG_MAXITER = 5,   /* PCG stopped at max_iterative_solver_iters     */
+  MFEM_ERR_LS_FAILED = 6,    /* line search hit max_linesearch_iterations     */
+  MFEM_ERR_PROCRUSTES = 7,   /* singular rotation Hessian (reference exit(1)) */
+  MFEM_ERR_TIMEOUT = 8,      /* a bounded device wait ran out                 */
+  MFEM_ERR_NO_DEVICE = 9,    /* no CUDA device visible                        */
+  MFEM_ERR_UNSUPPORTED = 10, /* option not implemented on this path           */
+  MFEM_ERR_CAPACITY = 11     /* request exceeds a fixed capacity              */
+};
+
+/* ---- material models: MaterialModelType, src/config.h:61-68 ----------- */
+enum {
+  MFEM_MATERIAL_SNH = 0,   /* "Stable-Neohookean" */
+  MFEM_MATERIAL_NH = 1,    /* "Neohookean"        */
+  MFEM_MATERIAL_COROT = 2, /* "Corot"             */
+  MFEM_MATERIAL_FCR = 3,   /* "FixedCorot"        */
+  MFEM_MATERIAL_ARAP = 4,  /* "ARAP"              */
+  MFEM_MATERIAL_FUNG = 5   /* "Fung"              */
+};
+
+/* ---- linear solvers: LinearSolverType, src/config.h:45-59 -------------- */
+enum {
+  MFEM_SOLVER_EIGEN_LLT = 0,       /* direct: oracle only                */
+  MFEM_SOLVER_EIGEN_CG_DIAG = 5,   /* "eigen-pcg-diag" -> GPU Jacobi PCG  */
+  MFEM_SOLVER_MINRES_ID = 8,       /* "minres-indefinite-block"          */
+  MFEM_SOLVER_GPU_PCG_BLOCK = 100  /* "gpu-pcg-block": 3x3 block-Jacobi  */
+};
+
+/* ---- scripted boundary conditions: BCScriptType, src/config.h:70-87 ---- */
+enum {
+  MFEM_BC_NULL = 0, MFEM_BC_SCALEF = 1, MFEM_BC_HANG = 2, MFEM_BC_HANGENDS = 3,
+  MFEM_BC_STRETCH = 4, MFEM_BC_BEND = 7, MFEM_BC_TWIST = 8,
+  MFEM_BC_ONEPOINT = 13, MFEM_BC_RANDOM = 14,
+  /* additions (no reference counterpart) */
+  MFEM_BC_PINMIN = 16,   /* "pinmin": min-side group pinned, static            */
+  MFEM_BC_COMPRESS = 17  /* "compress": min side pinned, max side moves along
+                            the axis at `velocity` (m/s)                         */
+};
+
+enum { MFEM_PRECISION_FP64 = 0, MFEM_PRECISION_MIXED = 1 };
+
+/* Scene descriptor.  One tetrahedral object (or several concatenated by the
+ * caller, as Meshes does in src/mesh/meshes.cpp:11-56).  Arrays are
+ * row-major: vertex i at [3*i .. 3*i+2], tet e at [4*e .. 4*e+3].         */
+typedef struct mfem_scene_desc {
+  int32_t n_vertices;
+  int32_t n_tets;
+  const double*  V_rest;       /* 3*n_vertices  rest positions (Vref_)           */
+  const double*  V_init;       /* 3*n_vertices  initial positions (NULL = rest)  */
+  const double*  v_init;       /* 3*n_vertices  initial velocities (NULL = 0)    */
+  const int32_t* tets;         /* 4*n_tets                                       */
+  const double*  mu;           /* n_tets  Lame mu per tet                        */
+  const double*  lambda;       /* n_tets  Lame lambda per tet                    */
+  const int32_t* material;     /* n_tets  MFEM_MATERIAL_* (NULL = all SNH)       */
+  const double*  density;      /* n_tets  mass density (NULL = density_const)    */
+  double         density_const;
+  const int32_t* is_fixed;     /* n_vertices 0/1 override (NULL = from BC script) */
+  int32_t bc_type;             /* MFEM_BC_*                                       */
+  int32_t bc_axis;
+  double  bc_ratio;
+  double  bc_velocity;
+  double  dt;                  /* SimConfig::h                                    */
+  double  body_force[3];       /* SimConfig::ext (acceleration)                   */
+  int32_t bdf_order;           /* 1..6                                            */
+  int32_t max_newton_iterations;      /* SimConfig::outer_steps                   */
+  int32_t max_linesearch_iterations;  /* SimConfig::ls_iters                      */
+  int32_t max_iterative_solver_iters; /* SimConfig::max_iterative_solver_iters    */
+  double  iterative_solver_tolerance; /* SimConfig::itr_tol                       */
+  double  newton_tol;                 /* SimConfig::newton_tol (max |delta|_inf)  */
+  double  newton_residual_tolerance;  /* >0: also stop when |rhs_k| <= it times
+                                         max(|rhs_0|, |h^2 P M f|)             */
+  int32_t linear_solver;              /* MFEM_SOLVER_*                            */
+  int32_t precision;                  /* MFEM_PRECISION_*                         */
+  int32_t reserved[8];
+} mfem_scene_desc;
+
+/* Per-step statistics (the reference prints these as its per-iteration
+ * table, src/optimizers/optimizer_data.cpp:28-123).                        */
+typedef struct mfem_step_stats {
+  int32_t status;              /* worst status seen during the step            */
+  int32_t newton_iterations;
+  int32_t cg_iterations;       /* summed over Newton iterations                */
+  int32_t ls_iterations;       /* summed backtracking halvings                 */
+  double  energy;              /* energy_func(0) of the last Newton iteration  */
+  double  energy_residual;     /* |E - E_prev| / (E + 1e-6)                    */
+  double  decrement;           /* max(|dx|_inf, |ds|_inf) of the last solve    */
+  double  alpha;               /* last accepted line-search step               */
+  double  residual0;           /* |rhs| at the first Newton iteration          */
+  double  residual;            /* |rhs| at the last evaluated iterate          */
+  double  cg_error;            /* |r|/|b| at the end of the last PCG solve     */
+  double  device_ms;           /* device time of the step (CUDA events)        */
+} mfem_step_stats;
+
+typedef struct mfem_scene mfem_scene;   /* one resident simulation instance */
+typedef struct mfem_batch mfem_batch;   /* a set of scenes stepped together */
+
+/* ---- library ------------------------------------------------------------ */
+int mfem_gpu_abi_version(void);
+/* Makes `device` current for the calling thread (one process per GPU). */
+int mfem_gpu_set_device(int device);
+/* Writes the device name and SM count; fails with MFEM_ERR_NO_DEVICE. */
+int mfem_gpu_device_info(char* name, int name_len, int* sm_count);
+const char* mfem_gpu_status_string(int status);
+
+/* ---- scenes ---------------------------------------------------------------
+ * mfem_gpu_scene_create replaces SimState<3>::load + NewtonOptimizer::reset
+ * (src/simulation_state.cpp:92-341, src/optimizers/newton_optimizer.cpp:127-140):
+ * builds the mesh quantities (Mesh::init, src/mesh/mesh.cpp:124-159), the
+ * BDF history, s0 = polar(F0) and lambda = 0 (mixed_stretch.cpp:261-304), and
+ * uploads everything once; state stays resident until destroy.           */
+int mfem_gpu_scene_create(const mfem_scene_desc* desc, mfem_scene** out);
+int mfem_gpu_scene_destroy(mfem_scene* scene);
+/* One timestep: NewtonOptimizer<3>::step, src/optimizers/newton_optimizer.cpp:11-89. */
+int mfem_gpu_scene_step(mfem_scene* scene, mfem_step_stats* stats);
+/* Bytes of device memory the scene holds (admission control). */
+int mfem_gpu_scene_footprint(const mfem_scene_desc* desc, int64_t* bytes);
+int mfem_gpu_scene_sizes(const mfem_scene* scene, int32_t* n_vertices,
+                         int32_t* n_tets, int32_t* n_free);
+/* Full vertex positions / velocities (3*n_vertices doubles), per-tet s
+ * (6*n_tets), R (9*n_tets, column-major 3x3) and lambda (6*n_tets). Any
+ * output pointer may be NULL.                                              */
+int mfem_gpu_scene_get_state(mfem_scene* scene, double* x, double* v,
+                             double* s, double* R, double* la);
+int mfem_gpu_scene_set_state(mfem_scene* scene, const double* x,
+                             const double* v, const double* s, const double* R);
+
+/* ---- batches: many independent scenes stepped by one launch per phase ----- */
+int mfem_gpu_batch_create(mfem_scene* const* scenes, int32_t n, mfem_batch** out);
+int mfem_gpu_batch_destroy(mfem_batch* batch);
+/* Steps every scene in the batch once; stats[i] belongs to scenes[i]. */
+int mfem_gpu_batch_step(mfem_batch* batch, mfem_step_stats* stats);
+
+/* Prescribed positions of the pinned vertices for the next step (3*n_pinned
+ * doubles in the order of mfem_gpu_scene_pinned), replacing the scripted
+ * boundary motion for that step (the role of Mesh::update_bcs,
+ * src/mesh/mesh.h:130-132, when the caller drives the pins).           */
+int mfem_gpu_scene_pinned(mfem_scene* scene, int32_t* n_pinned, int32_t* vertices);
+int mfem_gpu_scene_set_pins(mfem_scene* scene, const double* positions);
+
+/* ---- instrumentation (the reference's Timer keys, optimizer_data.cpp:125-183) --
+ * With profiling on, every kernel launch of the batch is bracketed by CUDA
+ * events on the batch's stream; kernel_stats returns the summed device time
+ * and the launch count of kernel `kernel` since profiling was switched on.
+ * Launches are counted whether or not profiling is on.                    */
+enum {
+  MFEM_K_ELEM_UPDATE = 0, MFEM_K_ASSEMBLE = 1, MFEM_K_CG_INIT = 2, MFEM_K_CG_SPMV = 3,
+  MFEM_K_CG_UPDATE = 4, MFEM_K_LOCAL_SOLVE = 5, MFEM_K_LS_ENERGY = 6, MFEM_K_APPLY = 7,
+  MFEM_K_STEP_BEGIN = 8, MFEM_K_STEP_END = 9, MFEM_K_SCALARS = 10, MFEM_K_COUNT = 11
+};
+int mfem_gpu_scene_solo_batch(mfem_scene* scene, mfem_batch** batch);
+int mfem_gpu_batch_set_profiling(mfem_batch* batch, int enable);
+int mfem_gpu_batch_kernel_stats(mfem_batch* batch, int kernel, double* total_ms,
+                                int64_t* launches);
+int mfem_gpu_kernel_name(int kernel, char* name, int name_len);
+
+/* ---- per-kernel parity entry points (host buffers in, host buffers out) ----
+ * elem_update: MixedStretch::update_rotations + update_derivatives for the
+ * current state at positions x (3*n_vertices, full) and time step h
+ * (mixed_stretch.cpp:133-204).  Outputs per tet (any may be NULL):
+ *   S[6], dSdF[54] (9x6 column-major, = Js^T*Sym), g[6] = h^2 grad psi,
+ *   H[36] = h^2 hess psi (psd-fixed), Hinv[36], Aloc[144] (12x12 col-major),
+ *   gl[6] (MixedStretch::rhs, :219-220), R[9] (updated rotation).       */
+int mfem_gpu_scene_elem_update(mfem_scene* scene, const double* x, double h,
+                               double* R, double* S, double* dSdF, double* g,
+                               double* H, double* Hinv, double* Aloc,
+                               double* gl);
+/* Assembled LHS = PMP + A_mixed as 3x3 BCSR over free vertices after the
+ * last elem_update/step iteration (Assembler::update_matrix + the sparse
+ * add of SystemMatrixPD::pre_solve, linear_system.h:18-31) and the RHS.
+ * row_ptr: n_free+1, col: nnzb, val: 9*nnzb (row-major 3x3), rhs: 3*n_free. */
+int mfem_gpu_scene_bcsr_sizes(mfem_scene* scene, int32_t* n_free, int32_t* nnzb);
+int mfem_gpu_scene_get_system(mfem_scene* scene, int32_t* row_ptr,
+                              int32_t* col, double* val, double* rhs);
+/* Solves LHS * dx = b with the scene's PCG on the last assembled matrix.
+ * b, dx: 3*n_free.  Returns iterations and |r|/|b|. */
+int mfem_gpu_scene_pcg(mfem_scene* scene, const double* b, double* dx,
+                       int32_t* iterations, double* rel_residual);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* MFEM_GB300_H */

@@ -1,0 +1,10 @@
+"""GB300-native mixed-FEM Newton timestep (tytrusty/mfem's mixed-stretch path).
+
+The compute path is libmfem_gb300.so (hand-written sm_103a CUDA behind a C
+ABI, include/mfem_gb300.h).  This package holds the host-side mirror of the
+reference's interfaces: scene specs and the scene-JSON schema, the factory
+name registries, scenes and batches on the GPU, and the serving loop.
+"""
+from . import abi  # noqa: F401
+
+__all__ = ["abi", "gpu", "configs", "meshgen", "desc", "factories", "scene_json", "server"]

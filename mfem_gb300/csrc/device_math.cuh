@@ -1,0 +1,555 @@
+// Per-element device math for the mixed-stretch Newton step: 3x3 polar
+// rotation by Newton on SO(3), the closed-form derivative of the stretch s
+// with respect to F, the six material models on the 6-vector s, and the
+// positive-semidefinite projection of their Hessians.  Every routine is
+// templated on Real (float for the mixed-precision path, double for the
+// all-FP64 path) and keeps its small matrices in registers.
+//
+// Conventions (those of the reference): 3x3 matrices column-major, m[r+3c];
+// s = [S00, S11, S22, S01, S02, S12] (src/variables/mixed_stretch.cpp:26-29);
+// Sym = diag(1,1,1,2,2,2), Syminv = diag(1,1,1,.5,.5,.5) (mixed_stretch.h:120-138).
+#pragma once
+#include <cuda_runtime.h>
+#include <math.h>
+#include <stdint.h>
+
+namespace mfem_gpu {
+
+template <typename T> struct Prec;
+template <> struct Prec<float> {
+  static constexpr bool kFP64 = false;
+  __device__ static float sqrt_(float x) { return sqrtf(x); }
+  __device__ static float rsqrt_(float x) { return rsqrtf(x); }
+  __device__ static void sincos_(float x, float* s, float* c) { sincosf(x, s, c); }
+  __device__ static float log_(float x) { return logf(x); }
+  __device__ static float exp_(float x) { return expf(x); }
+};
+template <> struct Prec<double> {
+  static constexpr bool kFP64 = true;
+  __device__ static double sqrt_(double x) { return sqrt(x); }
+  __device__ static double rsqrt_(double x) { return rsqrt(x); }
+  __device__ static void sincos_(double x, double* s, double* c) { sincos(x, s, c); }
+  __device__ static double log_(double x) { return log(x); }
+  __device__ static double exp_(double x) { return exp(x); }
+};
+
+#define MI __device__ __forceinline__
+
+// ---------------------------------------------------------------- 3x3 ----
+template <typename T> MI T tr_AB(const T* A, const T* B) {  // tr(A*B)
+  T s = 0;
+#pragma unroll
+  for (int i = 0; i < 3; ++i)
+#pragma unroll
+    for (int j = 0; j < 3; ++j) s += A[i + 3 * j] * B[j + 3 * i];
+  return s;
+}
+template <typename T> MI void mul33(const T* A, const T* B, T* C) {  // C = A*B
+#pragma unroll
+  for (int i = 0; i < 3; ++i)
+#pragma unroll
+    for (int j = 0; j < 3; ++j)
+      C[i + 3 * j] = A[i] * B[3 * j] + A[i + 3] * B[1 + 3 * j] + A[i + 6] * B[2 + 3 * j];
+}
+template <typename T> MI void mulAtB(const T* A, const T* B, T* C) {  // C = A^T*B
+#pragma unroll
+  for (int i = 0; i < 3; ++i)
+#pragma unroll
+    for (int j = 0; j < 3; ++j)
+      C[i + 3 * j] = A[3 * i] * B[3 * j] + A[1 + 3 * i] * B[1 + 3 * j] + A[2 + 3 * i] * B[2 + 3 * j];
+}
+template <typename T> MI void mulABt(const T* A, const T* B, T* C) {  // C = A*B^T
+#pragma unroll
+  for (int i = 0; i < 3; ++i)
+#pragma unroll
+    for (int j = 0; j < 3; ++j)
+      C[i + 3 * j] = A[i] * B[j] + A[i + 3] * B[j + 3] + A[i + 6] * B[j + 6];
+}
+
+// Rotation <-> unit quaternion (w, x, y, z).  Rotations are stored as
+// quaternions so that every reload is exactly orthonormal.
+template <typename T> MI void quat_to_rot(const T q_in[4], T* R) {
+  T w = q_in[0], x = q_in[1], y = q_in[2], z = q_in[3];
+  T n = w * w + x * x + y * y + z * z;
+  T s = n > T(0) ? T(2) / n : T(0);
+  R[0] = T(1) - s * (y * y + z * z);
+  R[3] = s * (x * y - w * z);
+  R[6] = s * (x * z + w * y);
+  R[1] = s * (x * y + w * z);
+  R[4] = T(1) - s * (x * x + z * z);
+  R[7] = s * (y * z - w * x);
+  R[2] = s * (x * z - w * y);
+  R[5] = s * (y * z + w * x);
+  R[8] = T(1) - s * (x * x + y * y);
+}
+template <typename T> MI void rot_to_quat(const T* R, T q[4]) {
+  T t = R[0] + R[4] + R[8];
+  if (t > T(0)) {
+    T s = Prec<T>::sqrt_(t + T(1)) * T(2);
+    q[0] = T(0.25) * s;
+    q[1] = (R[5] - R[7]) / s;
+    q[2] = (R[6] - R[2]) / s;
+    q[3] = (R[1] - R[3]) / s;
+  } else if (R[0] > R[4] && R[0] > R[8]) {
+    T s = Prec<T>::sqrt_(T(1) + R[0] - R[4] - R[8]) * T(2);
+    q[0] = (R[5] - R[7]) / s;
+    q[1] = T(0.25) * s;
+    q[2] = (R[3] + R[1]) / s;
+    q[3] = (R[6] + R[2]) / s;
+  } else if (R[4] > R[8]) {
+    T s = Prec<T>::sqrt_(T(1) + R[4] - R[0] - R[8]) * T(2);
+    q[0] = (R[6] - R[2]) / s;
+    q[1] = (R[3] + R[1]) / s;
+    q[2] = T(0.25) * s;
+    q[3] = (R[7] + R[5]) / s;
+  } else {
+    T s = Prec<T>::sqrt_(T(1) + R[8] - R[0] - R[4]) * T(2);
+    q[0] = (R[1] - R[3]) / s;
+    q[1] = (R[6] + R[2]) / s;
+    q[2] = (R[7] + R[5]) / s;
+    q[3] = T(0.25) * s;
+  }
+  T n = Prec<T>::rsqrt_(q[0] * q[0] + q[1] * q[1] + q[2] * q[2] + q[3] * q[3]);
+#pragma unroll
+  for (int i = 0; i < 4; ++i) q[i] *= n;
+}
+
+// rodrigues (src/svd/newton_procrustes.h:87-106): R = I + sin|w| K + (1-cos|w|) K^2.
+template <typename T> MI void rodrigues(const T w[3], T* R) {
+  T a2 = w[0] * w[0] + w[1] * w[1] + w[2] * w[2];
+  T angle = Prec<T>::sqrt_(a2);
+#pragma unroll
+  for (int i = 0; i < 9; ++i) R[i] = (i % 4 == 0) ? T(1) : T(0);
+  if (angle < T(1e-8)) return;
+  T inv = T(1) / angle;
+  T k0 = w[0] * inv, k1 = w[1] * inv, k2 = w[2] * inv;
+  T sa, ca;
+  Prec<T>::sincos_(angle, &sa, &ca);
+  T c1 = T(1) - ca;
+  // K = [k]x ; K^2 = k k^T - I
+  R[0] += c1 * (k0 * k0 - T(1));
+  R[4] += c1 * (k1 * k1 - T(1));
+  R[8] += c1 * (k2 * k2 - T(1));
+  R[3] += -sa * k2 + c1 * k0 * k1;  // (0,1)
+  R[1] += sa * k2 + c1 * k0 * k1;   // (1,0)
+  R[6] += sa * k1 + c1 * k0 * k2;   // (0,2)
+  R[2] += -sa * k1 + c1 * k0 * k2;  // (2,0)
+  R[7] += -sa * k0 + c1 * k1 * k2;  // (1,2)
+  R[5] += sa * k0 + c1 * k1 * k2;   // (2,1)
+}
+
+// Solve the symmetric 3x3 system H x = b (H given as xx,yy,zz,xy,xz,yz) by
+// its adjugate; returns false when H is numerically singular.
+template <typename T> MI bool solve_sym3(const T h[6], const T b[3], T x[3]) {
+  T a00 = h[1] * h[2] - h[5] * h[5];
+  T a01 = h[4] * h[5] - h[3] * h[2];
+  T a02 = h[3] * h[5] - h[4] * h[1];
+  T a11 = h[0] * h[2] - h[4] * h[4];
+  T a12 = h[3] * h[4] - h[0] * h[5];
+  T a22 = h[0] * h[1] - h[3] * h[3];
+  T det = h[0] * a00 + h[3] * a01 + h[4] * a02;
+  T scale = fabs(h[0]) + fabs(h[1]) + fabs(h[2]) + T(2) * (fabs(h[3]) + fabs(h[4]) + fabs(h[5]));
+  T tiny = (Prec<T>::kFP64 ? T(1e-14) : T(1e-6)) * scale * scale * scale;
+  if (!(fabs(det) > tiny)) return false;
+  T id = T(1) / det;
+  x[0] = (a00 * b[0] + a01 * b[1] + a02 * b[2]) * id;
+  x[1] = (a01 * b[0] + a11 * b[1] + a12 * b[2]) * id;
+  x[2] = (a02 * b[0] + a12 * b[1] + a22 * b[2]) * id;
+  return true;
+}
+
+// Gradient g_k = -tr(cp_k Y) and Hessian H_kl = -tr(cp_kl Y) of the
+// Procrustes energy (newton_procrustes.h:128,136-138), written out:
+// g is the axial part of Y and H = tr(sym Y) I - sym Y.
+template <typename T> MI void procrustes_gH(const T* Y, T g[3], T h[6]) {
+  g[0] = Y[5] - Y[7];  // Y21 - Y12
+  g[1] = Y[6] - Y[2];  // Y02 - Y20
+  g[2] = Y[1] - Y[3];  // Y10 - Y01
+  T t = Y[0] + Y[4] + Y[8];
+  h[0] = t - Y[0];
+  h[1] = t - Y[4];
+  h[2] = t - Y[8];
+  h[3] = T(-0.5) * (Y[3] + Y[1]);
+  h[4] = T(-0.5) * (Y[6] + Y[2]);
+  h[5] = T(-0.5) * (Y[7] + Y[5]);
+}
+
+// newton_procrustes with A = I, B = F (src/svd/newton_procrustes.h:108-159):
+// R (warm start in, rotation out) minimising |R - F|_F.  tol is the
+// reference's 1e-6 on |g| (mixed_stretch.cpp:21-22); in FP32 it is raised to
+// the rounding floor of |g|, and the 0.6-backtracking energy test is skipped
+// once |omega| < 4e-3, where a Newton step on this convex problem always
+// decreases the energy and the FP32 energy difference is below rounding.
+// Returns the iteration count, or -1 if the rotation Hessian was singular.
+template <typename T> MI int procrustes(T* R, const T* F, T tol, int max_iter) {
+  T Y[9];
+  mulABt(R, F, Y);  // Y = R*A*B^T with A = I
+  if (!Prec<T>::kFP64) {
+    T fn = 0;
+#pragma unroll
+    for (int i = 0; i < 9; ++i) fn += F[i] * F[i];
+    T floor_ = T(8) * T(1.1920929e-7) * Prec<T>::sqrt_(fn);
+    tol = tol > floor_ ? tol : floor_;
+  }
+  int it = 0;
+  bool singular = false;
+  for (; it < max_iter;) {
+    T g[3], h[6];
+    procrustes_gH(Y, g, h);
+    T gn2 = g[0] * g[0] + g[1] * g[1] + g[2] * g[2];
+    if (gn2 < tol * tol) break;
+    T om[3];
+    if (!solve_sym3(h, g, om)) {
+      singular = true;
+      T tr = h[0] + h[1] + h[2];
+      T inv = T(1) / (fabs(tr) + T(1));
+      om[0] = g[0] * inv;
+      om[1] = g[1] * inv;
+      om[2] = g[2] * inv;
+    }
+    om[0] = -om[0];
+    om[1] = -om[1];
+    om[2] = -om[2];
+    T dR[9];
+    T on2 = om[0] * om[0] + om[1] * om[1] + om[2] * om[2];
+    if (!Prec<T>::kFP64 && on2 < T(1.6e-5)) {
+      rodrigues(om, dR);
+    } else {
+      T E0 = -tr_AB(R, Y);  // as newton_procrustes.h:142
+      T E1;
+      do {
+        rodrigues(om, dR);
+        E1 = -tr_AB(dR, Y);
+        om[0] *= T(0.6);
+        om[1] *= T(0.6);
+        om[2] *= T(0.6);
+        on2 = om[0] * om[0] + om[1] * om[1] + om[2] * om[2];
+      } while (E1 > E0 && on2 > tol * tol);
+    }
+    T tmp[9];
+    mul33(dR, R, tmp);
+#pragma unroll
+    for (int i = 0; i < 9; ++i) R[i] = tmp[i];
+    mul33(dR, Y, tmp);
+#pragma unroll
+    for (int i = 0; i < 9; ++i) Y[i] = tmp[i];
+    ++it;
+  }
+  return singular ? -1 : it;
+}
+
+// s-vector of S = R^T F (mixed_stretch.cpp:25-29).
+template <typename T> MI void stretch_vec(const T* R, const T* F, T s[6]) {
+  T S[9];
+  mulAtB(R, F, S);
+  s[0] = S[0];
+  s[1] = S[4];
+  s[2] = S[8];
+  s[3] = T(0.5) * (S[1] + S[3]);
+  s[4] = T(0.5) * (S[2] + S[6]);
+  s[5] = T(0.5) * (S[5] + S[7]);
+}
+
+// Closed-form ds/dF at the polar optimum.  With S symmetric, F = R S and
+// W = (tr(S) I - S)^{-1}, the derivative of s_i with respect to F is
+//   ds_i/dF = R (E_i - [u_i]x),  u_i = W c_i,  c_{i,m} = <E_i, [e_m]x S>,
+// E_i the selector of s_i.  This is the product
+// (I(x)R^T)(I - (S^T(x)I) dR/dF) of mixed_stretch.cpp:32-41 with dR/dF of
+// newton_procrustes.h:161-187 evaluated analytically.  Output: u[6][3];
+// returns false if tr(S) I - S is singular (the reference exits there).
+template <typename T> MI bool stretch_derivative_u(const T s[6], T u[18]) {
+  // M = tr(S) I - S (symmetric)
+  T t = s[0] + s[1] + s[2];
+  T m[6] = {t - s[0], t - s[1], t - s[2], -s[3], -s[4], -s[5]};
+  // c_i vectors (rows), from S entries: S00=s0, S11=s1, S22=s2, S01=s3, S02=s4, S12=s5
+  T c[18] = {T(0), s[4], -s[3],                                  // i=0
+             -s[5], T(0), s[3],                                  // i=1
+             s[5], -s[4], T(0),                                  // i=2
+             T(-0.5) * s[4], T(0.5) * s[5], T(0.5) * (s[0] - s[1]),  // i=3
+             T(0.5) * s[3], T(0.5) * (s[2] - s[0]), T(-0.5) * s[5],  // i=4
+             T(0.5) * (s[1] - s[2]), T(-0.5) * s[3], T(0.5) * s[4]}; // i=5
+  bool ok = true;
+#pragma unroll
+  for (int i = 0; i < 6; ++i) ok = solve_sym3(m, &c[3 * i], &u[3 * i]) && ok;
+  if (!ok) {
+#pragma unroll
+    for (int i = 0; i < 18; ++i) u[i] = T(0);
+  }
+  return ok;
+}
+
+// <E_i - [u_i]x, M> for all six i, M a 3x3 matrix in the rotated frame.
+template <typename T> MI void ds_dot(const T u[18], const T* M, T out[6]) {
+  T a0 = M[5] - M[7], a1 = M[6] - M[2], a2 = M[1] - M[3];  // axial part
+  T e[6] = {M[0], M[4], M[8], T(0.5) * (M[1] + M[3]), T(0.5) * (M[2] + M[6]),
+            T(0.5) * (M[5] + M[7])};
+#pragma unroll
+  for (int i = 0; i < 6; ++i) out[i] = e[i] - (u[3 * i] * a0 + u[3 * i + 1] * a1 + u[3 * i + 2] * a2);
+}
+
+// G_i = ds_i/dF = R (E_i - [u_i]x), 3x3 column-major each (G[9*i + r + 3c]).
+template <typename T> MI void ds_dF(const T* R, const T u[18], T G[54]) {
+#pragma unroll
+  for (int i = 0; i < 6; ++i) {
+    T D[9];
+    const T u0 = u[3 * i], u1 = u[3 * i + 1], u2 = u[3 * i + 2];
+    // -[u]x
+    D[0] = 0; D[4] = 0; D[8] = 0;
+    D[3] = u2;  D[6] = -u1;  // (0,1), (0,2)
+    D[1] = -u2; D[7] = u0;   // (1,0), (1,2)
+    D[2] = u1;  D[5] = -u0;  // (2,0), (2,1)
+    if (i < 3) {
+      D[4 * i] += T(1);
+    } else {
+      int p = (i == 5) ? 1 : 0, q = (i == 3) ? 1 : 2;
+      D[p + 3 * q] += T(0.5);
+      D[q + 3 * p] += T(0.5);
+    }
+    mul33(R, D, &G[9 * i]);
+  }
+}
+
+// ------------------------------------------------------------ materials ---
+// psi = A(Q) + B(J) + C(t) with Q = |S|_F^2, J = det S, t = tr S; this is
+// the expression of every Vector6d energy of src/energies/*.cpp.
+enum { kSNH = 0, kNH = 1, kCOROT = 2, kFCR = 3, kARAP = 4, kFUNG = 5 };
+
+template <typename T> struct MatCoef {
+  T psi, A1, A2, B1, B2, C1, C2;
+  bool psd;
+};
+
+template <typename T> MI void invariants(const T* s, T& Q, T& J, T& t, T dJ[6]) {
+  Q = s[0] * s[0] + s[1] * s[1] + s[2] * s[2] + T(2) * (s[3] * s[3] + s[4] * s[4] + s[5] * s[5]);
+  J = s[0] * s[1] * s[2] + T(2) * s[3] * s[4] * s[5] - s[0] * s[5] * s[5] - s[1] * s[4] * s[4] -
+      s[2] * s[3] * s[3];
+  t = s[0] + s[1] + s[2];
+  dJ[0] = s[1] * s[2] - s[5] * s[5];
+  dJ[1] = s[0] * s[2] - s[4] * s[4];
+  dJ[2] = s[0] * s[1] - s[3] * s[3];
+  dJ[3] = T(2) * (s[4] * s[5] - s[2] * s[3]);
+  dJ[4] = T(2) * (s[3] * s[5] - s[1] * s[4]);
+  dJ[5] = T(2) * (s[3] * s[4] - s[0] * s[5]);
+}
+
+template <typename T>
+MI MatCoef<T> material_coef(int type, T mu, T la, T Q, T J, T t, bool need_psi) {
+  MatCoef<T> c{T(0), T(0), T(0), T(0), T(0), T(0), T(0), false};
+  switch (type) {
+    case kNH: {  // neohookean.cpp:8-94
+      T lj = Prec<T>::log_(J);
+      if (need_psi) c.psi = -mu * lj + T(0.5) * la * lj * lj + T(0.5) * mu * (Q - T(3));
+      c.A1 = T(0.5) * mu;
+      c.B1 = (-mu + la * lj) / J;
+      c.B2 = (mu + la * (T(1) - lj)) / (J * J);
+      c.psd = true;
+      break;
+    }
+    case kCOROT:  // corotational.cpp:8-60
+      if (need_psi) c.psi = T(0.5) * la * (t - T(3)) * (t - T(3)) + mu * (Q - T(2) * t + T(3));
+      c.A1 = mu;
+      c.C1 = la * (t - T(3)) - T(2) * mu;
+      c.C2 = la;
+      break;
+    case kFCR:  // fixed_corotational.cpp:8-…
+      if (need_psi) c.psi = T(0.5) * la * (J - T(1)) * (J - T(1)) + mu * (Q - T(2) * t + T(3));
+      c.A1 = mu;
+      c.B1 = la * (J - T(1));
+      c.B2 = la;
+      c.C1 = T(-2) * mu;
+      break;
+    case kARAP:  // arap.cpp:7-65
+      if (need_psi) c.psi = T(0.5) * mu * (Q - T(2) * t + T(3));
+      c.A1 = T(0.5) * mu;
+      c.C1 = -mu;
+      break;
+    case kFUNG: {  // fung.cpp:8-97 with c = 4
+      const T cf = T(4);
+      T e = Prec<T>::exp_(cf * (Q - T(3)) * T(0.5));
+      T k = (mu + cf * mu) / la;
+      if (need_psi)
+        c.psi = T(0.5) * mu * (e - T(1)) + T(0.5) * mu * (Q - T(3)) +
+                T(0.5) * la * (k + T(1) - J) * (k + T(1) - J);
+      c.A1 = mu * cf * e * T(0.25) + T(0.5) * mu;
+      c.A2 = mu * cf * cf * e * T(0.125);
+      c.B1 = -la * (k + T(1) - J);
+      c.B2 = la;
+      c.psd = true;
+      break;
+    }
+    default: {  // kSNH, stable_neohookean.cpp:8-95
+      T omj = T(1) - J;
+      if (need_psi) c.psi = mu * omj + T(0.5) * la * omj * omj + T(0.5) * mu * (Q - T(3));
+      c.A1 = T(0.5) * mu;
+      c.B1 = -mu - la * omj;
+      c.B2 = la;
+      c.psd = true;
+      break;
+    }
+  }
+  return c;
+}
+
+template <typename T> MI T material_psi(int type, T mu, T la, const T* s) {
+  T Q, J, t, dJ[6];
+  invariants(s, Q, J, t, dJ);
+  return material_coef<T>(type, mu, la, Q, J, t, true).psi;
+}
+
+// Gradient and (unfixed) Hessian of psi on the 6-vector; H full 6x6 column-major.
+template <typename T>
+MI bool material_grad_hess(int type, T mu, T la, const T* s, T g[6], T H[36]) {
+  T Q, J, t, dJ[6];
+  invariants(s, Q, J, t, dJ);
+  MatCoef<T> c = material_coef<T>(type, mu, la, Q, J, t, false);
+  const T w[6] = {T(1), T(1), T(1), T(2), T(2), T(2)};
+  T dQ[6];
+#pragma unroll
+  for (int i = 0; i < 6; ++i) {
+    dQ[i] = T(2) * w[i] * s[i];
+    g[i] = c.A1 * dQ[i] + c.B1 * dJ[i] + (i < 3 ? c.C1 : T(0));
+  }
+#pragma unroll
+  for (int j = 0; j < 6; ++j)
+#pragma unroll
+    for (int i = 0; i < 6; ++i) {
+      T v = c.A2 * dQ[i] * dQ[j] + c.B2 * dJ[i] * dJ[j];
+      if (i == j) v += T(2) * c.A1 * w[i];
+      if (i < 3 && j < 3) v += c.C2;
+      H[i + 6 * j] = v;
+    }
+  // + B1 * d2J/ds2 (symmetric pattern)
+  const T b = c.B1;
+  H[0 + 6 * 1] += b * s[2]; H[1 + 6 * 0] += b * s[2];
+  H[0 + 6 * 2] += b * s[1]; H[2 + 6 * 0] += b * s[1];
+  H[0 + 6 * 5] += b * T(-2) * s[5]; H[5 + 6 * 0] += b * T(-2) * s[5];
+  H[1 + 6 * 2] += b * s[0]; H[2 + 6 * 1] += b * s[0];
+  H[1 + 6 * 4] += b * T(-2) * s[4]; H[4 + 6 * 1] += b * T(-2) * s[4];
+  H[2 + 6 * 3] += b * T(-2) * s[3]; H[3 + 6 * 2] += b * T(-2) * s[3];
+  H[3 + 6 * 3] += b * T(-2) * s[2];
+  H[3 + 6 * 4] += b * T(2) * s[5]; H[4 + 6 * 3] += b * T(2) * s[5];
+  H[3 + 6 * 5] += b * T(2) * s[4]; H[5 + 6 * 3] += b * T(2) * s[4];
+  H[4 + 6 * 4] += b * T(-2) * s[1];
+  H[4 + 6 * 5] += b * T(2) * s[3]; H[5 + 6 * 4] += b * T(2) * s[3];
+  H[5 + 6 * 5] += b * T(-2) * s[0];
+  return c.psd;
+}
+
+// In-place lower Cholesky of the symmetric 6x6 H (column-major, lower part
+// used); succeeds only if every pivot exceeds `floor_`.
+template <typename T> MI bool cholesky6(T* A, T floor_) {
+  bool ok = true;
+#pragma unroll
+  for (int j = 0; j < 6; ++j) {
+    T d = A[j + 6 * j];
+#pragma unroll
+    for (int k = 0; k < j; ++k) d -= A[j + 6 * k] * A[j + 6 * k];
+    ok = ok && (d > floor_);
+    T ljj = Prec<T>::sqrt_(d > floor_ ? d : floor_);
+    A[j + 6 * j] = ljj;
+    T inv = T(1) / ljj;
+#pragma unroll
+    for (int i = j + 1; i < 6; ++i) {
+      T v = A[i + 6 * j];
+#pragma unroll
+      for (int k = 0; k < j; ++k) v -= A[i + 6 * k] * A[j + 6 * k];
+      A[i + 6 * j] = v * inv;
+    }
+  }
+  return ok;
+}
+
+// Cyclic Jacobi eigen-decomposition of the symmetric 6x6 A: on return the
+// diagonal of A holds the eigenvalues and V (column-major) the eigenvectors.
+template <typename T> MI void jacobi_eig6(T* A, T* V) {
+#pragma unroll
+  for (int i = 0; i < 36; ++i) V[i] = (i % 7 == 0) ? T(1) : T(0);
+  for (int sweep = 0; sweep < 12; ++sweep) {
+    T off = 0, tot = 0;
+#pragma unroll
+    for (int j = 0; j < 6; ++j)
+#pragma unroll
+      for (int i = 0; i < 6; ++i) {
+        T a = A[i + 6 * j] * A[i + 6 * j];
+        tot += a;
+        if (i != j) off += a;
+      }
+    if (!(off > (Prec<T>::kFP64 ? T(1e-30) : T(1e-14)) * tot)) break;
+#pragma unroll
+    for (int p = 0; p < 5; ++p)
+#pragma unroll
+      for (int q = p + 1; q < 6; ++q) {
+        T apq = A[p + 6 * q];
+        if (apq != T(0)) {
+          T theta = (A[q + 6 * q] - A[p + 6 * p]) / (T(2) * apq);
+          T tt = (theta >= T(0) ? T(1) : T(-1)) /
+                 (fabs(theta) + Prec<T>::sqrt_(theta * theta + T(1)));
+          T c = Prec<T>::rsqrt_(tt * tt + T(1)), sn = tt * c;
+#pragma unroll
+          for (int k = 0; k < 6; ++k) {
+            T akp = A[k + 6 * p], akq = A[k + 6 * q];
+            A[k + 6 * p] = c * akp - sn * akq;
+            A[k + 6 * q] = sn * akp + c * akq;
+          }
+#pragma unroll
+          for (int k = 0; k < 6; ++k) {
+            T apk = A[p + 6 * k], aqk = A[q + 6 * k];
+            A[p + 6 * k] = c * apk - sn * aqk;
+            A[q + 6 * k] = sn * apk + c * aqk;
+          }
+#pragma unroll
+          for (int k = 0; k < 6; ++k) {
+            T vkp = V[k + 6 * p], vkq = V[k + 6 * q];
+            V[k + 6 * p] = c * vkp - sn * vkq;
+            V[k + 6 * q] = sn * vkp + c * vkq;
+          }
+        }
+      }
+  }
+}
+
+// sim::simple_psd_fix with tol 1e-6 (stable_neohookean.cpp:91-93, Bartels):
+// eigenvalues below tol are raised to tol and H rebuilt; H is unchanged when
+// it is already positive definite.  The Cholesky test (pivots above tol)
+// decides the common case; only a failing H pays for the Jacobi
+// eigen-decomposition.  Returns true if H was modified.
+template <typename T> MI bool psd_fix(T* H, T tol) {
+  T L[36];
+#pragma unroll
+  for (int i = 0; i < 36; ++i) L[i] = H[i];
+  if (cholesky6(L, tol)) return false;
+  T V[36];
+#pragma unroll
+  for (int i = 0; i < 36; ++i) L[i] = H[i];
+  jacobi_eig6(L, V);
+  T lam[6];
+#pragma unroll
+  for (int k = 0; k < 6; ++k) lam[k] = L[k + 6 * k] < tol ? tol : L[k + 6 * k];
+#pragma unroll
+  for (int j = 0; j < 6; ++j)
+#pragma unroll
+    for (int i = 0; i < 6; ++i) {
+      T v = 0;
+#pragma unroll
+      for (int k = 0; k < 6; ++k) v += V[i + 6 * k] * lam[k] * V[j + 6 * k];
+      H[i + 6 * j] = v;
+    }
+  return true;
+}
+
+// ---------------------------------------------------- compensated sums ---
+struct KSum {
+  double s, c;
+  MI void add(double x) {  // Neumaier
+    double t = s + x;
+    c += (fabs(s) >= fabs(x)) ? (s - t) + x : (x - t) + s;
+    s = t;
+  }
+  MI void merge(const KSum& o) {
+    add(o.s);
+    c += o.c;
+  }
+  MI double value() const { return s + c; }
+};
+
+}  // namespace mfem_gpu

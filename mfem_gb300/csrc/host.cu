@@ -1,0 +1,1383 @@
+// Host side of the GB300 mixed-FEM Newton timestep: scene set-up (what
+// SimState::load + Mesh::init + the variables' reset() build in the
+// reference), batches of scenes, the Newton loop that launches the kernels,
+// and the C ABI of include/mfem_gb300.h.
+//
+// Reference correspondence (tytrusty/mfem):
+//   scene set-up      src/mesh/mesh.cpp:124-175, src/mesh/tet_mesh.cpp:31-75,
+//                     src/variables/displacement.cpp:75-98, mixed_stretch.cpp:261-304
+//   assembly pattern  src/utils/sparse_utils.cpp:19-138 (sorted free pairs)
+//   boundary scripts  src/boundary_conditions/*.h, boundary_condition.cpp:5-21
+//   Newton loop       src/optimizers/newton_optimizer.cpp:11-89
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <atomic>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <limits>
+#include <memory>
+#include <mutex>
+#include <new>
+#include <string>
+#include <vector>
+
+#include "../../include/mfem_gb300.h"
+#include "kernels.cuh"
+
+using namespace mfem_gpu;
+
+namespace {
+
+thread_local char g_last_error[256] = {0};
+
+void set_error(const char* what, cudaError_t e) {
+  snprintf(g_last_error, sizeof(g_last_error), "%s: %s", what, cudaGetErrorString(e));
+}
+
+#define CUDA_OR(expr, code)                 \
+  do {                                      \
+    cudaError_t e_ = (expr);                \
+    if (e_ != cudaSuccess) {                \
+      set_error(#expr, e_);                 \
+      return (code);                        \
+    }                                       \
+  } while (0)
+
+std::once_flag g_configured;
+
+size_t align_up(size_t v, size_t a) { return (v + a - 1) / a * a; }
+
+// Sub-allocations of one device allocation.
+struct Arena {
+  char* base = nullptr;
+  size_t used = 0;
+  template <typename T> T* take(size_t n) {
+    size_t off = align_up(used, 256);
+    used = off + n * sizeof(T);
+    return base ? reinterpret_cast<T*>(base + off) : nullptr;
+  }
+  void* take_bytes(size_t n) {
+    size_t off = align_up(used, 256);
+    used = off + n;
+    return base ? static_cast<void*>(base + off) : nullptr;
+  }
+};
+
+// Host-side structures of one scene, built once.
+struct HostMesh {
+  int nv = 0, nt = 0, nf = 0, npin = 0, nnzb = 0;
+  std::vector<double> V0;      // initial positions after BC init
+  std::vector<double> v0;      // initial velocities
+  std::vector<int> T;          // 4 nt
+  std::vector<double> dphi;    // 9 nt  (rows k = 1..3 of Dm^{-1}), element-major
+  std::vector<double> vol;
+  std::vector<double> mu, lam;
+  std::vector<int8_t> mat;
+  int material_uniform = 0;
+  std::vector<int> is_fixed, free_map, free_vert, pin_vert;
+  std::vector<int> m_ptr, m_col;
+  std::vector<double> m_val;
+  std::vector<int> b_ptr, b_col;
+  std::vector<double> b_mass;
+  std::vector<int> inc_ptr;
+  std::vector<int2> inc;
+  // boundary script
+  int bc_type = 0, bc_axis = 0;
+  double bc_vel = 0.0;
+  std::vector<int> pin_group;    // per pinned vertex: 0/1 BC group, -1 none
+  double twist_center[3] = {0, 0, 0};
+  double bend_center[2][3] = {{0, 0, 0}, {0, 0, 0}};
+};
+
+// Boundary groups (BoundaryCondition::init_boundary_groups): vertices within
+// ratio*range of the min / max of the axis, computed on the rest shape.
+void boundary_groups(const std::vector<double>& V, int nv, int axis, double ratio,
+                     std::vector<int>& group) {
+  double lo = std::numeric_limits<double>::infinity(), hi = -lo;
+  for (int v = 0; v < nv; ++v) {
+    lo = std::min(lo, V[3 * v + axis]);
+    hi = std::max(hi, V[3 * v + axis]);
+  }
+  const double range = hi - lo;
+  group.assign(nv, -1);
+  for (int v = 0; v < nv; ++v) {
+    const double c = V[3 * v + axis];
+    if (c < lo + range * ratio)
+      group[v] = 0;
+    else if (c > hi - range * ratio)
+      group[v] = 1;
+  }
+}
+
+void bbox_center(const std::vector<double>& V, int nv, double c[3]) {
+  for (int d = 0; d < 3; ++d) {
+    double lo = std::numeric_limits<double>::infinity(), hi = -lo;
+    for (int v = 0; v < nv; ++v) {
+      lo = std::min(lo, V[3 * v + d]);
+      hi = std::max(hi, V[3 * v + d]);
+    }
+    c[d] = 0.5 * (lo + hi);
+  }
+}
+
+void rotate_about(double* p, const double* o, int axis, double ang) {
+  double q[3] = {p[0] - o[0], p[1] - o[1], p[2] - o[2]};
+  const double c = std::cos(ang), s = std::sin(ang);
+  const int i = (axis + 1) % 3, j = (axis + 2) % 3;
+  const double qi = c * q[i] - s * q[j], qj = s * q[i] + c * q[j];
+  q[i] = qi;
+  q[j] = qj;
+  for (int d = 0; d < 3; ++d) p[d] = q[d] + o[d];
+}
+
+bool invert3(const double* A, double* Ai, double* det_out) {
+  // A column-major
+  const double c00 = A[4] * A[8] - A[7] * A[5];
+  const double c01 = A[7] * A[2] - A[1] * A[8];
+  const double c02 = A[1] * A[5] - A[4] * A[2];
+  const double det = A[0] * c00 + A[3] * c01 + A[6] * c02;
+  *det_out = det;
+  if (det == 0.0 || !std::isfinite(det)) return false;
+  const double id = 1.0 / det;
+  Ai[0] = c00 * id;
+  Ai[1] = c01 * id;
+  Ai[2] = c02 * id;
+  Ai[3] = (A[6] * A[5] - A[3] * A[8]) * id;
+  Ai[4] = (A[0] * A[8] - A[6] * A[2]) * id;
+  Ai[5] = (A[3] * A[2] - A[0] * A[5]) * id;
+  Ai[6] = (A[3] * A[7] - A[6] * A[4]) * id;
+  Ai[7] = (A[6] * A[1] - A[0] * A[7]) * id;
+  Ai[8] = (A[0] * A[4] - A[3] * A[1]) * id;
+  return true;
+}
+
+int build_host_mesh(const mfem_scene_desc* d, HostMesh& M) {
+  if (!d || d->n_vertices <= 0 || d->n_tets <= 0 || !d->V_rest || !d->tets || !d->mu ||
+      !d->lambda)
+    return MFEM_ERR_INVALID;
+  if (d->bdf_order < 1 || d->bdf_order > 6 || !(d->dt > 0)) return MFEM_ERR_INVALID;
+  if (d->bc_axis < 0 || d->bc_axis > 2) return MFEM_ERR_INVALID;
+  M.nv = d->n_vertices;
+  M.nt = d->n_tets;
+  const int nv = M.nv, nt = M.nt;
+  std::vector<double> Vref(d->V_rest, d->V_rest + 3 * (size_t)nv);
+  M.V0 = d->V_init ? std::vector<double>(d->V_init, d->V_init + 3 * (size_t)nv) : Vref;
+  M.v0 = d->v_init ? std::vector<double>(d->v_init, d->v_init + 3 * (size_t)nv)
+                   : std::vector<double>(3 * (size_t)nv, 0.0);
+  M.T.assign(d->tets, d->tets + 4 * (size_t)nt);
+  for (int v : M.T)
+    if (v < 0 || v >= nv) return MFEM_ERR_INVALID;
+  M.mu.assign(d->mu, d->mu + nt);
+  M.lam.assign(d->lambda, d->lambda + nt);
+  M.material_uniform = d->material ? d->material[0] : MFEM_MATERIAL_SNH;
+  if (d->material) {
+    M.mat.resize(nt);
+    for (int e = 0; e < nt; ++e) {
+      if (d->material[e] < 0 || d->material[e] > MFEM_MATERIAL_FUNG) return MFEM_ERR_INVALID;
+      M.mat[e] = (int8_t)d->material[e];
+      if (d->material[e] != M.material_uniform) M.material_uniform = -1;
+    }
+  }
+  // ---- boundary script (Mesh::init_bcs, mesh.cpp:161-175)
+  M.bc_type = d->bc_type;
+  M.bc_axis = d->bc_axis;
+  M.bc_vel = d->bc_velocity;
+  std::vector<int> group;
+  boundary_groups(Vref, nv, d->bc_axis, d->bc_ratio, group);
+  M.is_fixed.assign(nv, 0);
+  std::vector<int> g0, g1;
+  for (int v = 0; v < nv; ++v) {
+    if (group[v] == 0) g0.push_back(v);
+    if (group[v] == 1) g1.push_back(v);
+  }
+  switch (d->bc_type) {
+    case MFEM_BC_NULL:
+      break;
+    case MFEM_BC_SCALEF: {  // ScaleBC::init
+      double c[3];
+      bbox_center(M.V0, nv, c);
+      for (int v = 0; v < nv; ++v)
+        for (int k = 0; k < 3; ++k) M.V0[3 * v + k] = (M.V0[3 * v + k] - c[k]) * 1.5 + c[k];
+      break;
+    }
+    case MFEM_BC_RANDOM: {  // RandomizeBC::init with a seeded generator
+      double c[3], lo = 1e300, hi = -1e300;
+      bbox_center(M.V0, nv, c);
+      for (int v = 0; v < nv; ++v) {
+        lo = std::min(lo, M.V0[3 * v + 1]);
+        hi = std::max(hi, M.V0[3 * v + 1]);
+      }
+      uint64_t st = 0x9E3779B97F4A7C15ull;
+      for (auto& x : M.V0) {
+        st = st * 6364136223846793005ull + 1442695040888963407ull;
+        x = (double((st >> 11) & ((1ull << 53) - 1)) / double(1ull << 53) * 2 - 1) / 2.0;
+      }
+      c[1] += (hi - lo) * 0.5;
+      const double r0[3] = {M.V0[0], M.V0[1], M.V0[2]};
+      for (int v = 0; v < nv; ++v)
+        for (int k = 0; k < 3; ++k) M.V0[3 * v + k] += c[k] - r0[k];
+      break;
+    }
+    case MFEM_BC_ONEPOINT:
+      M.is_fixed[0] = 1;
+      break;
+    case MFEM_BC_HANG:
+      if (!g0.empty()) M.is_fixed[g0.back()] = 1;
+      if (!g1.empty()) M.is_fixed[g1.back()] = 1;
+      break;
+    case MFEM_BC_HANGENDS:
+      for (int v : g1) M.is_fixed[v] = 1;
+      break;
+    case MFEM_BC_PINMIN:
+      for (int v : g0) M.is_fixed[v] = 1;
+      break;
+    case MFEM_BC_STRETCH:
+    case MFEM_BC_COMPRESS:
+    case MFEM_BC_TWIST:
+    case MFEM_BC_BEND:
+      for (int v : g0) M.is_fixed[v] = 1;
+      for (int v : g1) M.is_fixed[v] = 1;
+      if (d->bc_type == MFEM_BC_TWIST) bbox_center(M.V0, nv, M.twist_center);
+      if (d->bc_type == MFEM_BC_BEND) {
+        const int a = g0.empty() ? 0 : g0.back(), b = g1.empty() ? 0 : g1.back();
+        for (int k = 0; k < 3; ++k) {
+          M.bend_center[0][k] = M.V0[3 * a + k];
+          M.bend_center[1][k] = M.V0[3 * b + k];
+        }
+      }
+      break;
+    default:
+      return MFEM_ERR_UNSUPPORTED;
+  }
+  if (d->is_fixed)
+    for (int v = 0; v < nv; ++v) M.is_fixed[v] = d->is_fixed[v] ? 1 : 0;
+  M.free_map.assign(nv, 0);
+  M.free_vert.clear();
+  M.pin_vert.clear();
+  M.pin_group.clear();
+  for (int v = 0; v < nv; ++v) {
+    if (M.is_fixed[v]) {
+      M.free_map[v] = -1 - (int)M.pin_vert.size();
+      M.pin_vert.push_back(v);
+      M.pin_group.push_back(group[v]);
+    } else {
+      M.free_map[v] = (int)M.free_vert.size();
+      M.free_vert.push_back(v);
+    }
+  }
+  M.nf = (int)M.free_vert.size();
+  M.npin = (int)M.pin_vert.size();
+  // ---- geometry: |det Dm|/6 and dphi/dX = rows of Dm^{-1} (tet_mesh.cpp:31-75)
+  M.vol.resize(nt);
+  M.dphi.resize(9 * (size_t)nt);
+  for (int e = 0; e < nt; ++e) {
+    const double* X0 = &Vref[3 * M.T[4 * e]];
+    double Dm[9], Di[9], det;
+    for (int k = 1; k < 4; ++k) {
+      const double* Xk = &Vref[3 * M.T[4 * e + k]];
+      for (int r = 0; r < 3; ++r) Dm[r + 3 * (k - 1)] = Xk[r] - X0[r];
+    }
+    if (!invert3(Dm, Di, &det)) return MFEM_ERR_INVALID;
+    M.vol[e] = std::fabs(det) / 6.0;
+    for (int k = 1; k < 4; ++k)
+      for (int c = 0; c < 3; ++c) M.dphi[9 * (size_t)e + 3 * (k - 1) + c] = Di[(k - 1) + 3 * c];
+  }
+  // ---- vertex -> tet incidence
+  std::vector<int> vt_ptr(nv + 1, 0), vt(4 * (size_t)nt);
+  for (int v : M.T) vt_ptr[v + 1]++;
+  for (int v = 0; v < nv; ++v) vt_ptr[v + 1] += vt_ptr[v];
+  {
+    std::vector<int> fill(vt_ptr.begin(), vt_ptr.end() - 1);
+    for (int e = 0; e < nt; ++e)
+      for (int k = 0; k < 4; ++k) vt[fill[M.T[4 * e + k]]++] = 4 * e + k;  // sorted by e
+  }
+  // ---- consistent P1 mass over all vertices (linear_tetmesh_mass_matrix)
+  const double* rho = d->density;
+  M.m_ptr.assign(nv + 1, 0);
+  M.m_col.clear();
+  M.m_val.clear();
+  {
+    std::vector<std::pair<int, double>> row;
+    for (int a = 0; a < nv; ++a) {
+      row.clear();
+      for (int q = vt_ptr[a]; q < vt_ptr[a + 1]; ++q) {
+        const int e = vt[q] / 4, i = vt[q] % 4;
+        const double m = (rho ? rho[e] : d->density_const) * M.vol[e] / 20.0;
+        for (int k = 0; k < 4; ++k) row.push_back({M.T[4 * e + k], k == i ? 2 * m : m});
+      }
+      std::sort(row.begin(), row.end(),
+                [](const std::pair<int, double>& x, const std::pair<int, double>& y) {
+                  return x.first < y.first;
+                });
+      for (size_t k = 0; k < row.size(); ++k) {
+        if (k > 0 && row[k].first == row[k - 1].first)
+          M.m_val.back() += row[k].second;
+        else {
+          M.m_col.push_back(row[k].first);
+          M.m_val.push_back(row[k].second);
+        }
+      }
+      M.m_ptr[a + 1] = (int)M.m_col.size();
+    }
+  }
+  // ---- block pattern over free vertices (the sorted free pairs of the Assembler)
+  M.b_ptr.assign(M.nf + 1, 0);
+  M.b_col.clear();
+  M.b_mass.clear();
+  M.inc_ptr.assign(M.nf + 1, 0);
+  M.inc.clear();
+  {
+    std::vector<int> cols;
+    for (int r = 0; r < M.nf; ++r) {
+      const int a = M.free_vert[r];
+      cols.clear();
+      for (int q = vt_ptr[a]; q < vt_ptr[a + 1]; ++q) {
+        const int e = vt[q] / 4;
+        for (int k = 0; k < 4; ++k) {
+          const int f = M.free_map[M.T[4 * e + k]];
+          if (f >= 0) cols.push_back(f);
+        }
+      }
+      std::sort(cols.begin(), cols.end());
+      cols.erase(std::unique(cols.begin(), cols.end()), cols.end());
+      if ((int)cols.size() > kMaxRowBlocks) return MFEM_ERR_CAPACITY;
+      const int rb = (int)M.b_col.size();
+      M.b_col.insert(M.b_col.end(), cols.begin(), cols.end());
+      M.b_ptr[r + 1] = (int)M.b_col.size();
+      // mass of each free-free block
+      for (size_t k = 0; k < cols.size(); ++k) M.b_mass.push_back(0.0);
+      for (int q = M.m_ptr[a]; q < M.m_ptr[a + 1]; ++q) {
+        const int f = M.free_map[M.m_col[q]];
+        if (f < 0) continue;
+        const int pos = int(std::lower_bound(cols.begin(), cols.end(), f) - cols.begin());
+        M.b_mass[rb + pos] += M.m_val[q];
+      }
+      // incidences (element, local vertex) in element order
+      for (int q = vt_ptr[a]; q < vt_ptr[a + 1]; ++q) {
+        const int e = vt[q] / 4, i = vt[q] % 4;
+        int code = i;
+        for (int k = 0; k < 4; ++k) {
+          const int f = M.free_map[M.T[4 * e + k]];
+          int slot = 127;
+          if (f >= 0) slot = int(std::lower_bound(cols.begin(), cols.end(), f) - cols.begin());
+          code |= slot << (2 + 7 * k);
+        }
+        M.inc.push_back(make_int2(e, code));
+      }
+      M.inc_ptr[r + 1] = (int)M.inc.size();
+    }
+  }
+  M.nnzb = (int)M.b_col.size();
+  return MFEM_OK;
+}
+
+}  // namespace
+
+// ---------------------------------------------------------------- types ---
+struct mfem_scene {
+  HostMesh M;
+  int fp64 = 0;
+  size_t rsz = 4;
+  int ntp = 0;
+  double h = 0, dt = 0, h2 = 0;
+  mfem_scene_desc cfg{};
+  std::vector<double> pin_pos;  // current pinned positions (host BC state)
+  char* dmem = nullptr;
+  size_t dbytes = 0;
+  SceneDev dev{};
+  SceneScalars* d_sc = nullptr;
+  double* d_pin_pos = nullptr;
+  mfem_batch* solo = nullptr;
+  int nnzb = 0;
+  bool pins_driven = false;  // pins set by the caller for the next step
+};
+
+struct mfem_batch {
+  std::vector<mfem_scene*> scenes;
+  int fp64 = 0;
+  cudaStream_t stream = nullptr;
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  char* dmem = nullptr;
+  Tile* d_tiles[TB_COUNT] = {nullptr, nullptr, nullptr, nullptr};
+  int ntiles[TB_COUNT] = {0, 0, 0, 0};
+  SceneDev* d_sds = nullptr;
+  std::vector<SceneDev> h_sds;
+  double* d_partials = nullptr;
+  BatchCounters* d_ctr = nullptr;
+  BatchCounters* h_ctr = nullptr;   // pinned
+  SceneScalars* h_sc = nullptr;     // pinned, one per scene
+  int max_newton = 0, max_ls = 0, max_cg = 0;
+  int cg_hint = 16;
+  // instrumentation
+  bool profiling = false;
+  std::vector<cudaEvent_t> ev_pool;
+  std::vector<int> ev_kernel;   // kernel id of each recorded pair
+  size_t ev_used = 0;           // pairs recorded since the last harvest
+  double k_ms[MFEM_K_COUNT] = {0};
+  int64_t k_launches[MFEM_K_COUNT] = {0};
+};
+
+namespace {
+
+// Brackets one kernel launch with CUDA events when profiling is on.
+struct KTimer {
+  mfem_batch* b;
+  int id;
+  cudaEvent_t e1 = nullptr;
+  KTimer(mfem_batch* batch, int kernel) : b(batch), id(kernel) {
+    b->k_launches[id] += 1;
+    if (!b->profiling) return;
+    if (b->ev_used * 2 + 2 > b->ev_pool.size()) {
+      for (int k = 0; k < 256; ++k) {
+        cudaEvent_t e;
+        cudaEventCreate(&e);
+        b->ev_pool.push_back(e);
+      }
+      b->ev_kernel.resize(b->ev_pool.size() / 2);
+    }
+    cudaEventRecord(b->ev_pool[2 * b->ev_used], b->stream);
+    e1 = b->ev_pool[2 * b->ev_used + 1];
+    b->ev_kernel[b->ev_used] = id;
+  }
+  ~KTimer() {
+    if (!e1) return;
+    cudaEventRecord(e1, b->stream);
+    b->ev_used += 1;
+  }
+};
+
+// Adds the recorded pairs to the per-kernel totals (after a stream sync).
+void harvest_timers(mfem_batch* b) {
+  for (size_t i = 0; i < b->ev_used; ++i) {
+    float ms = 0;
+    if (cudaEventElapsedTime(&ms, b->ev_pool[2 * i], b->ev_pool[2 * i + 1]) == cudaSuccess)
+      b->k_ms[b->ev_kernel[i]] += ms;
+  }
+  b->ev_used = 0;
+}
+
+Launch make_launch(mfem_batch* b, int table) {
+  Launch L;
+  L.stream = b->stream;
+  L.tiles = b->d_tiles[table];
+  L.ntiles = b->ntiles[table];
+  L.sds = b->d_sds;
+  L.partials = b->d_partials;
+  L.counters = b->d_ctr;
+  L.fp64 = b->fp64;
+  return L;
+}
+
+// Device layout of a scene (dry run with base == nullptr to size it).
+void layout_scene(mfem_scene* s, Arena& A) {
+  const HostMesh& M = s->M;
+  const size_t r = s->rsz, ntp = s->ntp;
+  SceneDev& D = s->dev;
+  const int I = s->cfg.bdf_order;
+  D.tets = A.take<int4>(M.nt);
+  D.dphi = A.take_bytes(9 * ntp * r);
+  D.vol = A.take_bytes(ntp * r);
+  D.mu = A.take_bytes(ntp * r);
+  D.lam = A.take_bytes(ntp * r);
+  D.mat = M.mat.empty() ? nullptr : A.take<int8_t>(ntp);
+  D.quat = A.take_bytes(4 * ntp * r);
+  D.s = A.take_bytes(6 * ntp * r);
+  D.la = A.take_bytes(6 * ntp * r);
+  D.S = A.take_bytes(6 * ntp * r);
+  D.ds = A.take_bytes(6 * ntp * r);
+  D.rec = A.take_bytes((size_t)kRec * M.nt * r);
+  D.x = A.take<double>(3 * (size_t)M.nv);
+  D.xt = A.take<double>(3 * (size_t)M.nv);
+  D.xhist = A.take<double>(3 * (size_t)M.nv * I);
+  D.vhist = A.take<double>(3 * (size_t)M.nv * I);
+  D.free_map = A.take<int>(M.nv);
+  D.free_vert = A.take<int>(std::max(M.nf, 1));
+  D.pin_vert = A.take<int>(std::max(M.npin, 1));
+  s->d_pin_pos = A.take<double>(3 * (size_t)std::max(M.npin, 1));
+  D.pin_pos = s->d_pin_pos;
+  D.m_ptr = A.take<int>(M.nv + 1);
+  D.m_col = A.take<int>(M.m_col.size());
+  D.m_val = A.take<double>(M.m_val.size());
+  D.b_ptr = A.take<int>(M.nf + 1);
+  D.b_col = A.take<int>(std::max(M.nnzb, 1));
+  D.b_mass = A.take_bytes(std::max(M.nnzb, 1) * r);
+  D.b_val = A.take_bytes(9 * (size_t)std::max(M.nnzb, 1) * r);
+  D.dinv = A.take_bytes(9 * (size_t)std::max(M.nf, 1) * r);
+  D.inc_ptr = A.take<int>(M.nf + 1);
+  D.inc = A.take<int2>(std::max<size_t>(M.inc.size(), 1));
+  const size_t n3 = 3 * (size_t)std::max(M.nf, 1);
+  D.rhs = A.take_bytes(n3 * r);
+  D.cg_x = A.take_bytes(n3 * r);
+  D.cg_r = A.take_bytes(n3 * r);
+  D.cg_z = A.take_bytes(n3 * r);
+  D.cg_p[0] = A.take_bytes(n3 * r);
+  D.cg_p[1] = A.take_bytes(n3 * r);
+  D.cg_Ap = A.take_bytes(n3 * r);
+  s->d_sc = A.take<SceneScalars>(1);
+  D.sc = s->d_sc;
+}
+
+template <typename T>
+std::vector<T> soa(const std::vector<double>& src, int n, int ncomp, int ntp) {
+  // element-major (ncomp per element) -> component-major with stride ntp
+  std::vector<T> out((size_t)ncomp * ntp, T(0));
+  for (int e = 0; e < n; ++e)
+    for (int k = 0; k < ncomp; ++k) out[(size_t)k * ntp + e] = T(src[(size_t)ncomp * e + k]);
+  return out;
+}
+
+template <typename T>
+int upload_reals(void* dst, const std::vector<double>& src, size_t count, cudaStream_t st) {
+  std::vector<T> tmp(count, T(0));
+  for (size_t i = 0; i < std::min(count, src.size()); ++i) tmp[i] = T(src[i]);
+  CUDA_OR(cudaMemcpyAsync(dst, tmp.data(), count * sizeof(T), cudaMemcpyHostToDevice, st), MFEM_ERR_CUDA);
+  CUDA_OR(cudaStreamSynchronize(st), MFEM_ERR_CUDA);
+  return MFEM_OK;
+}
+
+template <typename T>
+int upload_scene_reals(mfem_scene* s, cudaStream_t st) {
+  const HostMesh& M = s->M;
+  const int ntp = s->ntp;
+  SceneDev& D = s->dev;
+  auto put = [&](const void* dst, const std::vector<T>& v) -> int {
+    CUDA_OR(cudaMemcpyAsync(const_cast<void*>(dst), v.data(), v.size() * sizeof(T),
+                            cudaMemcpyHostToDevice, st),
+            MFEM_ERR_CUDA);
+    return MFEM_OK;
+  };
+  int rc;
+  if ((rc = put(D.dphi, soa<T>(M.dphi, M.nt, 9, ntp)))) return rc;
+  if ((rc = put(D.vol, soa<T>(M.vol, M.nt, 1, ntp)))) return rc;
+  if ((rc = put(D.mu, soa<T>(M.mu, M.nt, 1, ntp)))) return rc;
+  if ((rc = put(D.lam, soa<T>(M.lam, M.nt, 1, ntp)))) return rc;
+  std::vector<T> bm(std::max(M.nnzb, 1), T(0));
+  for (int k = 0; k < M.nnzb; ++k) bm[k] = T(M.b_mass[k]);
+  if ((rc = put(D.b_mass, bm))) return rc;
+  CUDA_OR(cudaStreamSynchronize(st), MFEM_ERR_CUDA);
+  return MFEM_OK;
+}
+
+int batch_build(mfem_scene* const* scenes, int n, mfem_batch** out);
+
+int sync_counters(mfem_batch* b) {
+  CUDA_OR(cudaMemcpyAsync(b->h_ctr, b->d_ctr, sizeof(BatchCounters), cudaMemcpyDeviceToHost, b->stream),
+          MFEM_ERR_CUDA);
+  CUDA_OR(cudaStreamSynchronize(b->stream), MFEM_ERR_CUDA);
+  return MFEM_OK;
+}
+
+// Moves the pinned vertices by one BC step on the host and uploads them
+// (Meshes::update_bcs, meshes.cpp:156-167).
+int bc_step_upload(mfem_scene* s, cudaStream_t st) {
+  HostMesh& M = s->M;
+  if (s->pins_driven) {  // the caller already uploaded this step's pins
+    s->pins_driven = false;
+    return MFEM_OK;
+  }
+  bool moved = false;
+  const double dt = s->h;
+  for (int p = 0; p < M.npin; ++p) {
+    const int grp = M.pin_group[p];
+    double* x = &s->pin_pos[3 * p];
+    switch (M.bc_type) {
+      case MFEM_BC_STRETCH:
+        if (grp >= 0) {
+          x[M.bc_axis] += (grp == 0 ? 1.0 : -1.0) * M.bc_vel * dt;
+          moved = true;
+        }
+        break;
+      case MFEM_BC_COMPRESS:
+        if (grp == 1) {
+          x[M.bc_axis] += M.bc_vel * dt;
+          moved = true;
+        }
+        break;
+      case MFEM_BC_TWIST:
+        if (grp >= 0) {
+          rotate_about(x, M.twist_center, 0, (grp == 0 ? 1.0 : -1.0) * M.bc_vel * M_PI * dt);
+          moved = true;
+        }
+        break;
+      case MFEM_BC_BEND:
+        if (grp >= 0) {
+          rotate_about(x, M.bend_center[grp], 2, (grp == 0 ? 1.0 : -1.0) * M.bc_vel * M_PI * dt);
+          moved = true;
+        }
+        break;
+      default:
+        break;
+    }
+  }
+  if (moved && M.npin > 0)
+    CUDA_OR(cudaMemcpyAsync(s->d_pin_pos, s->pin_pos.data(), 3 * sizeof(double) * M.npin,
+                            cudaMemcpyHostToDevice, st),
+            MFEM_ERR_CUDA);
+  return MFEM_OK;
+}
+
+int worst_status(const SceneScalars& sc) {
+  if (sc.status == MFEM_ERR_NONFINITE) return MFEM_ERR_NONFINITE;
+  if (sc.procrustes_fail) return MFEM_ERR_PROCRUSTES;
+  if (sc.status) return sc.status;
+  if (sc.cg_status) return sc.cg_status;
+  return MFEM_OK;
+}
+
+// The Newton loop of NewtonOptimizer::step for every scene of the batch.
+int batch_newton(mfem_batch* b) {
+  const int n = (int)b->scenes.size();
+  Launch Lev = make_launch(b, TB_EV);
+  { KTimer t(b, MFEM_K_SCALARS); launch_scalars_begin(Lev, n); }
+  { KTimer t(b, MFEM_K_STEP_BEGIN); launch_step_begin(Lev); }
+  int rc;
+  for (int newton = 0; newton <= b->max_newton + 1; ++newton) {
+    { KTimer t(b, MFEM_K_ELEM_UPDATE); launch_elem_update(make_launch(b, TB_ELEM), nullptr); }
+    { KTimer t(b, MFEM_K_ASSEMBLE); launch_assemble(make_launch(b, TB_ROW)); }
+    Launch Lcg = make_launch(b, TB_CG);
+    { KTimer t(b, MFEM_K_CG_INIT); launch_cg_init(Lcg); }
+    int done = 0;
+    int chunk = std::max(4, b->cg_hint);
+    while (done < b->max_cg) {
+      const int c = std::min(chunk, b->max_cg - done);
+      for (int k = 0; k < c; ++k) {
+        { KTimer t(b, MFEM_K_CG_SPMV); launch_cg_spmv(Lcg); }
+        { KTimer t(b, MFEM_K_CG_UPDATE); launch_cg_update(Lcg); }
+      }
+      done += c;
+      if ((rc = sync_counters(b))) return rc;
+      if (b->h_ctr->cg_active == 0) break;
+      chunk = 8;
+    }
+    b->cg_hint = std::max(4, (done * 3) / 4);
+    { KTimer t(b, MFEM_K_LOCAL_SOLVE); launch_local_solve(Lev); }
+    for (int l = 0; l < b->max_ls; ++l) {
+      { KTimer t(b, MFEM_K_LS_ENERGY); launch_ls_energy(Lev); }
+      if ((rc = sync_counters(b))) return rc;
+      if (b->h_ctr->ls_active == 0) break;
+    }
+    { KTimer t(b, MFEM_K_APPLY); launch_apply(Lev); }
+    if ((rc = sync_counters(b))) return rc;
+    if (b->h_ctr->newton_active == 0) break;
+  }
+  return MFEM_OK;
+}
+
+int batch_step_impl(mfem_batch* b, mfem_step_stats* stats) {
+  std::call_once(g_configured, configure_kernels);
+  const int n = (int)b->scenes.size();
+  CUDA_OR(cudaEventRecord(b->ev0, b->stream), MFEM_ERR_CUDA);
+  int rc = batch_newton(b);
+  if (rc) return rc;
+  for (int i = 0; i < n; ++i)
+    if ((rc = bc_step_upload(b->scenes[i], b->stream))) return rc;
+  { KTimer t(b, MFEM_K_STEP_END); launch_step_end(make_launch(b, TB_EV)); }
+  CUDA_OR(cudaEventRecord(b->ev1, b->stream), MFEM_ERR_CUDA);
+  for (int i = 0; i < n; ++i)
+    CUDA_OR(cudaMemcpyAsync(&b->h_sc[i], b->scenes[i]->d_sc, sizeof(SceneScalars),
+                            cudaMemcpyDeviceToHost, b->stream),
+            MFEM_ERR_CUDA);
+  CUDA_OR(cudaStreamSynchronize(b->stream), MFEM_ERR_CUDA);
+  CUDA_OR(cudaGetLastError(), MFEM_ERR_CUDA);
+  harvest_timers(b);
+  float ms = 0;
+  cudaEventElapsedTime(&ms, b->ev0, b->ev1);
+  int worst = MFEM_OK;
+  for (int i = 0; i < n; ++i) {
+    const SceneScalars& sc = b->h_sc[i];
+    if (stats) {
+      mfem_step_stats& st = stats[i];
+      st.status = worst_status(sc);
+      st.newton_iterations = sc.newton_iter;
+      st.cg_iterations = sc.cg_total;
+      st.ls_iterations = sc.ls_total;
+      st.energy = sc.E;
+      st.energy_residual = sc.eres;
+      st.decrement = sc.decrement;
+      st.alpha = sc.alpha_ls;
+      st.residual0 = sc.rhs_norm0;
+      st.residual = sc.rhs_norm;
+      st.cg_error = sc.cg_err;
+      st.device_ms = ms;
+    }
+    if (sc.status == MFEM_ERR_NONFINITE) worst = MFEM_ERR_NONFINITE;
+  }
+  return worst;
+}
+
+int upload_sds(mfem_batch* b) {
+  CUDA_OR(cudaMemcpyAsync(b->d_sds, b->h_sds.data(), sizeof(SceneDev) * b->h_sds.size(),
+                          cudaMemcpyHostToDevice, b->stream),
+          MFEM_ERR_CUDA);
+  CUDA_OR(cudaStreamSynchronize(b->stream), MFEM_ERR_CUDA);
+  return MFEM_OK;
+}
+
+int batch_build(mfem_scene* const* scenes, int n, mfem_batch** out) {
+  if (!scenes || n <= 0 || !out) return MFEM_ERR_INVALID;
+  auto b = std::make_unique<mfem_batch>();
+  b->fp64 = scenes[0]->fp64;
+  for (int i = 0; i < n; ++i) {
+    if (!scenes[i] || scenes[i]->fp64 != b->fp64) return MFEM_ERR_INVALID;
+    b->scenes.push_back(scenes[i]);
+  }
+  // tile tables
+  std::vector<Tile> tabs[TB_COUNT];
+  b->h_sds.resize(n);
+  for (int i = 0; i < n; ++i) {
+    mfem_scene* s = scenes[i];
+    SceneDev D = s->dev;
+    auto add = [&](int tb, int kind, int count, int per) {
+      for (int beg = 0; beg < count; beg += per) tabs[tb].push_back(Tile{i, kind, beg, std::min(count, beg + per)});
+    };
+    for (int tb = 0; tb < TB_COUNT; ++tb) D.tile_first[tb] = (int)tabs[tb].size();
+    add(TB_ELEM, 0, s->M.nt, kElemTile);
+    add(TB_ROW, 0, s->M.nf, kRowTile);
+    add(TB_CG, 0, s->M.nf, kCgRows);
+    add(TB_EV, 0, s->M.nt, kElemTile);
+    add(TB_EV, 1, s->M.nv, kVertTile);
+    for (int tb = 0; tb < TB_COUNT; ++tb) D.tile_count[tb] = (int)tabs[tb].size() - D.tile_first[tb];
+    b->h_sds[i] = D;
+    b->max_newton = std::max(b->max_newton, s->cfg.max_newton_iterations);
+    b->max_ls = std::max(b->max_ls, s->cfg.max_linesearch_iterations);
+    b->max_cg = std::max(b->max_cg, s->cfg.max_iterative_solver_iters);
+  }
+  size_t maxt = 1;
+  for (int tb = 0; tb < TB_COUNT; ++tb) {
+    b->ntiles[tb] = (int)tabs[tb].size();
+    maxt = std::max(maxt, tabs[tb].size());
+  }
+  Arena A;
+  auto lay = [&](Arena& a) {
+    for (int tb = 0; tb < TB_COUNT; ++tb) b->d_tiles[tb] = a.take<Tile>(std::max<size_t>(tabs[tb].size(), 1));
+    b->d_sds = a.take<SceneDev>(n);
+    b->d_partials = a.take<double>(maxt * kNumPartials);
+    b->d_ctr = a.take<BatchCounters>(1);
+  };
+  lay(A);
+  CUDA_OR(cudaMalloc(&b->dmem, A.used), MFEM_ERR_OOM);
+  Arena B;
+  B.base = b->dmem;
+  lay(B);
+  CUDA_OR(cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking), MFEM_ERR_CUDA);
+  CUDA_OR(cudaEventCreate(&b->ev0), MFEM_ERR_CUDA);
+  CUDA_OR(cudaEventCreate(&b->ev1), MFEM_ERR_CUDA);
+  CUDA_OR(cudaMallocHost(&b->h_ctr, sizeof(BatchCounters)), MFEM_ERR_OOM);
+  CUDA_OR(cudaMallocHost(&b->h_sc, sizeof(SceneScalars) * n), MFEM_ERR_OOM);
+  for (int tb = 0; tb < TB_COUNT; ++tb)
+    if (!tabs[tb].empty())
+      CUDA_OR(cudaMemcpyAsync(b->d_tiles[tb], tabs[tb].data(), sizeof(Tile) * tabs[tb].size(),
+                              cudaMemcpyHostToDevice, b->stream),
+              MFEM_ERR_CUDA);
+  CUDA_OR(cudaMemsetAsync(b->d_ctr, 0, sizeof(BatchCounters), b->stream), MFEM_ERR_CUDA);
+  int rc = upload_sds(b.get());
+  if (rc) return rc;
+  *out = b.release();
+  return MFEM_OK;
+}
+
+void batch_free(mfem_batch* b) {
+  if (!b) return;
+  if (b->stream) cudaStreamSynchronize(b->stream);
+  if (b->dmem) cudaFree(b->dmem);
+  if (b->h_ctr) cudaFreeHost(b->h_ctr);
+  if (b->h_sc) cudaFreeHost(b->h_sc);
+  for (cudaEvent_t e : b->ev_pool) cudaEventDestroy(e);
+  if (b->ev0) cudaEventDestroy(b->ev0);
+  if (b->ev1) cudaEventDestroy(b->ev1);
+  if (b->stream) cudaStreamDestroy(b->stream);
+  delete b;
+}
+
+int scene_layout_bytes(mfem_scene* s, size_t* bytes) {
+  Arena A;
+  layout_scene(s, A);
+  *bytes = A.used;
+  return MFEM_OK;
+}
+
+int scene_init_device(mfem_scene* s) {
+  const HostMesh& M = s->M;
+  Arena A;
+  layout_scene(s, A);
+  s->dbytes = A.used;
+  CUDA_OR(cudaMalloc(&s->dmem, s->dbytes), MFEM_ERR_OOM);
+  Arena B;
+  B.base = s->dmem;
+  layout_scene(s, B);
+  SceneDev& D = s->dev;
+  D.nv = M.nv;
+  D.nt = M.nt;
+  D.nf = M.nf;
+  D.nnzb = M.nnzb;
+  D.ntp = s->ntp;
+  D.npin = M.npin;
+  D.material_uniform = M.material_uniform;
+  D.block_jacobi = s->cfg.linear_solver == MFEM_SOLVER_GPU_PCG_BLOCK ? 1 : 0;
+  D.fp64 = s->fp64;
+  D.h2 = s->h2;
+  D.dt = s->dt;
+  D.newton_tol = s->cfg.newton_tol;
+  D.res_tol = s->cfg.newton_residual_tolerance;
+  D.cg_tol = s->cfg.iterative_solver_tolerance;
+  D.max_newton = s->cfg.max_newton_iterations;
+  D.max_ls = s->cfg.max_linesearch_iterations;
+  D.max_cg = s->cfg.max_iterative_solver_iters;
+  D.bdf_order = s->cfg.bdf_order;
+  static const double alphas[7][6] = {
+      {0},
+      {1.0},
+      {4.0 / 3, -1.0 / 3},
+      {18.0 / 11, -9.0 / 11, 2.0 / 11},
+      {48.0 / 25, -36.0 / 25, 16.0 / 25, -3.0 / 25},
+      {300.0 / 137, -300.0 / 137, 200.0 / 137, -75.0 / 137, 12.0 / 137},
+      {360.0 / 147, -450.0 / 147, 400.0 / 147, -225.0 / 147, 72.0 / 147, -10.0 / 147}};
+  for (int i = 0; i < 6; ++i) D.bdf_alpha[i] = alphas[D.bdf_order][i];
+  // SimConfig::ext is float[3]; the reference casts it to double (displacement.cpp:96).
+  for (int k = 0; k < 3; ++k) D.body[k] = double(float(s->cfg.body_force[k]));
+  {
+    double acc = 0;
+    for (int v = 0; v < M.nv; ++v) {
+      if (M.free_map[v] < 0) continue;
+      double m = 0;
+      for (int q = M.m_ptr[v]; q < M.m_ptr[v + 1]; ++q) m += M.m_val[q];
+      for (int k = 0; k < 3; ++k) acc += (s->h2 * m * D.body[k]) * (s->h2 * m * D.body[k]);
+    }
+    D.load_norm = std::sqrt(acc);
+  }
+  cudaStream_t st = nullptr;
+  CUDA_OR(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking), MFEM_ERR_CUDA);
+  auto put = [&](const void* dst, const void* src, size_t bytes) -> int {
+    if (bytes == 0) return MFEM_OK;
+    CUDA_OR(cudaMemcpyAsync(const_cast<void*>(dst), src, bytes, cudaMemcpyHostToDevice, st), MFEM_ERR_CUDA);
+    return MFEM_OK;
+  };
+  int rc = 0;
+  CUDA_OR(cudaMemsetAsync(s->dmem, 0, s->dbytes, st), MFEM_ERR_CUDA);
+  rc |= put(D.tets, M.T.data(), sizeof(int) * M.T.size());
+  if (D.mat) rc |= put(D.mat, M.mat.data(), M.mat.size());
+  rc |= put(D.x, M.V0.data(), sizeof(double) * M.V0.size());
+  for (int i = 0; i < D.bdf_order; ++i) {
+    rc |= put(D.xhist + 3 * (size_t)M.nv * i, M.V0.data(), sizeof(double) * M.V0.size());
+    rc |= put(D.vhist + 3 * (size_t)M.nv * i, M.v0.data(), sizeof(double) * M.v0.size());
+  }
+  rc |= put(D.free_map, M.free_map.data(), sizeof(int) * M.nv);
+  rc |= put(D.free_vert, M.free_vert.data(), sizeof(int) * M.nf);
+  rc |= put(D.pin_vert, M.pin_vert.data(), sizeof(int) * M.npin);
+  rc |= put(s->d_pin_pos, s->pin_pos.data(), sizeof(double) * s->pin_pos.size());
+  rc |= put(D.m_ptr, M.m_ptr.data(), sizeof(int) * M.m_ptr.size());
+  rc |= put(D.m_col, M.m_col.data(), sizeof(int) * M.m_col.size());
+  rc |= put(D.m_val, M.m_val.data(), sizeof(double) * M.m_val.size());
+  rc |= put(D.b_ptr, M.b_ptr.data(), sizeof(int) * M.b_ptr.size());
+  rc |= put(D.b_col, M.b_col.data(), sizeof(int) * M.b_col.size());
+  rc |= put(D.inc_ptr, M.inc_ptr.data(), sizeof(int) * M.inc_ptr.size());
+  rc |= put(D.inc, M.inc.data(), sizeof(int2) * M.inc.size());
+  if (rc) return MFEM_ERR_CUDA;
+  CUDA_OR(cudaStreamSynchronize(st), MFEM_ERR_CUDA);
+  rc = s->fp64 ? upload_scene_reals<double>(s, st) : upload_scene_reals<float>(s, st);
+  cudaStreamDestroy(st);
+  return rc;
+}
+
+template <typename T>
+void download_soa(const void* dsrc, int nt, int ntp, int ncomp, double* out, cudaStream_t st) {
+  std::vector<T> tmp((size_t)ncomp * ntp);
+  cudaMemcpyAsync(tmp.data(), dsrc, tmp.size() * sizeof(T), cudaMemcpyDeviceToHost, st);
+  cudaStreamSynchronize(st);
+  for (int e = 0; e < nt; ++e)
+    for (int k = 0; k < ncomp; ++k) out[(size_t)ncomp * e + k] = double(tmp[(size_t)k * ntp + e]);
+}
+
+template <typename T>
+void upload_soa(void* ddst, int nt, int ntp, int ncomp, const double* in, cudaStream_t st) {
+  std::vector<T> tmp((size_t)ncomp * ntp, T(0));
+  for (int e = 0; e < nt; ++e)
+    for (int k = 0; k < ncomp; ++k) tmp[(size_t)k * ntp + e] = T(in[(size_t)ncomp * e + k]);
+  cudaMemcpyAsync(ddst, tmp.data(), tmp.size() * sizeof(T), cudaMemcpyHostToDevice, st);
+  cudaStreamSynchronize(st);
+}
+
+// Gauss-Jordan inverse with partial pivoting of a column-major 6x6 (the
+// Hinv output of the element parity entry point).
+void inverse6_host(const double* A, double* Ai) {
+  double a[36];
+  for (int i = 0; i < 36; ++i) {
+    a[i] = A[i];
+    Ai[i] = (i % 7 == 0) ? 1.0 : 0.0;
+  }
+  for (int k = 0; k < 6; ++k) {
+    int p = k;
+    for (int i = k + 1; i < 6; ++i)
+      if (std::fabs(a[i + 6 * k]) > std::fabs(a[p + 6 * k])) p = i;
+    for (int j = 0; j < 6; ++j) {
+      std::swap(a[k + 6 * j], a[p + 6 * j]);
+      std::swap(Ai[k + 6 * j], Ai[p + 6 * j]);
+    }
+    const double inv = 1.0 / a[k + 6 * k];
+    for (int j = 0; j < 6; ++j) {
+      a[k + 6 * j] *= inv;
+      Ai[k + 6 * j] *= inv;
+    }
+    for (int i = 0; i < 6; ++i)
+      if (i != k) {
+        const double f = a[i + 6 * k];
+        for (int j = 0; j < 6; ++j) {
+          a[i + 6 * j] -= f * a[k + 6 * j];
+          Ai[i + 6 * j] -= f * Ai[k + 6 * j];
+        }
+      }
+  }
+}
+
+void quat_to_rot_h(const double q[4], double* R) {
+  const double w = q[0], x = q[1], y = q[2], z = q[3];
+  const double n = w * w + x * x + y * y + z * z;
+  const double s = n > 0 ? 2.0 / n : 0.0;
+  R[0] = 1 - s * (y * y + z * z);
+  R[3] = s * (x * y - w * z);
+  R[6] = s * (x * z + w * y);
+  R[1] = s * (x * y + w * z);
+  R[4] = 1 - s * (x * x + z * z);
+  R[7] = s * (y * z - w * x);
+  R[2] = s * (x * z - w * y);
+  R[5] = s * (y * z + w * x);
+  R[8] = 1 - s * (x * x + y * y);
+}
+
+void rot_to_quat_h(const double* R, double q[4]) {
+  const double t = R[0] + R[4] + R[8];
+  if (t > 0) {
+    const double s = std::sqrt(t + 1) * 2;
+    q[0] = 0.25 * s; q[1] = (R[5] - R[7]) / s; q[2] = (R[6] - R[2]) / s; q[3] = (R[1] - R[3]) / s;
+  } else if (R[0] > R[4] && R[0] > R[8]) {
+    const double s = std::sqrt(1 + R[0] - R[4] - R[8]) * 2;
+    q[0] = (R[5] - R[7]) / s; q[1] = 0.25 * s; q[2] = (R[3] + R[1]) / s; q[3] = (R[6] + R[2]) / s;
+  } else if (R[4] > R[8]) {
+    const double s = std::sqrt(1 + R[4] - R[0] - R[8]) * 2;
+    q[0] = (R[6] - R[2]) / s; q[1] = (R[3] + R[1]) / s; q[2] = 0.25 * s; q[3] = (R[7] + R[5]) / s;
+  } else {
+    const double s = std::sqrt(1 + R[8] - R[0] - R[4]) * 2;
+    q[0] = (R[1] - R[3]) / s; q[1] = (R[6] + R[2]) / s; q[2] = (R[7] + R[5]) / s; q[3] = 0.25 * s;
+  }
+  const double n = 1.0 / std::sqrt(q[0] * q[0] + q[1] * q[1] + q[2] * q[2] + q[3] * q[3]);
+  for (int i = 0; i < 4; ++i) q[i] *= n;
+}
+
+}  // namespace
+
+// ================================================================ C ABI ===
+extern "C" {
+
+int mfem_gpu_abi_version(void) { return MFEM_ABI_VERSION; }
+
+int mfem_gpu_set_device(int device) {
+  int n = 0;
+  if (cudaGetDeviceCount(&n) != cudaSuccess || n == 0) return MFEM_ERR_NO_DEVICE;
+  if (device < 0 || device >= n) return MFEM_ERR_INVALID;
+  CUDA_OR(cudaSetDevice(device), MFEM_ERR_CUDA);
+  return MFEM_OK;
+}
+
+const char* mfem_gpu_status_string(int status) {
+  switch (status) {
+    case MFEM_OK: return "ok";
+    case MFEM_ERR_INVALID: return "invalid argument";
+    case MFEM_ERR_OOM: return "out of device memory";
+    case MFEM_ERR_CUDA: return g_last_error[0] ? g_last_error : "CUDA error";
+    case MFEM_ERR_NONFINITE: return "non-finite value";
+    case MFEM_ERR_CG_MAXITER: return "PCG reached max iterations";
+    case MFEM_ERR_LS_FAILED: return "line search reached max iterations";
+    case MFEM_ERR_PROCRUSTES: return "singular rotation Hessian";
+    case MFEM_ERR_TIMEOUT: return "bounded device wait timed out";
+    case MFEM_ERR_NO_DEVICE: return "no CUDA device";
+    case MFEM_ERR_UNSUPPORTED: return "unsupported option";
+    case MFEM_ERR_CAPACITY: return "capacity exceeded";
+    default: return "unknown status";
+  }
+}
+
+int mfem_gpu_device_info(char* name, int name_len, int* sm_count) {
+  int n = 0;
+  if (cudaGetDeviceCount(&n) != cudaSuccess || n == 0) return MFEM_ERR_NO_DEVICE;
+  int dev = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceProp p;
+  CUDA_OR(cudaGetDeviceProperties(&p, dev), MFEM_ERR_CUDA);
+  if (name && name_len > 0) {
+    strncpy(name, p.name, name_len - 1);
+    name[name_len - 1] = 0;
+  }
+  if (sm_count) *sm_count = p.multiProcessorCount;
+  return MFEM_OK;
+}
+
+static int scene_prepare(const mfem_scene_desc* desc, std::unique_ptr<mfem_scene>& s) {
+  s.reset(new (std::nothrow) mfem_scene());
+  if (!s) return MFEM_ERR_OOM;
+  int rc = build_host_mesh(desc, s->M);
+  if (rc) return rc;
+  if (desc->precision != MFEM_PRECISION_FP64 && desc->precision != MFEM_PRECISION_MIXED)
+    return MFEM_ERR_INVALID;
+  if (desc->linear_solver != MFEM_SOLVER_EIGEN_CG_DIAG &&
+      desc->linear_solver != MFEM_SOLVER_GPU_PCG_BLOCK)
+    return MFEM_ERR_UNSUPPORTED;
+  if (desc->max_newton_iterations < 0 || desc->max_linesearch_iterations < 0 ||
+      desc->max_iterative_solver_iters < 0)
+    return MFEM_ERR_INVALID;
+  s->cfg = *desc;
+  // pointers in the copied descriptor are not kept
+  s->cfg.V_rest = s->cfg.V_init = s->cfg.v_init = nullptr;
+  s->cfg.tets = s->cfg.material = s->cfg.is_fixed = nullptr;
+  s->cfg.mu = s->cfg.lambda = s->cfg.density = nullptr;
+  s->fp64 = desc->precision == MFEM_PRECISION_FP64 ? 1 : 0;
+  s->rsz = s->fp64 ? 8 : 4;
+  s->ntp = (int)align_up((size_t)s->M.nt, 32);
+  static const double beta[7] = {0, 1.0, 2.0 / 3, 6.0 / 11, 12.0 / 25, 60.0 / 137, 60.0 / 147};
+  s->h = desc->dt;
+  s->dt = beta[desc->bdf_order] * desc->dt;
+  s->h2 = s->dt * s->dt;
+  s->nnzb = s->M.nnzb;
+  s->pin_pos.resize(3 * (size_t)s->M.npin);
+  for (int p = 0; p < s->M.npin; ++p)
+    for (int k = 0; k < 3; ++k) s->pin_pos[3 * p + k] = s->M.V0[3 * s->M.pin_vert[p] + k];
+  return MFEM_OK;
+}
+
+int mfem_gpu_scene_footprint(const mfem_scene_desc* desc, int64_t* bytes) {
+  if (!bytes) return MFEM_ERR_INVALID;
+  std::unique_ptr<mfem_scene> s;
+  int rc = scene_prepare(desc, s);
+  if (rc) return rc;
+  size_t b = 0;
+  scene_layout_bytes(s.get(), &b);
+  // plus the single-scene batch (tile tables, partials)
+  const size_t tiles = (size_t)(s->M.nt / kElemTile + 1) * 2 + s->M.nf / kRowTile + s->M.nf / kCgRows +
+                       s->M.nv / kVertTile + 8;
+  *bytes = (int64_t)(b + tiles * (sizeof(Tile) + kNumPartials * sizeof(double)) + 4096);
+  return MFEM_OK;
+}
+
+int mfem_gpu_scene_create(const mfem_scene_desc* desc, mfem_scene** out) {
+  if (!desc || !out) return MFEM_ERR_INVALID;
+  *out = nullptr;
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) return MFEM_ERR_NO_DEVICE;
+  std::call_once(g_configured, configure_kernels);
+  std::unique_ptr<mfem_scene> s;
+  int rc = scene_prepare(desc, s);
+  if (rc) return rc;
+  rc = scene_init_device(s.get());
+  if (rc) {
+    if (s->dmem) cudaFree(s->dmem);
+    return rc;
+  }
+  mfem_scene* raw = s.get();
+  rc = batch_build(&raw, 1, &s->solo);
+  if (rc) {
+    cudaFree(s->dmem);
+    return rc;
+  }
+  // s0 = polar(F0), R0 (MixedStretch::reset)
+  launch_elem_init(make_launch(s->solo, TB_ELEM));
+  CUDA_OR(cudaStreamSynchronize(s->solo->stream), MFEM_ERR_CUDA);
+  CUDA_OR(cudaGetLastError(), MFEM_ERR_CUDA);
+  *out = s.release();
+  return MFEM_OK;
+}
+
+int mfem_gpu_scene_destroy(mfem_scene* scene) {
+  if (!scene) return MFEM_ERR_INVALID;
+  batch_free(scene->solo);
+  if (scene->dmem) cudaFree(scene->dmem);
+  delete scene;
+  return MFEM_OK;
+}
+
+int mfem_gpu_scene_step(mfem_scene* scene, mfem_step_stats* stats) {
+  if (!scene) return MFEM_ERR_INVALID;
+  mfem_step_stats st{};
+  int rc = batch_step_impl(scene->solo, &st);
+  if (stats) *stats = st;
+  return rc;
+}
+
+int mfem_gpu_scene_sizes(const mfem_scene* scene, int32_t* nv, int32_t* nt, int32_t* nf) {
+  if (!scene) return MFEM_ERR_INVALID;
+  if (nv) *nv = scene->M.nv;
+  if (nt) *nt = scene->M.nt;
+  if (nf) *nf = scene->M.nf;
+  return MFEM_OK;
+}
+
+int mfem_gpu_scene_get_state(mfem_scene* s, double* x, double* v, double* sv, double* R,
+                             double* la) {
+  if (!s) return MFEM_ERR_INVALID;
+  cudaStream_t st = s->solo->stream;
+  CUDA_OR(cudaStreamSynchronize(st), MFEM_ERR_CUDA);
+  const HostMesh& M = s->M;
+  if (x)
+    CUDA_OR(cudaMemcpy(x, s->dev.x, sizeof(double) * 3 * M.nv, cudaMemcpyDeviceToHost), MFEM_ERR_CUDA);
+  if (v) {
+    SceneScalars sc;
+    CUDA_OR(cudaMemcpy(&sc, s->d_sc, sizeof(sc), cudaMemcpyDeviceToHost), MFEM_ERR_CUDA);
+    CUDA_OR(cudaMemcpy(v, s->dev.vhist + 3 * (size_t)M.nv * sc.hist_head, sizeof(double) * 3 * M.nv,
+                       cudaMemcpyDeviceToHost),
+            MFEM_ERR_CUDA);
+  }
+  if (sv) {
+    if (s->fp64) download_soa<double>(s->dev.s, M.nt, s->ntp, 6, sv, st);
+    else download_soa<float>(s->dev.s, M.nt, s->ntp, 6, sv, st);
+  }
+  if (la) {
+    if (s->fp64) download_soa<double>(s->dev.la, M.nt, s->ntp, 6, la, st);
+    else download_soa<float>(s->dev.la, M.nt, s->ntp, 6, la, st);
+  }
+  if (R) {
+    std::vector<double> q(4 * (size_t)M.nt);
+    if (s->fp64) download_soa<double>(s->dev.quat, M.nt, s->ntp, 4, q.data(), st);
+    else download_soa<float>(s->dev.quat, M.nt, s->ntp, 4, q.data(), st);
+    for (int e = 0; e < M.nt; ++e) quat_to_rot_h(&q[4 * (size_t)e], &R[9 * (size_t)e]);
+  }
+  return MFEM_OK;
+}
+
+int mfem_gpu_scene_set_state(mfem_scene* s, const double* x, const double* v, const double* sv,
+                             const double* R) {
+  if (!s) return MFEM_ERR_INVALID;
+  cudaStream_t st = s->solo->stream;
+  const HostMesh& M = s->M;
+  SceneScalars sc;
+  CUDA_OR(cudaMemcpy(&sc, s->d_sc, sizeof(sc), cudaMemcpyDeviceToHost), MFEM_ERR_CUDA);
+  if (x) {
+    CUDA_OR(cudaMemcpy(s->dev.x, x, sizeof(double) * 3 * M.nv, cudaMemcpyHostToDevice), MFEM_ERR_CUDA);
+    CUDA_OR(cudaMemcpy(s->dev.xhist + 3 * (size_t)M.nv * sc.hist_head, x, sizeof(double) * 3 * M.nv,
+                       cudaMemcpyHostToDevice),
+            MFEM_ERR_CUDA);
+    for (int p = 0; p < M.npin; ++p)
+      for (int k = 0; k < 3; ++k) s->pin_pos[3 * p + k] = x[3 * M.pin_vert[p] + k];
+    if (M.npin)
+      CUDA_OR(cudaMemcpy(s->d_pin_pos, s->pin_pos.data(), sizeof(double) * s->pin_pos.size(),
+                         cudaMemcpyHostToDevice),
+              MFEM_ERR_CUDA);
+  }
+  if (v)
+    CUDA_OR(cudaMemcpy(s->dev.vhist + 3 * (size_t)M.nv * sc.hist_head, v, sizeof(double) * 3 * M.nv,
+                       cudaMemcpyHostToDevice),
+            MFEM_ERR_CUDA);
+  if (sv) {
+    if (s->fp64) upload_soa<double>(s->dev.s, M.nt, s->ntp, 6, sv, st);
+    else upload_soa<float>(s->dev.s, M.nt, s->ntp, 6, sv, st);
+  }
+  if (R) {
+    std::vector<double> q(4 * (size_t)M.nt);
+    for (int e = 0; e < M.nt; ++e) rot_to_quat_h(&R[9 * (size_t)e], &q[4 * (size_t)e]);
+    if (s->fp64) upload_soa<double>(s->dev.quat, M.nt, s->ntp, 4, q.data(), st);
+    else upload_soa<float>(s->dev.quat, M.nt, s->ntp, 4, q.data(), st);
+  }
+  return MFEM_OK;
+}
+
+int mfem_gpu_scene_pinned(mfem_scene* s, int32_t* n_pinned, int32_t* vertices) {
+  if (!s) return MFEM_ERR_INVALID;
+  if (n_pinned) *n_pinned = s->M.npin;
+  if (vertices) std::memcpy(vertices, s->M.pin_vert.data(), sizeof(int) * s->M.npin);
+  return MFEM_OK;
+}
+
+int mfem_gpu_scene_set_pins(mfem_scene* s, const double* positions) {
+  if (!s || (!positions && s->M.npin)) return MFEM_ERR_INVALID;
+  if (s->M.npin == 0) return MFEM_OK;
+  std::memcpy(s->pin_pos.data(), positions, sizeof(double) * 3 * s->M.npin);
+  CUDA_OR(cudaMemcpyAsync(s->d_pin_pos, s->pin_pos.data(), sizeof(double) * 3 * s->M.npin,
+                          cudaMemcpyHostToDevice, s->solo->stream),
+          MFEM_ERR_CUDA);
+  s->pins_driven = true;
+  return MFEM_OK;
+}
+
+int mfem_gpu_scene_solo_batch(mfem_scene* s, mfem_batch** batch) {
+  if (!s || !batch) return MFEM_ERR_INVALID;
+  *batch = s->solo;
+  return MFEM_OK;
+}
+
+int mfem_gpu_batch_set_profiling(mfem_batch* b, int enable) {
+  if (!b) return MFEM_ERR_INVALID;
+  b->profiling = enable != 0;
+  for (int k = 0; k < MFEM_K_COUNT; ++k) {
+    b->k_ms[k] = 0;
+    b->k_launches[k] = 0;
+  }
+  return MFEM_OK;
+}
+
+int mfem_gpu_batch_kernel_stats(mfem_batch* b, int kernel, double* total_ms, int64_t* launches) {
+  if (!b || kernel < 0 || kernel >= MFEM_K_COUNT) return MFEM_ERR_INVALID;
+  if (total_ms) *total_ms = b->k_ms[kernel];
+  if (launches) *launches = b->k_launches[kernel];
+  return MFEM_OK;
+}
+
+int mfem_gpu_kernel_name(int kernel, char* name, int name_len) {
+  static const char* names[MFEM_K_COUNT] = {
+      "k_elem_update", "k_assemble", "k_cg_init", "k_cg_spmv", "k_cg_update", "k_local_solve",
+      "k_ls_energy", "k_apply", "k_step_begin", "k_step_end", "k_scalars_begin"};
+  if (kernel < 0 || kernel >= MFEM_K_COUNT || !name || name_len <= 0) return MFEM_ERR_INVALID;
+  strncpy(name, names[kernel], name_len - 1);
+  name[name_len - 1] = 0;
+  return MFEM_OK;
+}
+
+int mfem_gpu_batch_create(mfem_scene* const* scenes, int32_t n, mfem_batch** out) {
+  std::call_once(g_configured, configure_kernels);
+  return batch_build(scenes, n, out);
+}
+
+int mfem_gpu_batch_destroy(mfem_batch* batch) {
+  if (!batch) return MFEM_ERR_INVALID;
+  batch_free(batch);
+  return MFEM_OK;
+}
+
+int mfem_gpu_batch_step(mfem_batch* batch, mfem_step_stats* stats) {
+  if (!batch) return MFEM_ERR_INVALID;
+  return batch_step_impl(batch, stats);
+}
+
+int mfem_gpu_scene_elem_update(mfem_scene* s, const double* x, double h, double* R, double* S,
+                               double* dSdF, double* g, double* H, double* Hinv, double* Aloc,
+                               double* gl) {
+  if (!s || !x) return MFEM_ERR_INVALID;
+  mfem_batch* b = s->solo;
+  const int nt = s->M.nt;
+  CUDA_OR(cudaMemcpy(s->dev.x, x, sizeof(double) * 3 * s->M.nv, cudaMemcpyHostToDevice), MFEM_ERR_CUDA);
+  // run K1 with h^2 = h*h and FP64 debug outputs
+  SceneDev D = b->h_sds[0];
+  D.h2 = h * h;
+  CUDA_OR(cudaMemcpy(b->d_sds, &D, sizeof(D), cudaMemcpyHostToDevice), MFEM_ERR_CUDA);
+  const size_t per = 9 + 6 + 54 + 6 + 36 + 36 + 144 + 6;
+  double* dbuf = nullptr;
+  CUDA_OR(cudaMalloc(&dbuf, sizeof(double) * per * nt), MFEM_ERR_OOM);
+  ElemDebug dbg;
+  double* p = dbuf;
+  dbg.R = p; p += 9 * (size_t)nt;
+  dbg.S = p; p += 6 * (size_t)nt;
+  dbg.dSdF = p; p += 54 * (size_t)nt;
+  dbg.g = p; p += 6 * (size_t)nt;
+  dbg.H = p; p += 36 * (size_t)nt;
+  dbg.Hinv = nullptr; p += 36 * (size_t)nt;
+  dbg.Aloc = p; p += 144 * (size_t)nt;
+  dbg.gl = p;
+  launch_scalars_begin(make_launch(b, TB_EV), 1);
+  launch_elem_update(make_launch(b, TB_ELEM), &dbg);
+  cudaError_t e1 = cudaStreamSynchronize(b->stream);
+  cudaError_t e2 = cudaGetLastError();
+  std::vector<double> host(per * (size_t)nt);
+  cudaMemcpy(host.data(), dbuf, sizeof(double) * host.size(), cudaMemcpyDeviceToHost);
+  cudaFree(dbuf);
+  cudaMemcpy(b->d_sds, &b->h_sds[0], sizeof(SceneDev), cudaMemcpyHostToDevice);
+  if (e1 != cudaSuccess || e2 != cudaSuccess) {
+    set_error("elem_update", e1 != cudaSuccess ? e1 : e2);
+    return MFEM_ERR_CUDA;
+  }
+  const double* q = host.data();
+  auto out = [&](double* dst, size_t n) {
+    if (dst) std::memcpy(dst, q, sizeof(double) * n);
+    q += n;
+  };
+  out(R, 9 * (size_t)nt);
+  out(S, 6 * (size_t)nt);
+  out(dSdF, 54 * (size_t)nt);
+  out(g, 6 * (size_t)nt);
+  const double* Hsrc = q;
+  out(H, 36 * (size_t)nt);
+  q += 36 * (size_t)nt;  // the Hinv slot is filled on the host below
+  if (Hinv)
+    for (int e = 0; e < nt; ++e) inverse6_host(Hsrc + 36 * (size_t)e, Hinv + 36 * (size_t)e);
+  out(Aloc, 144 * (size_t)nt);
+  out(gl, 6 * (size_t)nt);
+  return MFEM_OK;
+}
+
+int mfem_gpu_scene_bcsr_sizes(mfem_scene* s, int32_t* nf, int32_t* nnzb) {
+  if (!s) return MFEM_ERR_INVALID;
+  if (nf) *nf = s->M.nf;
+  if (nnzb) *nnzb = s->M.nnzb;
+  return MFEM_OK;
+}
+
+// Assembles LHS and RHS at the current state (update_system + pre_solve).
+int mfem_gpu_scene_get_system(mfem_scene* s, int32_t* row_ptr, int32_t* col, double* val,
+                              double* rhs) {
+  if (!s) return MFEM_ERR_INVALID;
+  mfem_batch* b = s->solo;
+  launch_scalars_begin(make_launch(b, TB_EV), 1);
+  launch_step_begin(make_launch(b, TB_EV));
+  launch_elem_update(make_launch(b, TB_ELEM), nullptr);
+  launch_assemble(make_launch(b, TB_ROW));
+  CUDA_OR(cudaStreamSynchronize(b->stream), MFEM_ERR_CUDA);
+  CUDA_OR(cudaGetLastError(), MFEM_ERR_CUDA);
+  const HostMesh& M = s->M;
+  if (row_ptr) std::memcpy(row_ptr, M.b_ptr.data(), sizeof(int) * M.b_ptr.size());
+  if (col) std::memcpy(col, M.b_col.data(), sizeof(int) * M.b_col.size());
+  auto fetch = [&](const void* src, size_t n, double* dst) -> int {
+    if (!dst) return MFEM_OK;
+    if (s->fp64) {
+      CUDA_OR(cudaMemcpy(dst, src, n * 8, cudaMemcpyDeviceToHost), MFEM_ERR_CUDA);
+    } else {
+      std::vector<float> t(n);
+      CUDA_OR(cudaMemcpy(t.data(), src, n * 4, cudaMemcpyDeviceToHost), MFEM_ERR_CUDA);
+      for (size_t i = 0; i < n; ++i) dst[i] = t[i];
+    }
+    return MFEM_OK;
+  };
+  int rc = fetch(s->dev.b_val, 9 * (size_t)M.nnzb, val);
+  if (!rc) rc = fetch(s->dev.rhs, 3 * (size_t)M.nf, rhs);
+  return rc;
+}
+
+int mfem_gpu_scene_pcg(mfem_scene* s, const double* bvec, double* dx, int32_t* iterations,
+                       double* rel_residual) {
+  if (!s || !bvec || !dx) return MFEM_ERR_INVALID;
+  mfem_batch* b = s->solo;
+  const size_t n3 = 3 * (size_t)s->M.nf;
+  if (s->fp64) {
+    CUDA_OR(cudaMemcpy(s->dev.rhs, bvec, n3 * 8, cudaMemcpyHostToDevice), MFEM_ERR_CUDA);
+  } else {
+    std::vector<float> t(bvec, bvec + n3);
+    CUDA_OR(cudaMemcpy(s->dev.rhs, t.data(), n3 * 4, cudaMemcpyHostToDevice), MFEM_ERR_CUDA);
+  }
+  launch_scalars_begin(make_launch(b, TB_EV), 1);
+  Launch Lcg = make_launch(b, TB_CG);
+  launch_cg_init(Lcg);
+  int done = 0;
+  while (done < b->max_cg) {
+    const int c = std::min(8, b->max_cg - done);
+    for (int k = 0; k < c; ++k) {
+      launch_cg_spmv(Lcg);
+      launch_cg_update(Lcg);
+    }
+    done += c;
+    int rc = sync_counters(b);
+    if (rc) return rc;
+    if (b->h_ctr->cg_active == 0) break;
+  }
+  CUDA_OR(cudaStreamSynchronize(b->stream), MFEM_ERR_CUDA);
+  CUDA_OR(cudaGetLastError(), MFEM_ERR_CUDA);
+  if (s->fp64) {
+    CUDA_OR(cudaMemcpy(dx, s->dev.cg_x, n3 * 8, cudaMemcpyDeviceToHost), MFEM_ERR_CUDA);
+  } else {
+    std::vector<float> t(n3);
+    CUDA_OR(cudaMemcpy(t.data(), s->dev.cg_x, n3 * 4, cudaMemcpyDeviceToHost), MFEM_ERR_CUDA);
+    for (size_t i = 0; i < n3; ++i) dx[i] = t[i];
+  }
+  SceneScalars sc;
+  CUDA_OR(cudaMemcpy(&sc, s->d_sc, sizeof(sc), cudaMemcpyDeviceToHost), MFEM_ERR_CUDA);
+  if (iterations) *iterations = sc.cg_total;
+  if (rel_residual) *rel_residual = sc.cg_err;
+  return sc.cg_status;
+}
+
+}  // extern "C"

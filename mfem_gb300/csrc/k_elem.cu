@@ -1,0 +1,732 @@
+// Element-parallel kernels of the mixed-stretch Newton step.
+//
+//   k_elem_init     s0 = polar(F0)                    mixed_stretch.cpp:287-303
+//   k_elem_update   K1: F = J x, polar R (warm start), S, ds/dF, h^2 psi'/psi''
+//                   (psd-fixed), the 12x12 element block and the element's
+//                   right-hand-side share            mixed_stretch.cpp:133-226
+//   k_local_solve   K5: ds, lambda and E(0)          mixed_stretch.cpp:243-259,
+//                                                     newton_optimizer.cpp:34-52
+//   k_ls_energy     K6: E(alpha) for the backtracking line search
+//                                                     linesearch.h:80-129
+//   k_apply         x += alpha dx, s += alpha ds       linesearch.h:120-125
+//   k_step_begin/end  BDF x_tilde, BDF update, pins, lambda = 0
+//                                                     BDF.cpp:6-27, displacement.cpp:32-50
+//
+// One thread per element.  Element arrays are structure-of-arrays with
+// stride ntp; the element record written by K1 (upper 12x12 blocks + rhs
+// share) is staged in shared memory and stored contiguously.
+#include <cfloat>
+
+#include "device_math.cuh"
+#include "kernels.cuh"
+#include "reduce.cuh"
+
+namespace mfem_gpu {
+
+namespace {
+
+constexpr double kPsdTol = 1e-6;       // simple_psd_fix tolerance
+constexpr double kProcrustesTol = 1e-6;  // mixed_stretch.cpp:21-22
+constexpr int kProcrustesIters = 100;
+
+template <typename Real> struct ElemIn {
+  int4 tv;
+  Real dp[9];  // dphi_k/dX for k = 1..3: dp[3(k-1)+c]
+  Real vol, mu, lam;
+  int mat;
+};
+
+template <typename Real>
+__device__ __forceinline__ void load_elem(const SceneDev& sd, int e, ElemIn<Real>& in) {
+  const Real* dphi = static_cast<const Real*>(sd.dphi);
+  const int ntp = sd.ntp;
+  in.tv = sd.tets[e];
+#pragma unroll
+  for (int i = 0; i < 9; ++i) in.dp[i] = dphi[i * ntp + e];
+  in.vol = static_cast<const Real*>(sd.vol)[e];
+  in.mu = static_cast<const Real*>(sd.mu)[e];
+  in.lam = static_cast<const Real*>(sd.lam)[e];
+  in.mat = sd.material_uniform >= 0 ? sd.material_uniform : int(sd.mat[e]);
+}
+
+// F = sum_k (x_k - x_0) (x) dphi_k with the edge vectors formed in FP64
+// (TetrahedralMesh::deformation_gradient, tet_mesh.cpp:77-80).
+template <typename Real>
+__device__ __forceinline__ void deformation_gradient(const double* x, const double* dx,
+                                                     double alpha, const int* free_map,
+                                                     const ElemIn<Real>& in, Real* F) {
+  const int v[4] = {in.tv.x, in.tv.y, in.tv.z, in.tv.w};
+  double p[4][3];
+#pragma unroll
+  for (int k = 0; k < 4; ++k)
+#pragma unroll
+    for (int d = 0; d < 3; ++d) p[k][d] = x[3 * v[k] + d];
+  if (dx != nullptr) {
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+      int f = free_map[v[k]];
+      if (f >= 0) {
+#pragma unroll
+        for (int d = 0; d < 3; ++d) p[k][d] += alpha * dx[3 * f + d];
+      }
+    }
+  }
+  Real ed[9];
+#pragma unroll
+  for (int k = 1; k < 4; ++k)
+#pragma unroll
+    for (int r = 0; r < 3; ++r) ed[3 * (k - 1) + r] = Real(p[k][r] - p[0][r]);
+#pragma unroll
+  for (int c = 0; c < 3; ++c)
+#pragma unroll
+    for (int r = 0; r < 3; ++r)
+      F[r + 3 * c] = ed[r] * in.dp[c] + ed[3 + r] * in.dp[3 + c] + ed[6 + r] * in.dp[6 + c];
+}
+
+template <typename Real>
+__device__ __forceinline__ void load_quat(const SceneDev& sd, int e, Real* R) {
+  const Real* q = static_cast<const Real*>(sd.quat);
+  Real qq[4] = {q[e], q[sd.ntp + e], q[2 * sd.ntp + e], q[3 * sd.ntp + e]};
+  quat_to_rot(qq, R);
+}
+
+template <typename Real>
+__device__ __forceinline__ void store_quat(const SceneDev& sd, int e, const Real* R) {
+  Real* q = static_cast<Real*>(sd.quat);
+  Real qq[4];
+  rot_to_quat(R, qq);
+#pragma unroll
+  for (int i = 0; i < 4; ++i) q[i * sd.ntp + e] = qq[i];
+}
+
+template <typename Real>
+__device__ __forceinline__ void load6(const void* base, int ntp, int e, Real* v) {
+  const Real* p = static_cast<const Real*>(base);
+#pragma unroll
+  for (int i = 0; i < 6; ++i) v[i] = p[i * ntp + e];
+}
+template <typename Real>
+__device__ __forceinline__ void store6(void* base, int ntp, int e, const Real* v) {
+  Real* p = static_cast<Real*>(base);
+#pragma unroll
+  for (int i = 0; i < 6; ++i) p[i * ntp + e] = v[i];
+}
+
+// h^2 * gradient and psd-fixed h^2 * Hessian of psi at s.
+template <typename Real>
+__device__ __forceinline__ void material_gH(const ElemIn<Real>& in, const Real* s, Real h2,
+                                            Real* g, Real* H) {
+  bool psd = material_grad_hess<Real>(in.mat, in.mu, in.lam, s, g, H);
+  if (psd) psd_fix(H, Real(kPsdTol));
+#pragma unroll
+  for (int i = 0; i < 6; ++i) g[i] *= h2;
+#pragma unroll
+  for (int i = 0; i < 36; ++i) H[i] *= h2;
+}
+
+// Offset of entry (l, m) of block (a, b) in the element record: upper
+// blocks row-major, diagonal blocks as (xx, xy, xz, yy, yz, zz).
+__host__ __device__ constexpr int rec_block_start(int a) {
+  return a == 0 ? 0 : (a == 1 ? 33 : (a == 2 ? 57 : 72));
+}
+__host__ __device__ constexpr int sym_idx(int r, int c) {
+  return r == 0 ? c : (r == 1 ? 2 + c : 5);
+}
+
+// ------------------------------------------------------------------ K0 ---
+template <typename Real>
+__global__ void __launch_bounds__(kElemTile) k_elem_init(const Tile* tiles, const SceneDev* sds) {
+  const Tile t = tiles[blockIdx.x];
+  const SceneDev& sd = sds[t.scene];
+  const int e = t.begin + threadIdx.x;
+  if (e >= t.end) return;
+  ElemIn<Real> in;
+  load_elem(sd, e, in);
+  Real F[9], R[9];
+  deformation_gradient<Real>(sd.x, nullptr, 0.0, sd.free_map, in, F);
+#pragma unroll
+  for (int i = 0; i < 9; ++i) R[i] = (i % 4 == 0) ? Real(1) : Real(0);
+  int it = procrustes<Real>(R, F, Real(kProcrustesTol), kProcrustesIters);
+  if (it < 0) atomicAdd(&sd.sc->procrustes_fail, 1);
+  Real S6[6];
+  stretch_vec(R, F, S6);
+  store_quat(sd, e, R);
+  store6(sd.s, sd.ntp, e, S6);
+  store6(sd.S, sd.ntp, e, S6);
+  Real z[6] = {0, 0, 0, 0, 0, 0};
+  store6(sd.la, sd.ntp, e, z);
+  store6(sd.ds, sd.ntp, e, z);
+}
+
+// ------------------------------------------------------------------ K1 ---
+template <typename Real, bool DBG>
+__global__ void __launch_bounds__(kElemTile)
+    k_elem_update(const Tile* tiles, const SceneDev* sds, ElemDebug dbg) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  Real* buf = reinterpret_cast<Real*>(smem_raw);
+  const Tile t = tiles[blockIdx.x];
+  const SceneDev& sd = sds[t.scene];
+  if (!sd.sc->newton_active) return;
+  const int e = t.begin + threadIdx.x;
+  const Real h2 = Real(sd.h2);
+  if (e < t.end) {
+    Real* out = buf + threadIdx.x * kRecSmem;
+    ElemIn<Real> in;
+    load_elem(sd, e, in);
+    Real sv[6];
+    load6(sd.s, sd.ntp, e, sv);
+    // material derivatives at s: g = h^2 grad psi, H = h^2 hess psi (psd-fixed)
+    Real g[6], H[36];
+    material_gH(in, sv, h2, g, H);
+    // polar rotation from the previous rotation (update_rotations)
+    Real F[9], R[9];
+    deformation_gradient<Real>(sd.x, nullptr, 0.0, sd.free_map, in, F);
+    load_quat(sd, e, R);
+    int it = procrustes<Real>(R, F, Real(kProcrustesTol), kProcrustesIters);
+    Real S6[6];
+    stretch_vec(R, F, S6);
+    Real u[18];
+    bool ok = stretch_derivative_u(S6, u);
+    if (it < 0 || !ok) atomicAdd(&sd.sc->procrustes_fail, 1);
+    store_quat(sd, e, R);
+    store6(sd.S, sd.ntp, e, S6);
+    // B[i][a][l] = ds_i / dx_{a,l} = (G_i dphi_a)_l
+    Real B[72];
+    {
+      Real G[54];
+      ds_dF(R, u, G);
+      Real dph[12];
+#pragma unroll
+      for (int c = 0; c < 3; ++c) {
+        dph[3 + c] = in.dp[c];
+        dph[6 + c] = in.dp[3 + c];
+        dph[9 + c] = in.dp[6 + c];
+        dph[c] = -(in.dp[c] + in.dp[3 + c] + in.dp[6 + c]);
+      }
+#pragma unroll
+      for (int i = 0; i < 6; ++i)
+#pragma unroll
+        for (int a = 0; a < 4; ++a)
+#pragma unroll
+          for (int l = 0; l < 3; ++l)
+            B[12 * i + 3 * a + l] = G[9 * i + l] * dph[3 * a] + G[9 * i + l + 3] * dph[3 * a + 1] +
+                                    G[9 * i + l + 6] * dph[3 * a + 2];
+      if (DBG) {
+        const double sym[6] = {1, 1, 1, 2, 2, 2};
+        for (int i = 0; i < 6; ++i)
+          for (int r = 0; r < 9; ++r) dbg.dSdF[54 * (size_t)e + r + 9 * i] = sym[i] * double(G[9 * i + r]);
+      }
+    }
+    // q = H (S - s) + g ;  gl = Syminv q  (MixedStretch::rhs, mixed_stretch.cpp:219-220)
+    Real qv[6];
+    {
+      Real d[6];
+#pragma unroll
+      for (int i = 0; i < 6; ++i) d[i] = S6[i] - sv[i];
+#pragma unroll
+      for (int i = 0; i < 6; ++i) {
+        Real acc = g[i];
+#pragma unroll
+        for (int j = 0; j < 6; ++j) acc += H[i + 6 * j] * d[j];
+        qv[i] = acc;
+      }
+    }
+    // right-hand-side share of vertex a: -vol * sum_i q_i B[i][a]
+#pragma unroll
+    for (int a = 0; a < 4; ++a)
+#pragma unroll
+      for (int l = 0; l < 3; ++l) {
+        Real acc = 0;
+#pragma unroll
+        for (int i = 0; i < 6; ++i) acc += qv[i] * B[12 * i + 3 * a + l];
+        out[78 + 3 * a + l] = -in.vol * acc;
+      }
+    // upper 3x3 blocks of Aloc = vol * B^T H B  (mixed_stretch.cpp:174-175)
+#pragma unroll
+    for (int b = 0; b < 4; ++b) {
+      Real HB[18];
+#pragma unroll
+      for (int i = 0; i < 6; ++i)
+#pragma unroll
+        for (int m = 0; m < 3; ++m) {
+          Real acc = 0;
+#pragma unroll
+          for (int j = 0; j < 6; ++j) acc += H[i + 6 * j] * B[12 * j + 3 * b + m];
+          HB[3 * i + m] = acc;
+        }
+#pragma unroll
+      for (int a = 0; a <= b; ++a) {
+        const int base = rec_block_start(a) + (a == b ? 0 : 6 + 9 * (b - a - 1));
+#pragma unroll
+        for (int l = 0; l < 3; ++l)
+#pragma unroll
+          for (int m = 0; m < 3; ++m) {
+            if (a == b && m < l) continue;
+            Real acc = 0;
+#pragma unroll
+            for (int i = 0; i < 6; ++i) acc += B[12 * i + 3 * a + l] * HB[3 * i + m];
+            out[base + (a == b ? sym_idx(l, m) : 3 * l + m)] = in.vol * acc;
+          }
+      }
+    }
+    out[90] = Real(0);
+    out[91] = Real(0);
+    if (DBG) {
+      const size_t E = e;
+      for (int i = 0; i < 9; ++i) dbg.R[9 * E + i] = R[i];
+      for (int i = 0; i < 6; ++i) {
+        dbg.S[6 * E + i] = S6[i];
+        dbg.g[6 * E + i] = g[i];
+        dbg.gl[6 * E + i] = (i < 3 ? 1.0 : 0.5) * double(qv[i]);
+      }
+      for (int i = 0; i < 36; ++i) dbg.H[36 * E + i] = H[i];
+      for (int a = 0; a < 4; ++a)
+        for (int b = 0; b < 4; ++b)
+          for (int l = 0; l < 3; ++l)
+            for (int m = 0; m < 3; ++m) {
+              int aa = a, bb = b, ll = l, mm = m;
+              if (a > b) { aa = b; bb = a; ll = m; mm = l; }
+              int base = rec_block_start(aa) + (aa == bb ? 0 : 6 + 9 * (bb - aa - 1));
+              int off = (aa == bb) ? sym_idx(ll < mm ? ll : mm, ll < mm ? mm : ll) : 3 * ll + mm;
+              dbg.Aloc[144 * E + (3 * a + l) + 12 * (3 * b + m)] = out[base + off];
+            }
+    }
+  }
+  __syncthreads();
+  // contiguous store of the tile's records
+  const int n = t.end - t.begin;
+  Real* dst = static_cast<Real*>(sd.rec) + (size_t)t.begin * kRec;
+  for (int i = threadIdx.x; i < n * kRec; i += blockDim.x) {
+    int el = i / kRec;
+    dst[i] = buf[el * kRecSmem + (i - el * kRec)];
+  }
+}
+
+// ------------------------------------------------------------------ K5 ---
+// ds = S - s + dS/dF : dF(dx)  (the closed form of -H^{-1}(Sym la + g)),
+// la = -Syminv (H ds + g); also E(0) and max |ds|, max |dx|.
+template <typename Real>
+__global__ void __launch_bounds__(kElemTile) k_local_solve(const Tile* tiles, const SceneDev* sds,
+                                                           double* partials, BatchCounters* ctrs) {
+  const int tix = blockIdx.x;
+  const Tile t = tiles[tix];
+  const SceneDev& sd = sds[t.scene];
+  SceneScalars* sc = sd.sc;
+  if (!sc->newton_active) return;
+  const Real h2 = Real(sd.h2);
+  const Real* cgx = static_cast<const Real*>(sd.cg_x);
+  KSum en{0.0, 0.0};
+  double mx[2] = {0.0, 0.0};
+  double eabs[1] = {0.0};
+  const int idx = t.begin + threadIdx.x;
+  if (t.kind == 0) {
+    if (idx < t.end) {
+      const int e = idx;
+      ElemIn<Real> in;
+      load_elem(sd, e, in);
+      Real R[9], S6[6], sv[6];
+      load_quat(sd, e, R);
+      load6(sd.S, sd.ntp, e, S6);
+      load6(sd.s, sd.ntp, e, sv);
+      // dF = sum_k (dx_k - dx_0) (x) dphi_k
+      const int v[4] = {in.tv.x, in.tv.y, in.tv.z, in.tv.w};
+      Real d[4][3];
+#pragma unroll
+      for (int k = 0; k < 4; ++k) {
+        int f = sd.free_map[v[k]];
+#pragma unroll
+        for (int c = 0; c < 3; ++c) d[k][c] = f >= 0 ? cgx[3 * f + c] : Real(0);
+      }
+      Real dF[9];
+#pragma unroll
+      for (int c = 0; c < 3; ++c)
+#pragma unroll
+        for (int r = 0; r < 3; ++r)
+          dF[r + 3 * c] = (d[1][r] - d[0][r]) * in.dp[c] + (d[2][r] - d[0][r]) * in.dp[3 + c] +
+                          (d[3][r] - d[0][r]) * in.dp[6 + c];
+      Real dFh[9];
+      mulAtB(R, dF, dFh);
+      Real u[18], delta[6];
+      stretch_derivative_u(S6, u);
+      ds_dot(u, dFh, delta);
+      Real ds[6];
+#pragma unroll
+      for (int i = 0; i < 6; ++i) ds[i] = S6[i] - sv[i] + delta[i];
+      Real g[36 / 6], H[36];
+      material_gH(in, sv, h2, g, H);
+      Real la[6];
+#pragma unroll
+      for (int i = 0; i < 6; ++i) {
+        Real acc = g[i];
+#pragma unroll
+        for (int j = 0; j < 6; ++j) acc += H[i + 6 * j] * ds[j];
+        la[i] = -(i < 3 ? Real(1) : Real(0.5)) * acc;
+      }
+      store6(sd.ds, sd.ntp, e, ds);
+      store6(sd.la, sd.ntp, e, la);
+      // E(0): h^2 vol psi(s) - vol la . Sym (S - s)
+      Real psi = material_psi<Real>(in.mat, in.mu, in.lam, sv);
+      double con = 0;
+#pragma unroll
+      for (int i = 0; i < 6; ++i) con += double(la[i]) * (i < 3 ? 1.0 : 2.0) * double(S6[i] - sv[i]);
+      en.add(double(h2) * double(in.vol) * double(psi));
+      en.add(-double(in.vol) * con);
+      eabs[0] = fabs(double(h2) * double(in.vol) * double(psi)) + fabs(double(in.vol) * con);
+      Real m = 0;
+#pragma unroll
+      for (int i = 0; i < 6; ++i) m = fmax(m, fabs(ds[i]));
+      mx[0] = m;
+    }
+  } else {
+    if (idx < t.end) {
+      const int a = idx;
+      const double* x = sd.x;
+      const double* xt = sd.xt;
+      double Md[3] = {0, 0, 0};
+      for (int q = sd.m_ptr[a]; q < sd.m_ptr[a + 1]; ++q) {
+        const int b = sd.m_col[q];
+        const double m = sd.m_val[q];
+#pragma unroll
+        for (int c = 0; c < 3; ++c) Md[c] += m * (x[3 * b + c] - xt[3 * b + c]);
+      }
+      double e2 = 0;
+#pragma unroll
+      for (int c = 0; c < 3; ++c) e2 += (x[3 * a + c] - xt[3 * a + c]) * Md[c];
+      en.add(0.5 * e2);
+      const int f = sd.free_map[a];
+      if (f >= 0) {
+        double m = 0;
+#pragma unroll
+        for (int c = 0; c < 3; ++c) m = fmax(m, fabs(double(cgx[3 * f + c])));
+        mx[1] = m;
+      }
+    }
+  }
+  double* part = partials + (size_t)tix * kNumPartials;
+  block_ksum(en, part);
+  block_partial<2>(mx, 0, part + 2);
+  block_partial<1>(eabs, 1, part + 4);
+  if (last_tile(&sc->ctr[TB_EV], sd.tile_count[TB_EV])) {
+    if (threadIdx.x == 0) {
+      KSum E{0.0, 0.0};
+      double mds = 0, mdx = 0, eab = 0;
+      const int t0 = sd.tile_first[TB_EV];
+      for (int k = 0; k < sd.tile_count[TB_EV]; ++k) {
+        const double* p = partials + (size_t)(t0 + k) * kNumPartials;
+        E.merge(KSum{ld_partial(p), ld_partial(p + 1)});
+        mds = fmax(mds, ld_partial(p + 2));
+        mdx = fmax(mdx, ld_partial(p + 3));
+        eab += ld_partial(p + 4);
+      }
+      const double Ev = E.value();
+      sc->E_abs = eab;
+      sc->E = Ev;
+      sc->eres = fabs((Ev - sc->E_prev) / (Ev + 1e-6));
+      sc->E_prev = Ev;
+      sc->fx0 = Ev;
+      sc->max_ds = mds;
+      sc->max_dx = mdx;
+      sc->decrement = fmax(mdx, mds);
+      sc->alpha_ls = 1.0;
+      sc->ls_iter = 0;
+      sc->ls_ok = 0;
+      if (sd.max_ls > 0) {
+        sc->ls_active = 1;
+        atomicAdd(&ctrs->ls_active, 1);
+      } else {
+        sc->ls_active = 0;
+      }
+    }
+  }
+}
+
+// ------------------------------------------------------------------ K6 ---
+template <typename Real>
+__global__ void __launch_bounds__(kElemTile) k_ls_energy(const Tile* tiles, const SceneDev* sds,
+                                                         double* partials, BatchCounters* ctrs) {
+  const int tix = blockIdx.x;
+  const Tile t = tiles[tix];
+  const SceneDev& sd = sds[t.scene];
+  SceneScalars* sc = sd.sc;
+  if (!sc->ls_active) return;
+  const double alpha = sc->alpha_ls;
+  const Real h2 = Real(sd.h2);
+  const Real* cgx = static_cast<const Real*>(sd.cg_x);
+  KSum en{0.0, 0.0};
+  double eabs[1] = {0.0};
+  const int idx = t.begin + threadIdx.x;
+  if (t.kind == 0) {
+    if (idx < t.end) {
+      const int e = idx;
+      ElemIn<Real> in;
+      load_elem(sd, e, in);
+      Real F[9], R[9];
+      // x0 = x + alpha dx  (energy_func, newton_optimizer.cpp:37)
+      {
+        const int v[4] = {in.tv.x, in.tv.y, in.tv.z, in.tv.w};
+        double p[4][3];
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+          const int f = sd.free_map[v[k]];
+#pragma unroll
+          for (int c = 0; c < 3; ++c)
+            p[k][c] = sd.x[3 * v[k] + c] + (f >= 0 ? alpha * double(cgx[3 * f + c]) : 0.0);
+        }
+        Real ed[9];
+#pragma unroll
+        for (int k = 1; k < 4; ++k)
+#pragma unroll
+          for (int r = 0; r < 3; ++r) ed[3 * (k - 1) + r] = Real(p[k][r] - p[0][r]);
+#pragma unroll
+        for (int c = 0; c < 3; ++c)
+#pragma unroll
+          for (int r = 0; r < 3; ++r)
+            F[r + 3 * c] = ed[r] * in.dp[c] + ed[3 + r] * in.dp[3 + c] + ed[6 + r] * in.dp[6 + c];
+      }
+      load_quat(sd, e, R);
+      procrustes<Real>(R, F, Real(kProcrustesTol), kProcrustesIters);
+      Real St[6];
+      stretch_vec(R, F, St);
+      Real sv[6], dsv[6], la[6], si[6];
+      load6(sd.s, sd.ntp, e, sv);
+      load6(sd.ds, sd.ntp, e, dsv);
+      load6(sd.la, sd.ntp, e, la);
+#pragma unroll
+      for (int i = 0; i < 6; ++i) si[i] = Real(double(sv[i]) + alpha * double(dsv[i]));
+      Real psi = material_psi<Real>(in.mat, in.mu, in.lam, si);
+      double con = 0;
+#pragma unroll
+      for (int i = 0; i < 6; ++i) con += double(la[i]) * (i < 3 ? 1.0 : 2.0) * double(St[i] - si[i]);
+      en.add(double(h2) * double(in.vol) * double(psi));
+      en.add(-double(in.vol) * con);
+      eabs[0] = fabs(double(h2) * double(in.vol) * double(psi)) + fabs(double(in.vol) * con);
+    }
+  } else {
+    if (idx < t.end) {
+      const int a = idx;
+      const double* x = sd.x;
+      const double* xt = sd.xt;
+      double Md[3] = {0, 0, 0};
+      for (int q = sd.m_ptr[a]; q < sd.m_ptr[a + 1]; ++q) {
+        const int b = sd.m_col[q];
+        const double m = sd.m_val[q];
+        const int fb = sd.free_map[b];
+#pragma unroll
+        for (int c = 0; c < 3; ++c)
+          Md[c] += m * (x[3 * b + c] + (fb >= 0 ? alpha * double(cgx[3 * fb + c]) : 0.0) - xt[3 * b + c]);
+      }
+      const int fa = sd.free_map[a];
+      double e2 = 0;
+#pragma unroll
+      for (int c = 0; c < 3; ++c)
+        e2 += (x[3 * a + c] + (fa >= 0 ? alpha * double(cgx[3 * fa + c]) : 0.0) - xt[3 * a + c]) * Md[c];
+      en.add(0.5 * e2);
+    }
+  }
+  double* part = partials + (size_t)tix * kNumPartials;
+  block_ksum(en, part);
+  block_partial<1>(eabs, 1, part + 2);
+  if (last_tile(&sc->ctr[TB_EV], sd.tile_count[TB_EV])) {
+    if (threadIdx.x == 0) {
+      KSum E{0.0, 0.0};
+      double eab = 0;
+      const int t0 = sd.tile_first[TB_EV];
+      for (int k = 0; k < sd.tile_count[TB_EV]; ++k) {
+        const double* p = partials + (size_t)(t0 + k) * kNumPartials;
+        E.merge(KSum{ld_partial(p), ld_partial(p + 1)});
+        eab += ld_partial(p + 2);
+      }
+      const double fx = E.value();
+      sc->E_trial = fx;
+      // Armijo with c = 0 (newton_optimizer.cpp:58).  With FP32 element
+      // energies a difference below their rounding bound is not a decision
+      // the arithmetic can make; such a step is accepted.
+      const double noise = sd.fp64 ? 0.0 : 8.0 * 1.1920929e-7 * (eab + sc->E_abs);
+      if (fx < sc->fx0 + noise) {
+        sc->ls_active = 0;
+        sc->ls_ok = 1;
+        atomicSub(&ctrs->ls_active, 1);
+      } else {
+        sc->alpha_ls *= 0.5;
+        sc->ls_iter += 1;
+        if (sc->ls_iter >= sd.max_ls) {
+          sc->ls_active = 0;
+          sc->ls_ok = 0;
+          atomicSub(&ctrs->ls_active, 1);
+        }
+      }
+    }
+  }
+}
+
+// ---------------------------------------------------------------- apply ---
+template <typename Real>
+__global__ void __launch_bounds__(kElemTile) k_apply(const Tile* tiles, const SceneDev* sds,
+                                                     double* partials, BatchCounters* ctrs) {
+  const int tix = blockIdx.x;
+  const Tile t = tiles[tix];
+  const SceneDev& sd = sds[t.scene];
+  SceneScalars* sc = sd.sc;
+  if (!sc->newton_active) return;
+  const int idx = t.begin + threadIdx.x;
+  if (sc->ls_ok && idx < t.end) {
+    const double alpha = sc->alpha_ls;
+    if (t.kind == 0) {
+      Real* s = static_cast<Real*>(sd.s);
+      const Real* ds = static_cast<const Real*>(sd.ds);
+#pragma unroll
+      for (int i = 0; i < 6; ++i) {
+        const size_t k = (size_t)i * sd.ntp + idx;
+        s[k] = Real(double(s[k]) + alpha * double(ds[k]));
+      }
+    } else {
+      const int f = sd.free_map[idx];
+      if (f >= 0) {
+        const Real* cgx = static_cast<const Real*>(sd.cg_x);
+#pragma unroll
+        for (int c = 0; c < 3; ++c) sd.x[3 * idx + c] += alpha * double(cgx[3 * f + c]);
+      }
+    }
+  }
+  if (last_tile(&sc->ctr[TB_EV], sd.tile_count[TB_EV])) {
+    if (threadIdx.x == 0) {
+      sc->ls_total += sc->ls_iter;
+      if (!sc->ls_ok && sc->status == 0) sc->status = 6;  // MFEM_ERR_LS_FAILED
+      sc->newton_iter += 1;
+      // In FP32 the energy-change test measures rounding, not convergence;
+      // with a residual tolerance set, the mixed path stops on the residual.
+      const bool eres_ok = (!sd.fp64 && sd.res_tol > 0) ? true : sc->eres > 1e-12;
+      const bool go = sc->newton_iter < sd.max_newton && sc->decrement > sd.newton_tol && eres_ok;
+      if (!go) {
+        sc->newton_active = 0;
+        atomicSub(&ctrs->newton_active, 1);
+      }
+    }
+  }
+}
+
+// ------------------------------------------------------------ BDF steps ---
+// x_tilde + h^2 f, BDF<I>::x_tilde (BDF.cpp:6-9) and Displacement::gradient's
+// target (displacement.cpp:63-73).
+template <typename Real>
+__global__ void __launch_bounds__(kElemTile) k_step_begin(const Tile* tiles, const SceneDev* sds) {
+  const Tile t = tiles[blockIdx.x];
+  const SceneDev& sd = sds[t.scene];
+  if (t.kind == 0) return;
+  const int a = t.begin + threadIdx.x;
+  if (a >= t.end) return;
+  const int I = sd.bdf_order, head = sd.sc->hist_head;
+  const size_t n3 = 3 * (size_t)sd.nv;
+#pragma unroll
+  for (int c = 0; c < 3; ++c) {
+    double wx = 0, wv = 0;
+    for (int i = 0; i < I; ++i) {
+      const int slot = (head + i) % I;
+      wx += sd.bdf_alpha[i] * sd.xhist[slot * n3 + 3 * a + c];
+      wv += sd.bdf_alpha[i] * sd.vhist[slot * n3 + 3 * a + c];
+    }
+    sd.xt[3 * a + c] = wx + sd.dt * wv + sd.h2 * sd.body[c];
+  }
+}
+
+// Pins move to their post-BC-step positions, BDF<I>::update (BDF.cpp:11-21),
+// lambda = 0 (MixedStretch::post_solve, mixed_stretch.cpp:306-309).
+template <typename Real>
+__global__ void __launch_bounds__(kElemTile) k_step_end(const Tile* tiles, const SceneDev* sds,
+                                                        double* partials) {
+  const Tile t = tiles[blockIdx.x];
+  const SceneDev& sd = sds[t.scene];
+  SceneScalars* sc = sd.sc;
+  const int idx = t.begin + threadIdx.x;
+  const int I = sd.bdf_order, head = sc->hist_head;
+  const int nhead = (head + I - 1) % I;
+  if (idx < t.end) {
+    if (t.kind == 0) {
+      Real* la = static_cast<Real*>(sd.la);
+#pragma unroll
+      for (int i = 0; i < 6; ++i) la[(size_t)i * sd.ntp + idx] = Real(0);
+    } else {
+      const int a = idx;
+      const int f = sd.free_map[a];
+      const size_t n3 = 3 * (size_t)sd.nv;
+#pragma unroll
+      for (int c = 0; c < 3; ++c) {
+        double xv = (f < 0) ? sd.pin_pos[3 * (-1 - f) + c] : sd.x[3 * a + c];
+        double wx = 0;
+        for (int i = 0; i < I; ++i) wx += sd.bdf_alpha[i] * sd.xhist[((head + i) % I) * n3 + 3 * a + c];
+        const double vnew = (xv - wx) / sd.dt;
+        sd.x[3 * a + c] = xv;
+        sd.xhist[nhead * n3 + 3 * a + c] = xv;
+        sd.vhist[nhead * n3 + 3 * a + c] = vnew;
+      }
+    }
+  }
+  if (last_tile(&sc->ctr[TB_EV], sd.tile_count[TB_EV])) {
+    if (threadIdx.x == 0) sc->hist_head = nhead;
+  }
+}
+
+template <typename K>
+void set_smem(K kernel, int bytes) {
+  cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+}
+
+}  // namespace
+
+int elem_update_smem_bytes(int fp64) {
+  return kElemTile * kRecSmem * (fp64 ? 8 : 4);
+}
+
+void configure_kernels() {
+  set_smem(k_elem_update<float, false>, elem_update_smem_bytes(0));
+  set_smem(k_elem_update<float, true>, elem_update_smem_bytes(0));
+  set_smem(k_elem_update<double, false>, elem_update_smem_bytes(1));
+  set_smem(k_elem_update<double, true>, elem_update_smem_bytes(1));
+}
+
+void launch_elem_init(const Launch& L) {
+  if (L.ntiles == 0) return;
+  if (L.fp64)
+    k_elem_init<double><<<L.ntiles, kElemTile, 0, L.stream>>>(L.tiles, L.sds);
+  else
+    k_elem_init<float><<<L.ntiles, kElemTile, 0, L.stream>>>(L.tiles, L.sds);
+}
+
+void launch_elem_update(const Launch& L, const ElemDebug* dbg) {
+  if (L.ntiles == 0) return;
+  ElemDebug d{};
+  if (dbg) d = *dbg;
+  const int sm = elem_update_smem_bytes(L.fp64);
+  if (L.fp64) {
+    if (dbg)
+      k_elem_update<double, true><<<L.ntiles, kElemTile, sm, L.stream>>>(L.tiles, L.sds, d);
+    else
+      k_elem_update<double, false><<<L.ntiles, kElemTile, sm, L.stream>>>(L.tiles, L.sds, d);
+  } else {
+    if (dbg)
+      k_elem_update<float, true><<<L.ntiles, kElemTile, sm, L.stream>>>(L.tiles, L.sds, d);
+    else
+      k_elem_update<float, false><<<L.ntiles, kElemTile, sm, L.stream>>>(L.tiles, L.sds, d);
+  }
+}
+
+#define MFEM_LAUNCH_EV(kern, ...)                                                     \
+  do {                                                                                \
+    if (L.ntiles == 0) return;                                                        \
+    if (L.fp64)                                                                       \
+      kern<double><<<L.ntiles, kElemTile, 0, L.stream>>>(__VA_ARGS__);                \
+    else                                                                              \
+      kern<float><<<L.ntiles, kElemTile, 0, L.stream>>>(__VA_ARGS__);                 \
+  } while (0)
+
+void launch_local_solve(const Launch& L) {
+  MFEM_LAUNCH_EV(k_local_solve, L.tiles, L.sds, L.partials, L.counters);
+}
+void launch_ls_energy(const Launch& L) {
+  MFEM_LAUNCH_EV(k_ls_energy, L.tiles, L.sds, L.partials, L.counters);
+}
+void launch_apply(const Launch& L) { MFEM_LAUNCH_EV(k_apply, L.tiles, L.sds, L.partials, L.counters); }
+void launch_step_begin(const Launch& L) { MFEM_LAUNCH_EV(k_step_begin, L.tiles, L.sds); }
+void launch_step_end(const Launch& L) { MFEM_LAUNCH_EV(k_step_end, L.tiles, L.sds, L.partials); }
+
+}  // namespace mfem_gpu

@@ -1,0 +1,451 @@
+// Row-parallel kernels: deterministic assembly of the 3x3-block CSR system
+// and the Jacobi / block-Jacobi preconditioned conjugate gradient.
+//
+//   k_assemble   LHS = PMP + A_mixed and RHS = -PM(x - x~ - h^2 f) - PJW dSdF gl
+//                Assembler::update_matrix (sparse_utils.cpp:141-203) gathers
+//                each block's element contributions in a fixed sorted order;
+//                here one warp owns one block row and sums, in element order,
+//                the contributions of the elements incident to its vertex,
+//                so no atomics are used and the result is bit-reproducible.
+//   k_cg_*       Eigen::ConjugateGradient<.., Lower|Upper, DiagonalPreconditioner>
+//                with zero initial guess (eigen_iterative_solver.h:20-29):
+//                stop when |r|^2 < tol^2 |b|^2, at most max_iterative_solver_iters.
+//                Vectors are Real; every inner product is accumulated in FP64.
+#include <cfloat>
+
+#include "device_math.cuh"
+#include "kernels.cuh"
+#include "reduce.cuh"
+
+namespace mfem_gpu {
+
+namespace {
+
+// offset of entry (l, m) of local block (i, j) in the element record
+__device__ __forceinline__ int rec_offset(int i, int j, int l, int m) {
+  if (i > j) {
+    int t = i; i = j; j = t;
+    t = l; l = m; m = t;
+  }
+  const int start = (i == 0) ? 0 : (i == 1 ? 33 : (i == 2 ? 57 : 72));
+  if (i == j) {
+    if (l > m) { int t = l; l = m; m = t; }
+    return start + (l == 0 ? m : (l == 1 ? 2 + m : 5));
+  }
+  return start + 6 + 9 * (j - i - 1) + 3 * l + m;
+}
+
+constexpr int kMaxOut = 8;  // outputs per lane per chunk (32*8 = 256 = 28 blocks)
+
+template <typename Real>
+__global__ void __launch_bounds__(32 * kRowTile) k_assemble(const Tile* tiles, const SceneDev* sds,
+                                                            double* partials, BatchCounters* ctrs) {
+  __shared__ unsigned short offtab[4][4][9];
+  for (int k = threadIdx.x; k < 144; k += blockDim.x) {
+    const int i = k / 36, j = (k / 9) % 4, rc = k % 9;
+    offtab[i][j][rc] = (unsigned short)rec_offset(i, j, rc / 3, rc % 3);
+  }
+  __syncthreads();
+  const int tix = blockIdx.x;
+  const Tile t = tiles[tix];
+  const SceneDev& sd = sds[t.scene];
+  SceneScalars* sc = sd.sc;
+  if (!sc->newton_active) return;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int row = t.begin + warp;
+  double rn2 = 0.0;
+  if (row < t.end) {
+    const Real* rec = static_cast<const Real*>(sd.rec);
+    const int rb = sd.b_ptr[row], nb = sd.b_ptr[row + 1] - rb;
+    const int ib = sd.inc_ptr[row], ie = sd.inc_ptr[row + 1];
+    const int v = sd.free_vert[row];
+    // ---- right-hand side (FP64): -sum_b m_vb (x_b - xt_b) + element shares
+    double acc[3] = {0, 0, 0};
+    for (int q = sd.m_ptr[v] + lane; q < sd.m_ptr[v + 1]; q += 32) {
+      const int b = sd.m_col[q];
+      const double m = sd.m_val[q];
+#pragma unroll
+      for (int c = 0; c < 3; ++c) acc[c] -= m * (sd.x[3 * b + c] - sd.xt[3 * b + c]);
+    }
+    for (int k = ib + lane; k < ie; k += 32) {
+      const int2 ic = sd.inc[k];
+      const Real* rp = rec + (size_t)ic.x * kRec + 78 + 3 * (ic.y & 3);
+#pragma unroll
+      for (int c = 0; c < 3; ++c) acc[c] += double(rp[c]);
+    }
+#pragma unroll
+    for (int c = 0; c < 3; ++c)
+#pragma unroll
+      for (int off = 16; off > 0; off >>= 1) acc[c] += __shfl_down_sync(0xffffffffu, acc[c], off);
+    if (lane == 0) {
+      Real* rhs = static_cast<Real*>(sd.rhs);
+#pragma unroll
+      for (int c = 0; c < 3; ++c) rhs[3 * row + c] = Real(acc[c]);
+      rn2 = acc[0] * acc[0] + acc[1] * acc[1] + acc[2] * acc[2];
+    }
+    // ---- block values: each lane owns outputs o = base + lane + 32*kk
+    Real* val = static_cast<Real*>(sd.b_val) + (size_t)rb * 9;
+    const Real* bm = static_cast<const Real*>(sd.b_mass) + rb;
+    for (int base = 0; base < 9 * nb; base += 32 * kMaxOut) {
+      Real a[kMaxOut];
+      int oq[kMaxOut], orc[kMaxOut];
+#pragma unroll
+      for (int kk = 0; kk < kMaxOut; ++kk) {
+        const int o = base + lane + 32 * kk;
+        a[kk] = Real(0);
+        oq[kk] = (o < 9 * nb) ? o / 9 : -2;
+        orc[kk] = o % 9;
+      }
+      for (int k = ib; k < ie; ++k) {
+        const int2 ic = sd.inc[k];
+        const int i = ic.y & 3;
+        const int s0 = (ic.y >> 2) & 127, s1 = (ic.y >> 9) & 127, s2 = (ic.y >> 16) & 127,
+                  s3 = (ic.y >> 23) & 127;
+        const Real* rp = rec + (size_t)ic.x * kRec;
+#pragma unroll
+        for (int kk = 0; kk < kMaxOut; ++kk) {
+          const int q = oq[kk];
+          const int j = (s0 == q) ? 0 : (s1 == q) ? 1 : (s2 == q) ? 2 : (s3 == q) ? 3 : -1;
+          if (j >= 0) a[kk] += rp[offtab[i][j][orc[kk]]];
+        }
+      }
+#pragma unroll
+      for (int kk = 0; kk < kMaxOut; ++kk) {
+        const int o = base + lane + 32 * kk;
+        if (o < 9 * nb) {
+          const int rc = orc[kk];
+          val[o] = a[kk] + ((rc == 0 || rc == 4 || rc == 8) ? bm[oq[kk]] : Real(0));
+        }
+      }
+    }
+    __syncwarp();
+    // ---- preconditioner from the diagonal block
+    int qd = -1;
+    for (int q0 = 0; q0 < nb; q0 += 32) {
+      const bool hit = (q0 + lane < nb) && sd.b_col[rb + q0 + lane] == row;
+      const unsigned bal = __ballot_sync(0xffffffffu, hit);
+      if (bal && qd < 0) qd = q0 + __ffs(bal) - 1;
+    }
+    if (lane == 0) {
+      Real* dinv = static_cast<Real*>(sd.dinv);
+      Real D[9];
+#pragma unroll
+      for (int k = 0; k < 9; ++k) D[k] = (qd >= 0) ? val[9 * qd + k] : Real(0);
+      if (sd.block_jacobi) {
+        // inverse of the 3x3 diagonal block (row-major)
+        Real c00 = D[4] * D[8] - D[5] * D[7], c01 = D[5] * D[6] - D[3] * D[8],
+             c02 = D[3] * D[7] - D[4] * D[6];
+        Real det = D[0] * c00 + D[1] * c01 + D[2] * c02;
+        if (det != Real(0)) {
+          Real id = Real(1) / det;
+          dinv[9 * row + 0] = c00 * id;
+          dinv[9 * row + 1] = (D[2] * D[7] - D[1] * D[8]) * id;
+          dinv[9 * row + 2] = (D[1] * D[5] - D[2] * D[4]) * id;
+          dinv[9 * row + 3] = c01 * id;
+          dinv[9 * row + 4] = (D[0] * D[8] - D[2] * D[6]) * id;
+          dinv[9 * row + 5] = (D[2] * D[3] - D[0] * D[5]) * id;
+          dinv[9 * row + 6] = c02 * id;
+          dinv[9 * row + 7] = (D[1] * D[6] - D[0] * D[7]) * id;
+          dinv[9 * row + 8] = (D[0] * D[4] - D[1] * D[3]) * id;
+        } else {
+#pragma unroll
+          for (int k = 0; k < 9; ++k) dinv[9 * row + k] = (k % 4 == 0) ? Real(1) : Real(0);
+        }
+      } else {
+        // DiagonalPreconditioner: 1/a_ii, or 1 where a_ii == 0
+#pragma unroll
+        for (int c = 0; c < 3; ++c) {
+          const Real d = D[4 * c];
+          dinv[3 * row + c] = d != Real(0) ? Real(1) / d : Real(1);
+        }
+      }
+    }
+  }
+  double v1[1] = {rn2};
+  double* part = partials + (size_t)tix * kNumPartials;
+  block_partial<1>(v1, 1, part);
+  if (last_tile(&sc->ctr[TB_ROW], sd.tile_count[TB_ROW])) {
+    if (threadIdx.x == 0) {
+      double s = 0;
+      const int t0 = sd.tile_first[TB_ROW];
+      for (int k = 0; k < sd.tile_count[TB_ROW]; ++k) s += ld_partial(partials + (size_t)(t0 + k) * kNumPartials);
+      const double rn = sqrt(s);
+      if (sc->newton_iter == 0) sc->rhs_norm0 = rn;
+      sc->rhs_norm = rn;
+      // |rhs_k| <= tol * max(|rhs_0|, |h^2 P M f|)
+      if (sd.res_tol > 0 && ((sc->newton_iter > 0 && rn <= sd.res_tol * sc->rhs_norm0) ||
+                             rn <= sd.res_tol * sd.load_norm)) {
+        sc->converged_by_residual = 1;
+        sc->newton_active = 0;
+        atomicSub(&ctrs->newton_active, 1);
+      }
+      if (!(s == s) || isinf(s)) {
+        sc->status = 4;  // MFEM_ERR_NONFINITE
+        if (sc->newton_active) {
+          sc->newton_active = 0;
+          atomicSub(&ctrs->newton_active, 1);
+        }
+      }
+    }
+  }
+}
+
+// ---------------------------------------------------------------- PCG ---
+// Thread (row, lane_r): lane_r < 3 handles component lane_r of the row.
+template <typename Real>
+__device__ __forceinline__ void apply_prec(const SceneDev& sd, int row, int comp, Real rv,
+                                           const unsigned mask, Real& z) {
+  const Real* dinv = static_cast<const Real*>(sd.dinv);
+  if (sd.block_jacobi) {
+    // gather the 3 components of r within the row group (lanes 0..2 of it)
+    const int base = (threadIdx.x & 31) & ~(kCgTpr - 1);
+    Real r0 = __shfl_sync(mask, rv, base + 0);
+    Real r1 = __shfl_sync(mask, rv, base + 1);
+    Real r2 = __shfl_sync(mask, rv, base + 2);
+    const Real* Di = dinv + 9 * row + 3 * comp;
+    z = Di[0] * r0 + Di[1] * r1 + Di[2] * r2;
+  } else {
+    z = dinv[3 * row + comp] * rv;
+  }
+}
+
+template <typename Real>
+__global__ void __launch_bounds__(kCgRows * kCgTpr) k_cg_init(const Tile* tiles, const SceneDev* sds,
+                                                              double* partials, BatchCounters* ctrs) {
+  const int tix = blockIdx.x;
+  const Tile t = tiles[tix];
+  const SceneDev& sd = sds[t.scene];
+  SceneScalars* sc = sd.sc;
+  if (!sc->newton_active) return;
+  const int row = t.begin + threadIdx.x / kCgTpr;
+  const int comp = threadIdx.x % kCgTpr;
+  const bool on = (row < t.end) && comp < 3;
+  double v[2] = {0.0, 0.0};
+  Real rv = 0;
+  if (on) rv = static_cast<const Real*>(sd.rhs)[3 * row + comp];
+  Real z = 0;
+  // all lanes take part in the shuffles of the block preconditioner
+  apply_prec<Real>(sd, row < t.end ? row : t.begin, comp < 3 ? comp : 0, rv, 0xffffffffu, z);
+  if (on) {
+    static_cast<Real*>(sd.cg_r)[3 * row + comp] = rv;
+    static_cast<Real*>(sd.cg_z)[3 * row + comp] = z;
+    static_cast<Real*>(sd.cg_x)[3 * row + comp] = Real(0);
+    v[0] = double(rv) * double(rv);
+    v[1] = double(rv) * double(z);
+  }
+  double* part = partials + (size_t)tix * kNumPartials;
+  block_partial<2>(v, 2, part);
+  if (last_tile(&sc->ctr[TB_CG], sd.tile_count[TB_CG])) {
+    if (threadIdx.x == 0) {
+      double rr = 0, rz = 0;
+      const int t0 = sd.tile_first[TB_CG];
+      for (int k = 0; k < sd.tile_count[TB_CG]; ++k) {
+        const double* p = partials + (size_t)(t0 + k) * kNumPartials;
+        rr += ld_partial(p);
+        rz += ld_partial(p + 1);
+      }
+      sc->cg_rhs_norm2 = rr;
+      sc->cg_iter = 0;
+      sc->beta = 0.0;
+      sc->rz = rz;
+      sc->cg_err = 0.0;
+      if (rr == 0.0) {
+        sc->cg_active = 0;
+      } else {
+        const double thr = fmax(sd.cg_tol * sd.cg_tol * rr, DBL_MIN);
+        sc->cg_threshold = thr;
+        if (rr < thr || sd.max_cg <= 0) {
+          sc->cg_active = 0;
+          sc->cg_err = sqrt(rr / rr);
+        } else {
+          sc->cg_active = 1;
+          atomicAdd(&ctrs->cg_active, 1);
+        }
+      }
+    }
+  }
+}
+
+// Ap = A p with p = z + beta p_prev formed on the fly (so the p update needs
+// no kernel of its own); p is written to the other buffer of the pair.
+template <typename Real>
+__global__ void __launch_bounds__(kCgRows * kCgTpr) k_cg_spmv(const Tile* tiles, const SceneDev* sds,
+                                                              double* partials, BatchCounters* ctrs) {
+  const int tix = blockIdx.x;
+  const Tile t = tiles[tix];
+  const SceneDev& sd = sds[t.scene];
+  SceneScalars* sc = sd.sc;
+  if (!sc->cg_active) return;
+  const int it = sc->cg_iter;
+  const Real beta = Real(sc->beta);
+  const bool first = (it == 0);
+  const Real* z = static_cast<const Real*>(sd.cg_z);
+  const Real* pin = static_cast<const Real*>(sd.cg_p[(it + 1) & 1]);
+  Real* pout = static_cast<Real*>(sd.cg_p[it & 1]);
+  const Real* val = static_cast<const Real*>(sd.b_val);
+  const int row = t.begin + threadIdx.x / kCgTpr;
+  const int lr = threadIdx.x % kCgTpr;
+  Real acc[3] = {0, 0, 0};
+  const bool valid = row < t.end;
+  if (valid) {
+    const int q1 = sd.b_ptr[row + 1];
+    for (int q = sd.b_ptr[row] + lr; q < q1; q += kCgTpr) {
+      const int col = sd.b_col[q];
+      Real p[3];
+#pragma unroll
+      for (int c = 0; c < 3; ++c) p[c] = first ? z[3 * col + c] : z[3 * col + c] + beta * pin[3 * col + c];
+      const Real* b = val + 9 * (size_t)q;
+#pragma unroll
+      for (int r = 0; r < 3; ++r) acc[r] += b[3 * r] * p[0] + b[3 * r + 1] * p[1] + b[3 * r + 2] * p[2];
+    }
+  }
+#pragma unroll
+  for (int r = 0; r < 3; ++r)
+#pragma unroll
+    for (int off = kCgTpr / 2; off > 0; off >>= 1) acc[r] += __shfl_down_sync(0xffffffffu, acc[r], off, kCgTpr);
+  double v[1] = {0.0};
+  if (valid && lr == 0) {
+    Real* Ap = static_cast<Real*>(sd.cg_Ap);
+    double pAp = 0;
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+      const Real p = first ? z[3 * row + c] : z[3 * row + c] + beta * pin[3 * row + c];
+      pout[3 * row + c] = p;
+      Ap[3 * row + c] = acc[c];
+      pAp += double(p) * double(acc[c]);
+    }
+    v[0] = pAp;
+  }
+  double* part = partials + (size_t)tix * kNumPartials;
+  block_partial<1>(v, 1, part);
+  if (last_tile(&sc->ctr[TB_CG], sd.tile_count[TB_CG])) {
+    if (threadIdx.x == 0) {
+      double s = 0;
+      const int t0 = sd.tile_first[TB_CG];
+      for (int k = 0; k < sd.tile_count[TB_CG]; ++k) s += ld_partial(partials + (size_t)(t0 + k) * kNumPartials);
+      sc->alpha = sc->rz / s;
+    }
+  }
+}
+
+template <typename Real>
+__global__ void __launch_bounds__(kCgRows * kCgTpr) k_cg_update(const Tile* tiles, const SceneDev* sds,
+                                                                double* partials, BatchCounters* ctrs) {
+  const int tix = blockIdx.x;
+  const Tile t = tiles[tix];
+  const SceneDev& sd = sds[t.scene];
+  SceneScalars* sc = sd.sc;
+  if (!sc->cg_active) return;
+  const int it = sc->cg_iter;
+  const Real alpha = Real(sc->alpha);
+  const Real* p = static_cast<const Real*>(sd.cg_p[it & 1]);
+  const int row = t.begin + threadIdx.x / kCgTpr;
+  const int comp = threadIdx.x % kCgTpr;
+  const bool on = (row < t.end) && comp < 3;
+  double v[2] = {0.0, 0.0};
+  Real rv = 0;
+  if (on) {
+    const int k = 3 * row + comp;
+    Real* x = static_cast<Real*>(sd.cg_x);
+    Real* r = static_cast<Real*>(sd.cg_r);
+    x[k] += alpha * p[k];
+    rv = r[k] - alpha * static_cast<const Real*>(sd.cg_Ap)[k];
+    r[k] = rv;
+    v[0] = double(rv) * double(rv);
+  }
+  Real z = 0;
+  apply_prec<Real>(sd, row < t.end ? row : t.begin, comp < 3 ? comp : 0, rv, 0xffffffffu, z);
+  if (on) {
+    static_cast<Real*>(sd.cg_z)[3 * row + comp] = z;
+    v[1] = double(rv) * double(z);
+  }
+  double* part = partials + (size_t)tix * kNumPartials;
+  block_partial<2>(v, 2, part);
+  if (last_tile(&sc->ctr[TB_CG], sd.tile_count[TB_CG])) {
+    if (threadIdx.x == 0) {
+      double rr = 0, rz = 0;
+      const int t0 = sd.tile_first[TB_CG];
+      for (int k = 0; k < sd.tile_count[TB_CG]; ++k) {
+        const double* pp = partials + (size_t)(t0 + k) * kNumPartials;
+        rr += ld_partial(pp);
+        rz += ld_partial(pp + 1);
+      }
+      sc->cg_err = sqrt(rr / sc->cg_rhs_norm2);
+      bool stop = false;
+      if (rr < sc->cg_threshold) {
+        stop = true;
+      } else {
+        sc->beta = rz / sc->rz;
+        sc->rz = rz;
+        sc->cg_iter = it + 1;
+        if (it + 1 >= sd.max_cg) {
+          stop = true;
+          sc->cg_status = 5;  // MFEM_ERR_CG_MAXITER
+        }
+      }
+      if (!(rr == rr)) {
+        stop = true;
+        sc->status = 4;
+      }
+      if (stop) {
+        sc->cg_total += sc->cg_iter;
+        sc->cg_active = 0;
+        atomicSub(&ctrs->cg_active, 1);
+      }
+    }
+  }
+}
+
+__global__ void k_scalars_begin(const SceneDev* sds, int n, BatchCounters* ctrs) {
+  for (int i = threadIdx.x; i < n; i += blockDim.x) {
+    SceneScalars* sc = sds[i].sc;
+    sc->newton_active = 1;
+    sc->newton_iter = 0;
+    sc->converged_by_residual = 0;
+    sc->status = 0;
+    sc->E = 0;
+    sc->E_prev = 0;
+    sc->eres = 0;
+    sc->decrement = 0;
+    sc->rhs_norm0 = 0;
+    sc->rhs_norm = 0;
+    sc->cg_active = 0;
+    sc->cg_iter = 0;
+    sc->cg_total = 0;
+    sc->cg_status = 0;
+    sc->cg_err = 0;
+    sc->ls_active = 0;
+    sc->ls_iter = 0;
+    sc->ls_ok = 0;
+    sc->ls_total = 0;
+    sc->alpha_ls = 1.0;
+    sc->procrustes_fail = 0;
+  }
+  if (threadIdx.x == 0) {
+    ctrs->newton_active = n;
+    ctrs->cg_active = 0;
+    ctrs->ls_active = 0;
+  }
+}
+
+}  // namespace
+
+#define MFEM_LAUNCH_ROWS(kern, threads)                                                      \
+  do {                                                                                       \
+    if (L.ntiles == 0) return;                                                               \
+    if (L.fp64)                                                                              \
+      kern<double><<<L.ntiles, threads, 0, L.stream>>>(L.tiles, L.sds, L.partials, L.counters); \
+    else                                                                                     \
+      kern<float><<<L.ntiles, threads, 0, L.stream>>>(L.tiles, L.sds, L.partials, L.counters);  \
+  } while (0)
+
+void launch_assemble(const Launch& L) { MFEM_LAUNCH_ROWS(k_assemble, 32 * kRowTile); }
+void launch_cg_init(const Launch& L) { MFEM_LAUNCH_ROWS(k_cg_init, kCgRows * kCgTpr); }
+void launch_cg_spmv(const Launch& L) { MFEM_LAUNCH_ROWS(k_cg_spmv, kCgRows * kCgTpr); }
+void launch_cg_update(const Launch& L) { MFEM_LAUNCH_ROWS(k_cg_update, kCgRows * kCgTpr); }
+
+void launch_scalars_begin(const Launch& L, int nscenes) {
+  k_scalars_begin<<<1, 128, 0, L.stream>>>(L.sds, nscenes, L.counters);
+}
+
+}  // namespace mfem_gpu

@@ -1,0 +1,181 @@
+// Device-side layout of a scene and of a batch of scenes, and the launch
+// wrappers of every kernel of the Newton timestep.
+//
+// A batch concatenates any number of independent scenes.  Each kernel runs
+// over a tile table; a tile covers a contiguous range of ONE scene's elements,
+// rows or vertices, so per-scene reductions are tile partials summed in a
+// fixed order by the last tile of that scene to finish (deterministic, and
+// identical whether the scene runs alone or in a batch).
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace mfem_gpu {
+
+// Tile tables of a batch.
+enum TableKind {
+  TB_ELEM = 0,  // element tiles (kElemTile elements)               : K1
+  TB_ROW = 1,   // free-row tiles, one warp per row (kRowTile rows)  : assembly
+  TB_CG = 2,    // free-row tiles for PCG (kCgRows rows)              : PCG
+  TB_EV = 3,    // element tiles then vertex tiles of each scene      : local solve,
+                //                                                      line search, apply
+  TB_COUNT = 4
+};
+
+constexpr int kElemTile = 128;   // elements per element tile (one thread each)
+constexpr int kVertTile = 128;   // vertices per vertex tile (TB_EV: same block size)
+constexpr int kRowTile = 8;      // rows per assembly tile (one warp each)
+constexpr int kCgTpr = 8;        // threads per row in the PCG SpMV
+constexpr int kCgRows = 32;      // rows per PCG tile (kCgRows*kCgTpr threads)
+constexpr int kRec = 92;         // per-element record: 78 Aloc (upper blocks) + 12 rhs + 2 pad
+constexpr int kRecSmem = 93;     // odd shared-memory stride of the record
+constexpr int kMaxRowBlocks = 126;  // 7-bit column slots in the incidence code
+constexpr int kNumPartials = 8;  // doubles per tile partial
+
+struct Tile {
+  int scene;  // slot in the batch
+  int kind;   // 0 element range, 1 vertex range (TB_EV); row range otherwise
+  int begin;
+  int end;
+};
+
+// Per-scene scalars: the state machine of the Newton iteration, the PCG and
+// the line search, kept on the device so no step needs a host round trip
+// to decide what the next kernel does.
+struct SceneScalars {
+  // Newton (NewtonOptimizer::step, newton_optimizer.cpp:11-89)
+  int newton_active;
+  int newton_iter;
+  int converged_by_residual;
+  int status;
+  double rhs_norm0, rhs_norm;
+  double E, E_prev, eres, decrement;
+  // PCG (Eigen ConjugateGradient semantics)
+  int cg_active, cg_iter, cg_total, cg_status;
+  double cg_rhs_norm2, cg_threshold, rz, alpha, beta, cg_err;
+  // line search (linesearch.h:80-129 with c = 0, p = 0.5)
+  int ls_active, ls_iter, ls_ok, ls_total;
+  double fx0, alpha_ls, E_trial;
+  double E_abs;      // sum of |element energy terms| at alpha = 0 (rounding bound)
+  double max_ds, max_dx;
+  // BDF ring head
+  int hist_head;
+  int procrustes_fail;
+  // last-tile counters, one per table
+  unsigned int ctr[TB_COUNT];
+  double pad[1];
+};
+
+// Counters of a batch: scenes still active in each loop.
+struct BatchCounters {
+  int newton_active;
+  int cg_active;
+  int ls_active;
+  int pad;
+};
+
+// One scene as the kernels see it (pointers into the scene's arena).
+struct SceneDev {
+  int nv, nt, nf, nnzb;
+  int ntp;           // element SoA stride (nt rounded up)
+  int npin;
+  int material_uniform;  // material id when uniform, -1 when per element
+  int block_jacobi;  // 0: Jacobi (eigen-pcg-diag), 1: 3x3 block Jacobi
+  int fp64;          // 1: all-FP64 path, 0: FP32 element work
+  // parameters
+  double h2;         // (beta*h)^2
+  double dt;         // beta*h
+  double newton_tol, res_tol, cg_tol;
+  double load_norm;  // |h^2 P M f| over the free dofs (scale of the residual test)
+  int max_newton, max_ls, max_cg, bdf_order;
+  double bdf_alpha[6];
+  double body[3];    // body force (float-rounded, as SimConfig::ext is float)
+  // geometry
+  const int4* tets;
+  const void* dphi;  // 9 x ntp Real: [(3*(k-1)+c)*ntp + e] = dphi_k/dX_c, k = 1..3
+  const void* vol;   // ntp Real
+  const void* mu;
+  const void* lam;
+  const int8_t* mat; // ntp or null
+  // element state (Real SoA, stride ntp)
+  void* quat;        // 4 x ntp
+  void* s;           // 6 x ntp
+  void* la;          // 6 x ntp
+  void* S;           // 6 x ntp  stretch of the current x (K1 output)
+  void* ds;          // 6 x ntp
+  void* rec;         // nt x kRec  (AoS element records)
+  // vertices (double)
+  double* x;         // 3 nv current positions; pinned entries hold b
+  double* xt;        // 3 nv  x_tilde + h^2 f_ext (the inertial target)
+  double* xhist;     // bdf_order x 3 nv ring
+  double* vhist;     // bdf_order x 3 nv ring
+  const int* free_map;   // nv: free index, or -1-pin_index when pinned
+  const int* free_vert;  // nf
+  const int* pin_vert;   // npin
+  const double* pin_pos; // 3 npin  pinned positions after the next BC step
+  const int* m_ptr;  // nv+1 scalar mass CSR over all vertices
+  const int* m_col;
+  const double* m_val;
+  // BCSR over free vertices
+  const int* b_ptr;  // nf+1
+  const int* b_col;  // nnzb
+  const void* b_mass;  // nnzb Real: free-free mass m_ab
+  void* b_val;       // 9 nnzb Real, row-major 3x3 blocks
+  void* dinv;        // 9 nf Real (block) or 3 nf (Jacobi)
+  const int* inc_ptr;  // nf+1 incidences (element, local vertex) per free row
+  const int2* inc;     // (element, code): code = i | slot_j << (2+7j), slot 127 = pinned
+  // PCG vectors (Real, 3 nf)
+  void* rhs;
+  void* cg_x;
+  void* cg_r;
+  void* cg_z;
+  void* cg_p[2];
+  void* cg_Ap;
+  // tiles of this scene in each table
+  int tile_first[TB_COUNT];
+  int tile_count[TB_COUNT];
+  SceneScalars* sc;
+};
+
+// Optional FP64 per-element outputs of K1 (parity entry point only).
+struct ElemDebug {
+  double* R;     // 9 per tet
+  double* S;     // 6
+  double* dSdF;  // 54 (9x6 column-major)
+  double* g;     // 6
+  double* H;     // 36
+  double* Hinv;  // 36
+  double* Aloc;  // 144 (12x12 column-major)
+  double* gl;    // 6
+};
+
+struct Launch {
+  cudaStream_t stream;
+  const Tile* tiles;
+  int ntiles;
+  const SceneDev* sds;
+  double* partials;   // ntiles * kNumPartials
+  BatchCounters* counters;
+  int fp64;
+};
+
+// Element kernels (k_elem.cu)
+void launch_elem_init(const Launch& L);                        // s0 = polar(F0), R
+void launch_elem_update(const Launch& L, const ElemDebug* dbg); // K1
+void launch_local_solve(const Launch& L);                      // K5 + E(0)   (TB_EV)
+void launch_ls_energy(const Launch& L);                        // K6          (TB_EV)
+void launch_apply(const Launch& L);                            // x,s update  (TB_EV)
+void launch_step_begin(const Launch& L);                       // x_tilde     (TB_EV)
+void launch_step_end(const Launch& L);                         // BDF, la = 0 (TB_EV)
+// Row kernels (k_rows.cu)
+void launch_assemble(const Launch& L);  // K2 + K3 (TB_ROW)
+void launch_cg_init(const Launch& L);   // r = b, z, rz  (TB_CG)
+void launch_cg_spmv(const Launch& L);   // Ap, pAp, alpha (TB_CG)
+void launch_cg_update(const Launch& L); // x, r, z, beta  (TB_CG)
+void launch_scalars_begin(const Launch& L, int nscenes);        // reset Newton state
+
+// Maximum dynamic shared memory the element kernels need.
+int elem_update_smem_bytes(int fp64);
+void configure_kernels();
+
+}  // namespace mfem_gpu

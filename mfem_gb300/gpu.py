@@ -1,0 +1,182 @@
+"""Scenes and batches on the GPU, through the C ABI of libmfem_gb300.so."""
+import ctypes as C
+
+import numpy as np
+
+from . import abi
+from ._lib import check, load
+from .desc import SceneSpec, make_desc
+
+_dp = C.POINTER(C.c_double)
+_ip = C.POINTER(C.c_int32)
+
+
+def _p(a):
+    return None if a is None else a.ctypes.data_as(_dp)
+
+
+def device_info():
+    name = C.create_string_buffer(256)
+    sms = C.c_int32(0)
+    check(load().mfem_gpu_device_info(name, 256, C.byref(sms)), "device_info")
+    return name.value.decode(), sms.value
+
+
+def footprint(spec: SceneSpec) -> int:
+    d = make_desc(spec)
+    b = C.c_int64(0)
+    check(load().mfem_gpu_scene_footprint(C.addressof(d.struct), C.byref(b)), "footprint")
+    return b.value
+
+
+class Scene:
+    """One resident simulation instance (NewtonOptimizer<3> + its SimState)."""
+
+    def __init__(self, spec: SceneSpec):
+        L = load()
+        self.spec = spec
+        self._desc = make_desc(spec)
+        h = C.c_void_p()
+        check(L.mfem_gpu_scene_create(C.addressof(self._desc.struct), C.byref(h)), "scene_create")
+        self._h = h
+        nv, nt, nf = C.c_int32(), C.c_int32(), C.c_int32()
+        L.mfem_gpu_scene_sizes(self._h, C.byref(nv), C.byref(nt), C.byref(nf))
+        self.n_vertices, self.n_tets, self.n_free = nv.value, nt.value, nf.value
+        nb = C.c_int32()
+        L.mfem_gpu_scene_bcsr_sizes(self._h, None, C.byref(nb))
+        self.nnzb = nb.value
+
+    @property
+    def handle(self):
+        return self._h
+
+    def close(self):
+        if getattr(self, "_h", None) is not None and self._h.value:
+            load().mfem_gpu_scene_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def pinned(self):
+        n = C.c_int32()
+        check(load().mfem_gpu_scene_pinned(self._h, C.byref(n), None), "pinned")
+        v = np.zeros(n.value, dtype=np.int32)
+        check(load().mfem_gpu_scene_pinned(self._h, C.byref(n), v.ctypes.data_as(_ip)), "pinned")
+        return v
+
+    def set_pins(self, positions):
+        p = np.ascontiguousarray(positions, dtype=np.float64).ravel()
+        check(load().mfem_gpu_scene_set_pins(self._h, _p(p)), "set_pins")
+
+    def solo_batch_handle(self):
+        h = C.c_void_p()
+        check(load().mfem_gpu_scene_solo_batch(self._h, C.byref(h)), "solo_batch")
+        return h
+
+    def step(self):
+        st = abi.StepStats()
+        rc = load().mfem_gpu_scene_step(self._h, C.byref(st))
+        if rc not in (abi.OK,):
+            check(rc, "scene_step")
+        return st
+
+    def get_state(self):
+        x = np.zeros(3 * self.n_vertices)
+        v = np.zeros(3 * self.n_vertices)
+        s = np.zeros(6 * self.n_tets)
+        R = np.zeros(9 * self.n_tets)
+        la = np.zeros(6 * self.n_tets)
+        check(load().mfem_gpu_scene_get_state(self._h, _p(x), _p(v), _p(s), _p(R), _p(la)), "get_state")
+        return dict(x=x.reshape(-1, 3), v=v.reshape(-1, 3), s=s.reshape(-1, 6),
+                    R=R.reshape(-1, 9), la=la.reshape(-1, 6))
+
+    def set_state(self, x=None, v=None, s=None, R=None):
+        f = lambda a: None if a is None else np.ascontiguousarray(a, dtype=np.float64).ravel()
+        x, v, s, R = f(x), f(v), f(s), f(R)
+        check(load().mfem_gpu_scene_set_state(self._h, _p(x), _p(v), _p(s), _p(R)), "set_state")
+
+    def elem_update(self, x, h):
+        nt = self.n_tets
+        out = dict(R=np.zeros((nt, 9)), S=np.zeros((nt, 6)), dSdF=np.zeros((nt, 54)),
+                   g=np.zeros((nt, 6)), H=np.zeros((nt, 36)), Hinv=np.zeros((nt, 36)),
+                   Aloc=np.zeros((nt, 144)), gl=np.zeros((nt, 6)))
+        x = np.ascontiguousarray(x, dtype=np.float64).ravel()
+        check(load().mfem_gpu_scene_elem_update(self._h, _p(x), h, *(_p(out[k]) for k in
+              ("R", "S", "dSdF", "g", "H", "Hinv", "Aloc", "gl"))), "elem_update")
+        return out
+
+    def get_system(self):
+        rp = np.zeros(self.n_free + 1, dtype=np.int32)
+        col = np.zeros(self.nnzb, dtype=np.int32)
+        val = np.zeros(9 * self.nnzb)
+        rhs = np.zeros(3 * self.n_free)
+        check(load().mfem_gpu_scene_get_system(self._h, rp.ctypes.data_as(_ip), col.ctypes.data_as(_ip),
+                                               _p(val), _p(rhs)), "get_system")
+        return rp, col, val.reshape(-1, 3, 3), rhs
+
+    def pcg(self, b):
+        b = np.ascontiguousarray(b, dtype=np.float64)
+        x = np.zeros_like(b)
+        it = C.c_int32()
+        err = C.c_double()
+        rc = load().mfem_gpu_scene_pcg(self._h, _p(b), _p(x), C.byref(it), C.byref(err))
+        if rc not in (abi.OK, abi.ERR_CG_MAXITER):
+            check(rc, "pcg")
+        return x, it.value, err.value
+
+
+KERNELS = ["k_elem_update", "k_assemble", "k_cg_init", "k_cg_spmv", "k_cg_update",
+           "k_local_solve", "k_ls_energy", "k_apply", "k_step_begin", "k_step_end",
+           "k_scalars_begin"]
+
+
+def set_profiling(batch_handle, enable=True):
+    check(load().mfem_gpu_batch_set_profiling(batch_handle, int(enable)), "set_profiling")
+
+
+def kernel_stats(batch_handle):
+    """{kernel name: (total device ms, launches)} since profiling was enabled."""
+    out = {}
+    for k, name in enumerate(KERNELS):
+        ms = C.c_double()
+        n = C.c_int64()
+        check(load().mfem_gpu_batch_kernel_stats(batch_handle, k, C.byref(ms), C.byref(n)), "kernel_stats")
+        out[name] = (ms.value, n.value)
+    return out
+
+
+class Batch:
+    """Independent scenes stepped together: one launch per kernel phase."""
+
+    def __init__(self, scenes):
+        self.scenes = list(scenes)
+        arr = (C.c_void_p * len(self.scenes))(*[s.handle.value for s in self.scenes])
+        h = C.c_void_p()
+        check(load().mfem_gpu_batch_create(arr, len(self.scenes), C.byref(h)), "batch_create")
+        self._h = h
+        self._stats = (abi.StepStats * len(self.scenes))()
+
+    def close(self):
+        if getattr(self, "_h", None) is not None and self._h.value:
+            load().mfem_gpu_batch_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    @property
+    def handle(self):
+        return self._h
+
+    def step(self):
+        rc = load().mfem_gpu_batch_step(self._h, self._stats)
+        if rc != abi.OK:
+            check(rc, "batch_step")
+        return list(self._stats)

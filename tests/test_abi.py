@@ -1,0 +1,72 @@
+"""The C ABI library: builds, loads without a GPU, exports every symbol the
+header declares, and its structs have the layout the ctypes mirror assumes."""
+import ctypes as C
+import os
+import subprocess
+import tempfile
+
+import pytest
+
+from mfem_gb300 import _lib, abi
+
+ROOT = os.path.abspath(os.path.join(os.path.dirname(__file__), ".."))
+
+
+def test_library_exports_every_header_symbol(gpu_lib):
+    names = _lib.header_symbols()
+    assert len(names) >= 15
+    for n in names:
+        assert hasattr(gpu_lib, n), n
+    assert set(names) == set(_lib.SIGNATURES)
+
+
+def test_abi_version_and_status_strings(gpu_lib):
+    assert gpu_lib.mfem_gpu_abi_version() == abi.ABI_VERSION
+    for code in range(12):
+        assert gpu_lib.mfem_gpu_status_string(code)
+
+
+def _c_layout(struct, fields):
+    src = ['#include <stdio.h>', '#include <stddef.h>', '#include "mfem_gb300.h"', 'int main(void){']
+    src.append(f'printf("%zu\\n", sizeof({struct}));')
+    for f in fields:
+        src.append(f'printf("%zu\\n", offsetof({struct}, {f}));')
+    src.append('return 0;}')
+    with tempfile.TemporaryDirectory() as d:
+        c = os.path.join(d, "l.c")
+        exe = os.path.join(d, "l")
+        open(c, "w").write("\n".join(src))
+        subprocess.run(["gcc", "-I", os.path.join(ROOT, "include"), c, "-o", exe], check=True)
+        out = subprocess.run([exe], capture_output=True, text=True, check=True).stdout.split()
+    return [int(v) for v in out]
+
+
+@pytest.mark.parametrize("cname,py", [("mfem_scene_desc", abi.SceneDesc),
+                                      ("mfem_step_stats", abi.StepStats)])
+def test_struct_layout_matches_header(cname, py):
+    fields = [n for n, _ in py._fields_]
+    cfields = ["lambda" if f == "lam" else f for f in fields]
+    got = _c_layout(cname, cfields)
+    assert got[0] == C.sizeof(py)
+    for f, off in zip(fields, got[1:]):
+        assert getattr(py, f).offset == off, f
+
+
+def test_no_device_fails_loudly_without_gpu(gpu_lib):
+    """On a machine without a GPU, scene creation reports MFEM_ERR_NO_DEVICE
+    instead of falling back to a CPU path."""
+    import numpy as np
+    from mfem_gb300 import configs
+    from mfem_gb300.desc import make_desc
+    n = C.c_int32(0)
+    try:
+        import torch
+        has_gpu = torch.cuda.is_available()
+    except Exception:
+        has_gpu = None
+    if has_gpu:
+        pytest.skip("a GPU is present")
+    d = make_desc(configs.beam_c1())
+    h = C.c_void_p()
+    rc = gpu_lib.mfem_gpu_scene_create(C.addressof(d.struct), C.byref(h))
+    assert rc == abi.ERR_NO_DEVICE
