@@ -396,6 +396,16 @@ template <typename T> MI T material_psi(int type, T mu, T la, const T* s) {
   return material_coef<T>(type, mu, la, Q, J, t, true).psi;
 }
 
+// Gradient of psi on the 6-vector.
+template <typename T> MI void material_grad(int type, T mu, T la, const T* s, T g[6]) {
+  T Q, J, t, dJ[6];
+  invariants(s, Q, J, t, dJ);
+  MatCoef<T> c = material_coef<T>(type, mu, la, Q, J, t, false);
+#pragma unroll
+  for (int i = 0; i < 6; ++i)
+    g[i] = c.A1 * T(2) * (i < 3 ? T(1) : T(2)) * s[i] + c.B1 * dJ[i] + (i < 3 ? c.C1 : T(0));
+}
+
 // Gradient and (unfixed) Hessian of psi on the 6-vector; H full 6x6 column-major.
 template <typename T>
 MI bool material_grad_hess(int type, T mu, T la, const T* s, T g[6], T H[36]) {
@@ -535,6 +545,72 @@ template <typename T> MI bool psd_fix(T* H, T tol) {
       H[i + 6 * j] = v;
     }
   return true;
+}
+
+// Element force of the mixed residual, in the precision of T:
+//   f_a = -vol * P dphi_a,  P = sum_i q_i ds_i/dF = R (Q - [w]x),
+// Q = sum_i q_i E_i (symmetric), w = W sum_i q_i c_i (the u_i of
+// stretch_derivative_u contracted with q).  This is -PJW (dSdF gl) of
+// MixedStretch::rhs (mixed_stretch.cpp:206-226) for one element, with
+// q = Sym gl = H (S - s) + g.  Returns false if tr(S) I - S is singular.
+template <typename T>
+MI bool element_force(const T* R, const T s6[6], const T q[6], const T dph[12], T vol, T f[12]) {
+  T t = s6[0] + s6[1] + s6[2];
+  T m[6] = {t - s6[0], t - s6[1], t - s6[2], -s6[3], -s6[4], -s6[5]};
+  // sum_i q_i c_i with the c_i of stretch_derivative_u
+  T cq[3];
+  cq[0] = -q[1] * s6[5] + q[2] * s6[5] - T(0.5) * q[3] * s6[4] + T(0.5) * q[4] * s6[3] +
+          T(0.5) * q[5] * (s6[1] - s6[2]);
+  cq[1] = q[0] * s6[4] - q[2] * s6[4] + T(0.5) * q[3] * s6[5] + T(0.5) * q[4] * (s6[2] - s6[0]) -
+          T(0.5) * q[5] * s6[3];
+  cq[2] = -q[0] * s6[3] + q[1] * s6[3] + T(0.5) * q[3] * (s6[0] - s6[1]) - T(0.5) * q[4] * s6[5] +
+          T(0.5) * q[5] * s6[4];
+  T w[3];
+  bool ok = solve_sym3(m, cq, w);
+  if (!ok) w[0] = w[1] = w[2] = T(0);
+  // D = Q - [w]x (column-major)
+  T D[9];
+  D[0] = q[0];
+  D[4] = q[1];
+  D[8] = q[2];
+  D[3] = T(0.5) * q[3] + w[2];   // (0,1)
+  D[1] = T(0.5) * q[3] - w[2];   // (1,0)
+  D[6] = T(0.5) * q[4] - w[1];   // (0,2)
+  D[2] = T(0.5) * q[4] + w[1];   // (2,0)
+  D[7] = T(0.5) * q[5] + w[0];   // (1,2)
+  D[5] = T(0.5) * q[5] - w[0];   // (2,1)
+  T P[9];
+  mul33(R, D, P);
+#pragma unroll
+  for (int a = 0; a < 4; ++a)
+#pragma unroll
+    for (int r = 0; r < 3; ++r)
+      f[3 * a + r] = -vol * (P[r] * dph[3 * a] + P[r + 3] * dph[3 * a + 1] + P[r + 6] * dph[3 * a + 2]);
+  return ok;
+}
+
+// One Newton step of the Procrustes problem in the precision of T, with the
+// rotation update expanded to second order (|omega| is at rounding level
+// after a converged lower-precision solve).
+template <typename T> MI void polish_rotation(T* R, const T* F) {
+  T Y[9], g[3], h[6], om[3];
+  mulABt(R, F, Y);
+  procrustes_gH(Y, g, h);
+  if (!solve_sym3(h, g, om)) return;
+  om[0] = -om[0];
+  om[1] = -om[1];
+  om[2] = -om[2];
+  // dR = I + [om]x + 1/2 [om]x^2
+  T K[9] = {T(0), om[2], -om[1], -om[2], T(0), om[0], om[1], -om[0], T(0)};
+  T K2[9];
+  mul33(K, K, K2);
+  T dR[9];
+#pragma unroll
+  for (int i = 0; i < 9; ++i) dR[i] = ((i % 4 == 0) ? T(1) : T(0)) + K[i] + T(0.5) * K2[i];
+  T tmp[9];
+  mul33(dR, R, tmp);
+#pragma unroll
+  for (int i = 0; i < 9; ++i) R[i] = tmp[i];
 }
 
 // ---------------------------------------------------- compensated sums ---

@@ -410,6 +410,7 @@ struct mfem_batch {
   SceneScalars* h_sc = nullptr;     // pinned, one per scene
   int max_newton = 0, max_ls = 0, max_cg = 0;
   int cg_hint = 16;
+  int pstride = 0;  // tiles per partials quantity
   // instrumentation
   bool profiling = false;
   std::vector<cudaEvent_t> ev_pool;
@@ -465,6 +466,7 @@ Launch make_launch(mfem_batch* b, int table) {
   L.ntiles = b->ntiles[table];
   L.sds = b->d_sds;
   L.partials = b->d_partials;
+  L.pstride = b->pstride;
   L.counters = b->d_ctr;
   L.fp64 = b->fp64;
   return L;
@@ -483,11 +485,11 @@ void layout_scene(mfem_scene* s, Arena& A) {
   D.lam = A.take_bytes(ntp * r);
   D.mat = M.mat.empty() ? nullptr : A.take<int8_t>(ntp);
   D.quat = A.take_bytes(4 * ntp * r);
-  D.s = A.take_bytes(6 * ntp * r);
+  D.s = A.take<double>(6 * ntp);
   D.la = A.take_bytes(6 * ntp * r);
-  D.S = A.take_bytes(6 * ntp * r);
+  D.dS = A.take_bytes(6 * ntp * r);
   D.ds = A.take_bytes(6 * ntp * r);
-  D.rec = A.take_bytes((size_t)kRec * M.nt * r);
+  D.rec = A.take<unsigned char>((size_t)rec_bytes((int)r) * M.nt);
   D.x = A.take<double>(3 * (size_t)M.nv);
   D.xt = A.take<double>(3 * (size_t)M.nv);
   D.xhist = A.take<double>(3 * (size_t)M.nv * I);
@@ -517,6 +519,11 @@ void layout_scene(mfem_scene* s, Arena& A) {
   D.cg_Ap = A.take_bytes(n3 * r);
   s->d_sc = A.take<SceneScalars>(1);
   D.sc = s->d_sc;
+  // first-level ticket counters: one per group of kTicketGroup tiles per table
+  const int maxtiles = std::max({(M.nt + kElemTile - 1) / kElemTile + (M.nv + kVertTile - 1) / kVertTile,
+                                 (M.nf + kRowTile - 1) / kRowTile, (M.nf + kCgRows - 1) / kCgRows, 1});
+  D.gmax = (maxtiles + kTicketGroup - 1) / kTicketGroup;
+  D.gctr = A.take<unsigned int>((size_t)TB_COUNT * D.gmax);
 }
 
 template <typename T>
@@ -754,6 +761,7 @@ int batch_build(mfem_scene* const* scenes, int n, mfem_batch** out) {
     for (int tb = 0; tb < TB_COUNT; ++tb) b->d_tiles[tb] = a.take<Tile>(std::max<size_t>(tabs[tb].size(), 1));
     b->d_sds = a.take<SceneDev>(n);
     b->d_partials = a.take<double>(maxt * kNumPartials);
+    b->pstride = (int)maxt;
     b->d_ctr = a.take<BatchCounters>(1);
   };
   lay(A);
@@ -1054,7 +1062,7 @@ int mfem_gpu_scene_footprint(const mfem_scene_desc* desc, int64_t* bytes) {
   scene_layout_bytes(s.get(), &b);
   // plus the single-scene batch (tile tables, partials)
   const size_t tiles = (size_t)(s->M.nt / kElemTile + 1) * 2 + s->M.nf / kRowTile + s->M.nf / kCgRows +
-                       s->M.nv / kVertTile + 8;
+                       s->M.nv / kVertTile + 8;  // tile tables of the single-scene batch
   *bytes = (int64_t)(b + tiles * (sizeof(Tile) + kNumPartials * sizeof(double)) + 4096);
   return MFEM_OK;
 }
@@ -1126,10 +1134,7 @@ int mfem_gpu_scene_get_state(mfem_scene* s, double* x, double* v, double* sv, do
                        cudaMemcpyDeviceToHost),
             MFEM_ERR_CUDA);
   }
-  if (sv) {
-    if (s->fp64) download_soa<double>(s->dev.s, M.nt, s->ntp, 6, sv, st);
-    else download_soa<float>(s->dev.s, M.nt, s->ntp, 6, sv, st);
-  }
+  if (sv) download_soa<double>(s->dev.s, M.nt, s->ntp, 6, sv, st);
   if (la) {
     if (s->fp64) download_soa<double>(s->dev.la, M.nt, s->ntp, 6, la, st);
     else download_soa<float>(s->dev.la, M.nt, s->ntp, 6, la, st);
@@ -1166,10 +1171,7 @@ int mfem_gpu_scene_set_state(mfem_scene* s, const double* x, const double* v, co
     CUDA_OR(cudaMemcpy(s->dev.vhist + 3 * (size_t)M.nv * sc.hist_head, v, sizeof(double) * 3 * M.nv,
                        cudaMemcpyHostToDevice),
             MFEM_ERR_CUDA);
-  if (sv) {
-    if (s->fp64) upload_soa<double>(s->dev.s, M.nt, s->ntp, 6, sv, st);
-    else upload_soa<float>(s->dev.s, M.nt, s->ntp, 6, sv, st);
-  }
+  if (sv) upload_soa<double>(s->dev.s, M.nt, s->ntp, 6, sv, st);
   if (R) {
     std::vector<double> q(4 * (size_t)M.nt);
     for (int e = 0; e < M.nt; ++e) rot_to_quat_h(&R[9 * (size_t)e], &q[4 * (size_t)e]);

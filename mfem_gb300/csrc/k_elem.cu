@@ -49,40 +49,6 @@ __device__ __forceinline__ void load_elem(const SceneDev& sd, int e, ElemIn<Real
   in.mat = sd.material_uniform >= 0 ? sd.material_uniform : int(sd.mat[e]);
 }
 
-// F = sum_k (x_k - x_0) (x) dphi_k with the edge vectors formed in FP64
-// (TetrahedralMesh::deformation_gradient, tet_mesh.cpp:77-80).
-template <typename Real>
-__device__ __forceinline__ void deformation_gradient(const double* x, const double* dx,
-                                                     double alpha, const int* free_map,
-                                                     const ElemIn<Real>& in, Real* F) {
-  const int v[4] = {in.tv.x, in.tv.y, in.tv.z, in.tv.w};
-  double p[4][3];
-#pragma unroll
-  for (int k = 0; k < 4; ++k)
-#pragma unroll
-    for (int d = 0; d < 3; ++d) p[k][d] = x[3 * v[k] + d];
-  if (dx != nullptr) {
-#pragma unroll
-    for (int k = 0; k < 4; ++k) {
-      int f = free_map[v[k]];
-      if (f >= 0) {
-#pragma unroll
-        for (int d = 0; d < 3; ++d) p[k][d] += alpha * dx[3 * f + d];
-      }
-    }
-  }
-  Real ed[9];
-#pragma unroll
-  for (int k = 1; k < 4; ++k)
-#pragma unroll
-    for (int r = 0; r < 3; ++r) ed[3 * (k - 1) + r] = Real(p[k][r] - p[0][r]);
-#pragma unroll
-  for (int c = 0; c < 3; ++c)
-#pragma unroll
-    for (int r = 0; r < 3; ++r)
-      F[r + 3 * c] = ed[r] * in.dp[c] + ed[3 + r] * in.dp[3 + c] + ed[6 + r] * in.dp[6 + c];
-}
-
 template <typename Real>
 __device__ __forceinline__ void load_quat(const SceneDev& sd, int e, Real* R) {
   const Real* q = static_cast<const Real*>(sd.quat);
@@ -133,6 +99,39 @@ __host__ __device__ constexpr int sym_idx(int r, int c) {
   return r == 0 ? c : (r == 1 ? 2 + c : 5);
 }
 
+// Edge vectors x_k - x_0 (k = 1..3) in FP64 and F in FP64 and in Real.
+template <typename Real>
+__device__ __forceinline__ void deformation_gradients(const double* x, const ElemIn<Real>& in,
+                                                      double* F64, Real* F) {
+  const int v[4] = {in.tv.x, in.tv.y, in.tv.z, in.tv.w};
+  double ed[9];
+#pragma unroll
+  for (int k = 1; k < 4; ++k)
+#pragma unroll
+    for (int r = 0; r < 3; ++r) ed[3 * (k - 1) + r] = x[3 * v[k] + r] - x[3 * v[0] + r];
+#pragma unroll
+  for (int c = 0; c < 3; ++c)
+#pragma unroll
+    for (int r = 0; r < 3; ++r) {
+      F64[r + 3 * c] = ed[r] * double(in.dp[c]) + ed[3 + r] * double(in.dp[3 + c]) +
+                       ed[6 + r] * double(in.dp[6 + c]);
+      F[r + 3 * c] = Real(F64[r + 3 * c]);
+    }
+}
+
+__device__ __forceinline__ void load6d(const double* p, int ntp, int e, double* v) {
+#pragma unroll
+  for (int i = 0; i < 6; ++i) v[i] = p[(size_t)i * ntp + e];
+}
+
+// 32-bit-word stores into the staged element record (shared memory).
+__device__ __forceinline__ void put_word(unsigned int* w, int idx, float v) { w[idx] = __float_as_uint(v); }
+__device__ __forceinline__ void put_word(unsigned int* w, int idx, double v) {
+  const unsigned long long b = (unsigned long long)__double_as_longlong(v);
+  w[idx] = (unsigned int)(b & 0xffffffffull);
+  w[idx + 1] = (unsigned int)(b >> 32);
+}
+
 // ------------------------------------------------------------------ K0 ---
 template <typename Real>
 __global__ void __launch_bounds__(kElemTile) k_elem_init(const Tile* tiles, const SceneDev* sds) {
@@ -142,67 +141,121 @@ __global__ void __launch_bounds__(kElemTile) k_elem_init(const Tile* tiles, cons
   if (e >= t.end) return;
   ElemIn<Real> in;
   load_elem(sd, e, in);
+  double F64[9];
   Real F[9], R[9];
-  deformation_gradient<Real>(sd.x, nullptr, 0.0, sd.free_map, in, F);
+  deformation_gradients<Real>(sd.x, in, F64, F);
 #pragma unroll
   for (int i = 0; i < 9; ++i) R[i] = (i % 4 == 0) ? Real(1) : Real(0);
   int it = procrustes<Real>(R, F, Real(kProcrustesTol), kProcrustesIters);
   if (it < 0) atomicAdd(&sd.sc->procrustes_fail, 1);
-  Real S6[6];
-  stretch_vec(R, F, S6);
   store_quat(sd, e, R);
-  store6(sd.s, sd.ntp, e, S6);
-  store6(sd.S, sd.ntp, e, S6);
+  double R64[9], s64[6];
+#pragma unroll
+  for (int i = 0; i < 9; ++i) R64[i] = double(R[i]);
+  if (!Prec<Real>::kFP64) polish_rotation(R64, F64);
+  stretch_vec(R64, F64, s64);
+#pragma unroll
+  for (int i = 0; i < 6; ++i) sd.s[(size_t)i * sd.ntp + e] = s64[i];
   Real z[6] = {0, 0, 0, 0, 0, 0};
+  store6(sd.dS, sd.ntp, e, z);
   store6(sd.la, sd.ntp, e, z);
   store6(sd.ds, sd.ntp, e, z);
 }
 
 // ------------------------------------------------------------------ K1 ---
+// In the mixed path the rotation, S, S - s, h^2 psi'(s), q and the element
+// forces are carried in FP64 (one FP64 Newton polish of the FP32 rotation):
+// the element forces are tens of times the net residual in a loaded body, so
+// FP32 forces would floor the Newton residual near 1e-4.  The Hessian, the
+// derivative ds/dF and the element block stay in Real.
 template <typename Real, bool DBG>
 __global__ void __launch_bounds__(kElemTile)
     k_elem_update(const Tile* tiles, const SceneDev* sds, ElemDebug dbg) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  Real* buf = reinterpret_cast<Real*>(smem_raw);
+  unsigned int* words = reinterpret_cast<unsigned int*>(smem_raw);
+  constexpr int RB = sizeof(Real);
+  constexpr int kWords = rec_bytes(RB) / 4;       // words per record
+  constexpr int kStride = kWords + 1;              // odd stride: no bank conflicts
+  constexpr int kRhsWord = rec_rhs_offset(RB) / 4;
   const Tile t = tiles[blockIdx.x];
   const SceneDev& sd = sds[t.scene];
   if (!sd.sc->newton_active) return;
   const int e = t.begin + threadIdx.x;
   const Real h2 = Real(sd.h2);
   if (e < t.end) {
-    Real* out = buf + threadIdx.x * kRecSmem;
+    unsigned int* out = words + threadIdx.x * kStride;
     ElemIn<Real> in;
     load_elem(sd, e, in);
+    double s64[6];
+    load6d(sd.s, sd.ntp, e, s64);
     Real sv[6];
-    load6(sd.s, sd.ntp, e, sv);
-    // material derivatives at s: g = h^2 grad psi, H = h^2 hess psi (psd-fixed)
+#pragma unroll
+    for (int i = 0; i < 6; ++i) sv[i] = Real(s64[i]);
+    // h^2 hess psi (psd-fixed) at s
     Real g[6], H[36];
     material_gH(in, sv, h2, g, H);
     // polar rotation from the previous rotation (update_rotations)
+    double F64[9];
     Real F[9], R[9];
-    deformation_gradient<Real>(sd.x, nullptr, 0.0, sd.free_map, in, F);
+    deformation_gradients<Real>(sd.x, in, F64, F);
     load_quat(sd, e, R);
     int it = procrustes<Real>(R, F, Real(kProcrustesTol), kProcrustesIters);
+    store_quat(sd, e, R);
     Real S6[6];
     stretch_vec(R, F, S6);
     Real u[18];
     bool ok = stretch_derivative_u(S6, u);
     if (it < 0 || !ok) atomicAdd(&sd.sc->procrustes_fail, 1);
-    store_quat(sd, e, R);
-    store6(sd.S, sd.ntp, e, S6);
-    // B[i][a][l] = ds_i / dx_{a,l} = (G_i dphi_a)_l
+    Real dph[12];
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+      dph[3 + c] = in.dp[c];
+      dph[6 + c] = in.dp[3 + c];
+      dph[9 + c] = in.dp[6 + c];
+      dph[c] = -(in.dp[c] + in.dp[3 + c] + in.dp[6 + c]);
+    }
+    // ---- residual chain in FP64: S - s, q = H (S - s) + h^2 psi'(s), forces
+    {
+      double R64[9], S64[6], d64[6], g64[6], q64[6], dph64[12], f64[12];
+#pragma unroll
+      for (int i = 0; i < 9; ++i) R64[i] = double(R[i]);
+      if (!Prec<Real>::kFP64) polish_rotation(R64, F64);
+      stretch_vec(R64, F64, S64);
+      material_grad<double>(in.mat, double(in.mu), double(in.lam), s64, g64);
+#pragma unroll
+      for (int i = 0; i < 6; ++i) d64[i] = S64[i] - s64[i];
+#pragma unroll
+      for (int i = 0; i < 6; ++i) {
+        double acc = double(h2) * g64[i];
+#pragma unroll
+        for (int j = 0; j < 6; ++j) acc += double(H[i + 6 * j]) * d64[j];
+        q64[i] = acc;
+      }
+#pragma unroll
+      for (int i = 0; i < 12; ++i) dph64[i] = double(dph[i]);
+      element_force<double>(R64, S64, q64, dph64, double(in.vol), f64);
+#pragma unroll
+      for (int i = 0; i < 12; ++i) put_word(out, kRhsWord + 2 * i, f64[i]);
+      Real dS[6];
+#pragma unroll
+      for (int i = 0; i < 6; ++i) dS[i] = Real(d64[i]);
+      store6(sd.dS, sd.ntp, e, dS);
+      if (DBG) {
+        const size_t E = e;
+        for (int i = 0; i < 9; ++i) dbg.R[9 * E + i] = R64[i];
+        for (int i = 0; i < 6; ++i) {
+          dbg.S[6 * E + i] = S64[i];
+          dbg.g[6 * E + i] = double(h2) * g64[i];
+          dbg.gl[6 * E + i] = (i < 3 ? 1.0 : 0.5) * q64[i];
+        }
+        for (int i = 0; i < 36; ++i) dbg.H[36 * E + i] = H[i];
+      }
+    }
+    // ---- B[i][a][l] = ds_i / dx_{a,l} = (G_i dphi_a)_l
     Real B[72];
     {
       Real G[54];
       ds_dF(R, u, G);
-      Real dph[12];
-#pragma unroll
-      for (int c = 0; c < 3; ++c) {
-        dph[3 + c] = in.dp[c];
-        dph[6 + c] = in.dp[3 + c];
-        dph[9 + c] = in.dp[6 + c];
-        dph[c] = -(in.dp[c] + in.dp[3 + c] + in.dp[6 + c]);
-      }
 #pragma unroll
       for (int i = 0; i < 6; ++i)
 #pragma unroll
@@ -217,31 +270,7 @@ __global__ void __launch_bounds__(kElemTile)
           for (int r = 0; r < 9; ++r) dbg.dSdF[54 * (size_t)e + r + 9 * i] = sym[i] * double(G[9 * i + r]);
       }
     }
-    // q = H (S - s) + g ;  gl = Syminv q  (MixedStretch::rhs, mixed_stretch.cpp:219-220)
-    Real qv[6];
-    {
-      Real d[6];
-#pragma unroll
-      for (int i = 0; i < 6; ++i) d[i] = S6[i] - sv[i];
-#pragma unroll
-      for (int i = 0; i < 6; ++i) {
-        Real acc = g[i];
-#pragma unroll
-        for (int j = 0; j < 6; ++j) acc += H[i + 6 * j] * d[j];
-        qv[i] = acc;
-      }
-    }
-    // right-hand-side share of vertex a: -vol * sum_i q_i B[i][a]
-#pragma unroll
-    for (int a = 0; a < 4; ++a)
-#pragma unroll
-      for (int l = 0; l < 3; ++l) {
-        Real acc = 0;
-#pragma unroll
-        for (int i = 0; i < 6; ++i) acc += qv[i] * B[12 * i + 3 * a + l];
-        out[78 + 3 * a + l] = -in.vol * acc;
-      }
-    // upper 3x3 blocks of Aloc = vol * B^T H B  (mixed_stretch.cpp:174-175)
+    // ---- upper 3x3 blocks of Aloc = vol * B^T H B  (mixed_stretch.cpp:174-175)
 #pragma unroll
     for (int b = 0; b < 4; ++b) {
       Real HB[18];
@@ -265,49 +294,35 @@ __global__ void __launch_bounds__(kElemTile)
             Real acc = 0;
 #pragma unroll
             for (int i = 0; i < 6; ++i) acc += B[12 * i + 3 * a + l] * HB[3 * i + m];
-            out[base + (a == b ? sym_idx(l, m) : 3 * l + m)] = in.vol * acc;
+            const int k = base + (a == b ? sym_idx(l, m) : 3 * l + m);
+            put_word(out, k * (RB / 4), Real(in.vol * acc));
+            if (DBG) {
+              const size_t E = e;
+              const double v = double(Real(in.vol * acc));
+              dbg.Aloc[144 * E + (3 * a + l) + 12 * (3 * b + m)] = v;
+              dbg.Aloc[144 * E + (3 * b + m) + 12 * (3 * a + l)] = v;
+            }
           }
       }
     }
-    out[90] = Real(0);
-    out[91] = Real(0);
-    if (DBG) {
-      const size_t E = e;
-      for (int i = 0; i < 9; ++i) dbg.R[9 * E + i] = R[i];
-      for (int i = 0; i < 6; ++i) {
-        dbg.S[6 * E + i] = S6[i];
-        dbg.g[6 * E + i] = g[i];
-        dbg.gl[6 * E + i] = (i < 3 ? 1.0 : 0.5) * double(qv[i]);
-      }
-      for (int i = 0; i < 36; ++i) dbg.H[36 * E + i] = H[i];
-      for (int a = 0; a < 4; ++a)
-        for (int b = 0; b < 4; ++b)
-          for (int l = 0; l < 3; ++l)
-            for (int m = 0; m < 3; ++m) {
-              int aa = a, bb = b, ll = l, mm = m;
-              if (a > b) { aa = b; bb = a; ll = m; mm = l; }
-              int base = rec_block_start(aa) + (aa == bb ? 0 : 6 + 9 * (bb - aa - 1));
-              int off = (aa == bb) ? sym_idx(ll < mm ? ll : mm, ll < mm ? mm : ll) : 3 * ll + mm;
-              dbg.Aloc[144 * E + (3 * a + l) + 12 * (3 * b + m)] = out[base + off];
-            }
-    }
   }
   __syncthreads();
-  // contiguous store of the tile's records
+  // contiguous store of the tile's records as 32-bit words
   const int n = t.end - t.begin;
-  Real* dst = static_cast<Real*>(sd.rec) + (size_t)t.begin * kRec;
-  for (int i = threadIdx.x; i < n * kRec; i += blockDim.x) {
-    int el = i / kRec;
-    dst[i] = buf[el * kRecSmem + (i - el * kRec)];
+  unsigned int* dst = reinterpret_cast<unsigned int*>(sd.rec + (size_t)t.begin * rec_bytes(RB));
+  for (int i = threadIdx.x; i < n * kWords; i += blockDim.x) {
+    const int el = i / kWords;
+    dst[i] = words[el * kStride + (i - el * kWords)];
   }
 }
 
 // ------------------------------------------------------------------ K5 ---
-// ds = S - s + dS/dF : dF(dx)  (the closed form of -H^{-1}(Sym la + g)),
-// la = -Syminv (H ds + g); also E(0) and max |ds|, max |dx|.
+// ds = (S - s) + dS/dF : dF(dx)  (the closed form of -H^{-1}(Sym la + g),
+// MixedStretch::solve), la = -Syminv (H ds + g); E(0), max |ds|, max |dx|.
 template <typename Real>
 __global__ void __launch_bounds__(kElemTile) k_local_solve(const Tile* tiles, const SceneDev* sds,
-                                                           double* partials, BatchCounters* ctrs) {
+                                                           double* partials, int pstride,
+                                                           BatchCounters* ctrs) {
   const int tix = blockIdx.x;
   const Tile t = tiles[tix];
   const SceneDev& sd = sds[t.scene];
@@ -316,34 +331,38 @@ __global__ void __launch_bounds__(kElemTile) k_local_solve(const Tile* tiles, co
   const Real h2 = Real(sd.h2);
   const Real* cgx = static_cast<const Real*>(sd.cg_x);
   KSum en{0.0, 0.0};
-  double mx[2] = {0.0, 0.0};
-  double eabs[1] = {0.0};
+  double mds = 0.0, mdx = 0.0, eabs = 0.0;
   const int idx = t.begin + threadIdx.x;
   if (t.kind == 0) {
     if (idx < t.end) {
       const int e = idx;
       ElemIn<Real> in;
       load_elem(sd, e, in);
-      Real R[9], S6[6], sv[6];
+      Real R[9], d[6], sv[6], S6[6];
+      double s64[6];
       load_quat(sd, e, R);
-      load6(sd.S, sd.ntp, e, S6);
-      load6(sd.s, sd.ntp, e, sv);
-      // dF = sum_k (dx_k - dx_0) (x) dphi_k
+      load6(sd.dS, sd.ntp, e, d);
+      load6d(sd.s, sd.ntp, e, s64);
+#pragma unroll
+      for (int i = 0; i < 6; ++i) {
+        sv[i] = Real(s64[i]);
+        S6[i] = Real(s64[i] + double(d[i]));
+      }
       const int v[4] = {in.tv.x, in.tv.y, in.tv.z, in.tv.w};
-      Real d[4][3];
+      Real dd[4][3];
 #pragma unroll
       for (int k = 0; k < 4; ++k) {
-        int f = sd.free_map[v[k]];
+        const int f = sd.free_map[v[k]];
 #pragma unroll
-        for (int c = 0; c < 3; ++c) d[k][c] = f >= 0 ? cgx[3 * f + c] : Real(0);
+        for (int c = 0; c < 3; ++c) dd[k][c] = f >= 0 ? cgx[3 * f + c] : Real(0);
       }
       Real dF[9];
 #pragma unroll
       for (int c = 0; c < 3; ++c)
 #pragma unroll
         for (int r = 0; r < 3; ++r)
-          dF[r + 3 * c] = (d[1][r] - d[0][r]) * in.dp[c] + (d[2][r] - d[0][r]) * in.dp[3 + c] +
-                          (d[3][r] - d[0][r]) * in.dp[6 + c];
+          dF[r + 3 * c] = (dd[1][r] - dd[0][r]) * in.dp[c] + (dd[2][r] - dd[0][r]) * in.dp[3 + c] +
+                          (dd[3][r] - dd[0][r]) * in.dp[6 + c];
       Real dFh[9];
       mulAtB(R, dF, dFh);
       Real u[18], delta[6];
@@ -351,8 +370,8 @@ __global__ void __launch_bounds__(kElemTile) k_local_solve(const Tile* tiles, co
       ds_dot(u, dFh, delta);
       Real ds[6];
 #pragma unroll
-      for (int i = 0; i < 6; ++i) ds[i] = S6[i] - sv[i] + delta[i];
-      Real g[36 / 6], H[36];
+      for (int i = 0; i < 6; ++i) ds[i] = d[i] + delta[i];
+      Real g[6], H[36];
       material_gH(in, sv, h2, g, H);
       Real la[6];
 #pragma unroll
@@ -364,69 +383,60 @@ __global__ void __launch_bounds__(kElemTile) k_local_solve(const Tile* tiles, co
       }
       store6(sd.ds, sd.ntp, e, ds);
       store6(sd.la, sd.ntp, e, la);
-      // E(0): h^2 vol psi(s) - vol la . Sym (S - s)
-      Real psi = material_psi<Real>(in.mat, in.mu, in.lam, sv);
+      // E(0) = h^2 vol psi(s) - vol la . Sym (S - s)
+      const double psi = double(material_psi<Real>(in.mat, in.mu, in.lam, sv));
       double con = 0;
 #pragma unroll
-      for (int i = 0; i < 6; ++i) con += double(la[i]) * (i < 3 ? 1.0 : 2.0) * double(S6[i] - sv[i]);
-      en.add(double(h2) * double(in.vol) * double(psi));
-      en.add(-double(in.vol) * con);
-      eabs[0] = fabs(double(h2) * double(in.vol) * double(psi)) + fabs(double(in.vol) * con);
+      for (int i = 0; i < 6; ++i) con += double(la[i]) * (i < 3 ? 1.0 : 2.0) * double(d[i]);
+      const double e1 = double(h2) * double(in.vol) * psi, e2 = double(in.vol) * con;
+      en.add(e1);
+      en.add(-e2);
+      eabs = fabs(e1) + fabs(e2);
       Real m = 0;
 #pragma unroll
       for (int i = 0; i < 6; ++i) m = fmax(m, fabs(ds[i]));
-      mx[0] = m;
+      mds = m;
     }
-  } else {
-    if (idx < t.end) {
-      const int a = idx;
-      const double* x = sd.x;
-      const double* xt = sd.xt;
-      double Md[3] = {0, 0, 0};
-      for (int q = sd.m_ptr[a]; q < sd.m_ptr[a + 1]; ++q) {
-        const int b = sd.m_col[q];
-        const double m = sd.m_val[q];
+  } else if (idx < t.end) {
+    const int a = idx;
+    const double* x = sd.x;
+    const double* xt = sd.xt;
+    double Md[3] = {0, 0, 0};
+    for (int q = sd.m_ptr[a]; q < sd.m_ptr[a + 1]; ++q) {
+      const int b = sd.m_col[q];
+      const double m = sd.m_val[q];
 #pragma unroll
-        for (int c = 0; c < 3; ++c) Md[c] += m * (x[3 * b + c] - xt[3 * b + c]);
-      }
-      double e2 = 0;
+      for (int c = 0; c < 3; ++c) Md[c] += m * (x[3 * b + c] - xt[3 * b + c]);
+    }
+    double e2 = 0;
 #pragma unroll
-      for (int c = 0; c < 3; ++c) e2 += (x[3 * a + c] - xt[3 * a + c]) * Md[c];
-      en.add(0.5 * e2);
-      const int f = sd.free_map[a];
-      if (f >= 0) {
-        double m = 0;
+    for (int c = 0; c < 3; ++c) e2 += (x[3 * a + c] - xt[3 * a + c]) * Md[c];
+    en.add(0.5 * e2);
+    const int f = sd.free_map[a];
+    if (f >= 0) {
 #pragma unroll
-        for (int c = 0; c < 3; ++c) m = fmax(m, fabs(double(cgx[3 * f + c])));
-        mx[1] = m;
-      }
+      for (int c = 0; c < 3; ++c) mdx = fmax(mdx, fabs(double(cgx[3 * f + c])));
     }
   }
-  double* part = partials + (size_t)tix * kNumPartials;
-  block_ksum(en, part);
-  block_partial<2>(mx, 0, part + 2);
-  block_partial<1>(eabs, 1, part + 4);
-  if (last_tile(&sc->ctr[TB_EV], sd.tile_count[TB_EV])) {
+  put_ksum(en, partials, pstride, 0, tix);
+  put_max(mds, partials, pstride, 2, tix);
+  put_max(mdx, partials, pstride, 3, tix);
+  put_sum(eabs, partials, pstride, 4, tix);
+  if (last_tile(sd, TB_EV, tix)) {
+    const int t0 = sd.tile_first[TB_EV], tc = sd.tile_count[TB_EV];
+    const double Ev = scene_ksum(partials, pstride, 0, t0, tc);
+    const double ms = scene_max(partials, pstride, 2, t0, tc);
+    const double mx = scene_max(partials, pstride, 3, t0, tc);
+    const double ea = scene_sum(partials, pstride, 4, t0, tc);
     if (threadIdx.x == 0) {
-      KSum E{0.0, 0.0};
-      double mds = 0, mdx = 0, eab = 0;
-      const int t0 = sd.tile_first[TB_EV];
-      for (int k = 0; k < sd.tile_count[TB_EV]; ++k) {
-        const double* p = partials + (size_t)(t0 + k) * kNumPartials;
-        E.merge(KSum{ld_partial(p), ld_partial(p + 1)});
-        mds = fmax(mds, ld_partial(p + 2));
-        mdx = fmax(mdx, ld_partial(p + 3));
-        eab += ld_partial(p + 4);
-      }
-      const double Ev = E.value();
-      sc->E_abs = eab;
+      sc->E_abs = ea;
       sc->E = Ev;
       sc->eres = fabs((Ev - sc->E_prev) / (Ev + 1e-6));
       sc->E_prev = Ev;
       sc->fx0 = Ev;
-      sc->max_ds = mds;
-      sc->max_dx = mdx;
-      sc->decrement = fmax(mdx, mds);
+      sc->max_ds = ms;
+      sc->max_dx = mx;
+      sc->decrement = fmax(mx, ms);
       sc->alpha_ls = 1.0;
       sc->ls_iter = 0;
       sc->ls_ok = 0;
@@ -443,7 +453,8 @@ __global__ void __launch_bounds__(kElemTile) k_local_solve(const Tile* tiles, co
 // ------------------------------------------------------------------ K6 ---
 template <typename Real>
 __global__ void __launch_bounds__(kElemTile) k_ls_energy(const Tile* tiles, const SceneDev* sds,
-                                                         double* partials, BatchCounters* ctrs) {
+                                                         double* partials, int pstride,
+                                                         BatchCounters* ctrs) {
   const int tix = blockIdx.x;
   const Tile t = tiles[tix];
   const SceneDev& sd = sds[t.scene];
@@ -453,7 +464,7 @@ __global__ void __launch_bounds__(kElemTile) k_ls_energy(const Tile* tiles, cons
   const Real h2 = Real(sd.h2);
   const Real* cgx = static_cast<const Real*>(sd.cg_x);
   KSum en{0.0, 0.0};
-  double eabs[1] = {0.0};
+  double eabs = 0.0;
   const int idx = t.begin + threadIdx.x;
   if (t.kind == 0) {
     if (idx < t.end) {
@@ -487,56 +498,53 @@ __global__ void __launch_bounds__(kElemTile) k_ls_energy(const Tile* tiles, cons
       procrustes<Real>(R, F, Real(kProcrustesTol), kProcrustesIters);
       Real St[6];
       stretch_vec(R, F, St);
-      Real sv[6], dsv[6], la[6], si[6];
-      load6(sd.s, sd.ntp, e, sv);
+      double s64[6];
+      Real dsv[6], la[6], si[6];
+      load6d(sd.s, sd.ntp, e, s64);
       load6(sd.ds, sd.ntp, e, dsv);
       load6(sd.la, sd.ntp, e, la);
+      double si64[6];
 #pragma unroll
-      for (int i = 0; i < 6; ++i) si[i] = Real(double(sv[i]) + alpha * double(dsv[i]));
-      Real psi = material_psi<Real>(in.mat, in.mu, in.lam, si);
+      for (int i = 0; i < 6; ++i) {
+        si64[i] = s64[i] + alpha * double(dsv[i]);
+        si[i] = Real(si64[i]);
+      }
+      const double psi = double(material_psi<Real>(in.mat, in.mu, in.lam, si));
       double con = 0;
 #pragma unroll
-      for (int i = 0; i < 6; ++i) con += double(la[i]) * (i < 3 ? 1.0 : 2.0) * double(St[i] - si[i]);
-      en.add(double(h2) * double(in.vol) * double(psi));
-      en.add(-double(in.vol) * con);
-      eabs[0] = fabs(double(h2) * double(in.vol) * double(psi)) + fabs(double(in.vol) * con);
+      for (int i = 0; i < 6; ++i) con += double(la[i]) * (i < 3 ? 1.0 : 2.0) * (double(St[i]) - si64[i]);
+      const double e1 = double(h2) * double(in.vol) * psi, e2 = double(in.vol) * con;
+      en.add(e1);
+      en.add(-e2);
+      eabs = fabs(e1) + fabs(e2);
     }
-  } else {
-    if (idx < t.end) {
-      const int a = idx;
-      const double* x = sd.x;
-      const double* xt = sd.xt;
-      double Md[3] = {0, 0, 0};
-      for (int q = sd.m_ptr[a]; q < sd.m_ptr[a + 1]; ++q) {
-        const int b = sd.m_col[q];
-        const double m = sd.m_val[q];
-        const int fb = sd.free_map[b];
-#pragma unroll
-        for (int c = 0; c < 3; ++c)
-          Md[c] += m * (x[3 * b + c] + (fb >= 0 ? alpha * double(cgx[3 * fb + c]) : 0.0) - xt[3 * b + c]);
-      }
-      const int fa = sd.free_map[a];
-      double e2 = 0;
+  } else if (idx < t.end) {
+    const int a = idx;
+    const double* x = sd.x;
+    const double* xt = sd.xt;
+    double Md[3] = {0, 0, 0};
+    for (int q = sd.m_ptr[a]; q < sd.m_ptr[a + 1]; ++q) {
+      const int b = sd.m_col[q];
+      const double m = sd.m_val[q];
+      const int fb = sd.free_map[b];
 #pragma unroll
       for (int c = 0; c < 3; ++c)
-        e2 += (x[3 * a + c] + (fa >= 0 ? alpha * double(cgx[3 * fa + c]) : 0.0) - xt[3 * a + c]) * Md[c];
-      en.add(0.5 * e2);
+        Md[c] += m * (x[3 * b + c] + (fb >= 0 ? alpha * double(cgx[3 * fb + c]) : 0.0) - xt[3 * b + c]);
     }
+    const int fa = sd.free_map[a];
+    double e2 = 0;
+#pragma unroll
+    for (int c = 0; c < 3; ++c)
+      e2 += (x[3 * a + c] + (fa >= 0 ? alpha * double(cgx[3 * fa + c]) : 0.0) - xt[3 * a + c]) * Md[c];
+    en.add(0.5 * e2);
   }
-  double* part = partials + (size_t)tix * kNumPartials;
-  block_ksum(en, part);
-  block_partial<1>(eabs, 1, part + 2);
-  if (last_tile(&sc->ctr[TB_EV], sd.tile_count[TB_EV])) {
+  put_ksum(en, partials, pstride, 0, tix);
+  put_sum(eabs, partials, pstride, 2, tix);
+  if (last_tile(sd, TB_EV, tix)) {
+    const int t0 = sd.tile_first[TB_EV], tc = sd.tile_count[TB_EV];
+    const double fx = scene_ksum(partials, pstride, 0, t0, tc);
+    const double eab = scene_sum(partials, pstride, 2, t0, tc);
     if (threadIdx.x == 0) {
-      KSum E{0.0, 0.0};
-      double eab = 0;
-      const int t0 = sd.tile_first[TB_EV];
-      for (int k = 0; k < sd.tile_count[TB_EV]; ++k) {
-        const double* p = partials + (size_t)(t0 + k) * kNumPartials;
-        E.merge(KSum{ld_partial(p), ld_partial(p + 1)});
-        eab += ld_partial(p + 2);
-      }
-      const double fx = E.value();
       sc->E_trial = fx;
       // Armijo with c = 0 (newton_optimizer.cpp:58).  With FP32 element
       // energies a difference below their rounding bound is not a decision
@@ -562,7 +570,8 @@ __global__ void __launch_bounds__(kElemTile) k_ls_energy(const Tile* tiles, cons
 // ---------------------------------------------------------------- apply ---
 template <typename Real>
 __global__ void __launch_bounds__(kElemTile) k_apply(const Tile* tiles, const SceneDev* sds,
-                                                     double* partials, BatchCounters* ctrs) {
+                                                     double* partials, int pstride,
+                                                     BatchCounters* ctrs) {
   const int tix = blockIdx.x;
   const Tile t = tiles[tix];
   const SceneDev& sd = sds[t.scene];
@@ -572,12 +581,11 @@ __global__ void __launch_bounds__(kElemTile) k_apply(const Tile* tiles, const Sc
   if (sc->ls_ok && idx < t.end) {
     const double alpha = sc->alpha_ls;
     if (t.kind == 0) {
-      Real* s = static_cast<Real*>(sd.s);
       const Real* ds = static_cast<const Real*>(sd.ds);
 #pragma unroll
       for (int i = 0; i < 6; ++i) {
         const size_t k = (size_t)i * sd.ntp + idx;
-        s[k] = Real(double(s[k]) + alpha * double(ds[k]));
+        sd.s[k] += alpha * double(ds[k]);
       }
     } else {
       const int f = sd.free_map[idx];
@@ -588,7 +596,7 @@ __global__ void __launch_bounds__(kElemTile) k_apply(const Tile* tiles, const Sc
       }
     }
   }
-  if (last_tile(&sc->ctr[TB_EV], sd.tile_count[TB_EV])) {
+  if (last_tile(sd, TB_EV, tix)) {
     if (threadIdx.x == 0) {
       sc->ls_total += sc->ls_iter;
       if (!sc->ls_ok && sc->status == 0) sc->status = 6;  // MFEM_ERR_LS_FAILED
@@ -632,9 +640,9 @@ __global__ void __launch_bounds__(kElemTile) k_step_begin(const Tile* tiles, con
 // Pins move to their post-BC-step positions, BDF<I>::update (BDF.cpp:11-21),
 // lambda = 0 (MixedStretch::post_solve, mixed_stretch.cpp:306-309).
 template <typename Real>
-__global__ void __launch_bounds__(kElemTile) k_step_end(const Tile* tiles, const SceneDev* sds,
-                                                        double* partials) {
-  const Tile t = tiles[blockIdx.x];
+__global__ void __launch_bounds__(kElemTile) k_step_end(const Tile* tiles, const SceneDev* sds) {
+  const int tix = blockIdx.x;
+  const Tile t = tiles[tix];
   const SceneDev& sd = sds[t.scene];
   SceneScalars* sc = sd.sc;
   const int idx = t.begin + threadIdx.x;
@@ -651,7 +659,7 @@ __global__ void __launch_bounds__(kElemTile) k_step_end(const Tile* tiles, const
       const size_t n3 = 3 * (size_t)sd.nv;
 #pragma unroll
       for (int c = 0; c < 3; ++c) {
-        double xv = (f < 0) ? sd.pin_pos[3 * (-1 - f) + c] : sd.x[3 * a + c];
+        const double xv = (f < 0) ? sd.pin_pos[3 * (-1 - f) + c] : sd.x[3 * a + c];
         double wx = 0;
         for (int i = 0; i < I; ++i) wx += sd.bdf_alpha[i] * sd.xhist[((head + i) % I) * n3 + 3 * a + c];
         const double vnew = (xv - wx) / sd.dt;
@@ -661,7 +669,7 @@ __global__ void __launch_bounds__(kElemTile) k_step_end(const Tile* tiles, const
       }
     }
   }
-  if (last_tile(&sc->ctr[TB_EV], sd.tile_count[TB_EV])) {
+  if (last_tile(sd, TB_EV, tix)) {
     if (threadIdx.x == 0) sc->hist_head = nhead;
   }
 }
@@ -674,7 +682,7 @@ void set_smem(K kernel, int bytes) {
 }  // namespace
 
 int elem_update_smem_bytes(int fp64) {
-  return kElemTile * kRecSmem * (fp64 ? 8 : 4);
+  return kElemTile * (rec_bytes(fp64 ? 8 : 4) / 4 + 1) * 4;
 }
 
 void configure_kernels() {
@@ -720,13 +728,15 @@ void launch_elem_update(const Launch& L, const ElemDebug* dbg) {
   } while (0)
 
 void launch_local_solve(const Launch& L) {
-  MFEM_LAUNCH_EV(k_local_solve, L.tiles, L.sds, L.partials, L.counters);
+  MFEM_LAUNCH_EV(k_local_solve, L.tiles, L.sds, L.partials, L.pstride, L.counters);
 }
 void launch_ls_energy(const Launch& L) {
-  MFEM_LAUNCH_EV(k_ls_energy, L.tiles, L.sds, L.partials, L.counters);
+  MFEM_LAUNCH_EV(k_ls_energy, L.tiles, L.sds, L.partials, L.pstride, L.counters);
 }
-void launch_apply(const Launch& L) { MFEM_LAUNCH_EV(k_apply, L.tiles, L.sds, L.partials, L.counters); }
+void launch_apply(const Launch& L) {
+  MFEM_LAUNCH_EV(k_apply, L.tiles, L.sds, L.partials, L.pstride, L.counters);
+}
 void launch_step_begin(const Launch& L) { MFEM_LAUNCH_EV(k_step_begin, L.tiles, L.sds); }
-void launch_step_end(const Launch& L) { MFEM_LAUNCH_EV(k_step_end, L.tiles, L.sds, L.partials); }
+void launch_step_end(const Launch& L) { MFEM_LAUNCH_EV(k_step_end, L.tiles, L.sds); }
 
 }  // namespace mfem_gpu

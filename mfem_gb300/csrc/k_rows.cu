@@ -38,8 +38,9 @@ __device__ __forceinline__ int rec_offset(int i, int j, int l, int m) {
 constexpr int kMaxOut = 8;  // outputs per lane per chunk (32*8 = 256 = 28 blocks)
 
 template <typename Real>
-__global__ void __launch_bounds__(32 * kRowTile) k_assemble(const Tile* tiles, const SceneDev* sds,
-                                                            double* partials, BatchCounters* ctrs) {
+__global__ void __launch_bounds__(256) k_assemble(const Tile* tiles, const SceneDev* sds,
+                                                            double* partials, int pstride,
+                                                            BatchCounters* ctrs) {
   __shared__ unsigned short offtab[4][4][9];
   for (int k = threadIdx.x; k < 144; k += blockDim.x) {
     const int i = k / 36, j = (k / 9) % 4, rc = k % 9;
@@ -52,10 +53,11 @@ __global__ void __launch_bounds__(32 * kRowTile) k_assemble(const Tile* tiles, c
   SceneScalars* sc = sd.sc;
   if (!sc->newton_active) return;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int row = t.begin + warp;
   double rn2 = 0.0;
+  for (int rr = warp; rr < kRowTile; rr += 8) {
+  const int row = t.begin + rr;
   if (row < t.end) {
-    const Real* rec = static_cast<const Real*>(sd.rec);
+    constexpr int RB = sizeof(Real);
     const int rb = sd.b_ptr[row], nb = sd.b_ptr[row + 1] - rb;
     const int ib = sd.inc_ptr[row], ie = sd.inc_ptr[row + 1];
     const int v = sd.free_vert[row];
@@ -69,9 +71,10 @@ __global__ void __launch_bounds__(32 * kRowTile) k_assemble(const Tile* tiles, c
     }
     for (int k = ib + lane; k < ie; k += 32) {
       const int2 ic = sd.inc[k];
-      const Real* rp = rec + (size_t)ic.x * kRec + 78 + 3 * (ic.y & 3);
+      const double* rp = reinterpret_cast<const double*>(sd.rec + (size_t)ic.x * rec_bytes(RB) +
+                                                         rec_rhs_offset(RB)) + 3 * (ic.y & 3);
 #pragma unroll
-      for (int c = 0; c < 3; ++c) acc[c] += double(rp[c]);
+      for (int c = 0; c < 3; ++c) acc[c] += rp[c];
     }
 #pragma unroll
     for (int c = 0; c < 3; ++c)
@@ -81,7 +84,7 @@ __global__ void __launch_bounds__(32 * kRowTile) k_assemble(const Tile* tiles, c
       Real* rhs = static_cast<Real*>(sd.rhs);
 #pragma unroll
       for (int c = 0; c < 3; ++c) rhs[3 * row + c] = Real(acc[c]);
-      rn2 = acc[0] * acc[0] + acc[1] * acc[1] + acc[2] * acc[2];
+      rn2 += acc[0] * acc[0] + acc[1] * acc[1] + acc[2] * acc[2];
     }
     // ---- block values: each lane owns outputs o = base + lane + 32*kk
     Real* val = static_cast<Real*>(sd.b_val) + (size_t)rb * 9;
@@ -101,7 +104,7 @@ __global__ void __launch_bounds__(32 * kRowTile) k_assemble(const Tile* tiles, c
         const int i = ic.y & 3;
         const int s0 = (ic.y >> 2) & 127, s1 = (ic.y >> 9) & 127, s2 = (ic.y >> 16) & 127,
                   s3 = (ic.y >> 23) & 127;
-        const Real* rp = rec + (size_t)ic.x * kRec;
+        const Real* rp = reinterpret_cast<const Real*>(sd.rec + (size_t)ic.x * rec_bytes(RB));
 #pragma unroll
         for (int kk = 0; kk < kMaxOut; ++kk) {
           const int q = oq[kk];
@@ -161,14 +164,11 @@ __global__ void __launch_bounds__(32 * kRowTile) k_assemble(const Tile* tiles, c
       }
     }
   }
-  double v1[1] = {rn2};
-  double* part = partials + (size_t)tix * kNumPartials;
-  block_partial<1>(v1, 1, part);
-  if (last_tile(&sc->ctr[TB_ROW], sd.tile_count[TB_ROW])) {
+  }
+  put_sum(rn2, partials, pstride, 0, tix);
+  if (last_tile(sd, TB_ROW, tix)) {
+    const double s = scene_sum(partials, pstride, 0, sd.tile_first[TB_ROW], sd.tile_count[TB_ROW]);
     if (threadIdx.x == 0) {
-      double s = 0;
-      const int t0 = sd.tile_first[TB_ROW];
-      for (int k = 0; k < sd.tile_count[TB_ROW]; ++k) s += ld_partial(partials + (size_t)(t0 + k) * kNumPartials);
       const double rn = sqrt(s);
       if (sc->newton_iter == 0) sc->rhs_norm0 = rn;
       sc->rhs_norm = rn;
@@ -191,72 +191,68 @@ __global__ void __launch_bounds__(32 * kRowTile) k_assemble(const Tile* tiles, c
 }
 
 // ---------------------------------------------------------------- PCG ---
-// Thread (row, lane_r): lane_r < 3 handles component lane_r of the row.
+// z = D^{-1} r for one row (Jacobi or 3x3 block Jacobi).
 template <typename Real>
-__device__ __forceinline__ void apply_prec(const SceneDev& sd, int row, int comp, Real rv,
-                                           const unsigned mask, Real& z) {
+__device__ __forceinline__ void apply_prec(const SceneDev& sd, int row, const Real r[3], Real z[3]) {
   const Real* dinv = static_cast<const Real*>(sd.dinv);
   if (sd.block_jacobi) {
-    // gather the 3 components of r within the row group (lanes 0..2 of it)
-    const int base = (threadIdx.x & 31) & ~(kCgTpr - 1);
-    Real r0 = __shfl_sync(mask, rv, base + 0);
-    Real r1 = __shfl_sync(mask, rv, base + 1);
-    Real r2 = __shfl_sync(mask, rv, base + 2);
-    const Real* Di = dinv + 9 * row + 3 * comp;
-    z = Di[0] * r0 + Di[1] * r1 + Di[2] * r2;
+    const Real* D = dinv + 9 * (size_t)row;
+#pragma unroll
+    for (int c = 0; c < 3; ++c) z[c] = D[3 * c] * r[0] + D[3 * c + 1] * r[1] + D[3 * c + 2] * r[2];
   } else {
-    z = dinv[3 * row + comp] * rv;
+#pragma unroll
+    for (int c = 0; c < 3; ++c) z[c] = dinv[3 * (size_t)row + c] * r[c];
   }
 }
 
+// r = b, z = D^{-1} b, x = 0, rz; one thread per row.
 template <typename Real>
-__global__ void __launch_bounds__(kCgRows * kCgTpr) k_cg_init(const Tile* tiles, const SceneDev* sds,
-                                                              double* partials, BatchCounters* ctrs) {
+__global__ void __launch_bounds__(kCgThreads) k_cg_init(const Tile* tiles, const SceneDev* sds,
+                                                        double* partials, int pstride,
+                                                        BatchCounters* ctrs) {
   const int tix = blockIdx.x;
   const Tile t = tiles[tix];
   const SceneDev& sd = sds[t.scene];
   SceneScalars* sc = sd.sc;
   if (!sc->newton_active) return;
-  const int row = t.begin + threadIdx.x / kCgTpr;
-  const int comp = threadIdx.x % kCgTpr;
-  const bool on = (row < t.end) && comp < 3;
-  double v[2] = {0.0, 0.0};
-  Real rv = 0;
-  if (on) rv = static_cast<const Real*>(sd.rhs)[3 * row + comp];
-  Real z = 0;
-  // all lanes take part in the shuffles of the block preconditioner
-  apply_prec<Real>(sd, row < t.end ? row : t.begin, comp < 3 ? comp : 0, rv, 0xffffffffu, z);
-  if (on) {
-    static_cast<Real*>(sd.cg_r)[3 * row + comp] = rv;
-    static_cast<Real*>(sd.cg_z)[3 * row + comp] = z;
-    static_cast<Real*>(sd.cg_x)[3 * row + comp] = Real(0);
-    v[0] = double(rv) * double(rv);
-    v[1] = double(rv) * double(z);
+  double rr = 0.0, rz = 0.0;
+  const int row = t.begin + threadIdx.x;
+  if (row < t.end) {
+    const Real* b = static_cast<const Real*>(sd.rhs) + 3 * (size_t)row;
+    Real r[3] = {b[0], b[1], b[2]}, z[3];
+    apply_prec<Real>(sd, row, r, z);
+    Real* pr = static_cast<Real*>(sd.cg_r) + 3 * (size_t)row;
+    Real* pz = static_cast<Real*>(sd.cg_z) + 3 * (size_t)row;
+    Real* px = static_cast<Real*>(sd.cg_x) + 3 * (size_t)row;
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+      pr[c] = r[c];
+      pz[c] = z[c];
+      px[c] = Real(0);
+      rr += double(r[c]) * double(r[c]);
+      rz += double(r[c]) * double(z[c]);
+    }
   }
-  double* part = partials + (size_t)tix * kNumPartials;
-  block_partial<2>(v, 2, part);
-  if (last_tile(&sc->ctr[TB_CG], sd.tile_count[TB_CG])) {
+  put_sum(rr, partials, pstride, 0, tix);
+  put_sum(rz, partials, pstride, 1, tix);
+  if (last_tile(sd, TB_CG, tix)) {
+    const int t0 = sd.tile_first[TB_CG], tc = sd.tile_count[TB_CG];
+    const double rrs = scene_sum(partials, pstride, 0, t0, tc);
+    const double rzs = scene_sum(partials, pstride, 1, t0, tc);
     if (threadIdx.x == 0) {
-      double rr = 0, rz = 0;
-      const int t0 = sd.tile_first[TB_CG];
-      for (int k = 0; k < sd.tile_count[TB_CG]; ++k) {
-        const double* p = partials + (size_t)(t0 + k) * kNumPartials;
-        rr += ld_partial(p);
-        rz += ld_partial(p + 1);
-      }
-      sc->cg_rhs_norm2 = rr;
+      sc->cg_rhs_norm2 = rrs;
       sc->cg_iter = 0;
       sc->beta = 0.0;
-      sc->rz = rz;
+      sc->rz = rzs;
       sc->cg_err = 0.0;
-      if (rr == 0.0) {
+      if (rrs == 0.0) {
         sc->cg_active = 0;
       } else {
-        const double thr = fmax(sd.cg_tol * sd.cg_tol * rr, DBL_MIN);
+        const double thr = fmax(sd.cg_tol * sd.cg_tol * rrs, DBL_MIN);
         sc->cg_threshold = thr;
-        if (rr < thr || sd.max_cg <= 0) {
+        if (rrs < thr || sd.max_cg <= 0) {
           sc->cg_active = 0;
-          sc->cg_err = sqrt(rr / rr);
+          sc->cg_err = 1.0;
         } else {
           sc->cg_active = 1;
           atomicAdd(&ctrs->cg_active, 1);
@@ -268,9 +264,12 @@ __global__ void __launch_bounds__(kCgRows * kCgTpr) k_cg_init(const Tile* tiles,
 
 // Ap = A p with p = z + beta p_prev formed on the fly (so the p update needs
 // no kernel of its own); p is written to the other buffer of the pair.
+// kCgTpr lanes share a row; the 32 row groups of a tile walk its rows with
+// stride 32 so that each pass reads a contiguous run of block rows.
 template <typename Real>
-__global__ void __launch_bounds__(kCgRows * kCgTpr) k_cg_spmv(const Tile* tiles, const SceneDev* sds,
-                                                              double* partials, BatchCounters* ctrs) {
+__global__ void __launch_bounds__(kCgThreads) k_cg_spmv(const Tile* tiles, const SceneDev* sds,
+                                                        double* partials, int pstride,
+                                                        BatchCounters* ctrs) {
   const int tix = blockIdx.x;
   const Tile t = tiles[tix];
   const SceneDev& sd = sds[t.scene];
@@ -283,54 +282,54 @@ __global__ void __launch_bounds__(kCgRows * kCgTpr) k_cg_spmv(const Tile* tiles,
   const Real* pin = static_cast<const Real*>(sd.cg_p[(it + 1) & 1]);
   Real* pout = static_cast<Real*>(sd.cg_p[it & 1]);
   const Real* val = static_cast<const Real*>(sd.b_val);
-  const int row = t.begin + threadIdx.x / kCgTpr;
-  const int lr = threadIdx.x % kCgTpr;
-  Real acc[3] = {0, 0, 0};
-  const bool valid = row < t.end;
-  if (valid) {
-    const int q1 = sd.b_ptr[row + 1];
-    for (int q = sd.b_ptr[row] + lr; q < q1; q += kCgTpr) {
-      const int col = sd.b_col[q];
-      Real p[3];
+  Real* Ap = static_cast<Real*>(sd.cg_Ap);
+  const int grp = threadIdx.x / kCgTpr, lr = threadIdx.x % kCgTpr;
+  double pAp = 0.0;
+  constexpr int kGroups = kCgThreads / kCgTpr;
+#pragma unroll 2
+  for (int rr = grp; rr < kCgRows; rr += kGroups) {
+    const int row = t.begin + rr;
+    Real acc[3] = {0, 0, 0};
+    const bool valid = row < t.end;
+    if (valid) {
+      const int q1 = sd.b_ptr[row + 1];
+      for (int q = sd.b_ptr[row] + lr; q < q1; q += kCgTpr) {
+        const int col = sd.b_col[q];
+        Real p[3];
 #pragma unroll
-      for (int c = 0; c < 3; ++c) p[c] = first ? z[3 * col + c] : z[3 * col + c] + beta * pin[3 * col + c];
-      const Real* b = val + 9 * (size_t)q;
+        for (int c = 0; c < 3; ++c) p[c] = first ? z[3 * col + c] : z[3 * col + c] + beta * pin[3 * col + c];
+        const Real* b = val + 9 * (size_t)q;
 #pragma unroll
-      for (int r = 0; r < 3; ++r) acc[r] += b[3 * r] * p[0] + b[3 * r + 1] * p[1] + b[3 * r + 2] * p[2];
+        for (int r = 0; r < 3; ++r) acc[r] += b[3 * r] * p[0] + b[3 * r + 1] * p[1] + b[3 * r + 2] * p[2];
+      }
+    }
+#pragma unroll
+    for (int r = 0; r < 3; ++r)
+#pragma unroll
+      for (int off = kCgTpr / 2; off > 0; off >>= 1)
+        acc[r] += __shfl_down_sync(0xffffffffu, acc[r], off, kCgTpr);
+    if (valid && lr == 0) {
+#pragma unroll
+      for (int c = 0; c < 3; ++c) {
+        const Real p = first ? z[3 * row + c] : z[3 * row + c] + beta * pin[3 * row + c];
+        pout[3 * row + c] = p;
+        Ap[3 * row + c] = acc[c];
+        pAp += double(p) * double(acc[c]);
+      }
     }
   }
-#pragma unroll
-  for (int r = 0; r < 3; ++r)
-#pragma unroll
-    for (int off = kCgTpr / 2; off > 0; off >>= 1) acc[r] += __shfl_down_sync(0xffffffffu, acc[r], off, kCgTpr);
-  double v[1] = {0.0};
-  if (valid && lr == 0) {
-    Real* Ap = static_cast<Real*>(sd.cg_Ap);
-    double pAp = 0;
-#pragma unroll
-    for (int c = 0; c < 3; ++c) {
-      const Real p = first ? z[3 * row + c] : z[3 * row + c] + beta * pin[3 * row + c];
-      pout[3 * row + c] = p;
-      Ap[3 * row + c] = acc[c];
-      pAp += double(p) * double(acc[c]);
-    }
-    v[0] = pAp;
-  }
-  double* part = partials + (size_t)tix * kNumPartials;
-  block_partial<1>(v, 1, part);
-  if (last_tile(&sc->ctr[TB_CG], sd.tile_count[TB_CG])) {
-    if (threadIdx.x == 0) {
-      double s = 0;
-      const int t0 = sd.tile_first[TB_CG];
-      for (int k = 0; k < sd.tile_count[TB_CG]; ++k) s += ld_partial(partials + (size_t)(t0 + k) * kNumPartials);
-      sc->alpha = sc->rz / s;
-    }
+  put_sum(pAp, partials, pstride, 0, tix);
+  if (last_tile(sd, TB_CG, tix)) {
+    const double s = scene_sum(partials, pstride, 0, sd.tile_first[TB_CG], sd.tile_count[TB_CG]);
+    if (threadIdx.x == 0) sc->alpha = sc->rz / s;
   }
 }
 
+// x += alpha p, r -= alpha Ap, z = D^{-1} r, then beta and the stopping test.
 template <typename Real>
-__global__ void __launch_bounds__(kCgRows * kCgTpr) k_cg_update(const Tile* tiles, const SceneDev* sds,
-                                                                double* partials, BatchCounters* ctrs) {
+__global__ void __launch_bounds__(kCgThreads) k_cg_update(const Tile* tiles, const SceneDev* sds,
+                                                          double* partials, int pstride,
+                                                          BatchCounters* ctrs) {
   const int tix = blockIdx.x;
   const Tile t = tiles[tix];
   const SceneDev& sd = sds[t.scene];
@@ -338,52 +337,51 @@ __global__ void __launch_bounds__(kCgRows * kCgTpr) k_cg_update(const Tile* tile
   if (!sc->cg_active) return;
   const int it = sc->cg_iter;
   const Real alpha = Real(sc->alpha);
-  const Real* p = static_cast<const Real*>(sd.cg_p[it & 1]);
-  const int row = t.begin + threadIdx.x / kCgTpr;
-  const int comp = threadIdx.x % kCgTpr;
-  const bool on = (row < t.end) && comp < 3;
-  double v[2] = {0.0, 0.0};
-  Real rv = 0;
-  if (on) {
-    const int k = 3 * row + comp;
-    Real* x = static_cast<Real*>(sd.cg_x);
-    Real* r = static_cast<Real*>(sd.cg_r);
-    x[k] += alpha * p[k];
-    rv = r[k] - alpha * static_cast<const Real*>(sd.cg_Ap)[k];
-    r[k] = rv;
-    v[0] = double(rv) * double(rv);
+  double rr = 0.0, rz = 0.0;
+  const int row = t.begin + threadIdx.x;
+  if (row < t.end) {
+    const size_t k = 3 * (size_t)row;
+    const Real* p = static_cast<const Real*>(sd.cg_p[it & 1]) + k;
+    const Real* Ap = static_cast<const Real*>(sd.cg_Ap) + k;
+    Real* x = static_cast<Real*>(sd.cg_x) + k;
+    Real* r = static_cast<Real*>(sd.cg_r) + k;
+    Real rv[3], z[3];
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+      x[c] += alpha * p[c];
+      rv[c] = r[c] - alpha * Ap[c];
+      r[c] = rv[c];
+      rr += double(rv[c]) * double(rv[c]);
+    }
+    apply_prec<Real>(sd, row, rv, z);
+    Real* pz = static_cast<Real*>(sd.cg_z) + k;
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+      pz[c] = z[c];
+      rz += double(rv[c]) * double(z[c]);
+    }
   }
-  Real z = 0;
-  apply_prec<Real>(sd, row < t.end ? row : t.begin, comp < 3 ? comp : 0, rv, 0xffffffffu, z);
-  if (on) {
-    static_cast<Real*>(sd.cg_z)[3 * row + comp] = z;
-    v[1] = double(rv) * double(z);
-  }
-  double* part = partials + (size_t)tix * kNumPartials;
-  block_partial<2>(v, 2, part);
-  if (last_tile(&sc->ctr[TB_CG], sd.tile_count[TB_CG])) {
+  put_sum(rr, partials, pstride, 0, tix);
+  put_sum(rz, partials, pstride, 1, tix);
+  if (last_tile(sd, TB_CG, tix)) {
+    const int t0 = sd.tile_first[TB_CG], tc = sd.tile_count[TB_CG];
+    const double rrs = scene_sum(partials, pstride, 0, t0, tc);
+    const double rzs = scene_sum(partials, pstride, 1, t0, tc);
     if (threadIdx.x == 0) {
-      double rr = 0, rz = 0;
-      const int t0 = sd.tile_first[TB_CG];
-      for (int k = 0; k < sd.tile_count[TB_CG]; ++k) {
-        const double* pp = partials + (size_t)(t0 + k) * kNumPartials;
-        rr += ld_partial(pp);
-        rz += ld_partial(pp + 1);
-      }
-      sc->cg_err = sqrt(rr / sc->cg_rhs_norm2);
+      sc->cg_err = sqrt(rrs / sc->cg_rhs_norm2);
       bool stop = false;
-      if (rr < sc->cg_threshold) {
+      if (rrs < sc->cg_threshold) {
         stop = true;
       } else {
-        sc->beta = rz / sc->rz;
-        sc->rz = rz;
+        sc->beta = rzs / sc->rz;
+        sc->rz = rzs;
         sc->cg_iter = it + 1;
         if (it + 1 >= sd.max_cg) {
           stop = true;
           sc->cg_status = 5;  // MFEM_ERR_CG_MAXITER
         }
       }
-      if (!(rr == rr)) {
+      if (!(rrs == rrs)) {
         stop = true;
         sc->status = 4;
       }
@@ -434,15 +432,17 @@ __global__ void k_scalars_begin(const SceneDev* sds, int n, BatchCounters* ctrs)
   do {                                                                                       \
     if (L.ntiles == 0) return;                                                               \
     if (L.fp64)                                                                              \
-      kern<double><<<L.ntiles, threads, 0, L.stream>>>(L.tiles, L.sds, L.partials, L.counters); \
+      kern<double><<<L.ntiles, threads, 0, L.stream>>>(L.tiles, L.sds, L.partials, L.pstride,   \
+                                                       L.counters);                          \
     else                                                                                     \
-      kern<float><<<L.ntiles, threads, 0, L.stream>>>(L.tiles, L.sds, L.partials, L.counters);  \
+      kern<float><<<L.ntiles, threads, 0, L.stream>>>(L.tiles, L.sds, L.partials, L.pstride,    \
+                                                      L.counters);                           \
   } while (0)
 
-void launch_assemble(const Launch& L) { MFEM_LAUNCH_ROWS(k_assemble, 32 * kRowTile); }
-void launch_cg_init(const Launch& L) { MFEM_LAUNCH_ROWS(k_cg_init, kCgRows * kCgTpr); }
-void launch_cg_spmv(const Launch& L) { MFEM_LAUNCH_ROWS(k_cg_spmv, kCgRows * kCgTpr); }
-void launch_cg_update(const Launch& L) { MFEM_LAUNCH_ROWS(k_cg_update, kCgRows * kCgTpr); }
+void launch_assemble(const Launch& L) { MFEM_LAUNCH_ROWS(k_assemble, 256); }
+void launch_cg_init(const Launch& L) { MFEM_LAUNCH_ROWS(k_cg_init, kCgThreads); }
+void launch_cg_spmv(const Launch& L) { MFEM_LAUNCH_ROWS(k_cg_spmv, kCgThreads); }
+void launch_cg_update(const Launch& L) { MFEM_LAUNCH_ROWS(k_cg_update, kCgThreads); }
 
 void launch_scalars_begin(const Launch& L, int nscenes) {
   k_scalars_begin<<<1, 128, 0, L.stream>>>(L.sds, nscenes, L.counters);

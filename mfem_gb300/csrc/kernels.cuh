@@ -24,11 +24,16 @@ enum TableKind {
 
 constexpr int kElemTile = 128;   // elements per element tile (one thread each)
 constexpr int kVertTile = 128;   // vertices per vertex tile (TB_EV: same block size)
-constexpr int kRowTile = 8;      // rows per assembly tile (one warp each)
+constexpr int kRowTile = 32;     // rows per assembly tile (8 warps, 4 rows each)
 constexpr int kCgTpr = 8;        // threads per row in the PCG SpMV
-constexpr int kCgRows = 32;      // rows per PCG tile (kCgRows*kCgTpr threads)
-constexpr int kRec = 92;         // per-element record: 78 Aloc (upper blocks) + 12 rhs + 2 pad
-constexpr int kRecSmem = 93;     // odd shared-memory stride of the record
+constexpr int kCgThreads = 256;  // threads per PCG tile
+constexpr int kCgRows = 256;     // rows per PCG tile
+constexpr int kTicketGroup = 32; // tiles per first-level ticket counter
+// Per-element record written by K1 and gathered by the assembly: the 78
+// upper-triangle entries of the 12x12 element block (Real) followed, at a
+// 16-byte boundary, by the element's 12 right-hand-side shares (double).
+__host__ __device__ constexpr int rec_rhs_offset(int real_bytes) { return real_bytes == 4 ? 320 : 624; }
+__host__ __device__ constexpr int rec_bytes(int real_bytes) { return rec_rhs_offset(real_bytes) + 96; }
 constexpr int kMaxRowBlocks = 126;  // 7-bit column slots in the incidence code
 constexpr int kNumPartials = 8;  // doubles per tile partial
 
@@ -99,11 +104,11 @@ struct SceneDev {
   const int8_t* mat; // ntp or null
   // element state (Real SoA, stride ntp)
   void* quat;        // 4 x ntp
-  void* s;           // 6 x ntp
+  double* s;         // 6 x ntp  mixed stretch variable (FP64 in both paths)
   void* la;          // 6 x ntp
-  void* S;           // 6 x ntp  stretch of the current x (K1 output)
+  void* dS;          // 6 x ntp  S(x) - s of the current x (K1 output)
   void* ds;          // 6 x ntp
-  void* rec;         // nt x kRec  (AoS element records)
+  unsigned char* rec;  // nt x rec_bytes  (AoS element records)
   // vertices (double)
   double* x;         // 3 nv current positions; pinned entries hold b
   double* xt;        // 3 nv  x_tilde + h^2 f_ext (the inertial target)
@@ -134,6 +139,8 @@ struct SceneDev {
   // tiles of this scene in each table
   int tile_first[TB_COUNT];
   int tile_count[TB_COUNT];
+  int gmax;                // ticket groups per table (capacity of gctr rows)
+  unsigned int* gctr;      // TB_COUNT x gmax first-level ticket counters
   SceneScalars* sc;
 };
 
@@ -154,7 +161,8 @@ struct Launch {
   const Tile* tiles;
   int ntiles;
   const SceneDev* sds;
-  double* partials;   // ntiles * kNumPartials
+  double* partials;   // kNumPartials x pstride (quantity-major)
+  int pstride;
   BatchCounters* counters;
   int fp64;
 };
