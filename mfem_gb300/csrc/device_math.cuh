@@ -13,6 +13,8 @@
 #include <math.h>
 #include <stdint.h>
 
+#include "df64.cuh"
+
 namespace mfem_gpu {
 
 template <typename T> struct Prec;
@@ -31,6 +33,17 @@ template <> struct Prec<double> {
   __device__ static void sincos_(double x, double* s, double* c) { sincos(x, s, c); }
   __device__ static double log_(double x) { return log(x); }
   __device__ static double exp_(double x) { return exp(x); }
+};
+
+template <> struct Prec<df64> {
+  static constexpr bool kFP64 = true;
+  __device__ static df64 sqrt_(df64 x) {
+    const float s = sqrtf(x.hi);
+    if (s == 0.f) return df64(0.f);
+    return df64(s) + (x - two_prod(s, s)) / df64(2.f * s);
+  }
+  __device__ static df64 log_(df64 x) { return df64(log(x.to_double())); }
+  __device__ static df64 exp_(df64 x) { return df64(exp(x.to_double())); }
 };
 
 #define MI __device__ __forceinline__

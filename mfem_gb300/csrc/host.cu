@@ -485,15 +485,15 @@ void layout_scene(mfem_scene* s, Arena& A) {
   D.lam = A.take_bytes(ntp * r);
   D.mat = M.mat.empty() ? nullptr : A.take<int8_t>(ntp);
   D.quat = A.take_bytes(4 * ntp * r);
-  D.s = A.take<double>(6 * ntp);
+  D.s = A.take_bytes(6 * ntp * 8);
   D.la = A.take_bytes(6 * ntp * r);
   D.dS = A.take_bytes(6 * ntp * r);
   D.ds = A.take_bytes(6 * ntp * r);
   D.rec = A.take<unsigned char>((size_t)rec_bytes((int)r) * M.nt);
-  D.x = A.take<double>(3 * (size_t)M.nv);
-  D.xt = A.take<double>(3 * (size_t)M.nv);
-  D.xhist = A.take<double>(3 * (size_t)M.nv * I);
-  D.vhist = A.take<double>(3 * (size_t)M.nv * I);
+  D.x = A.take_bytes(3 * (size_t)M.nv * 8);
+  D.xt = A.take_bytes(3 * (size_t)M.nv * 8);
+  D.xhist = A.take_bytes(3 * (size_t)M.nv * I * 8);
+  D.vhist = A.take_bytes(3 * (size_t)M.nv * I * 8);
   D.free_map = A.take<int>(M.nv);
   D.free_vert = A.take<int>(std::max(M.nf, 1));
   D.pin_vert = A.take<int>(std::max(M.npin, 1));
@@ -501,7 +501,7 @@ void layout_scene(mfem_scene* s, Arena& A) {
   D.pin_pos = s->d_pin_pos;
   D.m_ptr = A.take<int>(M.nv + 1);
   D.m_col = A.take<int>(M.m_col.size());
-  D.m_val = A.take<double>(M.m_val.size());
+  D.m_val = A.take_bytes(M.m_val.size() * r);
   D.b_ptr = A.take<int>(M.nf + 1);
   D.b_col = A.take<int>(std::max(M.nnzb, 1));
   D.b_mass = A.take_bytes(std::max(M.nnzb, 1) * r);
@@ -535,6 +535,43 @@ std::vector<T> soa(const std::vector<double>& src, int n, int ncomp, int ntp) {
   return out;
 }
 
+// Ext storage of doubles: doubles in the FP64 path, (hi, lo) float pairs
+// with hi + lo == v to ~48 bits in the mixed path; 8 bytes per value either way.
+std::vector<double> to_ext(const double* v, size_t n, int fp64) {
+  std::vector<double> out(n);
+  if (fp64) {
+    std::memcpy(out.data(), v, n * 8);
+  } else {
+    float* f = reinterpret_cast<float*>(out.data());
+    for (size_t i = 0; i < n; ++i) {
+      const float hi = float(v[i]);
+      f[2 * i] = hi;
+      f[2 * i + 1] = float(v[i] - double(hi));
+    }
+  }
+  return out;
+}
+void from_ext(const void* buf, size_t n, int fp64, double* out) {
+  if (fp64) {
+    std::memcpy(out, buf, n * 8);
+  } else {
+    const float* f = static_cast<const float*>(buf);
+    for (size_t i = 0; i < n; ++i) out[i] = double(f[2 * i]) + double(f[2 * i + 1]);
+  }
+}
+int put_ext(void* dst, const double* src, size_t n, int fp64) {
+  std::vector<double> e = to_ext(src, n, fp64);
+  CUDA_OR(cudaMemcpy(dst, e.data(), n * 8, cudaMemcpyHostToDevice), MFEM_ERR_CUDA);
+  return MFEM_OK;
+}
+int get_ext(double* dst, const void* src, size_t n, int fp64) {
+  std::vector<double> e(n);
+  CUDA_OR(cudaMemcpy(e.data(), src, n * 8, cudaMemcpyDeviceToHost), MFEM_ERR_CUDA);
+  from_ext(e.data(), n, fp64, dst);
+  return MFEM_OK;
+}
+char* byte_ptr(void* p, size_t off) { return static_cast<char*>(p) + off; }
+
 template <typename T>
 int upload_reals(void* dst, const std::vector<double>& src, size_t count, cudaStream_t st) {
   std::vector<T> tmp(count, T(0));
@@ -560,6 +597,11 @@ int upload_scene_reals(mfem_scene* s, cudaStream_t st) {
   if ((rc = put(D.vol, soa<T>(M.vol, M.nt, 1, ntp)))) return rc;
   if ((rc = put(D.mu, soa<T>(M.mu, M.nt, 1, ntp)))) return rc;
   if ((rc = put(D.lam, soa<T>(M.lam, M.nt, 1, ntp)))) return rc;
+  {
+    std::vector<T> mv(M.m_val.size());
+    for (size_t k = 0; k < mv.size(); ++k) mv[k] = T(M.m_val[k]);
+    if ((rc = put(D.m_val, mv))) return rc;
+  }
   std::vector<T> bm(std::max(M.nnzb, 1), T(0));
   for (int k = 0; k < M.nnzb; ++k) bm[k] = T(M.b_mass[k]);
   if ((rc = put(D.b_mass, bm))) return rc;
@@ -866,10 +908,12 @@ int scene_init_device(mfem_scene* s) {
   CUDA_OR(cudaMemsetAsync(s->dmem, 0, s->dbytes, st), MFEM_ERR_CUDA);
   rc |= put(D.tets, M.T.data(), sizeof(int) * M.T.size());
   if (D.mat) rc |= put(D.mat, M.mat.data(), M.mat.size());
-  rc |= put(D.x, M.V0.data(), sizeof(double) * M.V0.size());
+  const std::vector<double> x0e = to_ext(M.V0.data(), M.V0.size(), s->fp64);
+  const std::vector<double> v0e = to_ext(M.v0.data(), M.v0.size(), s->fp64);
+  rc |= put(D.x, x0e.data(), 8 * x0e.size());
   for (int i = 0; i < D.bdf_order; ++i) {
-    rc |= put(D.xhist + 3 * (size_t)M.nv * i, M.V0.data(), sizeof(double) * M.V0.size());
-    rc |= put(D.vhist + 3 * (size_t)M.nv * i, M.v0.data(), sizeof(double) * M.v0.size());
+    rc |= put(byte_ptr(D.xhist, 24 * (size_t)M.nv * i), x0e.data(), 8 * x0e.size());
+    rc |= put(byte_ptr(D.vhist, 24 * (size_t)M.nv * i), v0e.data(), 8 * v0e.size());
   }
   rc |= put(D.free_map, M.free_map.data(), sizeof(int) * M.nv);
   rc |= put(D.free_vert, M.free_vert.data(), sizeof(int) * M.nf);
@@ -877,7 +921,6 @@ int scene_init_device(mfem_scene* s) {
   rc |= put(s->d_pin_pos, s->pin_pos.data(), sizeof(double) * s->pin_pos.size());
   rc |= put(D.m_ptr, M.m_ptr.data(), sizeof(int) * M.m_ptr.size());
   rc |= put(D.m_col, M.m_col.data(), sizeof(int) * M.m_col.size());
-  rc |= put(D.m_val, M.m_val.data(), sizeof(double) * M.m_val.size());
   rc |= put(D.b_ptr, M.b_ptr.data(), sizeof(int) * M.b_ptr.size());
   rc |= put(D.b_col, M.b_col.data(), sizeof(int) * M.b_col.size());
   rc |= put(D.inc_ptr, M.inc_ptr.data(), sizeof(int) * M.inc_ptr.size());
@@ -1125,16 +1168,21 @@ int mfem_gpu_scene_get_state(mfem_scene* s, double* x, double* v, double* sv, do
   cudaStream_t st = s->solo->stream;
   CUDA_OR(cudaStreamSynchronize(st), MFEM_ERR_CUDA);
   const HostMesh& M = s->M;
-  if (x)
-    CUDA_OR(cudaMemcpy(x, s->dev.x, sizeof(double) * 3 * M.nv, cudaMemcpyDeviceToHost), MFEM_ERR_CUDA);
+  int rc;
+  if (x && (rc = get_ext(x, s->dev.x, 3 * (size_t)M.nv, s->fp64))) return rc;
   if (v) {
     SceneScalars sc;
     CUDA_OR(cudaMemcpy(&sc, s->d_sc, sizeof(sc), cudaMemcpyDeviceToHost), MFEM_ERR_CUDA);
-    CUDA_OR(cudaMemcpy(v, s->dev.vhist + 3 * (size_t)M.nv * sc.hist_head, sizeof(double) * 3 * M.nv,
-                       cudaMemcpyDeviceToHost),
-            MFEM_ERR_CUDA);
+    if ((rc = get_ext(v, byte_ptr(s->dev.vhist, 24 * (size_t)M.nv * sc.hist_head), 3 * (size_t)M.nv,
+                      s->fp64)))
+      return rc;
   }
-  if (sv) download_soa<double>(s->dev.s, M.nt, s->ntp, 6, sv, st);
+  if (sv) {
+    std::vector<double> t(6 * (size_t)s->ntp);
+    if ((rc = get_ext(t.data(), s->dev.s, t.size(), s->fp64))) return rc;
+    for (int e = 0; e < M.nt; ++e)
+      for (int k = 0; k < 6; ++k) sv[6 * (size_t)e + k] = t[(size_t)k * s->ntp + e];
+  }
   if (la) {
     if (s->fp64) download_soa<double>(s->dev.la, M.nt, s->ntp, 6, la, st);
     else download_soa<float>(s->dev.la, M.nt, s->ntp, 6, la, st);
@@ -1155,11 +1203,12 @@ int mfem_gpu_scene_set_state(mfem_scene* s, const double* x, const double* v, co
   const HostMesh& M = s->M;
   SceneScalars sc;
   CUDA_OR(cudaMemcpy(&sc, s->d_sc, sizeof(sc), cudaMemcpyDeviceToHost), MFEM_ERR_CUDA);
+  int rc;
   if (x) {
-    CUDA_OR(cudaMemcpy(s->dev.x, x, sizeof(double) * 3 * M.nv, cudaMemcpyHostToDevice), MFEM_ERR_CUDA);
-    CUDA_OR(cudaMemcpy(s->dev.xhist + 3 * (size_t)M.nv * sc.hist_head, x, sizeof(double) * 3 * M.nv,
-                       cudaMemcpyHostToDevice),
-            MFEM_ERR_CUDA);
+    if ((rc = put_ext(s->dev.x, x, 3 * (size_t)M.nv, s->fp64))) return rc;
+    if ((rc = put_ext(byte_ptr(s->dev.xhist, 24 * (size_t)M.nv * sc.hist_head), x, 3 * (size_t)M.nv,
+                      s->fp64)))
+      return rc;
     for (int p = 0; p < M.npin; ++p)
       for (int k = 0; k < 3; ++k) s->pin_pos[3 * p + k] = x[3 * M.pin_vert[p] + k];
     if (M.npin)
@@ -1167,11 +1216,15 @@ int mfem_gpu_scene_set_state(mfem_scene* s, const double* x, const double* v, co
                          cudaMemcpyHostToDevice),
               MFEM_ERR_CUDA);
   }
-  if (v)
-    CUDA_OR(cudaMemcpy(s->dev.vhist + 3 * (size_t)M.nv * sc.hist_head, v, sizeof(double) * 3 * M.nv,
-                       cudaMemcpyHostToDevice),
-            MFEM_ERR_CUDA);
-  if (sv) upload_soa<double>(s->dev.s, M.nt, s->ntp, 6, sv, st);
+  if (v && (rc = put_ext(byte_ptr(s->dev.vhist, 24 * (size_t)M.nv * sc.hist_head), v, 3 * (size_t)M.nv,
+                         s->fp64)))
+    return rc;
+  if (sv) {
+    std::vector<double> t(6 * (size_t)s->ntp, 0.0);
+    for (int e = 0; e < M.nt; ++e)
+      for (int k = 0; k < 6; ++k) t[(size_t)k * s->ntp + e] = sv[6 * (size_t)e + k];
+    if ((rc = put_ext(s->dev.s, t.data(), t.size(), s->fp64))) return rc;
+  }
   if (R) {
     std::vector<double> q(4 * (size_t)M.nt);
     for (int e = 0; e < M.nt; ++e) rot_to_quat_h(&R[9 * (size_t)e], &q[4 * (size_t)e]);
@@ -1254,7 +1307,8 @@ int mfem_gpu_scene_elem_update(mfem_scene* s, const double* x, double h, double*
   if (!s || !x) return MFEM_ERR_INVALID;
   mfem_batch* b = s->solo;
   const int nt = s->M.nt;
-  CUDA_OR(cudaMemcpy(s->dev.x, x, sizeof(double) * 3 * s->M.nv, cudaMemcpyHostToDevice), MFEM_ERR_CUDA);
+  int rc0 = put_ext(s->dev.x, x, 3 * (size_t)s->M.nv, s->fp64);
+  if (rc0) return rc0;
   // run K1 with h^2 = h*h and FP64 debug outputs
   SceneDev D = b->h_sds[0];
   D.h2 = h * h;

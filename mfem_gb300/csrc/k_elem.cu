@@ -13,8 +13,8 @@
 //                                                     BDF.cpp:6-27, displacement.cpp:32-50
 //
 // One thread per element.  Element arrays are structure-of-arrays with
-// stride ntp; the element record written by K1 (upper 12x12 blocks + rhs
-// share) is staged in shared memory and stored contiguously.
+// stride ntp.  Real is the working precision (float in the mixed path) and
+// Ext the high precision (df64 / double) of positions, s and the residual.
 #include <cfloat>
 
 #include "device_math.cuh"
@@ -25,7 +25,7 @@ namespace mfem_gpu {
 
 namespace {
 
-constexpr double kPsdTol = 1e-6;       // simple_psd_fix tolerance
+constexpr double kPsdTol = 1e-6;         // simple_psd_fix tolerance
 constexpr double kProcrustesTol = 1e-6;  // mixed_stretch.cpp:21-22
 constexpr int kProcrustesIters = 100;
 
@@ -47,6 +47,61 @@ __device__ __forceinline__ void load_elem(const SceneDev& sd, int e, ElemIn<Real
   in.mu = static_cast<const Real*>(sd.mu)[e];
   in.lam = static_cast<const Real*>(sd.lam)[e];
   in.mat = sd.material_uniform >= 0 ? sd.material_uniform : int(sd.mat[e]);
+}
+
+template <typename Real>
+__device__ __forceinline__ void dphi12(const ElemIn<Real>& in, Real* dph) {
+#pragma unroll
+  for (int c = 0; c < 3; ++c) {
+    dph[3 + c] = in.dp[c];
+    dph[6 + c] = in.dp[3 + c];
+    dph[9 + c] = in.dp[6 + c];
+    dph[c] = -(in.dp[c] + in.dp[3 + c] + in.dp[6 + c]);
+  }
+}
+
+// F = sum_k (x_k - x_0) (x) dphi_k with the edge vectors in Ext (optionally
+// at x + alpha dx), returned in Ext (when FE is given) and rounded to Real.
+template <typename Real>
+__device__ __forceinline__ void deformation_gradients(const SceneDev& sd, const ElemIn<Real>& in,
+                                                      const Real* dx, typename Ext<Real>::T alpha,
+                                                      typename Ext<Real>::T* FE, Real* F) {
+  using E = typename Ext<Real>::T;
+  const int v[4] = {in.tv.x, in.tv.y, in.tv.z, in.tv.w};
+  E p[4][3];
+#pragma unroll
+  for (int k = 0; k < 4; ++k)
+#pragma unroll
+    for (int d = 0; d < 3; ++d) p[k][d] = Ext<Real>::ld(sd.x, 3 * (size_t)v[k] + d);
+  if (dx != nullptr) {
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+      const int f = sd.free_map[v[k]];
+      if (f >= 0) {
+#pragma unroll
+        for (int d = 0; d < 3; ++d) p[k][d] = p[k][d] + alpha * E(dx[3 * f + d]);
+      }
+    }
+  }
+  E ed[9];
+#pragma unroll
+  for (int k = 1; k < 4; ++k)
+#pragma unroll
+    for (int r = 0; r < 3; ++r) ed[3 * (k - 1) + r] = p[k][r] - p[0][r];
+#pragma unroll
+  for (int c = 0; c < 3; ++c)
+#pragma unroll
+    for (int r = 0; r < 3; ++r) {
+      if (FE) {
+        const E f = ed[r] * E(in.dp[c]) + ed[3 + r] * E(in.dp[3 + c]) + ed[6 + r] * E(in.dp[6 + c]);
+        FE[r + 3 * c] = f;
+        F[r + 3 * c] = Real(Ext<Real>::to_real(f));
+      } else {
+        F[r + 3 * c] = Real(Ext<Real>::to_real(ed[r])) * in.dp[c] +
+                       Real(Ext<Real>::to_real(ed[3 + r])) * in.dp[3 + c] +
+                       Real(Ext<Real>::to_real(ed[6 + r])) * in.dp[6 + c];
+      }
+    }
 }
 
 template <typename Real>
@@ -77,6 +132,11 @@ __device__ __forceinline__ void store6(void* base, int ntp, int e, const Real* v
 #pragma unroll
   for (int i = 0; i < 6; ++i) p[i * ntp + e] = v[i];
 }
+template <typename Real>
+__device__ __forceinline__ void load6e(const SceneDev& sd, int e, typename Ext<Real>::T* v) {
+#pragma unroll
+  for (int i = 0; i < 6; ++i) v[i] = Ext<Real>::ld(sd.s, (size_t)i * sd.ntp + e);
+}
 
 // h^2 * gradient and psd-fixed h^2 * Hessian of psi at s.
 template <typename Real>
@@ -95,34 +155,7 @@ __device__ __forceinline__ void material_gH(const ElemIn<Real>& in, const Real* 
 __host__ __device__ constexpr int rec_block_start(int a) {
   return a == 0 ? 0 : (a == 1 ? 33 : (a == 2 ? 57 : 72));
 }
-__host__ __device__ constexpr int sym_idx(int r, int c) {
-  return r == 0 ? c : (r == 1 ? 2 + c : 5);
-}
-
-// Edge vectors x_k - x_0 (k = 1..3) in FP64 and F in FP64 and in Real.
-template <typename Real>
-__device__ __forceinline__ void deformation_gradients(const double* x, const ElemIn<Real>& in,
-                                                      double* F64, Real* F) {
-  const int v[4] = {in.tv.x, in.tv.y, in.tv.z, in.tv.w};
-  double ed[9];
-#pragma unroll
-  for (int k = 1; k < 4; ++k)
-#pragma unroll
-    for (int r = 0; r < 3; ++r) ed[3 * (k - 1) + r] = x[3 * v[k] + r] - x[3 * v[0] + r];
-#pragma unroll
-  for (int c = 0; c < 3; ++c)
-#pragma unroll
-    for (int r = 0; r < 3; ++r) {
-      F64[r + 3 * c] = ed[r] * double(in.dp[c]) + ed[3 + r] * double(in.dp[3 + c]) +
-                       ed[6 + r] * double(in.dp[6 + c]);
-      F[r + 3 * c] = Real(F64[r + 3 * c]);
-    }
-}
-
-__device__ __forceinline__ void load6d(const double* p, int ntp, int e, double* v) {
-#pragma unroll
-  for (int i = 0; i < 6; ++i) v[i] = p[(size_t)i * ntp + e];
-}
+__host__ __device__ constexpr int sym_idx(int r, int c) { return r == 0 ? c : (r == 1 ? 2 + c : 5); }
 
 // 32-bit-word stores into the staged element record (shared memory).
 __device__ __forceinline__ void put_word(unsigned int* w, int idx, float v) { w[idx] = __float_as_uint(v); }
@@ -131,31 +164,36 @@ __device__ __forceinline__ void put_word(unsigned int* w, int idx, double v) {
   w[idx] = (unsigned int)(b & 0xffffffffull);
   w[idx + 1] = (unsigned int)(b >> 32);
 }
+__device__ __forceinline__ void put_word(unsigned int* w, int idx, df64 v) {
+  w[idx] = __float_as_uint(v.hi);
+  w[idx + 1] = __float_as_uint(v.lo);
+}
 
 // ------------------------------------------------------------------ K0 ---
 template <typename Real>
 __global__ void __launch_bounds__(kElemTile) k_elem_init(const Tile* tiles, const SceneDev* sds) {
+  using E = typename Ext<Real>::T;
   const Tile t = tiles[blockIdx.x];
   const SceneDev& sd = sds[t.scene];
   const int e = t.begin + threadIdx.x;
   if (e >= t.end) return;
   ElemIn<Real> in;
   load_elem(sd, e, in);
-  double F64[9];
+  E FE[9];
   Real F[9], R[9];
-  deformation_gradients<Real>(sd.x, in, F64, F);
+  deformation_gradients<Real>(sd, in, nullptr, E(0), FE, F);
 #pragma unroll
   for (int i = 0; i < 9; ++i) R[i] = (i % 4 == 0) ? Real(1) : Real(0);
   int it = procrustes<Real>(R, F, Real(kProcrustesTol), kProcrustesIters);
   if (it < 0) atomicAdd(&sd.sc->procrustes_fail, 1);
   store_quat(sd, e, R);
-  double R64[9], s64[6];
+  E RE[9], sE[6];
 #pragma unroll
-  for (int i = 0; i < 9; ++i) R64[i] = double(R[i]);
-  if (!Prec<Real>::kFP64) polish_rotation(R64, F64);
-  stretch_vec(R64, F64, s64);
+  for (int i = 0; i < 9; ++i) RE[i] = E(R[i]);
+  if (!Prec<Real>::kFP64) polish_rotation(RE, FE);
+  stretch_vec(RE, FE, sE);
 #pragma unroll
-  for (int i = 0; i < 6; ++i) sd.s[(size_t)i * sd.ntp + e] = s64[i];
+  for (int i = 0; i < 6; ++i) Ext<Real>::st(sd.s, (size_t)i * sd.ntp + e, sE[i]);
   Real z[6] = {0, 0, 0, 0, 0, 0};
   store6(sd.dS, sd.ntp, e, z);
   store6(sd.la, sd.ntp, e, z);
@@ -163,19 +201,20 @@ __global__ void __launch_bounds__(kElemTile) k_elem_init(const Tile* tiles, cons
 }
 
 // ------------------------------------------------------------------ K1 ---
-// In the mixed path the rotation, S, S - s, h^2 psi'(s), q and the element
-// forces are carried in FP64 (one FP64 Newton polish of the FP32 rotation):
-// the element forces are tens of times the net residual in a loaded body, so
-// FP32 forces would floor the Newton residual near 1e-4.  The Hessian, the
-// derivative ds/dF and the element block stay in Real.
+// The residual chain (one Ext polish of the Real rotation, S, S - s,
+// h^2 psi'(s), q and the element forces) runs in Ext: in a loaded body the
+// element forces are tens of times the net residual, so Real forces would
+// floor the Newton residual near 1e-4.  The Hessian, ds/dF and the element
+// block stay in Real.
 template <typename Real, bool DBG>
 __global__ void __launch_bounds__(kElemTile)
     k_elem_update(const Tile* tiles, const SceneDev* sds, ElemDebug dbg) {
+  using E = typename Ext<Real>::T;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   unsigned int* words = reinterpret_cast<unsigned int*>(smem_raw);
   constexpr int RB = sizeof(Real);
-  constexpr int kWords = rec_bytes(RB) / 4;       // words per record
-  constexpr int kStride = kWords + 1;              // odd stride: no bank conflicts
+  constexpr int kWords = rec_bytes(RB) / 4;  // words per record
+  constexpr int kStride = kWords + 1;         // odd stride: no bank conflicts
   constexpr int kRhsWord = rec_rhs_offset(RB) / 4;
   const Tile t = tiles[blockIdx.x];
   const SceneDev& sd = sds[t.scene];
@@ -186,18 +225,16 @@ __global__ void __launch_bounds__(kElemTile)
     unsigned int* out = words + threadIdx.x * kStride;
     ElemIn<Real> in;
     load_elem(sd, e, in);
-    double s64[6];
-    load6d(sd.s, sd.ntp, e, s64);
+    E sE[6];
+    load6e<Real>(sd, e, sE);
     Real sv[6];
 #pragma unroll
-    for (int i = 0; i < 6; ++i) sv[i] = Real(s64[i]);
-    // h^2 hess psi (psd-fixed) at s
+    for (int i = 0; i < 6; ++i) sv[i] = Real(Ext<Real>::to_real(sE[i]));
     Real g[6], H[36];
     material_gH(in, sv, h2, g, H);
-    // polar rotation from the previous rotation (update_rotations)
-    double F64[9];
+    E FE[9];
     Real F[9], R[9];
-    deformation_gradients<Real>(sd.x, in, F64, F);
+    deformation_gradients<Real>(sd, in, nullptr, E(0), FE, F);
     load_quat(sd, e, R);
     int it = procrustes<Real>(R, F, Real(kProcrustesTol), kProcrustesIters);
     store_quat(sd, e, R);
@@ -207,48 +244,43 @@ __global__ void __launch_bounds__(kElemTile)
     bool ok = stretch_derivative_u(S6, u);
     if (it < 0 || !ok) atomicAdd(&sd.sc->procrustes_fail, 1);
     Real dph[12];
-#pragma unroll
-    for (int c = 0; c < 3; ++c) {
-      dph[3 + c] = in.dp[c];
-      dph[6 + c] = in.dp[3 + c];
-      dph[9 + c] = in.dp[6 + c];
-      dph[c] = -(in.dp[c] + in.dp[3 + c] + in.dp[6 + c]);
-    }
-    // ---- residual chain in FP64: S - s, q = H (S - s) + h^2 psi'(s), forces
+    dphi12(in, dph);
+    // ---- residual chain in Ext: S - s, q = H (S - s) + h^2 psi'(s), forces
     {
-      double R64[9], S64[6], d64[6], g64[6], q64[6], dph64[12], f64[12];
+      E RE[9], SE[6], dE[6], gE[6], qE[6], dphE[12], fE[12];
 #pragma unroll
-      for (int i = 0; i < 9; ++i) R64[i] = double(R[i]);
-      if (!Prec<Real>::kFP64) polish_rotation(R64, F64);
-      stretch_vec(R64, F64, S64);
-      material_grad<double>(in.mat, double(in.mu), double(in.lam), s64, g64);
+      for (int i = 0; i < 9; ++i) RE[i] = E(R[i]);
+      if (!Prec<Real>::kFP64) polish_rotation(RE, FE);
+      stretch_vec(RE, FE, SE);
+      material_grad<E>(in.mat, E(in.mu), E(in.lam), sE, gE);
+      const E h2E = E(sd.h2);
 #pragma unroll
-      for (int i = 0; i < 6; ++i) d64[i] = S64[i] - s64[i];
+      for (int i = 0; i < 6; ++i) dE[i] = SE[i] - sE[i];
 #pragma unroll
       for (int i = 0; i < 6; ++i) {
-        double acc = double(h2) * g64[i];
+        E acc = h2E * gE[i];
 #pragma unroll
-        for (int j = 0; j < 6; ++j) acc += double(H[i + 6 * j]) * d64[j];
-        q64[i] = acc;
+        for (int j = 0; j < 6; ++j) acc = acc + E(H[i + 6 * j]) * dE[j];
+        qE[i] = acc;
       }
 #pragma unroll
-      for (int i = 0; i < 12; ++i) dph64[i] = double(dph[i]);
-      element_force<double>(R64, S64, q64, dph64, double(in.vol), f64);
+      for (int i = 0; i < 12; ++i) dphE[i] = E(dph[i]);
+      element_force<E>(RE, SE, qE, dphE, E(in.vol), fE);
 #pragma unroll
-      for (int i = 0; i < 12; ++i) put_word(out, kRhsWord + 2 * i, f64[i]);
+      for (int i = 0; i < 12; ++i) put_word(out, kRhsWord + 2 * i, fE[i]);
       Real dS[6];
 #pragma unroll
-      for (int i = 0; i < 6; ++i) dS[i] = Real(d64[i]);
+      for (int i = 0; i < 6; ++i) dS[i] = Real(Ext<Real>::to_real(dE[i]));
       store6(sd.dS, sd.ntp, e, dS);
       if (DBG) {
-        const size_t E = e;
-        for (int i = 0; i < 9; ++i) dbg.R[9 * E + i] = R64[i];
+        const size_t Ei = e;
+        for (int i = 0; i < 9; ++i) dbg.R[9 * Ei + i] = to_double_any(RE[i]);
         for (int i = 0; i < 6; ++i) {
-          dbg.S[6 * E + i] = S64[i];
-          dbg.g[6 * E + i] = double(h2) * g64[i];
-          dbg.gl[6 * E + i] = (i < 3 ? 1.0 : 0.5) * q64[i];
+          dbg.S[6 * Ei + i] = to_double_any(SE[i]);
+          dbg.g[6 * Ei + i] = to_double_any(h2E * gE[i]);
+          dbg.gl[6 * Ei + i] = (i < 3 ? 1.0 : 0.5) * to_double_any(qE[i]);
         }
-        for (int i = 0; i < 36; ++i) dbg.H[36 * E + i] = H[i];
+        for (int i = 0; i < 36; ++i) dbg.H[36 * Ei + i] = H[i];
       }
     }
     // ---- B[i][a][l] = ds_i / dx_{a,l} = (G_i dphi_a)_l
@@ -295,12 +327,12 @@ __global__ void __launch_bounds__(kElemTile)
 #pragma unroll
             for (int i = 0; i < 6; ++i) acc += B[12 * i + 3 * a + l] * HB[3 * i + m];
             const int k = base + (a == b ? sym_idx(l, m) : 3 * l + m);
-            put_word(out, k * (RB / 4), Real(in.vol * acc));
+            const Real v = in.vol * acc;
+            put_word(out, k * (RB / 4), v);
             if (DBG) {
-              const size_t E = e;
-              const double v = double(Real(in.vol * acc));
-              dbg.Aloc[144 * E + (3 * a + l) + 12 * (3 * b + m)] = v;
-              dbg.Aloc[144 * E + (3 * b + m) + 12 * (3 * a + l)] = v;
+              const size_t Ei = e;
+              dbg.Aloc[144 * Ei + (3 * a + l) + 12 * (3 * b + m)] = double(v);
+              dbg.Aloc[144 * Ei + (3 * b + m) + 12 * (3 * a + l)] = double(v);
             }
           }
       }
@@ -316,13 +348,45 @@ __global__ void __launch_bounds__(kElemTile)
   }
 }
 
+// Vertex part of the energy: 1/2 diff^T M diff with diff = x + alpha dx - xt.
+template <typename Real>
+__device__ __forceinline__ typename Ext<Real>::T vertex_energy(const SceneDev& sd, int a,
+                                                               const Real* dx,
+                                                               typename Ext<Real>::T alpha) {
+  using E = typename Ext<Real>::T;
+  const Real* mval = static_cast<const Real*>(sd.m_val);
+  E Md[3] = {E(0), E(0), E(0)};
+  for (int q = sd.m_ptr[a]; q < sd.m_ptr[a + 1]; ++q) {
+    const int b = sd.m_col[q];
+    const E m = E(mval[q]);
+    const int fb = sd.free_map[b];
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+      E d = Ext<Real>::ld(sd.x, 3 * (size_t)b + c) - Ext<Real>::ld(sd.xt, 3 * (size_t)b + c);
+      if (dx && fb >= 0) d = d + alpha * E(dx[3 * fb + c]);
+      Md[c] = Md[c] + m * d;
+    }
+  }
+  const int fa = sd.free_map[a];
+  E e2 = E(0);
+#pragma unroll
+  for (int c = 0; c < 3; ++c) {
+    E d = Ext<Real>::ld(sd.x, 3 * (size_t)a + c) - Ext<Real>::ld(sd.xt, 3 * (size_t)a + c);
+    if (dx && fa >= 0) d = d + alpha * E(dx[3 * fa + c]);
+    e2 = e2 + d * Md[c];
+  }
+  return E(0.5) * e2;
+}
+
 // ------------------------------------------------------------------ K5 ---
 // ds = (S - s) + dS/dF : dF(dx)  (the closed form of -H^{-1}(Sym la + g),
 // MixedStretch::solve), la = -Syminv (H ds + g); E(0), max |ds|, max |dx|.
+// Tile partials: 0,1 E(0) (compensated pair), 2 sum |terms|, 3 max|ds|, 4 max|dx|.
 template <typename Real>
 __global__ void __launch_bounds__(kElemTile) k_local_solve(const Tile* tiles, const SceneDev* sds,
                                                            double* partials, int pstride,
                                                            BatchCounters* ctrs) {
+  using E = typename Ext<Real>::T;
   const int tix = blockIdx.x;
   const Tile t = tiles[tix];
   const SceneDev& sd = sds[t.scene];
@@ -330,8 +394,8 @@ __global__ void __launch_bounds__(kElemTile) k_local_solve(const Tile* tiles, co
   if (!sc->newton_active) return;
   const Real h2 = Real(sd.h2);
   const Real* cgx = static_cast<const Real*>(sd.cg_x);
-  KSum en{0.0, 0.0};
-  double mds = 0.0, mdx = 0.0, eabs = 0.0;
+  E sums[2] = {E(0), E(0)};
+  double maxs[2] = {0.0, 0.0};
   const int idx = t.begin + threadIdx.x;
   if (t.kind == 0) {
     if (idx < t.end) {
@@ -339,14 +403,14 @@ __global__ void __launch_bounds__(kElemTile) k_local_solve(const Tile* tiles, co
       ElemIn<Real> in;
       load_elem(sd, e, in);
       Real R[9], d[6], sv[6], S6[6];
-      double s64[6];
+      E sE[6];
       load_quat(sd, e, R);
       load6(sd.dS, sd.ntp, e, d);
-      load6d(sd.s, sd.ntp, e, s64);
+      load6e<Real>(sd, e, sE);
 #pragma unroll
       for (int i = 0; i < 6; ++i) {
-        sv[i] = Real(s64[i]);
-        S6[i] = Real(s64[i] + double(d[i]));
+        sv[i] = Real(Ext<Real>::to_real(sE[i]));
+        S6[i] = Real(Ext<Real>::to_real(sE[i] + E(d[i])));
       }
       const int v[4] = {in.tv.x, in.tv.y, in.tv.z, in.tv.w};
       Real dd[4][3];
@@ -384,50 +448,36 @@ __global__ void __launch_bounds__(kElemTile) k_local_solve(const Tile* tiles, co
       store6(sd.ds, sd.ntp, e, ds);
       store6(sd.la, sd.ntp, e, la);
       // E(0) = h^2 vol psi(s) - vol la . Sym (S - s)
-      const double psi = double(material_psi<Real>(in.mat, in.mu, in.lam, sv));
-      double con = 0;
+      const Real psi = material_psi<Real>(in.mat, in.mu, in.lam, sv);
+      Real con = 0;
 #pragma unroll
-      for (int i = 0; i < 6; ++i) con += double(la[i]) * (i < 3 ? 1.0 : 2.0) * double(d[i]);
-      const double e1 = double(h2) * double(in.vol) * psi, e2 = double(in.vol) * con;
-      en.add(e1);
-      en.add(-e2);
-      eabs = fabs(e1) + fabs(e2);
+      for (int i = 0; i < 6; ++i) con += la[i] * (i < 3 ? Real(1) : Real(2)) * d[i];
+      const Real e1 = h2 * in.vol * psi, e2 = in.vol * con;
+      sums[0] = E(e1) - E(e2);
+      sums[1] = E(Real(fabs(e1))) + E(Real(fabs(e2)));
       Real m = 0;
 #pragma unroll
-      for (int i = 0; i < 6; ++i) m = fmax(m, fabs(ds[i]));
-      mds = m;
+      for (int i = 0; i < 6; ++i) m = fmax(m, Real(fabs(ds[i])));
+      maxs[0] = double(m);
     }
   } else if (idx < t.end) {
     const int a = idx;
-    const double* x = sd.x;
-    const double* xt = sd.xt;
-    double Md[3] = {0, 0, 0};
-    for (int q = sd.m_ptr[a]; q < sd.m_ptr[a + 1]; ++q) {
-      const int b = sd.m_col[q];
-      const double m = sd.m_val[q];
-#pragma unroll
-      for (int c = 0; c < 3; ++c) Md[c] += m * (x[3 * b + c] - xt[3 * b + c]);
-    }
-    double e2 = 0;
-#pragma unroll
-    for (int c = 0; c < 3; ++c) e2 += (x[3 * a + c] - xt[3 * a + c]) * Md[c];
-    en.add(0.5 * e2);
+    sums[0] = vertex_energy<Real>(sd, a, nullptr, E(0));
     const int f = sd.free_map[a];
     if (f >= 0) {
+      Real m = 0;
 #pragma unroll
-      for (int c = 0; c < 3; ++c) mdx = fmax(mdx, fabs(double(cgx[3 * f + c])));
+      for (int c = 0; c < 3; ++c) m = fmax(m, Real(fabs(cgx[3 * f + c])));
+      maxs[1] = double(m);
     }
   }
-  put_ksum(en, partials, pstride, 0, tix);
-  put_max(mds, partials, pstride, 2, tix);
-  put_max(mdx, partials, pstride, 3, tix);
-  put_sum(eabs, partials, pstride, 4, tix);
+  tile_partials<E, 2, 2>(sums, maxs, partials, pstride, 0, tix, 1);
   if (last_tile(sd, TB_EV, tix)) {
     const int t0 = sd.tile_first[TB_EV], tc = sd.tile_count[TB_EV];
     const double Ev = scene_ksum(partials, pstride, 0, t0, tc);
-    const double ms = scene_max(partials, pstride, 2, t0, tc);
-    const double mx = scene_max(partials, pstride, 3, t0, tc);
-    const double ea = scene_sum(partials, pstride, 4, t0, tc);
+    const double ea = scene_sum(partials, pstride, 2, t0, tc);
+    const double ms = scene_max(partials, pstride, 3, t0, tc);
+    const double mx = scene_max(partials, pstride, 4, t0, tc);
     if (threadIdx.x == 0) {
       sc->E_abs = ea;
       sc->E = Ev;
@@ -451,20 +501,21 @@ __global__ void __launch_bounds__(kElemTile) k_local_solve(const Tile* tiles, co
 }
 
 // ------------------------------------------------------------------ K6 ---
+// Tile partials: 0,1 E(alpha) (compensated pair), 2 sum |terms|.
 template <typename Real>
 __global__ void __launch_bounds__(kElemTile) k_ls_energy(const Tile* tiles, const SceneDev* sds,
                                                          double* partials, int pstride,
                                                          BatchCounters* ctrs) {
+  using E = typename Ext<Real>::T;
   const int tix = blockIdx.x;
   const Tile t = tiles[tix];
   const SceneDev& sd = sds[t.scene];
   SceneScalars* sc = sd.sc;
   if (!sc->ls_active) return;
-  const double alpha = sc->alpha_ls;
+  const E alpha = E(sc->alpha_ls);
   const Real h2 = Real(sd.h2);
   const Real* cgx = static_cast<const Real*>(sd.cg_x);
-  KSum en{0.0, 0.0};
-  double eabs = 0.0;
+  E sums[2] = {E(0), E(0)};
   const int idx = t.begin + threadIdx.x;
   if (t.kind == 0) {
     if (idx < t.end) {
@@ -473,73 +524,34 @@ __global__ void __launch_bounds__(kElemTile) k_ls_energy(const Tile* tiles, cons
       load_elem(sd, e, in);
       Real F[9], R[9];
       // x0 = x + alpha dx  (energy_func, newton_optimizer.cpp:37)
-      {
-        const int v[4] = {in.tv.x, in.tv.y, in.tv.z, in.tv.w};
-        double p[4][3];
-#pragma unroll
-        for (int k = 0; k < 4; ++k) {
-          const int f = sd.free_map[v[k]];
-#pragma unroll
-          for (int c = 0; c < 3; ++c)
-            p[k][c] = sd.x[3 * v[k] + c] + (f >= 0 ? alpha * double(cgx[3 * f + c]) : 0.0);
-        }
-        Real ed[9];
-#pragma unroll
-        for (int k = 1; k < 4; ++k)
-#pragma unroll
-          for (int r = 0; r < 3; ++r) ed[3 * (k - 1) + r] = Real(p[k][r] - p[0][r]);
-#pragma unroll
-        for (int c = 0; c < 3; ++c)
-#pragma unroll
-          for (int r = 0; r < 3; ++r)
-            F[r + 3 * c] = ed[r] * in.dp[c] + ed[3 + r] * in.dp[3 + c] + ed[6 + r] * in.dp[6 + c];
-      }
+      deformation_gradients<Real>(sd, in, cgx, alpha, nullptr, F);
       load_quat(sd, e, R);
       procrustes<Real>(R, F, Real(kProcrustesTol), kProcrustesIters);
       Real St[6];
       stretch_vec(R, F, St);
-      double s64[6];
+      E sE[6];
       Real dsv[6], la[6], si[6];
-      load6d(sd.s, sd.ntp, e, s64);
+      load6e<Real>(sd, e, sE);
       load6(sd.ds, sd.ntp, e, dsv);
       load6(sd.la, sd.ntp, e, la);
-      double si64[6];
+      Real con = 0;
 #pragma unroll
       for (int i = 0; i < 6; ++i) {
-        si64[i] = s64[i] + alpha * double(dsv[i]);
-        si[i] = Real(si64[i]);
+        const E siE = sE[i] + alpha * E(dsv[i]);
+        si[i] = Real(Ext<Real>::to_real(siE));
+        // S(x0) - s(alpha) formed in Ext before rounding
+        const Real diff = Real(Ext<Real>::to_real(E(St[i]) - siE));
+        con += la[i] * (i < 3 ? Real(1) : Real(2)) * diff;
       }
-      const double psi = double(material_psi<Real>(in.mat, in.mu, in.lam, si));
-      double con = 0;
-#pragma unroll
-      for (int i = 0; i < 6; ++i) con += double(la[i]) * (i < 3 ? 1.0 : 2.0) * (double(St[i]) - si64[i]);
-      const double e1 = double(h2) * double(in.vol) * psi, e2 = double(in.vol) * con;
-      en.add(e1);
-      en.add(-e2);
-      eabs = fabs(e1) + fabs(e2);
+      const Real psi = material_psi<Real>(in.mat, in.mu, in.lam, si);
+      const Real e1 = h2 * in.vol * psi, e2 = in.vol * con;
+      sums[0] = E(e1) - E(e2);
+      sums[1] = E(Real(fabs(e1))) + E(Real(fabs(e2)));
     }
   } else if (idx < t.end) {
-    const int a = idx;
-    const double* x = sd.x;
-    const double* xt = sd.xt;
-    double Md[3] = {0, 0, 0};
-    for (int q = sd.m_ptr[a]; q < sd.m_ptr[a + 1]; ++q) {
-      const int b = sd.m_col[q];
-      const double m = sd.m_val[q];
-      const int fb = sd.free_map[b];
-#pragma unroll
-      for (int c = 0; c < 3; ++c)
-        Md[c] += m * (x[3 * b + c] + (fb >= 0 ? alpha * double(cgx[3 * fb + c]) : 0.0) - xt[3 * b + c]);
-    }
-    const int fa = sd.free_map[a];
-    double e2 = 0;
-#pragma unroll
-    for (int c = 0; c < 3; ++c)
-      e2 += (x[3 * a + c] + (fa >= 0 ? alpha * double(cgx[3 * fa + c]) : 0.0) - xt[3 * a + c]) * Md[c];
-    en.add(0.5 * e2);
+    sums[0] = vertex_energy<Real>(sd, idx, cgx, alpha);
   }
-  put_ksum(en, partials, pstride, 0, tix);
-  put_sum(eabs, partials, pstride, 2, tix);
+  tile_partials<E, 2, 0>(sums, nullptr, partials, pstride, 0, tix, 1);
   if (last_tile(sd, TB_EV, tix)) {
     const int t0 = sd.tile_first[TB_EV], tc = sd.tile_count[TB_EV];
     const double fx = scene_ksum(partials, pstride, 0, t0, tc);
@@ -572,6 +584,7 @@ template <typename Real>
 __global__ void __launch_bounds__(kElemTile) k_apply(const Tile* tiles, const SceneDev* sds,
                                                      double* partials, int pstride,
                                                      BatchCounters* ctrs) {
+  using E = typename Ext<Real>::T;
   const int tix = blockIdx.x;
   const Tile t = tiles[tix];
   const SceneDev& sd = sds[t.scene];
@@ -579,20 +592,23 @@ __global__ void __launch_bounds__(kElemTile) k_apply(const Tile* tiles, const Sc
   if (!sc->newton_active) return;
   const int idx = t.begin + threadIdx.x;
   if (sc->ls_ok && idx < t.end) {
-    const double alpha = sc->alpha_ls;
+    const E alpha = E(sc->alpha_ls);
     if (t.kind == 0) {
       const Real* ds = static_cast<const Real*>(sd.ds);
 #pragma unroll
       for (int i = 0; i < 6; ++i) {
         const size_t k = (size_t)i * sd.ntp + idx;
-        sd.s[k] += alpha * double(ds[k]);
+        Ext<Real>::st(sd.s, k, Ext<Real>::ld(sd.s, k) + alpha * E(ds[k]));
       }
     } else {
       const int f = sd.free_map[idx];
       if (f >= 0) {
         const Real* cgx = static_cast<const Real*>(sd.cg_x);
 #pragma unroll
-        for (int c = 0; c < 3; ++c) sd.x[3 * idx + c] += alpha * double(cgx[3 * f + c]);
+        for (int c = 0; c < 3; ++c) {
+          const size_t k = 3 * (size_t)idx + c;
+          Ext<Real>::st(sd.x, k, Ext<Real>::ld(sd.x, k) + alpha * E(cgx[3 * f + c]));
+        }
       }
     }
   }
@@ -618,6 +634,7 @@ __global__ void __launch_bounds__(kElemTile) k_apply(const Tile* tiles, const Sc
 // target (displacement.cpp:63-73).
 template <typename Real>
 __global__ void __launch_bounds__(kElemTile) k_step_begin(const Tile* tiles, const SceneDev* sds) {
+  using E = typename Ext<Real>::T;
   const Tile t = tiles[blockIdx.x];
   const SceneDev& sd = sds[t.scene];
   if (t.kind == 0) return;
@@ -625,15 +642,17 @@ __global__ void __launch_bounds__(kElemTile) k_step_begin(const Tile* tiles, con
   if (a >= t.end) return;
   const int I = sd.bdf_order, head = sd.sc->hist_head;
   const size_t n3 = 3 * (size_t)sd.nv;
+  const E dt = E(sd.dt), h2 = E(sd.h2);
 #pragma unroll
   for (int c = 0; c < 3; ++c) {
-    double wx = 0, wv = 0;
+    E wx = E(0), wv = E(0);
     for (int i = 0; i < I; ++i) {
-      const int slot = (head + i) % I;
-      wx += sd.bdf_alpha[i] * sd.xhist[slot * n3 + 3 * a + c];
-      wv += sd.bdf_alpha[i] * sd.vhist[slot * n3 + 3 * a + c];
+      const size_t slot = (size_t)((head + i) % I) * n3 + 3 * (size_t)a + c;
+      const E al = E(sd.bdf_alpha[i]);
+      wx = wx + al * Ext<Real>::ld(sd.xhist, slot);
+      wv = wv + al * Ext<Real>::ld(sd.vhist, slot);
     }
-    sd.xt[3 * a + c] = wx + sd.dt * wv + sd.h2 * sd.body[c];
+    Ext<Real>::st(sd.xt, 3 * (size_t)a + c, wx + dt * wv + h2 * E(sd.body[c]));
   }
 }
 
@@ -641,6 +660,7 @@ __global__ void __launch_bounds__(kElemTile) k_step_begin(const Tile* tiles, con
 // lambda = 0 (MixedStretch::post_solve, mixed_stretch.cpp:306-309).
 template <typename Real>
 __global__ void __launch_bounds__(kElemTile) k_step_end(const Tile* tiles, const SceneDev* sds) {
+  using E = typename Ext<Real>::T;
   const int tix = blockIdx.x;
   const Tile t = tiles[tix];
   const SceneDev& sd = sds[t.scene];
@@ -657,15 +677,18 @@ __global__ void __launch_bounds__(kElemTile) k_step_end(const Tile* tiles, const
       const int a = idx;
       const int f = sd.free_map[a];
       const size_t n3 = 3 * (size_t)sd.nv;
+      const E dt = E(sd.dt);
 #pragma unroll
       for (int c = 0; c < 3; ++c) {
-        const double xv = (f < 0) ? sd.pin_pos[3 * (-1 - f) + c] : sd.x[3 * a + c];
-        double wx = 0;
-        for (int i = 0; i < I; ++i) wx += sd.bdf_alpha[i] * sd.xhist[((head + i) % I) * n3 + 3 * a + c];
-        const double vnew = (xv - wx) / sd.dt;
-        sd.x[3 * a + c] = xv;
-        sd.xhist[nhead * n3 + 3 * a + c] = xv;
-        sd.vhist[nhead * n3 + 3 * a + c] = vnew;
+        const size_t k = 3 * (size_t)a + c;
+        const E xv = (f < 0) ? E(sd.pin_pos[3 * (-1 - f) + c]) : Ext<Real>::ld(sd.x, k);
+        E wx = E(0);
+        for (int i = 0; i < I; ++i)
+          wx = wx + E(sd.bdf_alpha[i]) * Ext<Real>::ld(sd.xhist, (size_t)((head + i) % I) * n3 + k);
+        const E vnew = (xv - wx) / dt;
+        Ext<Real>::st(sd.x, k, xv);
+        Ext<Real>::st(sd.xhist, (size_t)nhead * n3 + k, xv);
+        Ext<Real>::st(sd.vhist, (size_t)nhead * n3 + k, vnew);
       }
     }
   }
@@ -681,9 +704,7 @@ void set_smem(K kernel, int bytes) {
 
 }  // namespace
 
-int elem_update_smem_bytes(int fp64) {
-  return kElemTile * (rec_bytes(fp64 ? 8 : 4) / 4 + 1) * 4;
-}
+int elem_update_smem_bytes(int fp64) { return kElemTile * (rec_bytes(fp64 ? 8 : 4) / 4 + 1) * 4; }
 
 void configure_kernels() {
   set_smem(k_elem_update<float, false>, elem_update_smem_bytes(0));

@@ -35,13 +35,14 @@ __device__ __forceinline__ int rec_offset(int i, int j, int l, int m) {
   return start + 6 + 9 * (j - i - 1) + 3 * l + m;
 }
 
-constexpr int kMaxOut = 8;  // outputs per lane per chunk (32*8 = 256 = 28 blocks)
+constexpr int kAsmWindow = 64;  // block slots per warp accumulated in shared memory per pass
 
 template <typename Real>
 __global__ void __launch_bounds__(256) k_assemble(const Tile* tiles, const SceneDev* sds,
                                                             double* partials, int pstride,
                                                             BatchCounters* ctrs) {
   __shared__ unsigned short offtab[4][4][9];
+  __shared__ Real acc_s[8][kAsmWindow * 9];
   for (int k = threadIdx.x; k < 144; k += blockDim.x) {
     const int i = k / 36, j = (k / 9) % 4, rc = k % 9;
     offtab[i][j][rc] = (unsigned short)rec_offset(i, j, rc / 3, rc % 3);
@@ -53,7 +54,7 @@ __global__ void __launch_bounds__(256) k_assemble(const Tile* tiles, const Scene
   SceneScalars* sc = sd.sc;
   if (!sc->newton_active) return;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  double rn2 = 0.0;
+  typename Ext<Real>::T rn2 = typename Ext<Real>::T(0);
   for (int rr = warp; rr < kRowTile; rr += 8) {
   const int row = t.begin + rr;
   if (row < t.end) {
@@ -61,65 +62,70 @@ __global__ void __launch_bounds__(256) k_assemble(const Tile* tiles, const Scene
     const int rb = sd.b_ptr[row], nb = sd.b_ptr[row + 1] - rb;
     const int ib = sd.inc_ptr[row], ie = sd.inc_ptr[row + 1];
     const int v = sd.free_vert[row];
-    // ---- right-hand side (FP64): -sum_b m_vb (x_b - xt_b) + element shares
-    double acc[3] = {0, 0, 0};
+    // ---- right-hand side in Ext: -sum_b m_vb (x_b - xt_b) + element shares
+    using E = typename Ext<Real>::T;
+    const Real* mval = static_cast<const Real*>(sd.m_val);
+    E acc[3] = {E(0), E(0), E(0)};
     for (int q = sd.m_ptr[v] + lane; q < sd.m_ptr[v + 1]; q += 32) {
       const int b = sd.m_col[q];
-      const double m = sd.m_val[q];
+      const E m = E(mval[q]);
 #pragma unroll
-      for (int c = 0; c < 3; ++c) acc[c] -= m * (sd.x[3 * b + c] - sd.xt[3 * b + c]);
+      for (int c = 0; c < 3; ++c)
+        acc[c] = acc[c] - m * (Ext<Real>::ld(sd.x, 3 * (size_t)b + c) - Ext<Real>::ld(sd.xt, 3 * (size_t)b + c));
     }
     for (int k = ib + lane; k < ie; k += 32) {
       const int2 ic = sd.inc[k];
-      const double* rp = reinterpret_cast<const double*>(sd.rec + (size_t)ic.x * rec_bytes(RB) +
-                                                         rec_rhs_offset(RB)) + 3 * (ic.y & 3);
+      const void* rp = sd.rec + (size_t)ic.x * rec_bytes(RB) + rec_rhs_offset(RB);
 #pragma unroll
-      for (int c = 0; c < 3; ++c) acc[c] += rp[c];
+      for (int c = 0; c < 3; ++c) acc[c] = acc[c] + Ext<Real>::ld(rp, 3 * (ic.y & 3) + c);
     }
 #pragma unroll
     for (int c = 0; c < 3; ++c)
 #pragma unroll
-      for (int off = 16; off > 0; off >>= 1) acc[c] += __shfl_down_sync(0xffffffffu, acc[c], off);
+      for (int off = 16; off > 0; off >>= 1) acc[c] = acc[c] + shfl_down(acc[c], off);
     if (lane == 0) {
       Real* rhs = static_cast<Real*>(sd.rhs);
+      E r2 = E(0);
 #pragma unroll
-      for (int c = 0; c < 3; ++c) rhs[3 * row + c] = Real(acc[c]);
-      rn2 += acc[0] * acc[0] + acc[1] * acc[1] + acc[2] * acc[2];
+      for (int c = 0; c < 3; ++c) {
+        rhs[3 * row + c] = Real(Ext<Real>::to_real(acc[c]));
+        r2 = r2 + acc[c] * acc[c];
+      }
+      rn2 = rn2 + r2;
     }
-    // ---- block values: each lane owns outputs o = base + lane + 32*kk
+    // ---- block values: the warp accumulates the row's blocks in shared
+    // memory, one incidence (element, local vertex i) at a time; lane l < 36
+    // adds entry l % 9 of local block (i, l / 9) to that block's column slot.
+    // Slots of one incidence are distinct, so the adds never collide, and
+    // every entry sums its contributions in element order.
     Real* val = static_cast<Real*>(sd.b_val) + (size_t)rb * 9;
     const Real* bm = static_cast<const Real*>(sd.b_mass) + rb;
-    for (int base = 0; base < 9 * nb; base += 32 * kMaxOut) {
-      Real a[kMaxOut];
-      int oq[kMaxOut], orc[kMaxOut];
-#pragma unroll
-      for (int kk = 0; kk < kMaxOut; ++kk) {
-        const int o = base + lane + 32 * kk;
-        a[kk] = Real(0);
-        oq[kk] = (o < 9 * nb) ? o / 9 : -2;
-        orc[kk] = o % 9;
-      }
+    Real* acc_w = acc_s[warp];
+    for (int w0 = 0; w0 < nb; w0 += kAsmWindow) {
+      const int wn = min(kAsmWindow, nb - w0);
+      for (int o = lane; o < 9 * wn; o += 32) acc_w[o] = Real(0);
+      __syncwarp();
       for (int k = ib; k < ie; ++k) {
         const int2 ic = sd.inc[k];
         const int i = ic.y & 3;
-        const int s0 = (ic.y >> 2) & 127, s1 = (ic.y >> 9) & 127, s2 = (ic.y >> 16) & 127,
-                  s3 = (ic.y >> 23) & 127;
         const Real* rp = reinterpret_cast<const Real*>(sd.rec + (size_t)ic.x * rec_bytes(RB));
 #pragma unroll
-        for (int kk = 0; kk < kMaxOut; ++kk) {
-          const int q = oq[kk];
-          const int j = (s0 == q) ? 0 : (s1 == q) ? 1 : (s2 == q) ? 2 : (s3 == q) ? 3 : -1;
-          if (j >= 0) a[kk] += rp[offtab[i][j][orc[kk]]];
+        for (int pass = 0; pass < 2; ++pass) {
+          const int l = lane + 32 * pass;
+          if (l < 36) {
+            const int j = l / 9, ent = l - 9 * j;
+            const int slot = (ic.y >> (2 + 7 * j)) & 127;
+            const int sl = slot - w0;
+            if (slot != 127 && sl >= 0 && sl < wn) acc_w[9 * sl + ent] += rp[offtab[i][j][ent]];
+          }
         }
+        __syncwarp();
       }
-#pragma unroll
-      for (int kk = 0; kk < kMaxOut; ++kk) {
-        const int o = base + lane + 32 * kk;
-        if (o < 9 * nb) {
-          const int rc = orc[kk];
-          val[o] = a[kk] + ((rc == 0 || rc == 4 || rc == 8) ? bm[oq[kk]] : Real(0));
-        }
+      for (int o = lane; o < 9 * wn; o += 32) {
+        const int q = o / 9, ent = o - 9 * q;
+        val[9 * w0 + o] = acc_w[o] + ((ent == 0 || ent == 4 || ent == 8) ? bm[w0 + q] : Real(0));
       }
+      __syncwarp();
     }
     __syncwarp();
     // ---- preconditioner from the diagonal block
@@ -165,7 +171,10 @@ __global__ void __launch_bounds__(256) k_assemble(const Tile* tiles, const Scene
     }
   }
   }
-  put_sum(rn2, partials, pstride, 0, tix);
+  {
+    typename Ext<Real>::T sums[1] = {rn2};
+    tile_partials<typename Ext<Real>::T, 1, 0>(sums, nullptr, partials, pstride, 0, tix, 0);
+  }
   if (last_tile(sd, TB_ROW, tix)) {
     const double s = scene_sum(partials, pstride, 0, sd.tile_first[TB_ROW], sd.tile_count[TB_ROW]);
     if (threadIdx.x == 0) {
@@ -191,6 +200,10 @@ __global__ void __launch_bounds__(256) k_assemble(const Tile* tiles, const Scene
 }
 
 // ---------------------------------------------------------------- PCG ---
+// Products of two Reals carried exactly in Ext (TwoProduct in the mixed path).
+__device__ __forceinline__ df64 exact_prod(float a, float b) { return two_prod(a, b); }
+__device__ __forceinline__ double exact_prod(double a, double b) { return a * b; }
+
 // z = D^{-1} r for one row (Jacobi or 3x3 block Jacobi).
 template <typename Real>
 __device__ __forceinline__ void apply_prec(const SceneDev& sd, int row, const Real r[3], Real z[3]) {
@@ -215,7 +228,8 @@ __global__ void __launch_bounds__(kCgThreads) k_cg_init(const Tile* tiles, const
   const SceneDev& sd = sds[t.scene];
   SceneScalars* sc = sd.sc;
   if (!sc->newton_active) return;
-  double rr = 0.0, rz = 0.0;
+  using E = typename Ext<Real>::T;
+  E dots[2] = {E(0), E(0)};  // r.r, r.z
   const int row = t.begin + threadIdx.x;
   if (row < t.end) {
     const Real* b = static_cast<const Real*>(sd.rhs) + 3 * (size_t)row;
@@ -229,12 +243,11 @@ __global__ void __launch_bounds__(kCgThreads) k_cg_init(const Tile* tiles, const
       pr[c] = r[c];
       pz[c] = z[c];
       px[c] = Real(0);
-      rr += double(r[c]) * double(r[c]);
-      rz += double(r[c]) * double(z[c]);
+      dots[0] = dots[0] + exact_prod(r[c], r[c]);
+      dots[1] = dots[1] + exact_prod(r[c], z[c]);
     }
   }
-  put_sum(rr, partials, pstride, 0, tix);
-  put_sum(rz, partials, pstride, 1, tix);
+  tile_partials<E, 2, 0>(dots, nullptr, partials, pstride, 0, tix, 0);
   if (last_tile(sd, TB_CG, tix)) {
     const int t0 = sd.tile_first[TB_CG], tc = sd.tile_count[TB_CG];
     const double rrs = scene_sum(partials, pstride, 0, t0, tc);
@@ -284,7 +297,8 @@ __global__ void __launch_bounds__(kCgThreads) k_cg_spmv(const Tile* tiles, const
   const Real* val = static_cast<const Real*>(sd.b_val);
   Real* Ap = static_cast<Real*>(sd.cg_Ap);
   const int grp = threadIdx.x / kCgTpr, lr = threadIdx.x % kCgTpr;
-  double pAp = 0.0;
+  using E = typename Ext<Real>::T;
+  E pAp[1] = {E(0)};
   constexpr int kGroups = kCgThreads / kCgTpr;
 #pragma unroll 2
   for (int rr = grp; rr < kCgRows; rr += kGroups) {
@@ -314,11 +328,11 @@ __global__ void __launch_bounds__(kCgThreads) k_cg_spmv(const Tile* tiles, const
         const Real p = first ? z[3 * row + c] : z[3 * row + c] + beta * pin[3 * row + c];
         pout[3 * row + c] = p;
         Ap[3 * row + c] = acc[c];
-        pAp += double(p) * double(acc[c]);
+        pAp[0] = pAp[0] + exact_prod(p, acc[c]);
       }
     }
   }
-  put_sum(pAp, partials, pstride, 0, tix);
+  tile_partials<E, 1, 0>(pAp, nullptr, partials, pstride, 0, tix, 0);
   if (last_tile(sd, TB_CG, tix)) {
     const double s = scene_sum(partials, pstride, 0, sd.tile_first[TB_CG], sd.tile_count[TB_CG]);
     if (threadIdx.x == 0) sc->alpha = sc->rz / s;
@@ -337,7 +351,8 @@ __global__ void __launch_bounds__(kCgThreads) k_cg_update(const Tile* tiles, con
   if (!sc->cg_active) return;
   const int it = sc->cg_iter;
   const Real alpha = Real(sc->alpha);
-  double rr = 0.0, rz = 0.0;
+  using E = typename Ext<Real>::T;
+  E dots[2] = {E(0), E(0)};  // r.r, r.z
   const int row = t.begin + threadIdx.x;
   if (row < t.end) {
     const size_t k = 3 * (size_t)row;
@@ -351,18 +366,17 @@ __global__ void __launch_bounds__(kCgThreads) k_cg_update(const Tile* tiles, con
       x[c] += alpha * p[c];
       rv[c] = r[c] - alpha * Ap[c];
       r[c] = rv[c];
-      rr += double(rv[c]) * double(rv[c]);
+      dots[0] = dots[0] + exact_prod(rv[c], rv[c]);
     }
     apply_prec<Real>(sd, row, rv, z);
     Real* pz = static_cast<Real*>(sd.cg_z) + k;
 #pragma unroll
     for (int c = 0; c < 3; ++c) {
       pz[c] = z[c];
-      rz += double(rv[c]) * double(z[c]);
+      dots[1] = dots[1] + exact_prod(rv[c], z[c]);
     }
   }
-  put_sum(rr, partials, pstride, 0, tix);
-  put_sum(rz, partials, pstride, 1, tix);
+  tile_partials<E, 2, 0>(dots, nullptr, partials, pstride, 0, tix, 0);
   if (last_tile(sd, TB_CG, tix)) {
     const int t0 = sd.tile_first[TB_CG], tc = sd.tile_count[TB_CG];
     const double rrs = scene_sum(partials, pstride, 0, t0, tc);

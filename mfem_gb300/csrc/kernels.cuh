@@ -104,23 +104,23 @@ struct SceneDev {
   const int8_t* mat; // ntp or null
   // element state (Real SoA, stride ntp)
   void* quat;        // 4 x ntp
-  double* s;         // 6 x ntp  mixed stretch variable (FP64 in both paths)
+  void* s;           // 6 x ntp  mixed stretch variable (Ext: float pairs / double)
   void* la;          // 6 x ntp
   void* dS;          // 6 x ntp  S(x) - s of the current x (K1 output)
   void* ds;          // 6 x ntp
   unsigned char* rec;  // nt x rec_bytes  (AoS element records)
-  // vertices (double)
-  double* x;         // 3 nv current positions; pinned entries hold b
-  double* xt;        // 3 nv  x_tilde + h^2 f_ext (the inertial target)
-  double* xhist;     // bdf_order x 3 nv ring
-  double* vhist;     // bdf_order x 3 nv ring
+  // vertices (Ext: float pairs in the mixed path, double in the FP64 path)
+  void* x;           // 3 nv current positions; pinned entries hold b
+  void* xt;          // 3 nv  x_tilde + h^2 f_ext (the inertial target)
+  void* xhist;       // bdf_order x 3 nv ring
+  void* vhist;       // bdf_order x 3 nv ring
   const int* free_map;   // nv: free index, or -1-pin_index when pinned
   const int* free_vert;  // nf
   const int* pin_vert;   // npin
   const double* pin_pos; // 3 npin  pinned positions after the next BC step
   const int* m_ptr;  // nv+1 scalar mass CSR over all vertices
   const int* m_col;
-  const double* m_val;
+  const void* m_val;   // Real
   // BCSR over free vertices
   const int* b_ptr;  // nf+1
   const int* b_col;  // nnzb
