@@ -81,6 +81,7 @@ struct HostMesh {
   std::vector<double> m_val;
   std::vector<int> b_ptr, b_col;
   std::vector<double> b_mass;
+  std::vector<int> slice_off, ell_col;  // sliced-ELL layout of the block values
   std::vector<int> inc_ptr;
   std::vector<int2> inc;
   // boundary script
@@ -370,6 +371,29 @@ int build_host_mesh(const mfem_scene_desc* d, HostMesh& M) {
     }
   }
   M.nnzb = (int)M.b_col.size();
+  // sliced-ELL layout: slices of 32 rows padded to their longest row;
+  // padding blocks point at the row itself (their values are zero)
+  {
+    const int ns = (M.nf + 31) / 32;
+    M.slice_off.assign(ns + 1, 0);
+    for (int sl = 0; sl < ns; ++sl) {
+      int len = 0;
+      for (int r = 32 * sl; r < std::min(M.nf, 32 * sl + 32); ++r) len = std::max(len, M.b_ptr[r + 1] - M.b_ptr[r]);
+      M.slice_off[sl + 1] = M.slice_off[sl] + 32 * len;
+    }
+    M.ell_col.assign(M.slice_off[ns], 0);
+    for (int sl = 0; sl < ns; ++sl) {
+      const int len = (M.slice_off[sl + 1] - M.slice_off[sl]) / 32;
+      for (int rs = 0; rs < 32; ++rs) {
+        const int r = 32 * sl + rs;
+        for (int k = 0; k < len; ++k) {
+          int c = (r < M.nf) ? r : 0;
+          if (r < M.nf && k < M.b_ptr[r + 1] - M.b_ptr[r]) c = M.b_col[M.b_ptr[r] + k];
+          M.ell_col[M.slice_off[sl] + 32 * k + rs] = c;
+        }
+      }
+    }
+  }
   return MFEM_OK;
 }
 
@@ -505,7 +529,9 @@ void layout_scene(mfem_scene* s, Arena& A) {
   D.b_ptr = A.take<int>(M.nf + 1);
   D.b_col = A.take<int>(std::max(M.nnzb, 1));
   D.b_mass = A.take_bytes(std::max(M.nnzb, 1) * r);
-  D.b_val = A.take_bytes(9 * (size_t)std::max(M.nnzb, 1) * r);
+  D.slice_off = A.take<int>(M.slice_off.size());
+  D.ell_col = A.take<int>(std::max<size_t>(M.ell_col.size(), 1));
+  D.ell_val = A.take_bytes(9 * std::max<size_t>(M.ell_col.size(), 1) * r);
   D.dinv = A.take_bytes(9 * (size_t)std::max(M.nf, 1) * r);
   D.inc_ptr = A.take<int>(M.nf + 1);
   D.inc = A.take<int2>(std::max<size_t>(M.inc.size(), 1));
@@ -923,6 +949,8 @@ int scene_init_device(mfem_scene* s) {
   rc |= put(D.m_col, M.m_col.data(), sizeof(int) * M.m_col.size());
   rc |= put(D.b_ptr, M.b_ptr.data(), sizeof(int) * M.b_ptr.size());
   rc |= put(D.b_col, M.b_col.data(), sizeof(int) * M.b_col.size());
+  rc |= put(D.slice_off, M.slice_off.data(), sizeof(int) * M.slice_off.size());
+  rc |= put(D.ell_col, M.ell_col.data(), sizeof(int) * M.ell_col.size());
   rc |= put(D.inc_ptr, M.inc_ptr.data(), sizeof(int) * M.inc_ptr.size());
   rc |= put(D.inc, M.inc.data(), sizeof(int2) * M.inc.size());
   if (rc) return MFEM_ERR_CUDA;
@@ -1389,7 +1417,17 @@ int mfem_gpu_scene_get_system(mfem_scene* s, int32_t* row_ptr, int32_t* col, dou
     }
     return MFEM_OK;
   };
-  int rc = fetch(s->dev.b_val, 9 * (size_t)M.nnzb, val);
+  int rc = MFEM_OK;
+  if (val) {
+    std::vector<double> ell(9 * M.ell_col.size());
+    rc = fetch(s->dev.ell_val, ell.size(), ell.data());
+    for (int r = 0; r < M.nf && !rc; ++r) {
+      const int sl = r / 32, rs = r % 32;
+      for (int k = 0; k < M.b_ptr[r + 1] - M.b_ptr[r]; ++k)
+        for (int e = 0; e < 9; ++e)
+          val[9 * (size_t)(M.b_ptr[r] + k) + e] = ell[9 * ((size_t)M.slice_off[sl] + 32 * k) + 32 * e + rs];
+    }
+  }
   if (!rc) rc = fetch(s->dev.rhs, 3 * (size_t)M.nf, rhs);
   return rc;
 }

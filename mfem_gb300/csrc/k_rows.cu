@@ -98,7 +98,9 @@ __global__ void __launch_bounds__(256) k_assemble(const Tile* tiles, const Scene
     // adds entry l % 9 of local block (i, l / 9) to that block's column slot.
     // Slots of one incidence are distinct, so the adds never collide, and
     // every entry sums its contributions in element order.
-    Real* val = static_cast<Real*>(sd.b_val) + (size_t)rb * 9;
+    const int slice = row >> 5, rs = row & 31;
+    const int soff = sd.slice_off[slice], slen = (sd.slice_off[slice + 1] - soff) >> 5;
+    Real* val = static_cast<Real*>(sd.ell_val) + (size_t)soff * 9 + rs;
     const Real* bm = static_cast<const Real*>(sd.b_mass) + rb;
     Real* acc_w = acc_s[warp];
     for (int w0 = 0; w0 < nb; w0 += kAsmWindow) {
@@ -123,11 +125,16 @@ __global__ void __launch_bounds__(256) k_assemble(const Tile* tiles, const Scene
       }
       for (int o = lane; o < 9 * wn; o += 32) {
         const int q = o / 9, ent = o - 9 * q;
-        val[9 * w0 + o] = acc_w[o] + ((ent == 0 || ent == 4 || ent == 8) ? bm[w0 + q] : Real(0));
+        val[(size_t)288 * (w0 + q) + 32 * ent] =
+            acc_w[o] + ((ent == 0 || ent == 4 || ent == 8) ? bm[w0 + q] : Real(0));
       }
       __syncwarp();
     }
-    __syncwarp();
+    // padding blocks of the slice beyond this row's length are zero
+    for (int o = lane; o < 9 * (slen - nb); o += 32) {
+      const int q = nb + o / 9, ent = o % 9;
+      val[(size_t)288 * q + 32 * ent] = Real(0);
+    }
     // ---- preconditioner from the diagonal block
     int qd = -1;
     for (int q0 = 0; q0 < nb; q0 += 32) {
@@ -139,7 +146,7 @@ __global__ void __launch_bounds__(256) k_assemble(const Tile* tiles, const Scene
       Real* dinv = static_cast<Real*>(sd.dinv);
       Real D[9];
 #pragma unroll
-      for (int k = 0; k < 9; ++k) D[k] = (qd >= 0) ? val[9 * qd + k] : Real(0);
+      for (int k = 0; k < 9; ++k) D[k] = (qd >= 0) ? val[(size_t)288 * qd + 32 * k] : Real(0);
       if (sd.block_jacobi) {
         // inverse of the 3x3 diagonal block (row-major)
         Real c00 = D[4] * D[8] - D[5] * D[7], c01 = D[5] * D[6] - D[3] * D[8],
@@ -277,8 +284,9 @@ __global__ void __launch_bounds__(kCgThreads) k_cg_init(const Tile* tiles, const
 
 // Ap = A p with p = z + beta p_prev formed on the fly (so the p update needs
 // no kernel of its own); p is written to the other buffer of the pair.
-// kCgTpr lanes share a row; the 32 row groups of a tile walk its rows with
-// stride 32 so that each pass reads a contiguous run of block rows.
+// One thread per row over the sliced-ELL layout: every column and value
+// load of a warp is one coalesced 128-byte access, and the block loop is
+// unrolled so that several blocks' loads are in flight per thread.
 template <typename Real>
 __global__ void __launch_bounds__(kCgThreads) k_cg_spmv(const Tile* tiles, const SceneDev* sds,
                                                         double* partials, int pstride,
@@ -294,42 +302,41 @@ __global__ void __launch_bounds__(kCgThreads) k_cg_spmv(const Tile* tiles, const
   const Real* z = static_cast<const Real*>(sd.cg_z);
   const Real* pin = static_cast<const Real*>(sd.cg_p[(it + 1) & 1]);
   Real* pout = static_cast<Real*>(sd.cg_p[it & 1]);
-  const Real* val = static_cast<const Real*>(sd.b_val);
   Real* Ap = static_cast<Real*>(sd.cg_Ap);
-  const int grp = threadIdx.x / kCgTpr, lr = threadIdx.x % kCgTpr;
   using E = typename Ext<Real>::T;
   E pAp[1] = {E(0)};
-  constexpr int kGroups = kCgThreads / kCgTpr;
-#pragma unroll 2
-  for (int rr = grp; rr < kCgRows; rr += kGroups) {
-    const int row = t.begin + rr;
-    Real acc[3] = {0, 0, 0};
-    const bool valid = row < t.end;
-    if (valid) {
-      const int q1 = sd.b_ptr[row + 1];
-      for (int q = sd.b_ptr[row] + lr; q < q1; q += kCgTpr) {
-        const int col = sd.b_col[q];
-        Real p[3];
-#pragma unroll
-        for (int c = 0; c < 3; ++c) p[c] = first ? z[3 * col + c] : z[3 * col + c] + beta * pin[3 * col + c];
-        const Real* b = val + 9 * (size_t)q;
-#pragma unroll
-        for (int r = 0; r < 3; ++r) acc[r] += b[3 * r] * p[0] + b[3 * r + 1] * p[1] + b[3 * r + 2] * p[2];
+  const int row = t.begin + threadIdx.x;
+  if (row < t.end) {
+    const int slice = row >> 5, rs = row & 31;
+    const int soff = sd.slice_off[slice], slen = (sd.slice_off[slice + 1] - soff) >> 5;
+    const int* colp = sd.ell_col + soff + rs;
+    const Real* vp = static_cast<const Real*>(sd.ell_val) + (size_t)soff * 9 + rs;
+    Real acc0 = 0, acc1 = 0, acc2 = 0;
+#pragma unroll 4
+    for (int k = 0; k < slen; ++k) {
+      const int col = colp[32 * k];
+      const Real* v = vp + (size_t)288 * k;
+      Real p0, p1, p2;
+      if (first) {
+        p0 = z[3 * col];
+        p1 = z[3 * col + 1];
+        p2 = z[3 * col + 2];
+      } else {
+        p0 = z[3 * col] + beta * pin[3 * col];
+        p1 = z[3 * col + 1] + beta * pin[3 * col + 1];
+        p2 = z[3 * col + 2] + beta * pin[3 * col + 2];
       }
+      acc0 += v[0] * p0 + v[32] * p1 + v[64] * p2;
+      acc1 += v[96] * p0 + v[128] * p1 + v[160] * p2;
+      acc2 += v[192] * p0 + v[224] * p1 + v[256] * p2;
     }
+    const Real acc[3] = {acc0, acc1, acc2};
 #pragma unroll
-    for (int r = 0; r < 3; ++r)
-#pragma unroll
-      for (int off = kCgTpr / 2; off > 0; off >>= 1)
-        acc[r] += __shfl_down_sync(0xffffffffu, acc[r], off, kCgTpr);
-    if (valid && lr == 0) {
-#pragma unroll
-      for (int c = 0; c < 3; ++c) {
-        const Real p = first ? z[3 * row + c] : z[3 * row + c] + beta * pin[3 * row + c];
-        pout[3 * row + c] = p;
-        Ap[3 * row + c] = acc[c];
-        pAp[0] = pAp[0] + exact_prod(p, acc[c]);
-      }
+    for (int c = 0; c < 3; ++c) {
+      const Real p = first ? z[3 * row + c] : z[3 * row + c] + beta * pin[3 * row + c];
+      pout[3 * row + c] = p;
+      Ap[3 * row + c] = acc[c];
+      pAp[0] = pAp[0] + exact_prod(p, acc[c]);
     }
   }
   tile_partials<E, 1, 0>(pAp, nullptr, partials, pstride, 0, tix, 0);

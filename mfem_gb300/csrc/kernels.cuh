@@ -121,11 +121,19 @@ struct SceneDev {
   const int* m_ptr;  // nv+1 scalar mass CSR over all vertices
   const int* m_col;
   const void* m_val;   // Real
-  // BCSR over free vertices
+  // Block pattern over free vertices (sorted columns per row, the BCSR of
+  // the Assembler) and the sliced-ELL layout the values are stored in:
+  // rows go in slices of 32; block k of row r of slice s sits at block
+  // position slice_off[s] + 32 k + (r mod 32), its 9 entries (row-major 3x3)
+  // at ell_val[9*(slice_off[s] + 32 k) + 32 e + (r mod 32)], so that a warp
+  // reads entry e of block k of 32 rows as one coalesced 128-byte access.
+  // Blocks k >= the row's length are zero and point at the row itself.
   const int* b_ptr;  // nf+1
   const int* b_col;  // nnzb
   const void* b_mass;  // nnzb Real: free-free mass m_ab
-  void* b_val;       // 9 nnzb Real, row-major 3x3 blocks
+  const int* slice_off;  // nslices+1 (in blocks)
+  const int* ell_col;    // slice_off[nslices]
+  void* ell_val;         // 9 * slice_off[nslices] Real
   void* dinv;        // 9 nf Real (block) or 3 nf (Jacobi)
   const int* inc_ptr;  // nf+1 incidences (element, local vertex) per free row
   const int2* inc;     // (element, code): code = i | slot_j << (2+7j), slot 127 = pinned
