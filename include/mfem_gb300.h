@@ -214,6 +214,33 @@ int mfem_gpu_scene_get_system(mfem_scene* scene, int32_t* row_ptr,
 int mfem_gpu_scene_pcg(mfem_scene* scene, const double* b, double* dx,
                        int32_t* iterations, double* rel_residual);
 
+/* ---- allocation-free PCG (no counterpart in the reference) ------------
+ * Block-Jacobi PCG on a caller-owned 3x3 block-CSR matrix already in device
+ * memory (the layout mfem_gpu_scene_get_system returns: row_ptr n+1, col
+ * nnzb, val 9*nnzb row-major blocks, all FP64), solving A x = b from x = 0
+ * with the stopping rule of mfem_gpu_scene_pcg: |r|^2 < tol^2 |b|^2, or
+ * MFEM_ERR_CG_MAXITER after max_iters iterations.  It calls no allocator:
+ * its scratch (five vectors, the inverted diagonal blocks, tile partials,
+ * tickets and scalars, about 6 MiB) is one static __device__ array sized for
+ * MFEM_NOALLOC_PCG_MAX_ROWS block rows; larger systems are rejected with
+ * MFEM_ERR_CAPACITY.  It exists for callers that must not allocate device
+ * memory at solve time: a host framework that hands out all device memory
+ * from its own budget or pool, or a real-time loop where cudaMalloc's
+ * implicit device synchronisation would stall other streams.
+ * The first call on a device (with that device current) looks up the
+ * scratch address with cudaGetSymbolAddress; make it before any stream
+ * capture.  Calls on one device share the scratch, so they are serialised
+ * by a process-wide lock held until the call's stream has drained.  All
+ * pointers must be device memory of the current device; `stream` is a
+ * cudaStream_t (NULL: the legacy default stream).  Returns iterations and
+ * |r|/|b| like mfem_gpu_scene_pcg. */
+#define MFEM_NOALLOC_PCG_MAX_ROWS 32768
+int mfem_gpu_bsr_pcg_noalloc(int32_t n_block_rows, int32_t nnzb,
+                             const int32_t* row_ptr, const int32_t* col,
+                             const double* val, const double* b, double* x,
+                             int32_t max_iters, double tol, void* stream,
+                             int32_t* iterations, double* rel_residual);
+
 #ifdef __cplusplus
 }
 #endif

@@ -1,6 +1,6 @@
 """Builds the CUDA library libmfem_gb300.so in-tree for sm_103a (GB300).
 
-The three translation units compile in parallel with nvcc and link into
+The translation units compile in parallel with nvcc and link into
 mfem_gb300/_build/libmfem_gb300.so.  No CMake, no torch extension machinery.
 """
 import concurrent.futures as cf
@@ -13,7 +13,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 OUT_DIR = os.path.join(HERE, "_build")
 LIB_NAME = "libmfem_gb300.so"
-SOURCES = ["k_elem.cu", "k_rows.cu", "host.cu"]
+SOURCES = ["k_elem.cu", "k_rows.cu", "k_noalloc.cu", "host.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 
