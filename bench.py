@@ -10,14 +10,16 @@ there is no dataset in this workload.
 One JSON line on rank 0:
   value       timesteps/s of the whole job, state resident in HBM, from the
               per-step CUDA-event times of the library's stream
-  e2e         the same metric through the C ABI with host buffers: every step
-              uploads the pinned positions from host memory and reads the new
-              vertex positions back
+  e2e         the same steps again from the same starting state, through the
+              C ABI with pinned host buffers: every step uploads the pinned
+              vertices' targets and reads all vertex positions back
   roofline    the dominant kernel's algorithmic bytes per launch / its average
               launch time (CUDA events around every launch in the timed steps)
-  cpu_baseline  the FP64 oracle port on the host cores, one Newton iteration of
-              the same scene (bounded sample), scaled by Newton iterations/step
-  --impl reference  the same oracle port as the reference's CPU arm.
+  cpu_baseline  the FP64 oracle port on the host cores (bounded sample): one
+              Newton iteration of the same scene without its PCG and one PCG
+              iteration, combined with this run's iterations per step
+  --impl reference  the same oracle port as the reference's CPU arm, with the
+              oracle's own iteration counts (oracle/calibration.json).
 
 Multi-GPU (torchrun): independent replicas, one scene per rank (the path has
 no exchange step); value = N * steps / max over ranks of the timed seconds.
@@ -53,6 +55,7 @@ def parse():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--cpu-threads", type=int, default=0)
+    ap.add_argument("--pcg-kernel", default="persistent", choices=["persistent", "split", "fused"])
     return ap.parse_args()
 
 
@@ -140,12 +143,22 @@ class ClockSampler:
 
 
 # ---------------------------------------------------------- byte models --
-def kernel_bytes(kind, sizes, rsz):
-    """Algorithmic bytes per launch (each array read or written once)."""
+def kernel_bytes(kind, sizes, rsz, cg_per_launch=None):
+    """Algorithmic bytes per launch (each array read or written once).
+    k_cg_solve runs a whole PCG solve: cg_per_launch iterations of SpMV +
+    update."""
     nt, nv, nf, nnzb, n_inc, nnz_m = (sizes[k] for k in ("nt", "nv", "nf", "nnzb", "n_inc", "nnz_m"))
+    if kind == "k_cg_solve":
+        if not cg_per_launch:
+            return None
+        return cg_per_launch * (kernel_bytes("k_cg_spmv", sizes, rsz) + kernel_bytes("k_cg_update", sizes, rsz))
     if kind == "k_cg_spmv":
         # values + block cols + row ptr, z and p_prev read, Ap and p written
         return nnzb * (9 * rsz + 4) + 4 * (nf + 1) + 4 * 3 * nf * rsz
+    if kind == "k_cgf_iter":
+        # one pass of the matrix; own rows: r, w, s, u, p, x read and r, w, s,
+        # u, p, x written (neighbour values come from caches)
+        return nnzb * (9 * rsz + 4) + 4 * (nf + 1) + 12 * 3 * nf * rsz
     if kind == "k_cg_update":
         # x (rw), r (rw), p, Ap, z (w), Jacobi diagonal
         return 8 * 3 * nf * rsz
@@ -189,12 +202,15 @@ def make_spec(args, precision):
     from mfem_gb300 import abi, configs
     prec = abi.PRECISION_MIXED if precision == "mixed" else abi.PRECISION_FP64
     solver = abi.SOLVER_EIGEN_CG_DIAG if args.solver == "eigen-pcg-diag" else abi.SOLVER_GPU_PCG_BLOCK
+    kern = {"persistent": abi.PCG_KERNEL_PERSISTENT, "split": abi.PCG_KERNEL_SPLIT,
+            "fused": abi.PCG_KERNEL_FUSED}[args.pcg_kernel]
     if args.config == "c1":
-        return configs.beam_c1(precision=prec, linear_solver=solver), "beam_c1_200tets"
+        return configs.beam_c1(precision=prec, linear_solver=solver, pcg_kernel=kern), "beam_c1_200tets"
     if args.config == "c3":
-        return configs.stress_c3(precision=prec, linear_solver=solver), "stress_c3_135k"
+        return configs.stress_c3(precision=prec, linear_solver=solver, pcg_kernel=kern), "stress_c3_135k"
     n = args.size
-    return configs.cube_c2(n=n, precision=prec, linear_solver=solver), f"cube_c2_{n}^3_{5 * n ** 3}tets"
+    return configs.cube_c2(n=n, precision=prec, linear_solver=solver, pcg_kernel=kern), \
+        f"cube_c2_{n}^3_{5 * n ** 3}tets"
 
 
 def scene_sizes(spec, scene):
@@ -212,19 +228,46 @@ def scene_sizes(spec, scene):
 
 
 # ------------------------------------------------------------ CPU sample --
-def cpu_newton_sample(spec, threads):
-    """FP64 oracle: seconds of one Newton iteration of the scene (update,
-    assembly, PCG to the scene's tolerance, local solve, line search)."""
+def cpu_costs(spec, threads, samples, warmup, budget_s):
+    """FP64 oracle on the host cores: seconds of one Newton iteration without
+    its PCG (timed from the same state every sample) and of one PCG iteration
+    (one solve of that Newton system).  Sampling stops early once budget_s
+    has passed, keeping at least one timed sample."""
     import copy
     import oracle
     oracle.set_threads(threads)
     s = copy.copy(spec)
     s.max_newton_iterations = 1
     sc = oracle.OracleScene(s)
-    t0 = time.perf_counter()
-    st = sc.step()
-    t1 = time.perf_counter()
-    return t1 - t0, st
+    state0 = sc.get_state()
+    _, _, _, rhs = sc.get_system()
+    t = time.perf_counter()
+    _, cg_its, _ = sc.pcg(rhs)
+    t_cg = (time.perf_counter() - t) / max(cg_its, 1)
+    t_start = time.perf_counter()
+    rest = []
+    for i in range(warmup + samples):
+        sc.set_state(**state0)
+        t = time.perf_counter()
+        st = sc.step()
+        dt = time.perf_counter() - t
+        if i >= warmup:
+            rest.append(max(dt - st.cg_iterations * t_cg, 0.0))
+        if rest and time.perf_counter() - t_start > budget_s:
+            break
+    return {"t_newton": float(np.mean(rest)), "t_cg": t_cg, "samples": len(rest),
+            "pcg_iterations_timed": cg_its, "threads": threads}
+
+
+def cpu_line(costs, newton, cgits, workload, where):
+    t_step = newton * costs["t_newton"] + cgits * costs["t_cg"]
+    return {"value": 1.0 / t_step, "unit": UNIT, "cores": costs["threads"], "kind": "port",
+            "sample": (f"FP64 oracle on {costs['threads']} host threads, {workload}: one Newton "
+                       f"iteration without its PCG {costs['t_newton']:.3f} s (mean of "
+                       f"{costs['samples']} from the same state), one Jacobi-PCG iteration "
+                       f"{1e3 * costs['t_cg']:.2f} ms (from a {costs['pcg_iterations_timed']}-iteration "
+                       f"solve); per step = {newton:.2f} Newton x {costs['t_newton']:.3f} s + "
+                       f"{cgits:.0f} PCG x {1e3 * costs['t_cg']:.2f} ms ({where})")}
 
 
 def run_reference(args):
@@ -232,42 +275,40 @@ def run_reference(args):
     if rank != 0:
         return 0
     import oracle  # noqa: F401  (the reference arm is the FP64 port on the host cores)
-    from mfem_gb300 import abi
     threads = args.cpu_threads or os.cpu_count()
     spec, workload = make_spec(args, "fp64")
-    iters_per_step = _newton_iters_hint(args)
-    times = []
-    for i in range(args.warmup + args.steps):
-        t, st = cpu_newton_sample(spec, threads)
-        if i >= args.warmup:
-            times.append(t)
-    t_iter = float(np.mean(times))
-    value = 1.0 / (t_iter * iters_per_step)
+    newton, cgits, where = _iteration_counts(args)
+    costs = cpu_costs(spec, threads, args.steps, min(args.warmup, 1), budget_s=150.0)
+    cb = cpu_line(costs, newton, cgits, workload, where)
+    value = cb["value"]
     line = {
         "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000.0 / value,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
         "data": "synthetic", "config": {"workload": workload, "precision": "fp64",
                                         "solver": args.solver},
-        "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
-                         "sample": f"one Newton iteration of {workload} per step "
-                                   f"({t_iter:.2f} s), x {iters_per_step} Newton iterations/step"},
+        "cpu_baseline": cb,
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
     return 0
 
 
-def _newton_iters_hint(args):
-    """Newton iterations per step of this workload at the 1e-5 residual test
-    (measured by the oracle, oracle/calibration.json), default 4."""
+def _iteration_counts(args):
+    """Newton and PCG iterations per step of the timed window (steps
+    warmup+1 .. warmup+steps), measured by the FP64 oracle
+    (oracle/calibration.json, made by oracle/calibrate.py)."""
     p = os.path.join(ROOT, "oracle", "calibration.json")
+    key = f"{args.config}_{args.size}" if args.config == "c2" else args.config
     if os.path.exists(p):
-        d = json.load(open(p))
-        key = f"{args.config}_{args.size}" if args.config == "c2" else args.config
-        if key in d:
-            return float(d[key]["newton_iterations_per_step"])
-    return 4.0
+        d = json.load(open(p)).get(key)
+        if d and "newton_iterations" in d:
+            its, cgs = d["newton_iterations"], d["cg_iterations"]
+            w = its[args.warmup:args.warmup + args.steps] or its
+            c = cgs[args.warmup:args.warmup + args.steps] or cgs
+            return (float(np.mean(w)), float(np.mean(c)),
+                    f"oracle counts of steps {args.warmup + 1}..{args.warmup + len(w)}")
+    return 4.0, 1000.0, "no calibration: assumed 4 Newton and 1000 PCG iterations per step"
 
 
 # ----------------------------------------------------------------- ours --
@@ -292,6 +333,7 @@ def run_ours(args):
 
     for _ in range(args.warmup):
         st = scene.step()
+    state0 = scene.get_state()
     barrier(pg)
     gpu.set_profiling(batch_h, True)
     sampler = ClockSampler(local)
@@ -310,40 +352,54 @@ def run_ours(args):
     dev_s_max = allmax(pg, dev_s)
     value = ws * args.steps / dev_s_max
 
-    # ---- end to end through the C ABI with host buffers
+    # ---- end to end through the C ABI with host buffers: the same steps
+    # again from the state the timed region started from
     e2e = None
     if not args.no_e2e:
+        import torch
         pins = scene.pinned()
-        state = scene.get_state()
-        pin_host = np.ascontiguousarray(state["x"][pins])
-        x_host = np.zeros((scene.n_vertices, 3))
-        n_e2e = max(3, args.steps // 2)
+        scene.set_state(x=state0["x"], v=state0["v"], s=state0["s"], R=state0["R"])
+        pin_host = torch.from_numpy(np.ascontiguousarray(state0["x"][pins])).pin_memory()
+        x_host = torch.zeros((scene.n_vertices, 3), dtype=torch.float64).pin_memory()
+        dptr = ctypes.POINTER(ctypes.c_double)
+        e2e_stats = []
         barrier(pg)
         t0 = time.perf_counter()
-        for _ in range(n_e2e):
-            scene.set_pins(pin_host)                       # H2D: this step's pinned targets
-            scene.step()
-            L.mfem_gpu_scene_get_state(scene.handle, x_host.ctypes.data_as(
-                ctypes.POINTER(ctypes.c_double)), None, None, None, None)  # D2H: positions
+        for _ in range(args.steps):
+            L.mfem_gpu_scene_set_pins(scene.handle, ctypes.cast(pin_host.data_ptr(), dptr))  # H2D
+            e2e_stats.append(scene.step())
+            L.mfem_gpu_scene_get_state(scene.handle, ctypes.cast(x_host.data_ptr(), dptr),
+                                       None, None, None, None)                          # D2H
         e2e_s = allmax(pg, time.perf_counter() - t0)
-        e2e = {"value": ws * n_e2e / e2e_s, "unit": UNIT,
-               "h2d_bytes_per_step": int(pin_host.nbytes), "d2h_bytes_per_step": int(x_host.nbytes),
-               "steps": n_e2e}
+        e2e = {"value": ws * args.steps / e2e_s, "unit": UNIT,
+               "h2d_bytes_per_step": int(pin_host.numel() * 8),
+               "d2h_bytes_per_step": int(x_host.numel() * 8), "steps": args.steps,
+               "newton_iterations_per_step": float(np.mean([t.newton_iterations for t in e2e_stats])),
+               "cg_iterations_per_step": float(np.mean([t.cg_iterations for t in e2e_stats])),
+               "host_buffers": "pinned (cudaHostAlloc through torch.pin_memory)"}
 
     # ---- roofline of the dominant kernel
+    cg_total = float(sum(s["cg_iterations"] for s in stats))
+    cg_per_solve = cg_total / kstats["k_cg_solve"][1] if kstats.get("k_cg_solve", (0, 0))[1] else None
     dom = max(kstats, key=lambda k: kstats[k][0])
     dom_ms, dom_n = kstats[dom]
-    abytes = kernel_bytes(dom, sizes, rsz)
+    abytes = kernel_bytes(dom, sizes, rsz, cg_per_solve)
     peak, peak_src = measured_peak()
     achieved = abytes / (dom_ms / dom_n / 1e3) / 1e9 if abytes and dom_n else None
+    if dom == "k_cg_solve" and cg_per_solve:
+        # per PCG iteration, so that the figure compares with the split kernels
+        roof_note = f"k_cg_solve: {cg_per_solve:.1f} PCG iterations per launch"
+    else:
+        roof_note = None
     roof = {"kernel": dom, "bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+            "note": roof_note,
             "frac": achieved / peak if achieved else None, "traffic": read_traffic(dom, "c2"),
             "algorithmic_bytes_per_launch": abytes, "avg_launch_us": 1e3 * dom_ms / dom_n,
             "peak_source": f"{peak_src} (MEASURED_PEAKS.json hbm_gbs)"}
     per_kernel = {}
     for k, (kms, kn) in kstats.items():
         if kn:
-            b = kernel_bytes(k, sizes, rsz)
+            b = kernel_bytes(k, sizes, rsz, cg_per_solve)
             per_kernel[k] = {"ms": round(kms, 3), "launches": kn,
                              "share": round(kms / max(dev_s * 1e3, 1e-9), 4),
                              "GBps": round(b / (kms / kn / 1e3) / 1e9, 1) if (b and kms > 0) else None}
@@ -360,6 +416,7 @@ def run_ours(args):
         "config": {"workload": workload, "tets": sizes["nt"], "vertices": sizes["nv"],
                    "free_dofs": 3 * sizes["nf"], "blocks": sizes["nnzb"],
                    "precision": args.precision, "solver": args.solver,
+                   "pcg_kernel": args.pcg_kernel,
                    "newton_residual_tolerance": spec.newton_residual_tolerance,
                    "pcg_tolerance": spec.iterative_solver_tolerance,
                    "l2": "working set > L2 (about 1 GB per step)",
@@ -374,11 +431,9 @@ def run_ours(args):
     if rank == 0 and ws == 1 and not args.no_cpu_baseline:
         threads = args.cpu_threads or os.cpu_count()
         ref_spec, _ = make_spec(args, "fp64")
-        t_it, _ = cpu_newton_sample(ref_spec, threads)
-        cpu_val = 1.0 / (t_it * newton)
-        line["cpu_baseline"] = {"value": cpu_val, "unit": UNIT, "cores": threads, "kind": "port",
-                                "sample": f"one FP64 Newton iteration of {workload} "
-                                          f"({t_it:.2f} s) x {newton:.2f} Newton iterations/step"}
+        costs = cpu_costs(ref_spec, threads, 1, 0, budget_s=60.0)
+        line["cpu_baseline"] = cpu_line(costs, newton, cgits, workload,
+                                        "this run's GPU iteration counts")
     if rank == 0:
         print(json.dumps(line), flush=True)
     scene.close()

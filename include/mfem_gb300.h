@@ -77,6 +77,15 @@ enum {
 
 enum { MFEM_PRECISION_FP64 = 0, MFEM_PRECISION_MIXED = 1 };
 
+/* How the PCG runs.  PERSISTENT: one cooperative (co-resident,
+ * grid-synchronised) launch per solve; SPLIT: two launches per iteration
+ * with a host check for convergence every few iterations (same arithmetic
+ * and bitwise the same results as PERSISTENT: Eigen's PCG iteration).
+ * FUSED: the single-reduction form of the same PCG (Chronopoulos and Gear,
+ * 1989), one launch per iteration; equal to the others in exact arithmetic,
+ * not bitwise. */
+enum { MFEM_PCG_KERNEL_PERSISTENT = 0, MFEM_PCG_KERNEL_SPLIT = 1, MFEM_PCG_KERNEL_FUSED = 2 };
+
 /* Scene descriptor.  One tetrahedral object (or several concatenated by the
  * caller, as Meshes does in src/mesh/meshes.cpp:11-56).  Arrays are
  * row-major: vertex i at [3*i .. 3*i+2], tet e at [4*e .. 4*e+3].         */
@@ -109,7 +118,9 @@ typedef struct mfem_scene_desc {
                                          max(|rhs_0|, |h^2 P M f|)             */
   int32_t linear_solver;              /* MFEM_SOLVER_*                            */
   int32_t precision;                  /* MFEM_PRECISION_*                         */
-  int32_t reserved[8];
+  int32_t pcg_kernel;                 /* MFEM_PCG_KERNEL_* (a batch uses the first
+                                         scene's choice)                         */
+  int32_t reserved[7];
 } mfem_scene_desc;
 
 /* Per-step statistics (the reference prints these as its per-iteration
@@ -183,7 +194,8 @@ int mfem_gpu_scene_set_pins(mfem_scene* scene, const double* positions);
 enum {
   MFEM_K_ELEM_UPDATE = 0, MFEM_K_ASSEMBLE = 1, MFEM_K_CG_INIT = 2, MFEM_K_CG_SPMV = 3,
   MFEM_K_CG_UPDATE = 4, MFEM_K_LOCAL_SOLVE = 5, MFEM_K_LS_ENERGY = 6, MFEM_K_APPLY = 7,
-  MFEM_K_STEP_BEGIN = 8, MFEM_K_STEP_END = 9, MFEM_K_SCALARS = 10, MFEM_K_COUNT = 11
+  MFEM_K_STEP_BEGIN = 8, MFEM_K_STEP_END = 9, MFEM_K_SCALARS = 10, MFEM_K_CG_SOLVE = 11,
+  MFEM_K_CGF_ITER = 12, MFEM_K_COUNT = 13
 };
 int mfem_gpu_scene_solo_batch(mfem_scene* scene, mfem_batch** batch);
 int mfem_gpu_batch_set_profiling(mfem_batch* batch, int enable);

@@ -54,6 +54,10 @@ BC_PINMIN, BC_COMPRESS = 16, 17
 PRECISION_FP64 = 0
 PRECISION_MIXED = 1
 
+PCG_KERNEL_PERSISTENT = 0
+PCG_KERNEL_SPLIT = 1
+PCG_KERNEL_FUSED = 2
+
 _dp = C.POINTER(C.c_double)
 _ip = C.POINTER(C.c_int32)
 
@@ -87,7 +91,8 @@ class SceneDesc(C.Structure):
         ("newton_residual_tolerance", C.c_double),
         ("linear_solver", C.c_int32),
         ("precision", C.c_int32),
-        ("reserved", C.c_int32 * 8),
+        ("pcg_kernel", C.c_int32),
+        ("reserved", C.c_int32 * 7),
     ]
 
 

@@ -49,6 +49,26 @@ std::once_flag g_configured;
 
 size_t align_up(size_t v, size_t a) { return (v + a - 1) / a * a; }
 
+// The column of a packed ELL slot, stored as the integer's bits in a Real word.
+template <typename T> T col_word(int c);
+template <> float col_word<float>(int c) {
+  float f;
+  std::memcpy(&f, &c, 4);
+  return f;
+}
+template <> double col_word<double>(int c) {
+  const long long l = c;
+  double d;
+  std::memcpy(&d, &l, 8);
+  return d;
+}
+
+// A double as a float pair hi + lo (df64) for the mixed path's constants.
+float2 split_df(double d) {
+  const float hi = float(d);
+  return make_float2(hi, float(d - double(hi)));
+}
+
 // Sub-allocations of one device allocation.
 struct Arena {
   char* base = nullptr;
@@ -82,6 +102,7 @@ struct HostMesh {
   std::vector<int> b_ptr, b_col;
   std::vector<double> b_mass;
   std::vector<int> slice_off, ell_col;  // sliced-ELL layout of the block values
+  std::vector<int> ref_of_row, row_of_ref;  // device free row <-> reference free index
   std::vector<int> inc_ptr;
   std::vector<int2> inc;
   // boundary script
@@ -258,17 +279,17 @@ int build_host_mesh(const mfem_scene_desc* d, HostMesh& M) {
   M.free_vert.clear();
   M.pin_vert.clear();
   M.pin_group.clear();
+  std::vector<int> ref_free;  // free vertices in vertex order (the reference's numbering)
   for (int v = 0; v < nv; ++v) {
     if (M.is_fixed[v]) {
       M.free_map[v] = -1 - (int)M.pin_vert.size();
       M.pin_vert.push_back(v);
       M.pin_group.push_back(group[v]);
     } else {
-      M.free_map[v] = (int)M.free_vert.size();
-      M.free_vert.push_back(v);
+      ref_free.push_back(v);
     }
   }
-  M.nf = (int)M.free_vert.size();
+  M.nf = (int)ref_free.size();
   M.npin = (int)M.pin_vert.size();
   // ---- geometry: |det Dm|/6 and dphi/dX = rows of Dm^{-1} (tet_mesh.cpp:31-75)
   M.vol.resize(nt);
@@ -293,6 +314,42 @@ int build_host_mesh(const mfem_scene_desc* d, HostMesh& M) {
     std::vector<int> fill(vt_ptr.begin(), vt_ptr.end() - 1);
     for (int e = 0; e < nt; ++e)
       for (int k = 0; k < 4; ++k) vt[fill[M.T[4 * e + k]]++] = 4 * e + k;  // sorted by e
+  }
+  // ---- device numbering of the free rows: within each window of kCgRows
+  // rows (vertex order), by decreasing block count, so that the sliced-ELL
+  // slices of 32 rows need almost no padding (SELL-C-sigma)
+  {
+    std::vector<int> cnt(M.nf, 0), mark(nv, -1);
+    for (int i = 0; i < M.nf; ++i) {
+      const int a = ref_free[i];
+      for (int q = vt_ptr[a]; q < vt_ptr[a + 1]; ++q) {
+        const int e = vt[q] / 4;
+        for (int k = 0; k < 4; ++k) {
+          const int b = M.T[4 * e + k];
+          if (!M.is_fixed[b] && mark[b] != i) {
+            mark[b] = i;
+            cnt[i] += 1;
+          }
+        }
+      }
+    }
+    std::vector<int> order(M.nf);
+    for (int i = 0; i < M.nf; ++i) order[i] = i;
+    for (int w = 0; w < M.nf; w += kCgRows) {
+      const int we = std::min(M.nf, w + kCgRows);
+      std::stable_sort(order.begin() + w, order.begin() + we,
+                       [&](int x, int y) { return cnt[x] > cnt[y]; });
+    }
+    M.free_vert.resize(M.nf);
+    M.ref_of_row.resize(M.nf);
+    M.row_of_ref.resize(M.nf);
+    for (int r = 0; r < M.nf; ++r) {
+      const int i = order[r];
+      M.free_vert[r] = ref_free[i];
+      M.free_map[ref_free[i]] = r;
+      M.ref_of_row[r] = i;
+      M.row_of_ref[i] = r;
+    }
   }
   // ---- consistent P1 mass over all vertices (linear_tetmesh_mass_matrix)
   const double* rho = d->density;
@@ -434,6 +491,8 @@ struct mfem_batch {
   SceneScalars* h_sc = nullptr;     // pinned, one per scene
   int max_newton = 0, max_ls = 0, max_cg = 0;
   int cg_hint = 16;
+  int pcg_kernel = MFEM_PCG_KERNEL_PERSISTENT;
+  int coop_grid = 0;  // blocks of the persistent PCG (all co-resident)
   int pstride = 0;  // tiles per partials quantity
   // instrumentation
   bool profiling = false;
@@ -530,19 +589,25 @@ void layout_scene(mfem_scene* s, Arena& A) {
   D.b_col = A.take<int>(std::max(M.nnzb, 1));
   D.b_mass = A.take_bytes(std::max(M.nnzb, 1) * r);
   D.slice_off = A.take<int>(M.slice_off.size());
-  D.ell_col = A.take<int>(std::max<size_t>(M.ell_col.size(), 1));
-  D.ell_val = A.take_bytes(9 * std::max<size_t>(M.ell_col.size(), 1) * r);
+  D.ell = A.take_bytes(10 * std::max<size_t>(M.ell_col.size(), 1) * r);
   D.dinv = A.take_bytes(9 * (size_t)std::max(M.nf, 1) * r);
   D.inc_ptr = A.take<int>(M.nf + 1);
   D.inc = A.take<int2>(std::max<size_t>(M.inc.size(), 1));
-  const size_t n3 = 3 * (size_t)std::max(M.nf, 1);
-  D.rhs = A.take_bytes(n3 * r);
-  D.cg_x = A.take_bytes(n3 * r);
-  D.cg_r = A.take_bytes(n3 * r);
-  D.cg_z = A.take_bytes(n3 * r);
-  D.cg_p[0] = A.take_bytes(n3 * r);
-  D.cg_p[1] = A.take_bytes(n3 * r);
-  D.cg_Ap = A.take_bytes(n3 * r);
+  const size_t n4 = 4 * (size_t)std::max(M.nf, 1);
+  D.rhs = A.take_bytes(n4 * r);
+  D.cg_x = A.take_bytes(n4 * r);
+  D.cg_r = A.take_bytes(n4 * r);
+  D.cg_z = A.take_bytes(n4 * r);
+  D.cg_p[0] = A.take_bytes(n4 * r);
+  D.cg_p[1] = A.take_bytes(n4 * r);
+  D.cg_Ap = A.take_bytes(n4 * r);
+  if (s->cfg.pcg_kernel == MFEM_PCG_KERNEL_FUSED) {
+    for (int k = 0; k < 2; ++k) {
+      D.cgf_r[k] = A.take_bytes(n4 * r);
+      D.cgf_w[k] = A.take_bytes(n4 * r);
+      D.cgf_s[k] = A.take_bytes(n4 * r);
+    }
+  }
   s->d_sc = A.take<SceneScalars>(1);
   D.sc = s->d_sc;
   // first-level ticket counters: one per group of kTicketGroup tiles per table
@@ -609,6 +674,7 @@ int upload_reals(void* dst, const std::vector<double>& src, size_t count, cudaSt
 
 template <typename T>
 int upload_scene_reals(mfem_scene* s, cudaStream_t st) {
+  static_assert(sizeof(T) == 4 || sizeof(T) == 8, "Real");
   const HostMesh& M = s->M;
   const int ntp = s->ntp;
   SceneDev& D = s->dev;
@@ -631,6 +697,19 @@ int upload_scene_reals(mfem_scene* s, cudaStream_t st) {
   std::vector<T> bm(std::max(M.nnzb, 1), T(0));
   for (int k = 0; k < M.nnzb; ++k) bm[k] = T(M.b_mass[k]);
   if ((rc = put(D.b_mass, bm))) return rc;
+  // packed ELL slots: the column word of every slot (values start at zero
+  // and are written by the assembly)
+  {
+    std::vector<T> ell(10 * std::max<size_t>(M.ell_col.size(), 1), T(0));
+    const int ns = (int)M.slice_off.size() - 1;
+    for (int sl = 0; sl < ns; ++sl) {
+      const int soff = M.slice_off[sl], len = (M.slice_off[sl + 1] - soff) / 32;
+      for (int k = 0; k < len; ++k)
+        for (int rs = 0; rs < 32; ++rs)
+          ell[2 * ell_pair(soff, k, rs, 0)] = col_word<T>(M.ell_col[soff + 32 * k + rs]);
+    }
+    if ((rc = put(D.ell, ell))) return rc;
+  }
   CUDA_OR(cudaStreamSynchronize(st), MFEM_ERR_CUDA);
   return MFEM_OK;
 }
@@ -701,6 +780,44 @@ int worst_status(const SceneScalars& sc) {
   return MFEM_OK;
 }
 
+// PCG iterations after k_cg_init: one cooperative launch for the whole solve,
+// or SpMV/update launch pairs in chunks with a host check of the active
+// count after each chunk.
+int run_pcg(mfem_batch* b, const Launch& Lcg) {
+  int rc;
+  const bool fused = b->pcg_kernel == MFEM_PCG_KERNEL_FUSED;
+  {
+    KTimer t(b, MFEM_K_CG_INIT);
+    if (fused) launch_cgf_init(Lcg);
+    else launch_cg_init(Lcg);
+  }
+  if (b->pcg_kernel == MFEM_PCG_KERNEL_PERSISTENT) {
+    cudaError_t e;
+    { KTimer t(b, MFEM_K_CG_SOLVE); e = launch_cg_solve(Lcg, b->coop_grid, b->max_cg + 1); }
+    CUDA_OR(e, MFEM_ERR_CUDA);
+    return MFEM_OK;
+  }
+  int it = 0;
+  int chunk = std::max(4, b->cg_hint);
+  while (it < b->max_cg) {
+    const int c = std::min(chunk, b->max_cg - it);
+    for (int k = 0; k < c; ++k, ++it) {
+      if (fused) {
+        KTimer t(b, MFEM_K_CGF_ITER);
+        launch_cgf_iter(Lcg);
+      } else {
+        { KTimer t(b, MFEM_K_CG_SPMV); launch_cg_spmv(Lcg); }
+        { KTimer t(b, MFEM_K_CG_UPDATE); launch_cg_update(Lcg); }
+      }
+    }
+    if ((rc = sync_counters(b))) return rc;
+    if (b->h_ctr->cg_active == 0) break;
+    chunk = 8;
+  }
+  b->cg_hint = std::max(4, (it * 3) / 4);
+  return MFEM_OK;
+}
+
 // The Newton loop of NewtonOptimizer::step for every scene of the batch.
 int batch_newton(mfem_batch* b) {
   const int n = (int)b->scenes.size();
@@ -711,22 +828,7 @@ int batch_newton(mfem_batch* b) {
   for (int newton = 0; newton <= b->max_newton + 1; ++newton) {
     { KTimer t(b, MFEM_K_ELEM_UPDATE); launch_elem_update(make_launch(b, TB_ELEM), nullptr); }
     { KTimer t(b, MFEM_K_ASSEMBLE); launch_assemble(make_launch(b, TB_ROW)); }
-    Launch Lcg = make_launch(b, TB_CG);
-    { KTimer t(b, MFEM_K_CG_INIT); launch_cg_init(Lcg); }
-    int done = 0;
-    int chunk = std::max(4, b->cg_hint);
-    while (done < b->max_cg) {
-      const int c = std::min(chunk, b->max_cg - done);
-      for (int k = 0; k < c; ++k) {
-        { KTimer t(b, MFEM_K_CG_SPMV); launch_cg_spmv(Lcg); }
-        { KTimer t(b, MFEM_K_CG_UPDATE); launch_cg_update(Lcg); }
-      }
-      done += c;
-      if ((rc = sync_counters(b))) return rc;
-      if (b->h_ctr->cg_active == 0) break;
-      chunk = 8;
-    }
-    b->cg_hint = std::max(4, (done * 3) / 4);
+    if ((rc = run_pcg(b, make_launch(b, TB_CG)))) return rc;
     { KTimer t(b, MFEM_K_LOCAL_SOLVE); launch_local_solve(Lev); }
     for (int l = 0; l < b->max_ls; ++l) {
       { KTimer t(b, MFEM_K_LS_ENERGY); launch_ls_energy(Lev); }
@@ -735,6 +837,7 @@ int batch_newton(mfem_batch* b) {
     }
     { KTimer t(b, MFEM_K_APPLY); launch_apply(Lev); }
     if ((rc = sync_counters(b))) return rc;
+    if (b->h_ctr->error) return MFEM_ERR_TIMEOUT;
     if (b->h_ctr->newton_active == 0) break;
   }
   return MFEM_OK;
@@ -824,6 +927,17 @@ int batch_build(mfem_scene* const* scenes, int n, mfem_batch** out) {
     b->ntiles[tb] = (int)tabs[tb].size();
     maxt = std::max(maxt, tabs[tb].size());
   }
+  b->pcg_kernel = scenes[0]->cfg.pcg_kernel;
+  for (int i = 1; i < n; ++i)
+    if (scenes[i]->cfg.pcg_kernel != b->pcg_kernel) return MFEM_ERR_INVALID;
+  if (b->pcg_kernel == MFEM_PCG_KERNEL_PERSISTENT) {
+    int dev = 0, sms = 0;
+    CUDA_OR(cudaGetDevice(&dev), MFEM_ERR_CUDA);
+    CUDA_OR(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev), MFEM_ERR_CUDA);
+    const int per_sm = cg_solve_blocks_per_sm(b->fp64);
+    if (per_sm <= 0) return MFEM_ERR_CUDA;
+    b->coop_grid = std::min(b->ntiles[TB_CG], per_sm * sms);
+  }
   Arena A;
   auto lay = [&](Arena& a) {
     for (int tb = 0; tb < TB_COUNT; ++tb) b->d_tiles[tb] = a.take<Tile>(std::max<size_t>(tabs[tb].size(), 1));
@@ -894,6 +1008,7 @@ int scene_init_device(mfem_scene* s) {
   D.block_jacobi = s->cfg.linear_solver == MFEM_SOLVER_GPU_PCG_BLOCK ? 1 : 0;
   D.fp64 = s->fp64;
   D.h2 = s->h2;
+  D.h2x = split_df(D.h2);
   D.dt = s->dt;
   D.newton_tol = s->cfg.newton_tol;
   D.res_tol = s->cfg.newton_residual_tolerance;
@@ -950,7 +1065,6 @@ int scene_init_device(mfem_scene* s) {
   rc |= put(D.b_ptr, M.b_ptr.data(), sizeof(int) * M.b_ptr.size());
   rc |= put(D.b_col, M.b_col.data(), sizeof(int) * M.b_col.size());
   rc |= put(D.slice_off, M.slice_off.data(), sizeof(int) * M.slice_off.size());
-  rc |= put(D.ell_col, M.ell_col.data(), sizeof(int) * M.ell_col.size());
   rc |= put(D.inc_ptr, M.inc_ptr.data(), sizeof(int) * M.inc_ptr.size());
   rc |= put(D.inc, M.inc.data(), sizeof(int2) * M.inc.size());
   if (rc) return MFEM_ERR_CUDA;
@@ -1104,6 +1218,9 @@ static int scene_prepare(const mfem_scene_desc* desc, std::unique_ptr<mfem_scene
     return MFEM_ERR_UNSUPPORTED;
   if (desc->max_newton_iterations < 0 || desc->max_linesearch_iterations < 0 ||
       desc->max_iterative_solver_iters < 0)
+    return MFEM_ERR_INVALID;
+  if (desc->pcg_kernel != MFEM_PCG_KERNEL_PERSISTENT && desc->pcg_kernel != MFEM_PCG_KERNEL_SPLIT &&
+      desc->pcg_kernel != MFEM_PCG_KERNEL_FUSED)
     return MFEM_ERR_INVALID;
   s->cfg = *desc;
   // pointers in the copied descriptor are not kept
@@ -1306,7 +1423,8 @@ int mfem_gpu_batch_kernel_stats(mfem_batch* b, int kernel, double* total_ms, int
 int mfem_gpu_kernel_name(int kernel, char* name, int name_len) {
   static const char* names[MFEM_K_COUNT] = {
       "k_elem_update", "k_assemble", "k_cg_init", "k_cg_spmv", "k_cg_update", "k_local_solve",
-      "k_ls_energy", "k_apply", "k_step_begin", "k_step_end", "k_scalars_begin"};
+      "k_ls_energy", "k_apply", "k_step_begin", "k_step_end", "k_scalars_begin",
+      "k_cg_solve", "k_cgf_iter"};
   if (kernel < 0 || kernel >= MFEM_K_COUNT || !name || name_len <= 0) return MFEM_ERR_INVALID;
   strncpy(name, names[kernel], name_len - 1);
   name[name_len - 1] = 0;
@@ -1340,6 +1458,7 @@ int mfem_gpu_scene_elem_update(mfem_scene* s, const double* x, double h, double*
   // run K1 with h^2 = h*h and FP64 debug outputs
   SceneDev D = b->h_sds[0];
   D.h2 = h * h;
+  D.h2x = split_df(D.h2);
   CUDA_OR(cudaMemcpy(b->d_sds, &D, sizeof(D), cudaMemcpyHostToDevice), MFEM_ERR_CUDA);
   const size_t per = 9 + 6 + 54 + 6 + 36 + 36 + 144 + 6;
   double* dbuf = nullptr;
@@ -1392,6 +1511,78 @@ int mfem_gpu_scene_bcsr_sizes(mfem_scene* s, int32_t* nf, int32_t* nnzb) {
   return MFEM_OK;
 }
 
+// Real vector of the device (4 Real per free row, device row order) to
+// FP64 in the reference's free order (3 per row, vertex order).
+int fetch_rows(const mfem_scene* s, const void* src, double* dst) {
+  const HostMesh& M = s->M;
+  const size_t n4 = 4 * (size_t)M.nf;
+  std::vector<double> t(n4);
+  if (s->fp64) {
+    CUDA_OR(cudaMemcpy(t.data(), src, n4 * 8, cudaMemcpyDeviceToHost), MFEM_ERR_CUDA);
+  } else {
+    std::vector<float> f(n4);
+    CUDA_OR(cudaMemcpy(f.data(), src, n4 * 4, cudaMemcpyDeviceToHost), MFEM_ERR_CUDA);
+    for (size_t i = 0; i < n4; ++i) t[i] = f[i];
+  }
+  for (int r = 0; r < M.nf; ++r)
+    for (int c = 0; c < 3; ++c) dst[3 * (size_t)M.ref_of_row[r] + c] = t[4 * (size_t)r + c];
+  return MFEM_OK;
+}
+
+int put_rows(const mfem_scene* s, const double* src, void* dst) {
+  const HostMesh& M = s->M;
+  const size_t n4 = 4 * (size_t)M.nf;
+  std::vector<double> t(n4, 0.0);
+  for (int r = 0; r < M.nf; ++r)
+    for (int c = 0; c < 3; ++c) t[4 * (size_t)r + c] = src[3 * (size_t)M.ref_of_row[r] + c];
+  if (s->fp64) {
+    CUDA_OR(cudaMemcpy(dst, t.data(), n4 * 8, cudaMemcpyHostToDevice), MFEM_ERR_CUDA);
+  } else {
+    std::vector<float> f(t.begin(), t.end());
+    CUDA_OR(cudaMemcpy(dst, f.data(), n4 * 4, cudaMemcpyHostToDevice), MFEM_ERR_CUDA);
+  }
+  return MFEM_OK;
+}
+
+// The assembled system as FP64 BCSR in the reference's free order: rows
+// and columns by vertex order of the free vertices (the Assembler's sorted
+// pairs), blocks row-major.
+int system_to_host(const mfem_scene* s, int32_t* row_ptr, int32_t* col, double* val, double* rhs) {
+  const HostMesh& M = s->M;
+  std::vector<double> ell;
+  if (val) {
+    const size_t nw = 10 * M.ell_col.size();
+    ell.resize(nw);
+    if (s->fp64) {
+      CUDA_OR(cudaMemcpy(ell.data(), s->dev.ell, nw * 8, cudaMemcpyDeviceToHost), MFEM_ERR_CUDA);
+    } else {
+      std::vector<float> f(nw);
+      CUDA_OR(cudaMemcpy(f.data(), s->dev.ell, nw * 4, cudaMemcpyDeviceToHost), MFEM_ERR_CUDA);
+      for (size_t i = 0; i < nw; ++i) ell[i] = f[i];
+    }
+  }
+  int32_t pos = 0;
+  if (row_ptr) row_ptr[0] = 0;
+  std::vector<std::pair<int, int>> cols;  // (reference column, block k of the device row)
+  for (int i = 0; i < M.nf; ++i) {
+    const int r = M.row_of_ref[i];
+    const int sl = r / 32, rs = r % 32, soff = M.slice_off[sl];
+    const int rb = M.b_ptr[r], nb = M.b_ptr[r + 1] - rb;
+    cols.clear();
+    for (int k = 0; k < nb; ++k) cols.push_back({M.ref_of_row[M.b_col[rb + k]], k});
+    std::sort(cols.begin(), cols.end());
+    for (int j = 0; j < nb; ++j) {
+      if (col) col[pos + j] = cols[j].first;
+      if (val)
+        for (int e = 0; e < 9; ++e) val[9 * (size_t)(pos + j) + e] = ell[ell_entry(soff, cols[j].second, rs, e)];
+    }
+    pos += nb;
+    if (row_ptr) row_ptr[i + 1] = pos;
+  }
+  if (rhs) return fetch_rows(s, s->dev.rhs, rhs);
+  return MFEM_OK;
+}
+
 // Assembles LHS and RHS at the current state (update_system + pre_solve).
 int mfem_gpu_scene_get_system(mfem_scene* s, int32_t* row_ptr, int32_t* col, double* val,
                               double* rhs) {
@@ -1403,70 +1594,21 @@ int mfem_gpu_scene_get_system(mfem_scene* s, int32_t* row_ptr, int32_t* col, dou
   launch_assemble(make_launch(b, TB_ROW));
   CUDA_OR(cudaStreamSynchronize(b->stream), MFEM_ERR_CUDA);
   CUDA_OR(cudaGetLastError(), MFEM_ERR_CUDA);
-  const HostMesh& M = s->M;
-  if (row_ptr) std::memcpy(row_ptr, M.b_ptr.data(), sizeof(int) * M.b_ptr.size());
-  if (col) std::memcpy(col, M.b_col.data(), sizeof(int) * M.b_col.size());
-  auto fetch = [&](const void* src, size_t n, double* dst) -> int {
-    if (!dst) return MFEM_OK;
-    if (s->fp64) {
-      CUDA_OR(cudaMemcpy(dst, src, n * 8, cudaMemcpyDeviceToHost), MFEM_ERR_CUDA);
-    } else {
-      std::vector<float> t(n);
-      CUDA_OR(cudaMemcpy(t.data(), src, n * 4, cudaMemcpyDeviceToHost), MFEM_ERR_CUDA);
-      for (size_t i = 0; i < n; ++i) dst[i] = t[i];
-    }
-    return MFEM_OK;
-  };
-  int rc = MFEM_OK;
-  if (val) {
-    std::vector<double> ell(9 * M.ell_col.size());
-    rc = fetch(s->dev.ell_val, ell.size(), ell.data());
-    for (int r = 0; r < M.nf && !rc; ++r) {
-      const int sl = r / 32, rs = r % 32;
-      for (int k = 0; k < M.b_ptr[r + 1] - M.b_ptr[r]; ++k)
-        for (int e = 0; e < 9; ++e)
-          val[9 * (size_t)(M.b_ptr[r] + k) + e] = ell[9 * ((size_t)M.slice_off[sl] + 32 * k) + 32 * e + rs];
-    }
-  }
-  if (!rc) rc = fetch(s->dev.rhs, 3 * (size_t)M.nf, rhs);
-  return rc;
+  return system_to_host(s, row_ptr, col, val, rhs);
 }
 
 int mfem_gpu_scene_pcg(mfem_scene* s, const double* bvec, double* dx, int32_t* iterations,
                        double* rel_residual) {
   if (!s || !bvec || !dx) return MFEM_ERR_INVALID;
   mfem_batch* b = s->solo;
-  const size_t n3 = 3 * (size_t)s->M.nf;
-  if (s->fp64) {
-    CUDA_OR(cudaMemcpy(s->dev.rhs, bvec, n3 * 8, cudaMemcpyHostToDevice), MFEM_ERR_CUDA);
-  } else {
-    std::vector<float> t(bvec, bvec + n3);
-    CUDA_OR(cudaMemcpy(s->dev.rhs, t.data(), n3 * 4, cudaMemcpyHostToDevice), MFEM_ERR_CUDA);
-  }
+  int rc = put_rows(s, bvec, s->dev.rhs);
+  if (rc) return rc;
   launch_scalars_begin(make_launch(b, TB_EV), 1);
-  Launch Lcg = make_launch(b, TB_CG);
-  launch_cg_init(Lcg);
-  int done = 0;
-  while (done < b->max_cg) {
-    const int c = std::min(8, b->max_cg - done);
-    for (int k = 0; k < c; ++k) {
-      launch_cg_spmv(Lcg);
-      launch_cg_update(Lcg);
-    }
-    done += c;
-    int rc = sync_counters(b);
-    if (rc) return rc;
-    if (b->h_ctr->cg_active == 0) break;
-  }
-  CUDA_OR(cudaStreamSynchronize(b->stream), MFEM_ERR_CUDA);
+  if ((rc = run_pcg(b, make_launch(b, TB_CG)))) return rc;
+  if ((rc = sync_counters(b))) return rc;
+  if (b->h_ctr->error) return MFEM_ERR_TIMEOUT;
   CUDA_OR(cudaGetLastError(), MFEM_ERR_CUDA);
-  if (s->fp64) {
-    CUDA_OR(cudaMemcpy(dx, s->dev.cg_x, n3 * 8, cudaMemcpyDeviceToHost), MFEM_ERR_CUDA);
-  } else {
-    std::vector<float> t(n3);
-    CUDA_OR(cudaMemcpy(t.data(), s->dev.cg_x, n3 * 4, cudaMemcpyDeviceToHost), MFEM_ERR_CUDA);
-    for (size_t i = 0; i < n3; ++i) dx[i] = t[i];
-  }
+  if ((rc = fetch_rows(s, s->dev.cg_x, dx))) return rc;
   SceneScalars sc;
   CUDA_OR(cudaMemcpy(&sc, s->d_sc, sizeof(sc), cudaMemcpyDeviceToHost), MFEM_ERR_CUDA);
   if (iterations) *iterations = sc.cg_total;

@@ -79,7 +79,7 @@ __device__ __forceinline__ void deformation_gradients(const SceneDev& sd, const 
       const int f = sd.free_map[v[k]];
       if (f >= 0) {
 #pragma unroll
-        for (int d = 0; d < 3; ++d) p[k][d] = p[k][d] + alpha * E(dx[3 * f + d]);
+        for (int d = 0; d < 3; ++d) p[k][d] = p[k][d] + alpha * E(dx[4 * f + d]);
       }
     }
   }
@@ -220,7 +220,7 @@ __global__ void __launch_bounds__(kElemTile)
   const SceneDev& sd = sds[t.scene];
   if (!sd.sc->newton_active) return;
   const int e = t.begin + threadIdx.x;
-  const Real h2 = Real(sd.h2);
+  const Real h2 = Ext<Real>::r(sd.h2, sd.h2x);
   if (e < t.end) {
     unsigned int* out = words + threadIdx.x * kStride;
     ElemIn<Real> in;
@@ -253,7 +253,7 @@ __global__ void __launch_bounds__(kElemTile)
       if (!Prec<Real>::kFP64) polish_rotation(RE, FE);
       stretch_vec(RE, FE, SE);
       material_grad<E>(in.mat, E(in.mu), E(in.lam), sE, gE);
-      const E h2E = E(sd.h2);
+      const E h2E = Ext<Real>::c(sd.h2, sd.h2x);
 #pragma unroll
       for (int i = 0; i < 6; ++i) dE[i] = SE[i] - sE[i];
 #pragma unroll
@@ -363,7 +363,7 @@ __device__ __forceinline__ typename Ext<Real>::T vertex_energy(const SceneDev& s
 #pragma unroll
     for (int c = 0; c < 3; ++c) {
       E d = Ext<Real>::ld(sd.x, 3 * (size_t)b + c) - Ext<Real>::ld(sd.xt, 3 * (size_t)b + c);
-      if (dx && fb >= 0) d = d + alpha * E(dx[3 * fb + c]);
+      if (dx && fb >= 0) d = d + alpha * E(dx[4 * fb + c]);
       Md[c] = Md[c] + m * d;
     }
   }
@@ -372,7 +372,7 @@ __device__ __forceinline__ typename Ext<Real>::T vertex_energy(const SceneDev& s
 #pragma unroll
   for (int c = 0; c < 3; ++c) {
     E d = Ext<Real>::ld(sd.x, 3 * (size_t)a + c) - Ext<Real>::ld(sd.xt, 3 * (size_t)a + c);
-    if (dx && fa >= 0) d = d + alpha * E(dx[3 * fa + c]);
+    if (dx && fa >= 0) d = d + alpha * E(dx[4 * fa + c]);
     e2 = e2 + d * Md[c];
   }
   return E(0.5) * e2;
@@ -381,7 +381,7 @@ __device__ __forceinline__ typename Ext<Real>::T vertex_energy(const SceneDev& s
 // ------------------------------------------------------------------ K5 ---
 // ds = (S - s) + dS/dF : dF(dx)  (the closed form of -H^{-1}(Sym la + g),
 // MixedStretch::solve), la = -Syminv (H ds + g); E(0), max |ds|, max |dx|.
-// Tile partials: 0,1 E(0) (compensated pair), 2 sum |terms|, 3 max|ds|, 4 max|dx|.
+// Tile partials: 0 E(0), 1 sum |terms|, 2 max|ds|, 3 max|dx|.
 template <typename Real>
 __global__ void __launch_bounds__(kElemTile) k_local_solve(const Tile* tiles, const SceneDev* sds,
                                                            double* partials, int pstride,
@@ -392,10 +392,10 @@ __global__ void __launch_bounds__(kElemTile) k_local_solve(const Tile* tiles, co
   const SceneDev& sd = sds[t.scene];
   SceneScalars* sc = sd.sc;
   if (!sc->newton_active) return;
-  const Real h2 = Real(sd.h2);
+  const Real h2 = Ext<Real>::r(sd.h2, sd.h2x);
   const Real* cgx = static_cast<const Real*>(sd.cg_x);
   E sums[2] = {E(0), E(0)};
-  double maxs[2] = {0.0, 0.0};
+  Real maxs[2] = {Real(0), Real(0)};
   const int idx = t.begin + threadIdx.x;
   if (t.kind == 0) {
     if (idx < t.end) {
@@ -418,7 +418,7 @@ __global__ void __launch_bounds__(kElemTile) k_local_solve(const Tile* tiles, co
       for (int k = 0; k < 4; ++k) {
         const int f = sd.free_map[v[k]];
 #pragma unroll
-        for (int c = 0; c < 3; ++c) dd[k][c] = f >= 0 ? cgx[3 * f + c] : Real(0);
+        for (int c = 0; c < 3; ++c) dd[k][c] = f >= 0 ? cgx[4 * f + c] : Real(0);
       }
       Real dF[9];
 #pragma unroll
@@ -458,7 +458,7 @@ __global__ void __launch_bounds__(kElemTile) k_local_solve(const Tile* tiles, co
       Real m = 0;
 #pragma unroll
       for (int i = 0; i < 6; ++i) m = fmax(m, Real(fabs(ds[i])));
-      maxs[0] = double(m);
+      maxs[0] = m;
     }
   } else if (idx < t.end) {
     const int a = idx;
@@ -467,27 +467,30 @@ __global__ void __launch_bounds__(kElemTile) k_local_solve(const Tile* tiles, co
     if (f >= 0) {
       Real m = 0;
 #pragma unroll
-      for (int c = 0; c < 3; ++c) m = fmax(m, Real(fabs(cgx[3 * f + c])));
-      maxs[1] = double(m);
+      for (int c = 0; c < 3; ++c) m = fmax(m, Real(fabs(cgx[4 * f + c])));
+      maxs[1] = m;
     }
   }
-  tile_partials<E, 2, 2>(sums, maxs, partials, pstride, 0, tix, 1);
+  tile_partials<E, Real, 2, 2>(sums, maxs, partials, pstride, 0, tix);
   if (last_tile(sd, TB_EV, tix)) {
     const int t0 = sd.tile_first[TB_EV], tc = sd.tile_count[TB_EV];
-    const double Ev = scene_ksum(partials, pstride, 0, t0, tc);
-    const double ea = scene_sum(partials, pstride, 2, t0, tc);
-    const double ms = scene_max(partials, pstride, 3, t0, tc);
-    const double mx = scene_max(partials, pstride, 4, t0, tc);
+    E v[2];
+    scene_sums<E, 2>(partials, pstride, 0, t0, tc, v);
+    const Real ms_ = scene_max<Real>(partials, pstride, 2, t0, tc);
+    const Real mx_ = scene_max<Real>(partials, pstride, 3, t0, tc);
     if (threadIdx.x == 0) {
+      const double Ev = to_double_any(v[0]), ea = to_double_any(v[1]);
+      const double ms = double(ms_), mx = double(mx_);
       sc->E_abs = ea;
       sc->E = Ev;
-      sc->eres = fabs((Ev - sc->E_prev) / (Ev + 1e-6));
+      sc->eres = fabs(Fin<Real>::div(Ev - sc->E_prev, Ev + 1e-6));
       sc->E_prev = Ev;
       sc->fx0 = Ev;
       sc->max_ds = ms;
       sc->max_dx = mx;
       sc->decrement = fmax(mx, ms);
       sc->alpha_ls = 1.0;
+      sc->alpha_ls_f = 1.0f;
       sc->ls_iter = 0;
       sc->ls_ok = 0;
       if (sd.max_ls > 0) {
@@ -501,7 +504,7 @@ __global__ void __launch_bounds__(kElemTile) k_local_solve(const Tile* tiles, co
 }
 
 // ------------------------------------------------------------------ K6 ---
-// Tile partials: 0,1 E(alpha) (compensated pair), 2 sum |terms|.
+// Tile partials: 0 E(alpha), 1 sum |terms|.
 template <typename Real>
 __global__ void __launch_bounds__(kElemTile) k_ls_energy(const Tile* tiles, const SceneDev* sds,
                                                          double* partials, int pstride,
@@ -512,8 +515,8 @@ __global__ void __launch_bounds__(kElemTile) k_ls_energy(const Tile* tiles, cons
   const SceneDev& sd = sds[t.scene];
   SceneScalars* sc = sd.sc;
   if (!sc->ls_active) return;
-  const E alpha = E(sc->alpha_ls);
-  const Real h2 = Real(sd.h2);
+  const E alpha = E(sc->alpha_ls_f);
+  const Real h2 = Ext<Real>::r(sd.h2, sd.h2x);
   const Real* cgx = static_cast<const Real*>(sd.cg_x);
   E sums[2] = {E(0), E(0)};
   const int idx = t.begin + threadIdx.x;
@@ -551,12 +554,13 @@ __global__ void __launch_bounds__(kElemTile) k_ls_energy(const Tile* tiles, cons
   } else if (idx < t.end) {
     sums[0] = vertex_energy<Real>(sd, idx, cgx, alpha);
   }
-  tile_partials<E, 2, 0>(sums, nullptr, partials, pstride, 0, tix, 1);
+  tile_partials<E, Real, 2, 0>(sums, nullptr, partials, pstride, 0, tix);
   if (last_tile(sd, TB_EV, tix)) {
     const int t0 = sd.tile_first[TB_EV], tc = sd.tile_count[TB_EV];
-    const double fx = scene_ksum(partials, pstride, 0, t0, tc);
-    const double eab = scene_sum(partials, pstride, 2, t0, tc);
+    E v[2];
+    scene_sums<E, 2>(partials, pstride, 0, t0, tc, v);
     if (threadIdx.x == 0) {
+      const double fx = to_double_any(v[0]), eab = to_double_any(v[1]);
       sc->E_trial = fx;
       // Armijo with c = 0 (newton_optimizer.cpp:58).  With FP32 element
       // energies a difference below their rounding bound is not a decision
@@ -568,6 +572,7 @@ __global__ void __launch_bounds__(kElemTile) k_ls_energy(const Tile* tiles, cons
         atomicSub(&ctrs->ls_active, 1);
       } else {
         sc->alpha_ls *= 0.5;
+        sc->alpha_ls_f = float(sc->alpha_ls);
         sc->ls_iter += 1;
         if (sc->ls_iter >= sd.max_ls) {
           sc->ls_active = 0;
@@ -592,7 +597,7 @@ __global__ void __launch_bounds__(kElemTile) k_apply(const Tile* tiles, const Sc
   if (!sc->newton_active) return;
   const int idx = t.begin + threadIdx.x;
   if (sc->ls_ok && idx < t.end) {
-    const E alpha = E(sc->alpha_ls);
+    const E alpha = E(sc->alpha_ls_f);
     if (t.kind == 0) {
       const Real* ds = static_cast<const Real*>(sd.ds);
 #pragma unroll
@@ -607,7 +612,7 @@ __global__ void __launch_bounds__(kElemTile) k_apply(const Tile* tiles, const Sc
 #pragma unroll
         for (int c = 0; c < 3; ++c) {
           const size_t k = 3 * (size_t)idx + c;
-          Ext<Real>::st(sd.x, k, Ext<Real>::ld(sd.x, k) + alpha * E(cgx[3 * f + c]));
+          Ext<Real>::st(sd.x, k, Ext<Real>::ld(sd.x, k) + alpha * E(cgx[4 * f + c]));
         }
       }
     }

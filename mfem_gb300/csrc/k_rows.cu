@@ -35,6 +35,55 @@ __device__ __forceinline__ int rec_offset(int i, int j, int l, int m) {
   return start + 6 + 9 * (j - i - 1) + 3 * l + m;
 }
 
+// Three components of a row of a 4-padded vector: one 16-byte access in
+// FP32, two in FP64.  kCo: the load bypasses L1 (data written by other
+// blocks earlier in the same launch).
+template <bool kCo>
+__device__ __forceinline__ void ld3(const float* p, float v[3]) {
+  const float4 t = kCo ? __ldcg(reinterpret_cast<const float4*>(p)) : *reinterpret_cast<const float4*>(p);
+  v[0] = t.x;
+  v[1] = t.y;
+  v[2] = t.z;
+}
+template <bool kCo>
+__device__ __forceinline__ void ld3(const double* p, double v[3]) {
+  const double2 a = kCo ? __ldcg(reinterpret_cast<const double2*>(p)) : *reinterpret_cast<const double2*>(p);
+  const double2 b = kCo ? __ldcg(reinterpret_cast<const double2*>(p) + 1) : reinterpret_cast<const double2*>(p)[1];
+  v[0] = a.x;
+  v[1] = a.y;
+  v[2] = b.x;
+}
+__device__ __forceinline__ void st3(float* p, const float v[3]) {
+  *reinterpret_cast<float4*>(p) = make_float4(v[0], v[1], v[2], 0.f);
+}
+__device__ __forceinline__ void st3(double* p, const double v[3]) {
+  reinterpret_cast<double2*>(p)[0] = make_double2(v[0], v[1]);
+  reinterpret_cast<double2*>(p)[1] = make_double2(v[2], 0.0);
+}
+
+// Loads of data that other blocks wrote earlier in the same launch: in the
+// persistent PCG (kCo) they bypass L1, which is not coherent across SMs;
+// between separate launches a plain load is fine.
+template <bool kCo, typename T> __device__ __forceinline__ T ldv(const T* p) {
+  if constexpr (kCo) return __ldcg(p);
+  else return *p;
+}
+
+// Pair w of a packed ELL slot; the column of pair 0 is stored as the
+// integer's bits in the first word.
+template <bool kCo>
+__device__ __forceinline__ float2 ld_pair(const float* ell, size_t pair) {
+  const float2* p = reinterpret_cast<const float2*>(ell) + pair;
+  return kCo ? __ldcg(p) : *p;
+}
+template <bool kCo>
+__device__ __forceinline__ double2 ld_pair(const double* ell, size_t pair) {
+  const double2* p = reinterpret_cast<const double2*>(ell) + pair;
+  return kCo ? __ldcg(p) : *p;
+}
+__device__ __forceinline__ int pair_col(float2 w) { return __float_as_int(w.x); }
+__device__ __forceinline__ int pair_col(double2 w) { return (int)__double_as_longlong(w.x); }
+
 constexpr int kAsmWindow = 64;  // block slots per warp accumulated in shared memory per pass
 
 template <typename Real>
@@ -86,11 +135,13 @@ __global__ void __launch_bounds__(256) k_assemble(const Tile* tiles, const Scene
     if (lane == 0) {
       Real* rhs = static_cast<Real*>(sd.rhs);
       E r2 = E(0);
+      Real rv[3];
 #pragma unroll
       for (int c = 0; c < 3; ++c) {
-        rhs[3 * row + c] = Real(Ext<Real>::to_real(acc[c]));
+        rv[c] = Real(Ext<Real>::to_real(acc[c]));
         r2 = r2 + acc[c] * acc[c];
       }
+      st3(rhs + 4 * (size_t)row, rv);
       rn2 = rn2 + r2;
     }
     // ---- block values: the warp accumulates the row's blocks in shared
@@ -100,7 +151,7 @@ __global__ void __launch_bounds__(256) k_assemble(const Tile* tiles, const Scene
     // every entry sums its contributions in element order.
     const int slice = row >> 5, rs = row & 31;
     const int soff = sd.slice_off[slice], slen = (sd.slice_off[slice + 1] - soff) >> 5;
-    Real* val = static_cast<Real*>(sd.ell_val) + (size_t)soff * 9 + rs;
+    Real* val = static_cast<Real*>(sd.ell);
     const Real* bm = static_cast<const Real*>(sd.b_mass) + rb;
     Real* acc_w = acc_s[warp];
     for (int w0 = 0; w0 < nb; w0 += kAsmWindow) {
@@ -125,7 +176,7 @@ __global__ void __launch_bounds__(256) k_assemble(const Tile* tiles, const Scene
       }
       for (int o = lane; o < 9 * wn; o += 32) {
         const int q = o / 9, ent = o - 9 * q;
-        val[(size_t)288 * (w0 + q) + 32 * ent] =
+        val[ell_entry(soff, w0 + q, rs, ent)] =
             acc_w[o] + ((ent == 0 || ent == 4 || ent == 8) ? bm[w0 + q] : Real(0));
       }
       __syncwarp();
@@ -133,7 +184,7 @@ __global__ void __launch_bounds__(256) k_assemble(const Tile* tiles, const Scene
     // padding blocks of the slice beyond this row's length are zero
     for (int o = lane; o < 9 * (slen - nb); o += 32) {
       const int q = nb + o / 9, ent = o % 9;
-      val[(size_t)288 * q + 32 * ent] = Real(0);
+      val[ell_entry(soff, q, rs, ent)] = Real(0);
     }
     // ---- preconditioner from the diagonal block
     int qd = -1;
@@ -146,7 +197,7 @@ __global__ void __launch_bounds__(256) k_assemble(const Tile* tiles, const Scene
       Real* dinv = static_cast<Real*>(sd.dinv);
       Real D[9];
 #pragma unroll
-      for (int k = 0; k < 9; ++k) D[k] = (qd >= 0) ? val[(size_t)288 * qd + 32 * k] : Real(0);
+      for (int k = 0; k < 9; ++k) D[k] = (qd >= 0) ? val[ell_entry(soff, qd, rs, k)] : Real(0);
       if (sd.block_jacobi) {
         // inverse of the 3x3 diagonal block (row-major)
         Real c00 = D[4] * D[8] - D[5] * D[7], c01 = D[5] * D[6] - D[3] * D[8],
@@ -169,23 +220,27 @@ __global__ void __launch_bounds__(256) k_assemble(const Tile* tiles, const Scene
         }
       } else {
         // DiagonalPreconditioner: 1/a_ii, or 1 where a_ii == 0
+        Real dj[3];
 #pragma unroll
         for (int c = 0; c < 3; ++c) {
           const Real d = D[4 * c];
-          dinv[3 * row + c] = d != Real(0) ? Real(1) / d : Real(1);
+          dj[c] = d != Real(0) ? Real(1) / d : Real(1);
         }
+        st3(dinv + 4 * (size_t)row, dj);
       }
     }
   }
   }
   {
     typename Ext<Real>::T sums[1] = {rn2};
-    tile_partials<typename Ext<Real>::T, 1, 0>(sums, nullptr, partials, pstride, 0, tix, 0);
+    tile_partials<typename Ext<Real>::T, Real, 1, 0>(sums, nullptr, partials, pstride, 0, tix);
   }
   if (last_tile(sd, TB_ROW, tix)) {
-    const double s = scene_sum(partials, pstride, 0, sd.tile_first[TB_ROW], sd.tile_count[TB_ROW]);
+    const auto s_ = scene_sum<typename Ext<Real>::T>(partials, pstride, 0, sd.tile_first[TB_ROW],
+                                                     sd.tile_count[TB_ROW]);
     if (threadIdx.x == 0) {
-      const double rn = sqrt(s);
+      const double s = to_double_any(s_);
+      const double rn = Fin<Real>::sqrt(s);
       if (sc->newton_iter == 0) sc->rhs_norm0 = rn;
       sc->rhs_norm = rn;
       // |rhs_k| <= tol * max(|rhs_0|, |h^2 P M f|)
@@ -220,10 +275,17 @@ __device__ __forceinline__ void apply_prec(const SceneDev& sd, int row, const Re
 #pragma unroll
     for (int c = 0; c < 3; ++c) z[c] = D[3 * c] * r[0] + D[3 * c + 1] * r[1] + D[3 * c + 2] * r[2];
   } else {
+    Real d[3];
+    ld3<false>(dinv + 4 * (size_t)row, d);
 #pragma unroll
-    for (int c = 0; c < 3; ++c) z[c] = dinv[3 * (size_t)row + c] * r[c];
+    for (int c = 0; c < 3; ++c) z[c] = d[c] * r[c];
   }
 }
+
+// ------------------------------------------------------------- PCG ------
+// Every kernel writes tile partials; the last tile of a scene to finish
+// (atomic tickets, no thread waits) reduces them in a fixed order and sets
+// the scene's scalars (alpha, beta, the stopping test) for the next kernel.
 
 // r = b, z = D^{-1} b, x = 0, rz; one thread per row.
 template <typename Real>
@@ -239,30 +301,31 @@ __global__ void __launch_bounds__(kCgThreads) k_cg_init(const Tile* tiles, const
   E dots[2] = {E(0), E(0)};  // r.r, r.z
   const int row = t.begin + threadIdx.x;
   if (row < t.end) {
-    const Real* b = static_cast<const Real*>(sd.rhs) + 3 * (size_t)row;
-    Real r[3] = {b[0], b[1], b[2]}, z[3];
+    const size_t k = 4 * (size_t)row;
+    Real r[3], z[3];
+    ld3<false>(static_cast<const Real*>(sd.rhs) + k, r);
     apply_prec<Real>(sd, row, r, z);
-    Real* pr = static_cast<Real*>(sd.cg_r) + 3 * (size_t)row;
-    Real* pz = static_cast<Real*>(sd.cg_z) + 3 * (size_t)row;
-    Real* px = static_cast<Real*>(sd.cg_x) + 3 * (size_t)row;
+    const Real zero[3] = {Real(0), Real(0), Real(0)};
+    st3(static_cast<Real*>(sd.cg_r) + k, r);
+    st3(static_cast<Real*>(sd.cg_z) + k, z);
+    st3(static_cast<Real*>(sd.cg_x) + k, zero);
 #pragma unroll
     for (int c = 0; c < 3; ++c) {
-      pr[c] = r[c];
-      pz[c] = z[c];
-      px[c] = Real(0);
       dots[0] = dots[0] + exact_prod(r[c], r[c]);
       dots[1] = dots[1] + exact_prod(r[c], z[c]);
     }
   }
-  tile_partials<E, 2, 0>(dots, nullptr, partials, pstride, 0, tix, 0);
+  tile_partials<E, Real, 2, 0>(dots, nullptr, partials, pstride, 0, tix);
   if (last_tile(sd, TB_CG, tix)) {
     const int t0 = sd.tile_first[TB_CG], tc = sd.tile_count[TB_CG];
-    const double rrs = scene_sum(partials, pstride, 0, t0, tc);
-    const double rzs = scene_sum(partials, pstride, 1, t0, tc);
+    E v[2];
+    scene_sums<E, 2>(partials, pstride, 0, t0, tc, v);
     if (threadIdx.x == 0) {
+      const double rrs = to_double_any(v[0]), rzs = to_double_any(v[1]);
       sc->cg_rhs_norm2 = rrs;
       sc->cg_iter = 0;
       sc->beta = 0.0;
+      sc->beta_f = 0.0f;
       sc->rz = rzs;
       sc->cg_err = 0.0;
       if (rrs == 0.0) {
@@ -284,117 +347,124 @@ __global__ void __launch_bounds__(kCgThreads) k_cg_init(const Tile* tiles, const
 
 // Ap = A p with p = z + beta p_prev formed on the fly (so the p update needs
 // no kernel of its own); p is written to the other buffer of the pair.
-// One thread per row over the sliced-ELL layout: every column and value
-// load of a warp is one coalesced 128-byte access, and the block loop is
-// unrolled so that several blocks' loads are in flight per thread.
-template <typename Real>
-__global__ void __launch_bounds__(kCgThreads) k_cg_spmv(const Tile* tiles, const SceneDev* sds,
-                                                        double* partials, int pstride,
-                                                        BatchCounters* ctrs) {
-  const int tix = blockIdx.x;
+// One thread per row over the sliced-ELL layout: every matrix load of a
+// warp is one coalesced access, the column arriving with the first pair.
+template <typename Real, bool kCo>
+__device__ __forceinline__ void cg_spmv_tile(int tix, const Tile* tiles, const SceneDev* sds,
+                                             double* partials, int pstride) {
   const Tile t = tiles[tix];
   const SceneDev& sd = sds[t.scene];
   SceneScalars* sc = sd.sc;
-  if (!sc->cg_active) return;
-  const int it = sc->cg_iter;
-  const Real beta = Real(sc->beta);
+  if (!ldv<kCo>(&sc->cg_active)) return;
+  const int it = ldv<kCo>(&sc->cg_iter);
+  const Real beta = sizeof(Real) == 4 ? Real(ldv<kCo>(&sc->beta_f)) : Real(ldv<kCo>(&sc->beta));
   const bool first = (it == 0);
   const Real* z = static_cast<const Real*>(sd.cg_z);
   const Real* pin = static_cast<const Real*>(sd.cg_p[(it + 1) & 1]);
   Real* pout = static_cast<Real*>(sd.cg_p[it & 1]);
   Real* Ap = static_cast<Real*>(sd.cg_Ap);
+  const Real* ell = static_cast<const Real*>(sd.ell);
   using E = typename Ext<Real>::T;
   E pAp[1] = {E(0)};
   const int row = t.begin + threadIdx.x;
   if (row < t.end) {
     const int slice = row >> 5, rs = row & 31;
     const int soff = sd.slice_off[slice], slen = (sd.slice_off[slice + 1] - soff) >> 5;
-    const int* colp = sd.ell_col + soff + rs;
-    const Real* vp = static_cast<const Real*>(sd.ell_val) + (size_t)soff * 9 + rs;
     Real acc0 = 0, acc1 = 0, acc2 = 0;
 #pragma unroll 4
     for (int k = 0; k < slen; ++k) {
-      const int col = colp[32 * k];
-      const Real* v = vp + (size_t)288 * k;
-      Real p0, p1, p2;
-      if (first) {
-        p0 = z[3 * col];
-        p1 = z[3 * col + 1];
-        p2 = z[3 * col + 2];
-      } else {
-        p0 = z[3 * col] + beta * pin[3 * col];
-        p1 = z[3 * col + 1] + beta * pin[3 * col + 1];
-        p2 = z[3 * col + 2] + beta * pin[3 * col + 2];
+      const size_t q = ell_pair(soff, k, rs, 0);
+      const auto w0 = ld_pair<false>(ell, q), w1 = ld_pair<false>(ell, q + 32),
+                 w2 = ld_pair<false>(ell, q + 64), w3 = ld_pair<false>(ell, q + 96),
+                 w4 = ld_pair<false>(ell, q + 128);
+      const int col = pair_col(w0);
+      Real p[3];
+      ld3<kCo>(z + 4 * (size_t)col, p);
+      if (!first) {
+        Real pp[3];
+        ld3<kCo>(pin + 4 * (size_t)col, pp);
+#pragma unroll
+        for (int c = 0; c < 3; ++c) p[c] += beta * pp[c];
       }
-      acc0 += v[0] * p0 + v[32] * p1 + v[64] * p2;
-      acc1 += v[96] * p0 + v[128] * p1 + v[160] * p2;
-      acc2 += v[192] * p0 + v[224] * p1 + v[256] * p2;
+      acc0 += w0.y * p[0] + w1.x * p[1] + w1.y * p[2];
+      acc1 += w2.x * p[0] + w2.y * p[1] + w3.x * p[2];
+      acc2 += w3.y * p[0] + w4.x * p[1] + w4.y * p[2];
     }
     const Real acc[3] = {acc0, acc1, acc2};
+    Real p[3];
+    ld3<kCo>(z + 4 * (size_t)row, p);
+    if (!first) {
+      Real pp[3];
+      ld3<kCo>(pin + 4 * (size_t)row, pp);
 #pragma unroll
-    for (int c = 0; c < 3; ++c) {
-      const Real p = first ? z[3 * row + c] : z[3 * row + c] + beta * pin[3 * row + c];
-      pout[3 * row + c] = p;
-      Ap[3 * row + c] = acc[c];
-      pAp[0] = pAp[0] + exact_prod(p, acc[c]);
+      for (int c = 0; c < 3; ++c) p[c] += beta * pp[c];
     }
+    st3(pout + 4 * (size_t)row, p);
+    st3(Ap + 4 * (size_t)row, acc);
+#pragma unroll
+    for (int c = 0; c < 3; ++c) pAp[0] = pAp[0] + exact_prod(p[c], acc[c]);
   }
-  tile_partials<E, 1, 0>(pAp, nullptr, partials, pstride, 0, tix, 0);
+  tile_partials<E, Real, 1, 0>(pAp, nullptr, partials, pstride, 0, tix);
   if (last_tile(sd, TB_CG, tix)) {
-    const double s = scene_sum(partials, pstride, 0, sd.tile_first[TB_CG], sd.tile_count[TB_CG]);
-    if (threadIdx.x == 0) sc->alpha = sc->rz / s;
+    E s[1];
+    scene_sums<E, 1>(partials, pstride, 0, sd.tile_first[TB_CG], sd.tile_count[TB_CG], s);
+    if (threadIdx.x == 0) {
+      const double a = Fin<Real>::div(ldv<kCo>(&sc->rz), to_double_any(s[0]));
+      sc->alpha = a;
+      sc->alpha_f = float(a);
+    }
   }
 }
 
 // x += alpha p, r -= alpha Ap, z = D^{-1} r, then beta and the stopping test.
-template <typename Real>
-__global__ void __launch_bounds__(kCgThreads) k_cg_update(const Tile* tiles, const SceneDev* sds,
-                                                          double* partials, int pstride,
-                                                          BatchCounters* ctrs) {
-  const int tix = blockIdx.x;
+template <typename Real, bool kCo>
+__device__ __forceinline__ void cg_update_tile(int tix, const Tile* tiles, const SceneDev* sds,
+                                               double* partials, int pstride, BatchCounters* ctrs) {
   const Tile t = tiles[tix];
   const SceneDev& sd = sds[t.scene];
   SceneScalars* sc = sd.sc;
-  if (!sc->cg_active) return;
-  const int it = sc->cg_iter;
-  const Real alpha = Real(sc->alpha);
+  if (!ldv<kCo>(&sc->cg_active)) return;
+  const int it = ldv<kCo>(&sc->cg_iter);
+  const Real alpha = sizeof(Real) == 4 ? Real(ldv<kCo>(&sc->alpha_f)) : Real(ldv<kCo>(&sc->alpha));
   using E = typename Ext<Real>::T;
   E dots[2] = {E(0), E(0)};  // r.r, r.z
   const int row = t.begin + threadIdx.x;
   if (row < t.end) {
-    const size_t k = 3 * (size_t)row;
-    const Real* p = static_cast<const Real*>(sd.cg_p[it & 1]) + k;
-    const Real* Ap = static_cast<const Real*>(sd.cg_Ap) + k;
+    const size_t k = 4 * (size_t)row;
     Real* x = static_cast<Real*>(sd.cg_x) + k;
     Real* r = static_cast<Real*>(sd.cg_r) + k;
-    Real rv[3], z[3];
+    Real xv[3], pv[3], rv[3], av[3], z[3];
+    ld3<kCo>(x, xv);
+    ld3<kCo>(static_cast<const Real*>(sd.cg_p[it & 1]) + k, pv);
+    ld3<kCo>(r, rv);
+    ld3<kCo>(static_cast<const Real*>(sd.cg_Ap) + k, av);
 #pragma unroll
     for (int c = 0; c < 3; ++c) {
-      x[c] += alpha * p[c];
-      rv[c] = r[c] - alpha * Ap[c];
-      r[c] = rv[c];
+      xv[c] += alpha * pv[c];
+      rv[c] -= alpha * av[c];
       dots[0] = dots[0] + exact_prod(rv[c], rv[c]);
     }
+    st3(x, xv);
+    st3(r, rv);
     apply_prec<Real>(sd, row, rv, z);
-    Real* pz = static_cast<Real*>(sd.cg_z) + k;
+    st3(static_cast<Real*>(sd.cg_z) + k, z);
 #pragma unroll
-    for (int c = 0; c < 3; ++c) {
-      pz[c] = z[c];
-      dots[1] = dots[1] + exact_prod(rv[c], z[c]);
-    }
+    for (int c = 0; c < 3; ++c) dots[1] = dots[1] + exact_prod(rv[c], z[c]);
   }
-  tile_partials<E, 2, 0>(dots, nullptr, partials, pstride, 0, tix, 0);
+  tile_partials<E, Real, 2, 0>(dots, nullptr, partials, pstride, 0, tix);
   if (last_tile(sd, TB_CG, tix)) {
-    const int t0 = sd.tile_first[TB_CG], tc = sd.tile_count[TB_CG];
-    const double rrs = scene_sum(partials, pstride, 0, t0, tc);
-    const double rzs = scene_sum(partials, pstride, 1, t0, tc);
+    E v[2];
+    scene_sums<E, 2>(partials, pstride, 0, sd.tile_first[TB_CG], sd.tile_count[TB_CG], v);
     if (threadIdx.x == 0) {
-      sc->cg_err = sqrt(rrs / sc->cg_rhs_norm2);
+      const double rrs = to_double_any(v[0]), rzs = to_double_any(v[1]);
+      sc->cg_err = Fin<Real>::sqrt_ratio(rrs, ldv<kCo>(&sc->cg_rhs_norm2));
       bool stop = false;
-      if (rrs < sc->cg_threshold) {
+      if (rrs < ldv<kCo>(&sc->cg_threshold)) {
         stop = true;
       } else {
-        sc->beta = rzs / sc->rz;
+        const double b = Fin<Real>::div(rzs, ldv<kCo>(&sc->rz));
+        sc->beta = b;
+        sc->beta_f = float(b);
         sc->rz = rzs;
         sc->cg_iter = it + 1;
         if (it + 1 >= sd.max_cg) {
@@ -407,11 +477,295 @@ __global__ void __launch_bounds__(kCgThreads) k_cg_update(const Tile* tiles, con
         sc->status = 4;
       }
       if (stop) {
-        sc->cg_total += sc->cg_iter;
+        sc->cg_total = ldv<kCo>(&sc->cg_total) + ldv<kCo>(&sc->cg_iter);
         sc->cg_active = 0;
         atomicSub(&ctrs->cg_active, 1);
       }
     }
+  }
+}
+
+// At most 40 registers in FP32, so that six blocks fit on an SM and a
+// 1M-tet scene's PCG rows (873 tiles) run in one wave on 152 SMs.
+template <typename Real>
+__global__ void __launch_bounds__(kCgThreads, sizeof(Real) == 4 ? 6 : 4) k_cg_spmv(
+    const Tile* tiles, const SceneDev* sds, double* partials, int pstride, BatchCounters* ctrs) {
+  cg_spmv_tile<Real, false>(blockIdx.x, tiles, sds, partials, pstride);
+}
+
+template <typename Real>
+__global__ void __launch_bounds__(kCgThreads) k_cg_update(const Tile* tiles, const SceneDev* sds,
+                                                          double* partials, int pstride,
+                                                          BatchCounters* ctrs) {
+  cg_update_tile<Real, false>(blockIdx.x, tiles, sds, partials, pstride, ctrs);
+}
+
+// ------------------------------------------- single-reduction PCG ---
+// Chronopoulos and Gear's PCG ("s-step" with s = 1): with u = M^{-1} r and
+// w = A u, one iteration is
+//   p_i = u_i + b_i p_{i-1},  s_i = w_i + b_i s_{i-1},
+//   x_{i+1} = x_i + a_i p_i,  r_{i+1} = r_i - a_i s_i,  u_{i+1} = M^{-1} r_{i+1},
+//   w_{i+1} = A u_{i+1},  g = (r, u), d = (w, u), rr = (r, r) at i+1,
+//   b_{i+1} = g_{i+1} / g_i,  a_{i+1} = g_{i+1} / (d_{i+1} - b_{i+1} g_{i+1} / a_i),
+// so its three inner products reduce together and an iteration is ONE
+// launch: the SpMV needs u_{i+1} at neighbouring rows, which each thread
+// forms from the previous iteration's r, w and s of that row (kept by
+// iteration parity, so no row is overwritten while another block reads it).
+// In exact arithmetic the iterates are those of the two-reduction PCG.
+
+// u_{i+1} of a row from r_i, w_i, s_{i-1}: the same operations, in the same
+// order, wherever a row's value is formed.
+template <typename Real>
+__device__ __forceinline__ void cgf_next(const SceneDev& sd, int row, const Real r[3], const Real w[3],
+                                         const Real sp[3], Real a, Real b, Real s[3], Real rn[3],
+                                         Real u[3]) {
+#pragma unroll
+  for (int c = 0; c < 3; ++c) {
+    s[c] = fma(b, sp[c], w[c]);
+    rn[c] = fma(-a, s[c], r[c]);
+  }
+  apply_prec<Real>(sd, row, rn, u);
+}
+
+// One launch of the single-reduction PCG (init: r0 = b, x = 0, p = 0,
+// s_{-1} = 0, u0 = M^{-1} b, w0 = A u0).  The scene's last tile reduces the
+// three inner products and sets a, b of the next iteration.
+template <typename Real, bool kInit>
+__device__ __forceinline__ void cgf_tile(int tix, const Tile* tiles, const SceneDev* sds,
+                                         double* partials, int pstride, BatchCounters* ctrs) {
+  const Tile t = tiles[tix];
+  const SceneDev& sd = sds[t.scene];
+  SceneScalars* sc = sd.sc;
+  if (kInit ? !sc->newton_active : !sc->cg_active) return;
+  const int it = kInit ? 0 : sc->cg_iter;
+  const Real a = kInit ? Real(0) : (sizeof(Real) == 4 ? Real(sc->alpha_f) : Real(sc->alpha));
+  const Real b = kInit ? Real(0) : (sizeof(Real) == 4 ? Real(sc->beta_f) : Real(sc->beta));
+  // old (read) and new (written) buffers of the ping-ponged vectors
+  const Real* r_old = static_cast<const Real*>(kInit ? sd.rhs : sd.cgf_r[it & 1]);
+  const Real* w_old = static_cast<const Real*>(sd.cgf_w[it & 1]);
+  const Real* s_old = static_cast<const Real*>(sd.cgf_s[(it + 1) & 1]);
+  Real* r_new = static_cast<Real*>(sd.cgf_r[kInit ? 0 : (it + 1) & 1]);
+  Real* w_new = static_cast<Real*>(sd.cgf_w[kInit ? 0 : (it + 1) & 1]);
+  Real* s_new = static_cast<Real*>(sd.cgf_s[kInit ? 1 : it & 1]);
+  Real* x = static_cast<Real*>(sd.cg_x);
+  Real* u = static_cast<Real*>(sd.cg_z);
+  Real* p = static_cast<Real*>(sd.cg_p[0]);
+  const Real* ell = static_cast<const Real*>(sd.ell);
+  using E = typename Ext<Real>::T;
+  E dots[3] = {E(0), E(0), E(0)};  // (r,r), (r,u), (w,u) at it+1
+  const int row = t.begin + threadIdx.x;
+  if (row < t.end) {
+    const size_t k4 = 4 * (size_t)row;
+    Real un[3], rn[3];
+    if (kInit) {
+      ld3<false>(r_old + k4, rn);
+      apply_prec<Real>(sd, row, rn, un);
+      const Real zero[3] = {Real(0), Real(0), Real(0)};
+      st3(x + k4, zero);
+      st3(p + k4, zero);
+      st3(s_new + k4, zero);
+    } else {
+      Real rv[3], wv[3], sp[3], sv[3], uv[3], pv[3], xv[3];
+      ld3<false>(r_old + k4, rv);
+      ld3<false>(w_old + k4, wv);
+      ld3<false>(s_old + k4, sp);
+      cgf_next<Real>(sd, row, rv, wv, sp, a, b, sv, rn, un);
+      ld3<false>(u + k4, uv);
+      ld3<false>(p + k4, pv);
+      ld3<false>(x + k4, xv);
+#pragma unroll
+      for (int c = 0; c < 3; ++c) {
+        pv[c] = fma(b, pv[c], uv[c]);
+        xv[c] = fma(a, pv[c], xv[c]);
+      }
+      st3(p + k4, pv);
+      st3(x + k4, xv);
+      st3(s_new + k4, sv);
+    }
+    st3(r_new + k4, rn);
+    st3(u + k4, un);
+    // w_{i+1} = A u_{i+1}
+    const int slice = row >> 5, rs = row & 31;
+    const int soff = sd.slice_off[slice], slen = (sd.slice_off[slice + 1] - soff) >> 5;
+    Real acc0 = 0, acc1 = 0, acc2 = 0;
+#pragma unroll 2
+    for (int k = 0; k < slen; ++k) {
+      const size_t q = ell_pair(soff, k, rs, 0);
+      const auto w0 = ld_pair<false>(ell, q), w1 = ld_pair<false>(ell, q + 32),
+                 w2 = ld_pair<false>(ell, q + 64), w3 = ld_pair<false>(ell, q + 96),
+                 w4 = ld_pair<false>(ell, q + 128);
+      const int col = pair_col(w0);
+      const size_t c4 = 4 * (size_t)col;
+      Real uc[3];
+      if (kInit) {
+        Real bc[3];
+        ld3<false>(r_old + c4, bc);
+        apply_prec<Real>(sd, col, bc, uc);
+      } else {
+        Real rc[3], wc[3], spc[3], sc_[3], rnc[3];
+        ld3<false>(r_old + c4, rc);
+        ld3<false>(w_old + c4, wc);
+        ld3<false>(s_old + c4, spc);
+        cgf_next<Real>(sd, col, rc, wc, spc, a, b, sc_, rnc, uc);
+      }
+      acc0 += w0.y * uc[0] + w1.x * uc[1] + w1.y * uc[2];
+      acc1 += w2.x * uc[0] + w2.y * uc[1] + w3.x * uc[2];
+      acc2 += w3.y * uc[0] + w4.x * uc[1] + w4.y * uc[2];
+    }
+    const Real wn[3] = {acc0, acc1, acc2};
+    st3(w_new + k4, wn);
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+      dots[0] = dots[0] + exact_prod(rn[c], rn[c]);
+      dots[1] = dots[1] + exact_prod(rn[c], un[c]);
+      dots[2] = dots[2] + exact_prod(wn[c], un[c]);
+    }
+  }
+  tile_partials<E, Real, 3, 0>(dots, nullptr, partials, pstride, 0, tix);
+  if (last_tile(sd, TB_CG, tix)) {
+    E v[3];
+    scene_sums<E, 3>(partials, pstride, 0, sd.tile_first[TB_CG], sd.tile_count[TB_CG], v);
+    if (threadIdx.x == 0) {
+      const double rr = to_double_any(v[0]), g = to_double_any(v[1]), d = to_double_any(v[2]);
+      if (kInit) {
+        sc->cg_rhs_norm2 = rr;
+        sc->cg_iter = 0;
+        sc->cg_err = 0.0;
+        const double thr = fmax(sd.cg_tol * sd.cg_tol * rr, DBL_MIN);
+        sc->cg_threshold = thr;
+        if (rr == 0.0) {
+          sc->cg_active = 0;
+        } else if (rr < thr || sd.max_cg <= 0) {
+          sc->cg_active = 0;
+          sc->cg_err = 1.0;
+        } else {
+          sc->cg_active = 1;
+          atomicAdd(&ctrs->cg_active, 1);
+        }
+        const double a0 = Fin<Real>::div(g, d);
+        sc->cgf_gamma[0] = g;
+        sc->alpha = a0;
+        sc->alpha_f = float(a0);
+        sc->beta = 0.0;
+        sc->beta_f = 0.0f;
+      } else {
+        bool stop = false;
+        sc->cg_err = Fin<Real>::sqrt_ratio(rr, sc->cg_rhs_norm2);
+        if (rr < sc->cg_threshold) {
+          stop = true;
+        } else {
+          const double bn = Fin<Real>::div(g, sc->cgf_gamma[0]);
+          const double an = Fin<Real>::div(g, d - Fin<Real>::div(bn * g, sc->alpha));
+          sc->beta = bn;
+          sc->beta_f = float(bn);
+          sc->alpha = an;
+          sc->alpha_f = float(an);
+          sc->cgf_gamma[0] = g;
+          sc->cg_iter = it + 1;
+          if (it + 1 >= sd.max_cg) {
+            stop = true;
+            sc->cg_status = 5;  // MFEM_ERR_CG_MAXITER
+          }
+        }
+        if (!(rr == rr)) {
+          stop = true;
+          sc->status = 4;
+        }
+        if (stop) {
+          sc->cg_total += sc->cg_iter;
+          sc->cg_active = 0;
+          atomicSub(&ctrs->cg_active, 1);
+        }
+      }
+    }
+  }
+}
+
+template <typename Real>
+__global__ void __launch_bounds__(kCgThreads) k_cgf_init(const Tile* tiles, const SceneDev* sds,
+                                                         double* partials, int pstride,
+                                                         BatchCounters* ctrs) {
+  cgf_tile<Real, true>(blockIdx.x, tiles, sds, partials, pstride, ctrs);
+}
+
+template <typename Real>
+__global__ void __launch_bounds__(kCgThreads, sizeof(Real) == 4 ? 6 : 4) k_cgf_iter(
+    const Tile* tiles, const SceneDev* sds, double* partials, int pstride, BatchCounters* ctrs) {
+  cgf_tile<Real, false>(blockIdx.x, tiles, sds, partials, pstride, ctrs);
+}
+
+// Nanoseconds of the GPU's global timer.
+__device__ __forceinline__ unsigned long long global_ns() {
+  unsigned long long t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+
+// Barrier over all blocks of a cooperative launch (every block is resident).
+// Arrival counter plus a generation word; the last arrival resets the
+// counter and advances the generation.  Every wait is bounded: after
+// kBarrierTimeoutNs (or kBarrierMaxPolls polls) the block raises
+// ctrs->error and every block leaves at its next barrier.  Returns false
+// when the launch must end.
+constexpr unsigned long long kBarrierTimeoutNs = 2000000000ull;
+constexpr unsigned int kBarrierMaxPolls = 1u << 26;
+
+__device__ __forceinline__ bool grid_barrier(BatchCounters* ctrs) {
+  __shared__ int s_ok;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    volatile unsigned int* gen = &ctrs->bar_gen;
+    volatile int* err = &ctrs->error;
+    int ok = (*err == 0);
+    if (ok) {
+      const unsigned int g = *gen;
+      __threadfence();
+      if (atomicAdd(&ctrs->bar_count, 1u) + 1u == gridDim.x) {
+        ctrs->bar_count = 0u;
+        __threadfence();
+        atomicAdd(&ctrs->bar_gen, 1u);
+      } else {
+        const unsigned long long t0 = global_ns();
+        unsigned int polls = 0;
+        while (*gen == g) {
+          if (*err) {
+            ok = 0;
+            break;
+          }
+          if (++polls >= kBarrierMaxPolls || ((polls & 255u) == 0 && global_ns() - t0 > kBarrierTimeoutNs)) {
+            atomicExch(&ctrs->error, 1);
+            ok = 0;
+            break;
+          }
+          __nanosleep(32);
+        }
+      }
+      __threadfence();
+    }
+    s_ok = ok;
+  }
+  __syncthreads();
+  return s_ok != 0;
+}
+
+// The whole PCG solve of every active scene in ONE cooperative launch: the
+// blocks walk the tile table in a grid-stride loop for the SpMV phase, meet
+// at a grid barrier, do the update phase, meet again.  The arithmetic and
+// its order are those of the two-launch form; the results are bitwise the
+// same.  Six resident blocks per SM in the mixed path (912 on 152 SMs)
+// cover a 1M-tet scene's 873 PCG tiles in one round.
+template <typename Real>
+__global__ void __launch_bounds__(kCgThreads, sizeof(Real) == 4 ? 6 : 4) k_cg_solve(
+    const Tile* tiles, int ntiles, const SceneDev* sds, double* partials, int pstride,
+    BatchCounters* ctrs, int max_iters) {
+  for (int it = 0; it < max_iters; ++it) {
+    if (*(volatile int*)&ctrs->cg_active == 0) return;
+    for (int t = blockIdx.x; t < ntiles; t += gridDim.x)
+      cg_spmv_tile<Real, true>(t, tiles, sds, partials, pstride);
+    if (!grid_barrier(ctrs)) return;
+    for (int t = blockIdx.x; t < ntiles; t += gridDim.x)
+      cg_update_tile<Real, true>(t, tiles, sds, partials, pstride, ctrs);
+    if (!grid_barrier(ctrs)) return;
   }
 }
 
@@ -438,12 +792,15 @@ __global__ void k_scalars_begin(const SceneDev* sds, int n, BatchCounters* ctrs)
     sc->ls_ok = 0;
     sc->ls_total = 0;
     sc->alpha_ls = 1.0;
+    sc->alpha_ls_f = 1.0f;
     sc->procrustes_fail = 0;
   }
   if (threadIdx.x == 0) {
     ctrs->newton_active = n;
     ctrs->cg_active = 0;
     ctrs->ls_active = 0;
+    ctrs->error = 0;
+    ctrs->bar_count = 0u;
   }
 }
 
@@ -464,6 +821,28 @@ void launch_assemble(const Launch& L) { MFEM_LAUNCH_ROWS(k_assemble, 256); }
 void launch_cg_init(const Launch& L) { MFEM_LAUNCH_ROWS(k_cg_init, kCgThreads); }
 void launch_cg_spmv(const Launch& L) { MFEM_LAUNCH_ROWS(k_cg_spmv, kCgThreads); }
 void launch_cg_update(const Launch& L) { MFEM_LAUNCH_ROWS(k_cg_update, kCgThreads); }
+void launch_cgf_init(const Launch& L) { MFEM_LAUNCH_ROWS(k_cgf_init, kCgThreads); }
+void launch_cgf_iter(const Launch& L) { MFEM_LAUNCH_ROWS(k_cgf_iter, kCgThreads); }
+
+int cg_solve_blocks_per_sm(int fp64) {
+  int nb = 0;
+  cudaError_t e = fp64 ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_cg_solve<double>, kCgThreads, 0)
+                       : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_cg_solve<float>, kCgThreads, 0);
+  return e == cudaSuccess ? nb : 0;
+}
+
+cudaError_t launch_cg_solve(const Launch& L, int grid, int max_iters) {
+  if (L.ntiles == 0 || grid <= 0) return cudaSuccess;
+  const Tile* tiles = L.tiles;
+  int ntiles = L.ntiles;
+  const SceneDev* sds = L.sds;
+  double* partials = L.partials;
+  int pstride = L.pstride;
+  BatchCounters* ctrs = L.counters;
+  void* args[] = {&tiles, &ntiles, &sds, &partials, &pstride, &ctrs, &max_iters};
+  const void* fn = L.fp64 ? (const void*)k_cg_solve<double> : (const void*)k_cg_solve<float>;
+  return cudaLaunchCooperativeKernel(fn, dim3(grid), dim3(kCgThreads), args, 0, L.stream);
+}
 
 void launch_scalars_begin(const Launch& L, int nscenes) {
   k_scalars_begin<<<1, 128, 0, L.stream>>>(L.sds, nscenes, L.counters);

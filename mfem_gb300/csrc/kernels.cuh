@@ -29,13 +29,23 @@ constexpr int kCgTpr = 8;        // threads per row in the PCG SpMV
 constexpr int kCgThreads = 256;  // threads per PCG tile
 constexpr int kCgRows = 256;     // rows per PCG tile
 constexpr int kTicketGroup = 32; // tiles per first-level ticket counter
+// Packed sliced-ELL addressing (see SceneDev::ell): the Real index of
+// entry e (row-major 3x3) of block k of the row in lane rs of the slice at
+// slot offset soff.
+__host__ __device__ constexpr size_t ell_pair(int soff, int k, int rs, int w) {
+  return 5 * (size_t)(soff + 32 * k) + 32 * (size_t)w + (size_t)rs;
+}
+__host__ __device__ constexpr size_t ell_entry(int soff, int k, int rs, int e) {
+  return 2 * ell_pair(soff, k, rs, (e + 1) >> 1) + (size_t)((e + 1) & 1);
+}
+
 // Per-element record written by K1 and gathered by the assembly: the 78
 // upper-triangle entries of the 12x12 element block (Real) followed, at a
 // 16-byte boundary, by the element's 12 right-hand-side shares (double).
 __host__ __device__ constexpr int rec_rhs_offset(int real_bytes) { return real_bytes == 4 ? 320 : 624; }
 __host__ __device__ constexpr int rec_bytes(int real_bytes) { return rec_rhs_offset(real_bytes) + 96; }
 constexpr int kMaxRowBlocks = 126;  // 7-bit column slots in the incidence code
-constexpr int kNumPartials = 8;  // doubles per tile partial
+constexpr int kNumPartials = 8;  // partial quantities per tile
 
 struct Tile {
   int scene;  // slot in the batch
@@ -58,6 +68,9 @@ struct SceneScalars {
   // PCG (Eigen ConjugateGradient semantics)
   int cg_active, cg_iter, cg_total, cg_status;
   double cg_rhs_norm2, cg_threshold, rz, alpha, beta, cg_err;
+  // single-reduction PCG: (r, u) and alpha of iteration i in slot i & 1
+  // (kernel i reads slot (i+1) & 1 and its first block writes slot i & 1)
+  double cgf_gamma[2], cgf_alpha[2];
   // line search (linesearch.h:80-129 with c = 0, p = 0.5)
   int ls_active, ls_iter, ls_ok, ls_total;
   double fx0, alpha_ls, E_trial;
@@ -68,7 +81,9 @@ struct SceneScalars {
   int procrustes_fail;
   // last-tile counters, one per table
   unsigned int ctr[TB_COUNT];
-  double pad[1];
+  // float copies of the step lengths every thread reads (the mixed path
+  // converts nothing per thread); alpha_ls is a power of two, exact in float
+  float alpha_f, beta_f, alpha_ls_f, pad_f;
 };
 
 // Counters of a batch: scenes still active in each loop.
@@ -76,7 +91,10 @@ struct BatchCounters {
   int newton_active;
   int cg_active;
   int ls_active;
-  int pad;
+  int error;                // a bounded wait of the persistent PCG ran out
+  unsigned int bar_count;   // grid barrier of the persistent PCG: arrivals
+  unsigned int bar_gen;     //   and generation
+  int pad[2];
 };
 
 // One scene as the kernels see it (pointers into the scene's arena).
@@ -90,6 +108,7 @@ struct SceneDev {
   // parameters
   double h2;         // (beta*h)^2
   double dt;         // beta*h
+  float2 h2x;        // h2 as a float pair (df64), and float(h2) in .x
   double newton_tol, res_tol, cg_tol;
   double load_norm;  // |h^2 P M f| over the free dofs (scale of the residual test)
   int max_newton, max_ls, max_cg, bdf_order;
@@ -122,28 +141,38 @@ struct SceneDev {
   const int* m_col;
   const void* m_val;   // Real
   // Block pattern over free vertices (sorted columns per row, the BCSR of
-  // the Assembler) and the sliced-ELL layout the values are stored in:
-  // rows go in slices of 32; block k of row r of slice s sits at block
-  // position slice_off[s] + 32 k + (r mod 32), its 9 entries (row-major 3x3)
-  // at ell_val[9*(slice_off[s] + 32 k) + 32 e + (r mod 32)], so that a warp
-  // reads entry e of block k of 32 rows as one coalesced 128-byte access.
-  // Blocks k >= the row's length are zero and point at the row itself.
+  // the Assembler) and the sliced-ELL layout the values are stored in.
+  // Free rows are numbered so that within each window of kCgRows rows they
+  // run by decreasing block count (SELL-C-sigma with C = 32, sigma =
+  // kCgRows), which leaves slices of 32 rows almost without padding.  Block
+  // k of row r of slice s is slot slice_off[s] + 32 k + (r mod 32); a slot
+  // is 10 Real words packed as 5 pairs (col, a00) (a01, a02) (a10, a11)
+  // (a12, a20) (a21, a22), pair w of slot (s, k, r) at pair index
+  // 5 (slice_off[s] + 32 k) + 32 w + (r mod 32): a warp loads pair w of
+  // block k of 32 rows as one coalesced access, and the column arrives with
+  // the first pair.  Blocks k >= the row's length are zero and point at the
+  // row itself.
   const int* b_ptr;  // nf+1
   const int* b_col;  // nnzb
   const void* b_mass;  // nnzb Real: free-free mass m_ab
   const int* slice_off;  // nslices+1 (in blocks)
-  const int* ell_col;    // slice_off[nslices]
-  void* ell_val;         // 9 * slice_off[nslices] Real
-  void* dinv;        // 9 nf Real (block) or 3 nf (Jacobi)
+  void* ell;             // 10 * slice_off[nslices] Real
+  void* dinv;        // 9 nf Real (block) or 4 nf (Jacobi, padded like the vectors)
   const int* inc_ptr;  // nf+1 incidences (element, local vertex) per free row
   const int2* inc;     // (element, code): code = i | slot_j << (2+7j), slot 127 = pinned
-  // PCG vectors (Real, 3 nf)
+  // PCG vectors (Real, 4 nf: x, y, z of a row and a zero pad, so that a
+  // row is one 16-byte (FP32) or two 16-byte (FP64) accesses)
   void* rhs;
   void* cg_x;
   void* cg_r;
   void* cg_z;
   void* cg_p[2];
   void* cg_Ap;
+  // single-reduction PCG (Chronopoulos-Gear): r, w = A u and s by
+  // iteration parity; x, u (= cg_z) and p (= cg_p[0]) single
+  void* cgf_r[2];
+  void* cgf_w[2];
+  void* cgf_s[2];
   // tiles of this scene in each table
   int tile_first[TB_COUNT];
   int tile_count[TB_COUNT];
@@ -189,6 +218,12 @@ void launch_cg_init(const Launch& L);   // r = b, z, rz  (TB_CG)
 void launch_cg_spmv(const Launch& L);   // Ap, pAp, alpha (TB_CG)
 void launch_cg_update(const Launch& L); // x, r, z, beta  (TB_CG)
 void launch_scalars_begin(const Launch& L, int nscenes);        // reset Newton state
+// The whole PCG in one cooperative launch of `grid` co-resident blocks.
+cudaError_t launch_cg_solve(const Launch& L, int grid, int max_iters);
+// Single-reduction PCG: init (r0, u0, w0 = A u0) and one launch per iteration.
+void launch_cgf_init(const Launch& L);
+void launch_cgf_iter(const Launch& L);
+int cg_solve_blocks_per_sm(int fp64);
 
 // Maximum dynamic shared memory the element kernels need.
 int elem_update_smem_bytes(int fp64);

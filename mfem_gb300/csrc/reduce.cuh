@@ -3,11 +3,11 @@
 // Ext is the high-precision type of a path: df64 (float pairs, FP32 pipe) in
 // the mixed path, double in the all-FP64 path.  Positions, the stretch
 // variable s, the residual chain and per-thread accumulations use Ext; a
-// warp reduces in Ext with a fixed shuffle tree and converts once to double;
-// a tile writes one double partial per quantity (quantity-major,
-// partials[q*pstride+tile]); the last tile of a scene (atomic tickets, no
-// thread waits) reduces that scene's partials with the whole block in a
-// fixed order.
+// warp reduces in Ext with a fixed shuffle tree; a tile writes one Ext
+// partial per quantity (quantity-major, partials[q*pstride+tile]); the last
+// tile of a scene (atomic tickets, no thread waits) reduces that scene's
+// partials in Ext with the whole block in a fixed order, and one thread
+// converts the result to double for the scene's scalars.
 #pragma once
 #include "device_math.cuh"
 #include "kernels.cuh"
@@ -17,6 +17,9 @@ namespace mfem_gpu {
 template <typename Real> struct Ext;
 template <> struct Ext<float> {
   using T = df64;
+  // a double constant of the scene as the path's Ext / Real value
+  __device__ static T c(double, float2 x) { return df64(x.x, x.y); }
+  __device__ static float r(double, float2 x) { return x.x; }
   __device__ static T ld(const void* p, size_t i) { return df_load(static_cast<const float2*>(p)[i]); }
   __device__ static void st(void* p, size_t i, T v) { static_cast<float2*>(p)[i] = df_store(v); }
   __device__ static double to_d(T v) { return v.to_double(); }
@@ -24,6 +27,8 @@ template <> struct Ext<float> {
 };
 template <> struct Ext<double> {
   using T = double;
+  __device__ static T c(double d, float2) { return d; }
+  __device__ static double r(double d, float2) { return d; }
   __device__ static T ld(const void* p, size_t i) { return static_cast<const double*>(p)[i]; }
   __device__ static void st(void* p, size_t i, T v) { static_cast<double*>(p)[i] = v; }
   __device__ static double to_d(T v) { return v; }
@@ -38,13 +43,41 @@ __device__ __forceinline__ float shfl_down(float v, int off) { return __shfl_dow
 __device__ __forceinline__ double to_double_any(df64 v) { return v.to_double(); }
 __device__ __forceinline__ double to_double_any(double v) { return v; }
 
-// Writes NS sums (Ext per thread) and NM maxima (double per thread) of the
-// block as tile partials at quantities q0, q0+1, ...: the first `npairs`
-// sums as compensated (s, c) pairs, the other sums as plain doubles, then
-// the maxima.
-template <typename E, int NS, int NM>
-__device__ __forceinline__ void tile_partials(E* sums, double* maxs, double* partials, int pstride,
-                                              int q0, int tile, int npairs) {
+// A tile partial is an 8-byte slot: a double (FP64 path), a df64 as a
+// float pair, or a float maximum (mixed path).  Keeping the whole reduction
+// (warp tree, block combine, scene sum) in the path's own types keeps FP64
+// instructions out of the mixed path: on GB300 one FP64 warp instruction
+// occupies the FP64 pipe for 64 cycles, so a scalar FP64 chain in a block's
+// tail stalls the whole block behind its thread 0.
+template <typename T> struct Slot;
+template <> struct Slot<df64> {
+  __device__ static void put(double* p, df64 v) { *reinterpret_cast<float2*>(p) = make_float2(v.hi, v.lo); }
+  __device__ static df64 get(const double* p) {
+    const float2 f = __ldcg(reinterpret_cast<const float2*>(p));
+    return df64(f.x, f.y);
+  }
+  __device__ static df64 sget(const double* p) {
+    const float2 f = *reinterpret_cast<const float2*>(p);
+    return df64(f.x, f.y);
+  }
+};
+template <> struct Slot<double> {
+  __device__ static void put(double* p, double v) { *p = v; }
+  __device__ static double get(const double* p) { return __ldcg(p); }
+  __device__ static double sget(const double* p) { return *p; }
+};
+template <> struct Slot<float> {
+  __device__ static void put(double* p, float v) { *reinterpret_cast<float*>(p) = v; }
+  __device__ static float get(const double* p) { return __ldcg(reinterpret_cast<const float*>(p)); }
+  __device__ static float sget(const double* p) { return *reinterpret_cast<const float*>(p); }
+};
+
+// Writes NS sums (type E) and NM maxima (type M) of the block as tile
+// partials at quantities q0, q0+1, ... (sums first).  Fixed reduction
+// order: a shuffle tree per warp, then warps in index order.
+template <typename E, typename M, int NS, int NM>
+__device__ __forceinline__ void tile_partials(E* sums, M* maxs, double* partials, int pstride,
+                                              int q0, int tile) {
   __shared__ double red[32][NS + NM];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
 #pragma unroll
@@ -58,123 +91,134 @@ __device__ __forceinline__ void tile_partials(E* sums, double* maxs, double* par
   __syncthreads();
   if (lane == 0) {
 #pragma unroll
-    for (int q = 0; q < NS; ++q) red[warp][q] = to_double_any(sums[q]);
+    for (int q = 0; q < NS; ++q) Slot<E>::put(&red[warp][q], sums[q]);
 #pragma unroll
-    for (int q = 0; q < NM; ++q) red[warp][NS + q] = maxs[q];
+    for (int q = 0; q < NM; ++q) Slot<M>::put(&red[warp][NS + q], maxs[q]);
   }
   __syncthreads();
   if (threadIdx.x == 0) {
-    int qo = q0;
 #pragma unroll
     for (int q = 0; q < NS; ++q) {
-      KSum a{red[0][q], 0.0};
-      for (int w = 1; w < nw; ++w) a.add(red[w][q]);
-      if (q < npairs) {
-        partials[(size_t)qo * pstride + tile] = a.s;
-        partials[(size_t)(qo + 1) * pstride + tile] = a.c;
-        qo += 2;
-      } else {
-        partials[(size_t)qo * pstride + tile] = a.value();
-        qo += 1;
-      }
+      E a = Slot<E>::sget(&red[0][q]);
+      for (int w = 1; w < nw; ++w) a = a + Slot<E>::sget(&red[w][q]);
+      Slot<E>::put(partials + (size_t)(q0 + q) * pstride + tile, a);
     }
 #pragma unroll
     for (int q = 0; q < NM; ++q) {
-      double m = red[0][NS + q];
-      for (int w = 1; w < nw; ++w) m = fmax(m, red[w][NS + q]);
-      partials[(size_t)qo * pstride + tile] = m;
-      qo += 1;
+      M m = Slot<M>::sget(&red[0][NS + q]);
+      for (int w = 1; w < nw; ++w) m = fmax(m, Slot<M>::sget(&red[w][NS + q]));
+      Slot<M>::put(partials + (size_t)(q0 + NS + q) * pstride + tile, m);
     }
   }
 }
 
-// Block-wide double reductions returning the result to every thread.
-__device__ __forceinline__ double block_sum_all(double v) {
+// Block-wide reductions returning the result to every thread.
+template <typename E>
+__device__ __forceinline__ E block_sum_all(E v) {
   __shared__ double red[32];
   __shared__ double out;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
 #pragma unroll
-  for (int off = 16; off > 0; off >>= 1) v += __shfl_down_sync(0xffffffffu, v, off);
+  for (int off = 16; off > 0; off >>= 1) v = v + shfl_down(v, off);
   __syncthreads();
-  if (lane == 0) red[warp] = v;
+  if (lane == 0) Slot<E>::put(&red[warp], v);
   __syncthreads();
   if (threadIdx.x == 0) {
-    double a = red[0];
-    for (int w = 1; w < nw; ++w) a += red[w];
-    out = a;
+    E a = Slot<E>::sget(&red[0]);
+    for (int w = 1; w < nw; ++w) a = a + Slot<E>::sget(&red[w]);
+    Slot<E>::put(&out, a);
   }
   __syncthreads();
-  return out;
+  return Slot<E>::sget(&out);
 }
 
-__device__ __forceinline__ double block_max_all(double v) {
+template <typename M>
+__device__ __forceinline__ M block_max_all(M v) {
   __shared__ double red[32];
   __shared__ double out;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
 #pragma unroll
-  for (int off = 16; off > 0; off >>= 1) v = fmax(v, __shfl_down_sync(0xffffffffu, v, off));
+  for (int off = 16; off > 0; off >>= 1) v = fmax(v, shfl_down(v, off));
   __syncthreads();
-  if (lane == 0) red[warp] = v;
+  if (lane == 0) Slot<M>::put(&red[warp], v);
   __syncthreads();
   if (threadIdx.x == 0) {
-    double a = red[0];
-    for (int w = 1; w < nw; ++w) a = fmax(a, red[w]);
-    out = a;
+    M a = Slot<M>::sget(&red[0]);
+    for (int w = 1; w < nw; ++w) a = fmax(a, Slot<M>::sget(&red[w]));
+    Slot<M>::put(&out, a);
   }
   __syncthreads();
-  return out;
+  return Slot<M>::sget(&out);
 }
 
-__device__ __forceinline__ KSum block_ksum_all(KSum v) {
-  __shared__ double rs[32], rc[32];
-  __shared__ double os, oc;
+// Reductions of a scene's partials [first, first+count) by the whole block,
+// each thread over a fixed strided subset, then the block tree.
+template <typename E>
+__device__ __forceinline__ E scene_sum(const double* partials, int pstride, int q, int first, int count) {
+  const double* p = partials + (size_t)q * pstride + first;
+  E s = E(0);
+  for (int i = threadIdx.x; i < count; i += blockDim.x) s = s + Slot<E>::get(p + i);
+  return block_sum_all<E>(s);
+}
+template <typename M>
+__device__ __forceinline__ M scene_max(const double* partials, int pstride, int q, int first, int count) {
+  const double* p = partials + (size_t)q * pstride + first;
+  M s = M(0);
+  for (int i = threadIdx.x; i < count; i += blockDim.x) s = fmax(s, Slot<M>::get(p + i));
+  return block_max_all<M>(s);
+}
+
+// NQ sums of a scene's partials at quantities q0.. in one pass: each thread
+// over a fixed strided subset of tiles, then one block tree for all NQ.
+template <typename E, int NQ>
+__device__ __forceinline__ void scene_sums(const double* partials, int pstride, int q0, int first,
+                                           int count, E* out) {
+  __shared__ double red[32][NQ];
+  __shared__ double res[NQ];
+  E s[NQ];
+#pragma unroll
+  for (int q = 0; q < NQ; ++q) s[q] = E(0);
+  for (int i = threadIdx.x; i < count; i += blockDim.x)
+#pragma unroll
+    for (int q = 0; q < NQ; ++q) s[q] = s[q] + Slot<E>::get(partials + (size_t)(q0 + q) * pstride + first + i);
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
 #pragma unroll
-  for (int off = 16; off > 0; off >>= 1) {
-    KSum o;
-    o.s = __shfl_down_sync(0xffffffffu, v.s, off);
-    o.c = __shfl_down_sync(0xffffffffu, v.c, off);
-    v.merge(o);
-  }
+  for (int q = 0; q < NQ; ++q)
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) s[q] = s[q] + shfl_down(s[q], off);
   __syncthreads();
-  if (lane == 0) {
-    rs[warp] = v.s;
-    rc[warp] = v.c;
-  }
+  if (lane == 0)
+#pragma unroll
+    for (int q = 0; q < NQ; ++q) Slot<E>::put(&red[warp][q], s[q]);
   __syncthreads();
-  if (threadIdx.x == 0) {
-    KSum a{rs[0], rc[0]};
-    for (int w = 1; w < nw; ++w) a.merge(KSum{rs[w], rc[w]});
-    os = a.s;
-    oc = a.c;
-  }
+  if (threadIdx.x == 0)
+#pragma unroll
+    for (int q = 0; q < NQ; ++q) {
+      E a = Slot<E>::sget(&red[0][q]);
+      for (int w = 1; w < nw; ++w) a = a + Slot<E>::sget(&red[w][q]);
+      Slot<E>::put(&res[q], a);
+    }
   __syncthreads();
-  return KSum{os, oc};
+#pragma unroll
+  for (int q = 0; q < NQ; ++q) out[q] = Slot<E>::sget(&res[q]);
 }
 
-// Reductions of a scene's partials [first, first+count) by the whole block.
-__device__ __forceinline__ double scene_sum(const double* partials, int pstride, int q, int first,
-                                            int count) {
-  const double* p = partials + (size_t)q * pstride + first;
-  double s = 0;
-  for (int i = threadIdx.x; i < count; i += blockDim.x) s += __ldcg(p + i);
-  return block_sum_all(s);
-}
-__device__ __forceinline__ double scene_max(const double* partials, int pstride, int q, int first,
-                                            int count) {
-  const double* p = partials + (size_t)q * pstride + first;
-  double s = 0;
-  for (int i = threadIdx.x; i < count; i += blockDim.x) s = fmax(s, __ldcg(p + i));
-  return block_max_all(s);
-}
-__device__ __forceinline__ double scene_ksum(const double* partials, int pstride, int q, int first,
-                                             int count) {
-  const double* ps = partials + (size_t)q * pstride + first;
-  const double* pc = partials + (size_t)(q + 1) * pstride + first;
-  KSum s{0.0, 0.0};
-  for (int i = threadIdx.x; i < count; i += blockDim.x) s.merge(KSum{__ldcg(ps + i), __ldcg(pc + i)});
-  return block_ksum_all(s).value();
-}
+// Scalar arithmetic of a scene's finalizer (one thread).  The mixed path
+// keeps FP64 division and square root out (each a multi-instruction
+// sequence on the 1/64-rate FP64 pipe, microseconds on one thread):
+// quotients in df64, square roots in FP32 (they only feed tolerance tests
+// and reports).
+template <typename Real> struct Fin;
+template <> struct Fin<float> {
+  __device__ static double div(double a, double b) { return (df64(a) / df64(b)).to_double(); }
+  __device__ static double sqrt(double a) { return double(sqrtf(float(a))); }
+  __device__ static double sqrt_ratio(double a, double b) { return double(sqrtf(float(a) / float(b))); }
+};
+template <> struct Fin<double> {
+  __device__ static double div(double a, double b) { return a / b; }
+  __device__ static double sqrt(double a) { return ::sqrt(a); }
+  __device__ static double sqrt_ratio(double a, double b) { return ::sqrt(a / b); }
+};
 
 // True in every thread of the block that finished a scene's tile set last.
 // No thread waits: the last arrival is decided by atomic tickets, first per

@@ -43,6 +43,7 @@ class SceneSpec:
     newton_residual_tolerance: float = 0.0
     linear_solver: int = abi.SOLVER_EIGEN_CG_DIAG
     precision: int = abi.PRECISION_FP64
+    pcg_kernel: int = abi.PCG_KERNEL_PERSISTENT
     name: str = ""
     extra: dict = field(default_factory=dict)
 
@@ -128,4 +129,5 @@ def make_desc(spec: SceneSpec) -> _Desc:
     d.newton_residual_tolerance = float(spec.newton_residual_tolerance)
     d.linear_solver = int(spec.linear_solver)
     d.precision = int(spec.precision)
+    d.pcg_kernel = int(spec.pcg_kernel)
     return _Desc(d, keep)

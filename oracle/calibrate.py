@@ -2,8 +2,9 @@
 iterations per timestep a workload takes at its stopping criterion, so that
 the CPU baseline timed per Newton iteration can be stated per timestep.
 
-Writes oracle/calibration.json.  Run from the repository root:
-    python oracle/calibrate.py [--steps 3]
+Writes oracle/calibration.json (per-step Newton and PCG iteration counts from
+the first step on).  Run from the repository root:
+    python oracle/calibrate.py --steps 23 --sizes 60
 """
 import argparse
 import json
@@ -37,6 +38,7 @@ def main():
             print(n, st.newton_iterations, st.cg_iterations, st.residual / st.residual0, secs[-1], flush=True)
         out[f"c2_{n}"] = {"newton_iterations_per_step": sum(its) / len(its),
                           "cg_iterations_per_step": sum(cgs) / len(cgs),
+                          "newton_iterations": its, "cg_iterations": cgs,
                           "steps": args.steps, "threads": oracle.lib().oracle_get_threads(),
                           "seconds_per_step_here": sum(secs) / len(secs),
                           "criterion": "relative residual 1e-5, PCG 1e-4"}

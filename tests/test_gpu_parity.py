@@ -238,3 +238,67 @@ def test_rerun_is_bitwise_deterministic(gpu_lib):
         runs.append(s.get_state())
     for k in runs[0]:
         assert np.array_equal(runs[0][k], runs[1][k]), k
+
+
+@pytest.mark.parametrize("prec", PRECS)
+def test_persistent_and_split_pcg_are_bitwise_equal(gpu_lib, prec):
+    """The one-launch cooperative PCG and the two-launches-per-iteration PCG
+    run the same arithmetic in the same order: same states, same counts.
+    The batch has more PCG tiles than one, so the grid barrier is used."""
+    states, counts = [], []
+    for kern in (abi.PCG_KERNEL_PERSISTENT, abi.PCG_KERNEL_SPLIT):
+        specs = _three_specs(prec)
+        V, T = cube_grid(12, 6, 6, 0.05)  # 637 free vertices: 3 PCG tiles
+        lam, mu = enu_to_lame(1e5, 0.4)
+        specs.append(SceneSpec(V_rest=V, tets=T, mu=np.full(len(T), mu), lam=np.full(len(T), lam),
+                               is_fixed=face_mask(V, 0, "min"), dt=1 / 60, max_newton_iterations=8,
+                               iterative_solver_tolerance=1e-6, newton_residual_tolerance=1e-6,
+                               precision=prec))
+        for sp in specs:
+            sp.pcg_kernel = kern
+        scenes = [gpu.Scene(sp) for sp in specs]
+        batch = gpu.Batch(scenes)
+        cg = []
+        for _ in range(3):
+            cg.append([st.cg_iterations for st in batch.step()])
+        states.append([s.get_state() for s in scenes])
+        counts.append(cg)
+    assert counts[0] == counts[1]
+    assert sum(map(sum, counts[0])) > 0
+    for a, b in zip(*states):
+        for k in ("x", "v", "s", "R"):
+            assert np.array_equal(a[k], b[k]), k
+
+
+@pytest.mark.parametrize("prec", PRECS)
+def test_fused_pcg_matches_two_reduction_pcg(gpu_lib, prec):
+    """The single-reduction PCG (one launch per iteration) and Eigen's PCG
+    iteration agree to the rounding of the path: same Newton and PCG counts
+    (within one PCG iteration per solve) and the same states."""
+    res = {}
+    for kern in (abi.PCG_KERNEL_SPLIT, abi.PCG_KERNEL_FUSED):
+        spec = configs.beam_c1(precision=prec, pcg_kernel=kern)
+        if prec == abi.PRECISION_MIXED:
+            spec.iterative_solver_tolerance = 1e-5
+            spec.newton_residual_tolerance = 1e-5
+        s = gpu.Scene(spec)
+        its = []
+        for _ in range(10):
+            st = s.step()
+            its.append((st.newton_iterations, st.cg_iterations))
+        res[kern] = (s.get_state()["x"], its)
+    xa, ia = res[abi.PCG_KERNEL_SPLIT]
+    xb, ib = res[abi.PCG_KERNEL_FUSED]
+    tol = 1e-9 if prec == abi.PRECISION_FP64 else 1e-5
+    assert np.abs(xa - xb).max() <= tol * bbox_diag(xa)
+    print("two-reduction", ia, "single-reduction", ib)
+    na, nb = sum(n for n, _ in ia), sum(n for n, _ in ib)
+    ca, cb = sum(c for _, c in ia), sum(c for _, c in ib)
+    if prec == abi.PRECISION_FP64:
+        # a stopping test that sits at its threshold may flip by one iteration
+        assert all(abs(p - q) <= 1 for (p, _), (q, _) in zip(ia, ib))
+        assert abs(ca - cb) <= 0.05 * ca + 10
+    else:
+        # FP32 Newton decisions at a 1e-5 residual are rounding-sensitive
+        assert abs(na - nb) <= 0.25 * na + 2
+        assert abs(ca - cb) <= 0.25 * ca + 10
