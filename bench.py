@@ -175,17 +175,22 @@ def kernel_bytes(kind, sizes, rsz, cg_per_launch=None):
     return None
 
 
-def read_traffic(kernel, workload):
-    """DRAM bytes per launch from the committed ncu summary, if present."""
+def read_traffic(kernel, workload, cg_per_launch=None):
+    """DRAM bytes per launch from the committed ncu summary, if present.
+    For the whole-PCG kernel the summary holds bytes per PCG iteration,
+    scaled here by this run's PCG iterations per launch."""
     path = os.path.join(ROOT, "profiles", f"{kernel}_{workload}.md")
     if not os.path.exists(path):
         return None
     for ln in open(path):
-        if ln.strip().startswith("dram_bytes_per_launch:"):
-            try:
-                return float(ln.split(":", 1)[1].split()[0])
-            except ValueError:
-                return None
+        key, _, val = ln.strip().partition(":")
+        try:
+            if key == "dram_bytes_per_launch":
+                return float(val.split()[0])
+            if key == "dram_bytes_per_pcg_iteration" and cg_per_launch:
+                return float(val.split()[0]) * cg_per_launch
+        except (ValueError, IndexError):
+            return None
     return None
 
 
@@ -393,7 +398,8 @@ def run_ours(args):
         roof_note = None
     roof = {"kernel": dom, "bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
             "note": roof_note,
-            "frac": achieved / peak if achieved else None, "traffic": read_traffic(dom, "c2"),
+            "frac": achieved / peak if achieved else None,
+            "traffic": read_traffic(dom, "c2", cg_per_solve) if args.config == "c2" and args.size == 60 else None,
             "algorithmic_bytes_per_launch": abytes, "avg_launch_us": 1e3 * dom_ms / dom_n,
             "peak_source": f"{peak_src} (MEASURED_PEAKS.json hbm_gbs)"}
     per_kernel = {}
