@@ -55,7 +55,7 @@ def parse():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--cpu-threads", type=int, default=0)
-    ap.add_argument("--pcg-kernel", default="persistent", choices=["persistent", "split", "fused"])
+    ap.add_argument("--pcg-kernel", default="fused", choices=["persistent", "split", "fused"])
     return ap.parse_args()
 
 

@@ -596,6 +596,7 @@ void layout_scene(mfem_scene* s, Arena& A) {
   const size_t n4 = 4 * (size_t)std::max(M.nf, 1);
   D.rhs = A.take_bytes(n4 * r);
   D.cg_x = A.take_bytes(n4 * r);
+  D.cg_xe = s->fp64 ? nullptr : A.take_bytes(n4 * 8);
   D.cg_r = A.take_bytes(n4 * r);
   D.cg_z = A.take_bytes(n4 * r);
   D.cg_p[0] = A.take_bytes(n4 * r);
@@ -808,6 +809,10 @@ int run_pcg(mfem_batch* b, const Launch& Lcg) {
       } else {
         { KTimer t(b, MFEM_K_CG_SPMV); launch_cg_spmv(Lcg); }
         { KTimer t(b, MFEM_K_CG_UPDATE); launch_cg_update(Lcg); }
+        if (!b->fp64 && (it + 1) % kCgReplace == 0) {
+          KTimer t(b, MFEM_K_CG_REPLACE);
+          launch_cg_replace(Lcg);
+        }
       }
     }
     if ((rc = sync_counters(b))) return rc;
@@ -1424,7 +1429,7 @@ int mfem_gpu_kernel_name(int kernel, char* name, int name_len) {
   static const char* names[MFEM_K_COUNT] = {
       "k_elem_update", "k_assemble", "k_cg_init", "k_cg_spmv", "k_cg_update", "k_local_solve",
       "k_ls_energy", "k_apply", "k_step_begin", "k_step_end", "k_scalars_begin",
-      "k_cg_solve", "k_cgf_iter"};
+      "k_cg_solve", "k_cgf_iter", "k_cg_replace"};
   if (kernel < 0 || kernel >= MFEM_K_COUNT || !name || name_len <= 0) return MFEM_ERR_INVALID;
   strncpy(name, names[kernel], name_len - 1);
   name[name_len - 1] = 0;

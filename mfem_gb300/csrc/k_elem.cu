@@ -111,13 +111,33 @@ __device__ __forceinline__ void load_quat(const SceneDev& sd, int e, Real* R) {
   quat_to_rot(qq, R);
 }
 
+// Stores R as its quaternion and returns, in RE, the rotation of that
+// quaternion evaluated in Ext.  In the mixed path the Real rotation is
+// orthogonal only to ~1e-7 and differs from one evaluation to the next
+// through the rounding of its quaternion; the polish of the residual chain
+// converges the rotation's angle but cannot repair a non-orthogonal start,
+// so the chain starts from the quaternion's exactly orthogonal rotation
+// (quat_to_rot normalises).  Otherwise S = R^T F would carry ~1e-7 of
+// evaluation-to-evaluation noise, i.e. 1e-4 of a 1e-3 strain, which floors
+// the Newton residual near 1e-5.
 template <typename Real>
-__device__ __forceinline__ void store_quat(const SceneDev& sd, int e, const Real* R) {
+__device__ __forceinline__ void store_quat(const SceneDev& sd, int e, const Real* R,
+                                           typename Ext<Real>::T* RE = nullptr) {
   Real* q = static_cast<Real*>(sd.quat);
   Real qq[4];
   rot_to_quat(R, qq);
 #pragma unroll
   for (int i = 0; i < 4; ++i) q[i * sd.ntp + e] = qq[i];
+  if (RE) {
+    using E = typename Ext<Real>::T;
+    if (Prec<Real>::kFP64) {
+#pragma unroll
+      for (int i = 0; i < 9; ++i) RE[i] = E(R[i]);
+    } else {
+      E qe[4] = {E(qq[0]), E(qq[1]), E(qq[2]), E(qq[3])};
+      quat_to_rot(qe, RE);
+    }
+  }
 }
 
 template <typename Real>
@@ -186,10 +206,8 @@ __global__ void __launch_bounds__(kElemTile) k_elem_init(const Tile* tiles, cons
   for (int i = 0; i < 9; ++i) R[i] = (i % 4 == 0) ? Real(1) : Real(0);
   int it = procrustes<Real>(R, F, Real(kProcrustesTol), kProcrustesIters);
   if (it < 0) atomicAdd(&sd.sc->procrustes_fail, 1);
-  store_quat(sd, e, R);
   E RE[9], sE[6];
-#pragma unroll
-  for (int i = 0; i < 9; ++i) RE[i] = E(R[i]);
+  store_quat(sd, e, R, RE);
   if (!Prec<Real>::kFP64) polish_rotation(RE, FE);
   stretch_vec(RE, FE, sE);
 #pragma unroll
@@ -237,7 +255,8 @@ __global__ void __launch_bounds__(kElemTile)
     deformation_gradients<Real>(sd, in, nullptr, E(0), FE, F);
     load_quat(sd, e, R);
     int it = procrustes<Real>(R, F, Real(kProcrustesTol), kProcrustesIters);
-    store_quat(sd, e, R);
+    E RE[9];
+    store_quat(sd, e, R, RE);
     Real S6[6];
     stretch_vec(R, F, S6);
     Real u[18];
@@ -247,9 +266,7 @@ __global__ void __launch_bounds__(kElemTile)
     dphi12(in, dph);
     // ---- residual chain in Ext: S - s, q = H (S - s) + h^2 psi'(s), forces
     {
-      E RE[9], SE[6], dE[6], gE[6], qE[6], dphE[12], fE[12];
-#pragma unroll
-      for (int i = 0; i < 9; ++i) RE[i] = E(R[i]);
+      E SE[6], dE[6], gE[6], qE[6], dphE[12], fE[12];
       if (!Prec<Real>::kFP64) polish_rotation(RE, FE);
       stretch_vec(RE, FE, SE);
       material_grad<E>(in.mat, E(in.mu), E(in.lam), sE, gE);

@@ -84,6 +84,24 @@ __device__ __forceinline__ double2 ld_pair(const double* ell, size_t pair) {
 __device__ __forceinline__ int pair_col(float2 w) { return __float_as_int(w.x); }
 __device__ __forceinline__ int pair_col(double2 w) { return (int)__double_as_longlong(w.x); }
 
+// x of the mixed-path PCG in df64: a row is 4 float pairs (32 bytes).
+struct X3 {
+  df64 v[3];
+};
+__device__ __forceinline__ X3 zero_x3() { return X3{{df64(0.f), df64(0.f), df64(0.f)}}; }
+template <bool kCo>
+__device__ __forceinline__ X3 xe_load(const void* base, int row) {
+  const float4* p = static_cast<const float4*>(base) + 2 * (size_t)row;
+  const float4 a = kCo ? __ldcg(p) : p[0];
+  const float4 b = kCo ? __ldcg(p + 1) : p[1];
+  return X3{{df64(a.x, a.y), df64(a.z, a.w), df64(b.x, b.y)}};
+}
+__device__ __forceinline__ void xe_store(void* base, int row, const X3& x) {
+  float4* p = static_cast<float4*>(base) + 2 * (size_t)row;
+  p[0] = make_float4(x.v[0].hi, x.v[0].lo, x.v[1].hi, x.v[1].lo);
+  p[1] = make_float4(x.v[2].hi, x.v[2].lo, 0.f, 0.f);
+}
+
 constexpr int kAsmWindow = 64;  // block slots per warp accumulated in shared memory per pass
 
 template <typename Real>
@@ -309,6 +327,7 @@ __global__ void __launch_bounds__(kCgThreads) k_cg_init(const Tile* tiles, const
     st3(static_cast<Real*>(sd.cg_r) + k, r);
     st3(static_cast<Real*>(sd.cg_z) + k, z);
     st3(static_cast<Real*>(sd.cg_x) + k, zero);
+    if (sd.cg_xe) xe_store(sd.cg_xe, row, zero_x3());
 #pragma unroll
     for (int c = 0; c < 3; ++c) {
       dots[0] = dots[0] + exact_prod(r[c], r[c]);
@@ -438,9 +457,21 @@ __device__ __forceinline__ void cg_update_tile(int tix, const Tile* tiles, const
     ld3<kCo>(static_cast<const Real*>(sd.cg_p[it & 1]) + k, pv);
     ld3<kCo>(r, rv);
     ld3<kCo>(static_cast<const Real*>(sd.cg_Ap) + k, av);
+    if (sizeof(Real) == 4 && sd.cg_xe) {
+      // x in df64: x += alpha p with the exact product, x rounded for readers
+      X3 xe = xe_load<kCo>(sd.cg_xe, row);
+#pragma unroll
+      for (int c = 0; c < 3; ++c) {
+        xe.v[c] = xe.v[c] + two_prod(float(alpha), float(pv[c]));
+        xv[c] = Real(Ext<float>::to_real(xe.v[c]));
+      }
+      xe_store(sd.cg_xe, row, xe);
+    } else {
+#pragma unroll
+      for (int c = 0; c < 3; ++c) xv[c] += alpha * pv[c];
+    }
 #pragma unroll
     for (int c = 0; c < 3; ++c) {
-      xv[c] += alpha * pv[c];
       rv[c] -= alpha * av[c];
       dots[0] = dots[0] + exact_prod(rv[c], rv[c]);
     }
@@ -462,9 +493,11 @@ __device__ __forceinline__ void cg_update_tile(int tix, const Tile* tiles, const
       if (rrs < ldv<kCo>(&sc->cg_threshold)) {
         stop = true;
       } else {
-        const double b = Fin<Real>::div(rzs, ldv<kCo>(&sc->rz));
+        const double rz_old = ldv<kCo>(&sc->rz);
+        const double b = Fin<Real>::div(rzs, rz_old);
         sc->beta = b;
         sc->beta_f = float(b);
+        sc->rz_prev = rz_old;
         sc->rz = rzs;
         sc->cg_iter = it + 1;
         if (it + 1 >= sd.max_cg) {
@@ -483,6 +516,86 @@ __device__ __forceinline__ void cg_update_tile(int tix, const Tile* tiles, const
       }
     }
   }
+}
+
+// Residual replacement of the mixed path (reliable updates): r = b - A x
+// with x in df64, each FP32 matrix entry times x as an exact product summed
+// in df64, then z = D^{-1} r, (r, r) and (r, z).  The last tile restarts
+// beta from the true (r, z) and applies the stopping test to the true
+// residual.  The search direction is kept.
+template <bool kCo>
+__device__ __forceinline__ void cg_replace_tile(int tix, const Tile* tiles, const SceneDev* sds,
+                                                double* partials, int pstride, BatchCounters* ctrs) {
+  const Tile t = tiles[tix];
+  const SceneDev& sd = sds[t.scene];
+  SceneScalars* sc = sd.sc;
+  if (!ldv<kCo>(&sc->cg_active) || !sd.cg_xe) return;
+  if (ldv<kCo>(&sc->cg_iter) % kCgReplace != 0) return;
+  const float* ell = static_cast<const float*>(sd.ell);
+  df64 dots[2] = {df64(0.f), df64(0.f)};
+  const int row = t.begin + threadIdx.x;
+  if (row < t.end) {
+    const int slice = row >> 5, rs = row & 31;
+    const int soff = sd.slice_off[slice], slen = (sd.slice_off[slice + 1] - soff) >> 5;
+    df64 acc[3] = {df64(0.f), df64(0.f), df64(0.f)};
+    for (int k = 0; k < slen; ++k) {
+      const size_t q = ell_pair(soff, k, rs, 0);
+      const float2 w0 = ld_pair<false>(ell, q), w1 = ld_pair<false>(ell, q + 32),
+                   w2 = ld_pair<false>(ell, q + 64), w3 = ld_pair<false>(ell, q + 96),
+                   w4 = ld_pair<false>(ell, q + 128);
+      const X3 xc = xe_load<kCo>(sd.cg_xe, pair_col(w0));
+      const float a[9] = {w0.y, w1.x, w1.y, w2.x, w2.y, w3.x, w3.y, w4.x, w4.y};
+#pragma unroll
+      for (int i = 0; i < 3; ++i)
+#pragma unroll
+        for (int j = 0; j < 3; ++j) {
+          const float aij = a[3 * i + j];
+          acc[i] = acc[i] + two_prod(aij, xc.v[j].hi) + df64(aij * xc.v[j].lo);
+        }
+    }
+    float b[3], r[3], z[3];
+    ld3<false>(static_cast<const float*>(sd.rhs) + 4 * (size_t)row, b);
+#pragma unroll
+    for (int c = 0; c < 3; ++c) r[c] = Ext<float>::to_real(df64(b[c]) - acc[c]);
+    apply_prec<float>(sd, row, r, z);
+    st3(static_cast<float*>(sd.cg_r) + 4 * (size_t)row, r);
+    st3(static_cast<float*>(sd.cg_z) + 4 * (size_t)row, z);
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+      dots[0] = dots[0] + exact_prod(r[c], r[c]);
+      dots[1] = dots[1] + exact_prod(r[c], z[c]);
+    }
+  }
+  tile_partials<df64, float, 2, 0>(dots, nullptr, partials, pstride, 0, tix);
+  if (last_tile(sd, TB_CG, tix)) {
+    df64 v[2];
+    scene_sums<df64, 2>(partials, pstride, 0, sd.tile_first[TB_CG], sd.tile_count[TB_CG], v);
+    if (threadIdx.x == 0) {
+      const double rrs = to_double_any(v[0]), rzs = to_double_any(v[1]);
+      sc->cg_err = Fin<float>::sqrt_ratio(rrs, ldv<kCo>(&sc->cg_rhs_norm2));
+      if (rrs < ldv<kCo>(&sc->cg_threshold) || !(rrs == rrs)) {
+        if (!(rrs == rrs)) sc->status = 4;
+        // x_{cg_iter} meets the threshold: as in Eigen, that iteration is not counted
+        const int done = ldv<kCo>(&sc->cg_iter) - 1;
+        sc->cg_iter = done;
+        sc->cg_total = ldv<kCo>(&sc->cg_total) + done;
+        sc->cg_status = 0;
+        sc->cg_active = 0;
+        atomicSub(&ctrs->cg_active, 1);
+      } else {
+        const double b2 = Fin<float>::div(rzs, ldv<kCo>(&sc->rz_prev));
+        sc->beta = b2;
+        sc->beta_f = float(b2);
+        sc->rz = rzs;
+      }
+    }
+  }
+}
+
+__global__ void __launch_bounds__(kCgThreads) k_cg_replace(const Tile* tiles, const SceneDev* sds,
+                                                           double* partials, int pstride,
+                                                           BatchCounters* ctrs) {
+  cg_replace_tile<false>(blockIdx.x, tiles, sds, partials, pstride, ctrs);
 }
 
 // At most 40 registers in FP32, so that six blocks fit on an SM and a
@@ -766,6 +879,11 @@ __global__ void __launch_bounds__(kCgThreads, sizeof(Real) == 4 ? 6 : 4) k_cg_so
     for (int t = blockIdx.x; t < ntiles; t += gridDim.x)
       cg_update_tile<Real, true>(t, tiles, sds, partials, pstride, ctrs);
     if (!grid_barrier(ctrs)) return;
+    if (sizeof(Real) == 4 && (it + 1) % kCgReplace == 0) {
+      for (int t = blockIdx.x; t < ntiles; t += gridDim.x)
+        cg_replace_tile<true>(t, tiles, sds, partials, pstride, ctrs);
+      if (!grid_barrier(ctrs)) return;
+    }
   }
 }
 
@@ -821,6 +939,10 @@ void launch_assemble(const Launch& L) { MFEM_LAUNCH_ROWS(k_assemble, 256); }
 void launch_cg_init(const Launch& L) { MFEM_LAUNCH_ROWS(k_cg_init, kCgThreads); }
 void launch_cg_spmv(const Launch& L) { MFEM_LAUNCH_ROWS(k_cg_spmv, kCgThreads); }
 void launch_cg_update(const Launch& L) { MFEM_LAUNCH_ROWS(k_cg_update, kCgThreads); }
+void launch_cg_replace(const Launch& L) {
+  if (L.ntiles == 0 || L.fp64) return;
+  k_cg_replace<<<L.ntiles, kCgThreads, 0, L.stream>>>(L.tiles, L.sds, L.partials, L.pstride, L.counters);
+}
 void launch_cgf_init(const Launch& L) { MFEM_LAUNCH_ROWS(k_cgf_init, kCgThreads); }
 void launch_cgf_iter(const Launch& L) { MFEM_LAUNCH_ROWS(k_cgf_iter, kCgThreads); }
 

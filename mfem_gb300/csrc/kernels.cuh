@@ -29,6 +29,11 @@ constexpr int kCgTpr = 8;        // threads per row in the PCG SpMV
 constexpr int kCgThreads = 256;  // threads per PCG tile
 constexpr int kCgRows = 256;     // rows per PCG tile
 constexpr int kTicketGroup = 32; // tiles per first-level ticket counter
+// Mixed path: every kCgReplace PCG iterations the recursive residual is
+// replaced by b - A x computed with x in df64 and exact products (reliable
+// updates), so FP32 rounding does not leave the true residual far above the
+// tolerance the recursion reports.
+constexpr int kCgReplace = 25;
 // Packed sliced-ELL addressing (see SceneDev::ell): the Real index of
 // entry e (row-major 3x3) of block k of the row in lane rs of the slice at
 // slot offset soff.
@@ -68,6 +73,7 @@ struct SceneScalars {
   // PCG (Eigen ConjugateGradient semantics)
   int cg_active, cg_iter, cg_total, cg_status;
   double cg_rhs_norm2, cg_threshold, rz, alpha, beta, cg_err;
+  double rz_prev;    // rz of the previous iteration (residual replacement)
   // single-reduction PCG: (r, u) and alpha of iteration i in slot i & 1
   // (kernel i reads slot (i+1) & 1 and its first block writes slot i & 1)
   double cgf_gamma[2], cgf_alpha[2];
@@ -164,6 +170,7 @@ struct SceneDev {
   // row is one 16-byte (FP32) or two 16-byte (FP64) accesses)
   void* rhs;
   void* cg_x;
+  void* cg_xe;       // mixed path: the PCG's x in df64 (4 float pairs per row)
   void* cg_r;
   void* cg_z;
   void* cg_p[2];
@@ -220,6 +227,7 @@ void launch_cg_update(const Launch& L); // x, r, z, beta  (TB_CG)
 void launch_scalars_begin(const Launch& L, int nscenes);        // reset Newton state
 // The whole PCG in one cooperative launch of `grid` co-resident blocks.
 cudaError_t launch_cg_solve(const Launch& L, int grid, int max_iters);
+void launch_cg_replace(const Launch& L);  // r = b - A x in df64 (mixed path)
 // Single-reduction PCG: init (r0, u0, w0 = A u0) and one launch per iteration.
 void launch_cgf_init(const Launch& L);
 void launch_cgf_iter(const Launch& L);

