@@ -54,6 +54,9 @@ def parse():
     ap.add_argument("--solver", default="eigen-pcg-diag", choices=["eigen-pcg-diag", "gpu-pcg-block"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-batch", action="store_true",
+                    help="skip the batched-vs-plain measurement on the 64-scene mix")
+    ap.add_argument("--batch-steps", type=int, default=3)
     ap.add_argument("--cpu-threads", type=int, default=0)
     ap.add_argument("--pcg-kernel", default="fused", choices=["persistent", "split", "fused"])
     return ap.parse_args()
@@ -440,10 +443,57 @@ def run_ours(args):
         costs = cpu_costs(ref_spec, threads, 1, 0, budget_s=60.0)
         line["cpu_baseline"] = cpu_line(costs, newton, cgits, workload,
                                         "this run's GPU iteration counts")
+    scene.close()
+    if rank == 0 and ws == 1 and not args.no_batch and args.config == "c2":
+        from mfem_gb300 import configs
+        line["batch_mix"] = run_batch_mix(args, gpu, abi, configs)
     if rank == 0:
         print(json.dumps(line), flush=True)
-    scene.close()
     return 0
+
+
+def run_batch_mix(args, gpu, abi, configs):
+    """The 64-scene mix (cube grids 4..30 per axis, random materials and
+    pinned face, seeded): the batch stepped together (one launch per kernel
+    phase for all scenes) against each scene stepped alone, one after the
+    other.  Both from rest after the same warm-up; timesteps/s counts
+    scene-steps; device time from CUDA events around each step."""
+    kern = {"persistent": abi.PCG_KERNEL_PERSISTENT, "split": abi.PCG_KERNEL_SPLIT,
+            "fused": abi.PCG_KERNEL_FUSED}[args.pcg_kernel]
+    specs = configs.batch_c4(pcg_kernel=kern)
+    n = len(specs)
+    tets = int(sum(s.n_tets for s in specs))
+    warm, steps = 2, max(1, args.batch_steps)
+    scenes = [gpu.Scene(s) for s in specs]
+    batch = gpu.Batch(scenes)
+    for _ in range(warm):
+        batch.step()
+    ms, newton = [], []
+    for _ in range(steps):
+        stats = batch.step()
+        ms.append(stats[0].device_ms)
+        newton.append(max(st.newton_iterations for st in stats))
+    batch.close()
+    for s in scenes:
+        s.close()
+    batched = n * steps / (sum(ms) / 1e3)
+    plain_ms, plain_steps = 0.0, 1
+    for sp in specs:
+        s = gpu.Scene(sp)
+        for _ in range(warm):
+            s.step()
+        for _ in range(plain_steps):
+            plain_ms += s.step().device_ms
+        s.close()
+    plain = n * plain_steps / (plain_ms / 1e3)
+    return {"workload": f"batch_c4_{n}_scenes", "scenes": n, "tets_total": tets,
+            "batched": {"value": batched, "unit": UNIT, "steps": steps, "warmup": warm,
+                        "ms_per_batch_step": float(np.mean(ms)),
+                        "p50_ms": float(np.percentile(ms, 50)), "p99_ms": float(np.percentile(ms, 99)),
+                        "newton_max_per_step": float(np.mean(newton))},
+            "plain": {"value": plain, "unit": UNIT, "steps_per_scene": plain_steps, "warmup": warm,
+                      "ms_per_scene_step": plain_ms / (n * plain_steps)},
+            "batched_vs_plain": batched / plain}
 
 
 def main():

@@ -121,6 +121,18 @@ __device__ __forceinline__ void load_quat(const SceneDev& sd, int e, Real* R) {
 // evaluation-to-evaluation noise, i.e. 1e-4 of a 1e-3 strain, which floors
 // the Newton residual near 1e-5.
 template <typename Real>
+__device__ __forceinline__ void quat_rot_ext(const Real qq[4], const Real* R, typename Ext<Real>::T* RE) {
+  using E = typename Ext<Real>::T;
+  if (Prec<Real>::kFP64) {
+#pragma unroll
+    for (int i = 0; i < 9; ++i) RE[i] = E(R[i]);
+  } else {
+    E qe[4] = {E(qq[0]), E(qq[1]), E(qq[2]), E(qq[3])};
+    quat_to_rot(qe, RE);
+  }
+}
+
+template <typename Real>
 __device__ __forceinline__ void store_quat(const SceneDev& sd, int e, const Real* R,
                                            typename Ext<Real>::T* RE = nullptr) {
   Real* q = static_cast<Real*>(sd.quat);
@@ -128,16 +140,23 @@ __device__ __forceinline__ void store_quat(const SceneDev& sd, int e, const Real
   rot_to_quat(R, qq);
 #pragma unroll
   for (int i = 0; i < 4; ++i) q[i * sd.ntp + e] = qq[i];
-  if (RE) {
-    using E = typename Ext<Real>::T;
-    if (Prec<Real>::kFP64) {
-#pragma unroll
-      for (int i = 0; i < 9; ++i) RE[i] = E(R[i]);
-    } else {
-      E qe[4] = {E(qq[0]), E(qq[1]), E(qq[2]), E(qq[3])};
-      quat_to_rot(qe, RE);
-    }
-  }
+  if (RE) quat_rot_ext<Real>(qq, R, RE);
+}
+
+// S(F) in Ext from a Real Procrustes rotation: the orthogonal Ext rotation
+// of its quaternion, polished against the Ext F in the mixed path (the same
+// construction as the residual chain of K1, so that the line-search energy
+// and the energy at alpha = 0 agree).
+template <typename Real>
+__device__ __forceinline__ void stretch_ext(const Real* R, const typename Ext<Real>::T* FE,
+                                            typename Ext<Real>::T* SE) {
+  using E = typename Ext<Real>::T;
+  Real qq[4];
+  rot_to_quat(R, qq);
+  E RE[9];
+  quat_rot_ext<Real>(qq, R, RE);
+  if (!Prec<Real>::kFP64) polish_rotation(RE, FE);
+  stretch_vec(RE, FE, SE);
 }
 
 template <typename Real>
@@ -464,14 +483,17 @@ __global__ void __launch_bounds__(kElemTile) k_local_solve(const Tile* tiles, co
       }
       store6(sd.ds, sd.ntp, e, ds);
       store6(sd.la, sd.ntp, e, la);
-      // E(0) = h^2 vol psi(s) - vol la . Sym (S - s)
-      const Real psi = material_psi<Real>(in.mat, in.mu, in.lam, sv);
+      // E(0) = h^2 vol psi(s) - vol la . Sym (S - s).  psi in Ext: near the
+      // rest state a Real psi is a difference of O(1) invariants whose
+      // rounding exceeds the energy changes the line search compares.
+      const E psiE = material_psi<E>(in.mat, E(in.mu), E(in.lam), sE);
       Real con = 0;
 #pragma unroll
       for (int i = 0; i < 6; ++i) con += la[i] * (i < 3 ? Real(1) : Real(2)) * d[i];
-      const Real e1 = h2 * in.vol * psi, e2 = in.vol * con;
-      sums[0] = E(e1) - E(e2);
-      sums[1] = E(Real(fabs(e1))) + E(Real(fabs(e2)));
+      const E e1 = Ext<Real>::c(sd.h2, sd.h2x) * E(in.vol) * psiE;
+      const Real e2 = in.vol * con;
+      sums[0] = e1 - E(e2);
+      sums[1] = E(Real(fabs(Ext<Real>::to_real(e1)))) + E(Real(fabs(e2)));
       Real m = 0;
 #pragma unroll
       for (int i = 0; i < 6; ++i) m = fmax(m, Real(fabs(ds[i])));
@@ -543,30 +565,32 @@ __global__ void __launch_bounds__(kElemTile) k_ls_energy(const Tile* tiles, cons
       ElemIn<Real> in;
       load_elem(sd, e, in);
       Real F[9], R[9];
+      E FE[9];
       // x0 = x + alpha dx  (energy_func, newton_optimizer.cpp:37)
-      deformation_gradients<Real>(sd, in, cgx, alpha, nullptr, F);
+      deformation_gradients<Real>(sd, in, cgx, alpha, FE, F);
       load_quat(sd, e, R);
       procrustes<Real>(R, F, Real(kProcrustesTol), kProcrustesIters);
-      Real St[6];
-      stretch_vec(R, F, St);
-      E sE[6];
-      Real dsv[6], la[6], si[6];
+      E StE[6];
+      stretch_ext<Real>(R, FE, StE);
+      E sE[6], siE[6];
+      Real dsv[6], la[6];
       load6e<Real>(sd, e, sE);
       load6(sd.ds, sd.ntp, e, dsv);
       load6(sd.la, sd.ntp, e, la);
       Real con = 0;
 #pragma unroll
       for (int i = 0; i < 6; ++i) {
-        const E siE = sE[i] + alpha * E(dsv[i]);
-        si[i] = Real(Ext<Real>::to_real(siE));
+        siE[i] = sE[i] + alpha * E(dsv[i]);
         // S(x0) - s(alpha) formed in Ext before rounding
-        const Real diff = Real(Ext<Real>::to_real(E(St[i]) - siE));
+        const Real diff = Real(Ext<Real>::to_real(StE[i] - siE[i]));
         con += la[i] * (i < 3 ? Real(1) : Real(2)) * diff;
       }
-      const Real psi = material_psi<Real>(in.mat, in.mu, in.lam, si);
-      const Real e1 = h2 * in.vol * psi, e2 = in.vol * con;
-      sums[0] = E(e1) - E(e2);
-      sums[1] = E(Real(fabs(e1))) + E(Real(fabs(e2)));
+      // psi in Ext (see K5)
+      const E psiE = material_psi<E>(in.mat, E(in.mu), E(in.lam), siE);
+      const E e1 = Ext<Real>::c(sd.h2, sd.h2x) * E(in.vol) * psiE;
+      const Real e2 = in.vol * con;
+      sums[0] = e1 - E(e2);
+      sums[1] = E(Real(fabs(Ext<Real>::to_real(e1)))) + E(Real(fabs(e2)));
     }
   } else if (idx < t.end) {
     sums[0] = vertex_energy<Real>(sd, idx, cgx, alpha);
