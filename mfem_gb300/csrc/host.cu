@@ -488,6 +488,8 @@ struct mfem_batch {
   double* d_partials = nullptr;
   BatchCounters* d_ctr = nullptr;
   BatchCounters* h_ctr = nullptr;   // pinned
+  BatchCounters* h_ctr_pipe = nullptr;  // pinned, 2 slots: PCG chunk checks in flight
+  cudaEvent_t ev_pipe[2] = {nullptr, nullptr};
   SceneScalars* h_sc = nullptr;     // pinned, one per scene
   int max_newton = 0, max_ls = 0, max_cg = 0;
   int cg_hint = 16;
@@ -798,7 +800,12 @@ int run_pcg(mfem_batch* b, const Launch& Lcg) {
     CUDA_OR(e, MFEM_ERR_CUDA);
     return MFEM_OK;
   }
-  int it = 0;
+  // Chunks of iterations with the convergence check one chunk behind: after
+  // each chunk the counters are copied to a pinned slot and an event is
+  // recorded; the host waits for the PREVIOUS chunk's copy, so the GPU
+  // always has the current chunk queued while the host reads.  Iterations
+  // launched after convergence return at once.
+  int it = 0, nchunk = 0;
   int chunk = std::max(4, b->cg_hint);
   while (it < b->max_cg) {
     const int c = std::min(chunk, b->max_cg - it);
@@ -815,8 +822,16 @@ int run_pcg(mfem_batch* b, const Launch& Lcg) {
         }
       }
     }
-    if ((rc = sync_counters(b))) return rc;
-    if (b->h_ctr->cg_active == 0) break;
+    const int slot = nchunk & 1;
+    CUDA_OR(cudaMemcpyAsync(&b->h_ctr_pipe[slot], b->d_ctr, sizeof(BatchCounters), cudaMemcpyDeviceToHost,
+                            b->stream),
+            MFEM_ERR_CUDA);
+    CUDA_OR(cudaEventRecord(b->ev_pipe[slot], b->stream), MFEM_ERR_CUDA);
+    if (nchunk > 0) {
+      CUDA_OR(cudaEventSynchronize(b->ev_pipe[slot ^ 1]), MFEM_ERR_CUDA);
+      if (b->h_ctr_pipe[slot ^ 1].cg_active == 0) break;
+    }
+    ++nchunk;
     chunk = 8;
   }
   b->cg_hint = std::max(4, (it * 3) / 4);
@@ -960,6 +975,9 @@ int batch_build(mfem_scene* const* scenes, int n, mfem_batch** out) {
   CUDA_OR(cudaEventCreate(&b->ev0), MFEM_ERR_CUDA);
   CUDA_OR(cudaEventCreate(&b->ev1), MFEM_ERR_CUDA);
   CUDA_OR(cudaMallocHost(&b->h_ctr, sizeof(BatchCounters)), MFEM_ERR_OOM);
+  CUDA_OR(cudaMallocHost(&b->h_ctr_pipe, 2 * sizeof(BatchCounters)), MFEM_ERR_OOM);
+  for (int k = 0; k < 2; ++k)
+    CUDA_OR(cudaEventCreateWithFlags(&b->ev_pipe[k], cudaEventDisableTiming), MFEM_ERR_CUDA);
   CUDA_OR(cudaMallocHost(&b->h_sc, sizeof(SceneScalars) * n), MFEM_ERR_OOM);
   for (int tb = 0; tb < TB_COUNT; ++tb)
     if (!tabs[tb].empty())
@@ -978,6 +996,9 @@ void batch_free(mfem_batch* b) {
   if (b->stream) cudaStreamSynchronize(b->stream);
   if (b->dmem) cudaFree(b->dmem);
   if (b->h_ctr) cudaFreeHost(b->h_ctr);
+  if (b->h_ctr_pipe) cudaFreeHost(b->h_ctr_pipe);
+  for (int k = 0; k < 2; ++k)
+    if (b->ev_pipe[k]) cudaEventDestroy(b->ev_pipe[k]);
   if (b->h_sc) cudaFreeHost(b->h_sc);
   for (cudaEvent_t e : b->ev_pool) cudaEventDestroy(e);
   if (b->ev0) cudaEventDestroy(b->ev0);
