@@ -72,9 +72,35 @@ template <> struct Slot<float> {
   __device__ static float sget(const double* p) { return *reinterpret_cast<const float*>(p); }
 };
 
+// Addition in the reduction trees.  df64: one TwoSum of the high parts with
+// the low parts folded in (about 2^-48 relative per addition, the accuracy
+// of the representation) instead of the two-TwoSum form -- half the FP32
+// instructions on the critical path of every block's tail.
+__device__ __forceinline__ df64 radd(df64 a, df64 b) {
+  df64 s = two_sum(a.hi, b.hi);
+  s.lo = __fadd_rn(s.lo, __fadd_rn(a.lo, b.lo));
+  return fast_two_sum(s.hi, s.lo);
+}
+__device__ __forceinline__ double radd(double a, double b) { return a + b; }
+
+// Reduces the per-warp values red[w][q] (w < nw <= 32) in warp 0 with a
+// shuffle tree; the result is valid in lane 0.  Fixed order.
+template <typename T, bool kSum>
+__device__ __forceinline__ T warp0_combine(const double* red_q, int stride, int nw) {
+  const int lane = threadIdx.x & 31;
+  T a = lane < nw ? Slot<T>::sget(red_q + (size_t)lane * stride) : T(0);
+#pragma unroll
+  for (int off = 16; off > 0; off >>= 1) {
+    const T o = shfl_down(a, off);
+    a = kSum ? radd(a, o) : fmax(a, o);
+  }
+  return a;
+}
+
 // Writes NS sums (type E) and NM maxima (type M) of the block as tile
 // partials at quantities q0, q0+1, ... (sums first).  Fixed reduction
-// order: a shuffle tree per warp, then warps in index order.
+// order: a shuffle tree per warp, then a shuffle tree over the warps in
+// warp 0; thread 0 writes the partials.
 template <typename E, typename M, int NS, int NM>
 __device__ __forceinline__ void tile_partials(E* sums, M* maxs, double* partials, int pstride,
                                               int q0, int tile) {
@@ -83,7 +109,7 @@ __device__ __forceinline__ void tile_partials(E* sums, M* maxs, double* partials
 #pragma unroll
   for (int q = 0; q < NS; ++q)
 #pragma unroll
-    for (int off = 16; off > 0; off >>= 1) sums[q] = sums[q] + shfl_down(sums[q], off);
+    for (int off = 16; off > 0; off >>= 1) sums[q] = radd(sums[q], shfl_down(sums[q], off));
 #pragma unroll
   for (int q = 0; q < NM; ++q)
 #pragma unroll
@@ -96,18 +122,16 @@ __device__ __forceinline__ void tile_partials(E* sums, M* maxs, double* partials
     for (int q = 0; q < NM; ++q) Slot<M>::put(&red[warp][NS + q], maxs[q]);
   }
   __syncthreads();
-  if (threadIdx.x == 0) {
+  if (warp == 0) {
 #pragma unroll
     for (int q = 0; q < NS; ++q) {
-      E a = Slot<E>::sget(&red[0][q]);
-      for (int w = 1; w < nw; ++w) a = a + Slot<E>::sget(&red[w][q]);
-      Slot<E>::put(partials + (size_t)(q0 + q) * pstride + tile, a);
+      const E a = warp0_combine<E, true>(&red[0][q], NS + NM, nw);
+      if (lane == 0) Slot<E>::put(partials + (size_t)(q0 + q) * pstride + tile, a);
     }
 #pragma unroll
     for (int q = 0; q < NM; ++q) {
-      M m = Slot<M>::sget(&red[0][NS + q]);
-      for (int w = 1; w < nw; ++w) m = fmax(m, Slot<M>::sget(&red[w][NS + q]));
-      Slot<M>::put(partials + (size_t)(q0 + NS + q) * pstride + tile, m);
+      const M m = warp0_combine<M, false>(&red[0][NS + q], NS + NM, nw);
+      if (lane == 0) Slot<M>::put(partials + (size_t)(q0 + NS + q) * pstride + tile, m);
     }
   }
 }
@@ -119,14 +143,13 @@ __device__ __forceinline__ E block_sum_all(E v) {
   __shared__ double out;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
 #pragma unroll
-  for (int off = 16; off > 0; off >>= 1) v = v + shfl_down(v, off);
+  for (int off = 16; off > 0; off >>= 1) v = radd(v, shfl_down(v, off));
   __syncthreads();
   if (lane == 0) Slot<E>::put(&red[warp], v);
   __syncthreads();
-  if (threadIdx.x == 0) {
-    E a = Slot<E>::sget(&red[0]);
-    for (int w = 1; w < nw; ++w) a = a + Slot<E>::sget(&red[w]);
-    Slot<E>::put(&out, a);
+  if (warp == 0) {
+    const E a = warp0_combine<E, true>(red, 1, nw);
+    if (lane == 0) Slot<E>::put(&out, a);
   }
   __syncthreads();
   return Slot<E>::sget(&out);
@@ -142,10 +165,9 @@ __device__ __forceinline__ M block_max_all(M v) {
   __syncthreads();
   if (lane == 0) Slot<M>::put(&red[warp], v);
   __syncthreads();
-  if (threadIdx.x == 0) {
-    M a = Slot<M>::sget(&red[0]);
-    for (int w = 1; w < nw; ++w) a = fmax(a, Slot<M>::sget(&red[w]));
-    Slot<M>::put(&out, a);
+  if (warp == 0) {
+    const M a = warp0_combine<M, false>(red, 1, nw);
+    if (lane == 0) Slot<M>::put(&out, a);
   }
   __syncthreads();
   return Slot<M>::sget(&out);
@@ -157,7 +179,7 @@ template <typename E>
 __device__ __forceinline__ E scene_sum(const double* partials, int pstride, int q, int first, int count) {
   const double* p = partials + (size_t)q * pstride + first;
   E s = E(0);
-  for (int i = threadIdx.x; i < count; i += blockDim.x) s = s + Slot<E>::get(p + i);
+  for (int i = threadIdx.x; i < count; i += blockDim.x) s = radd(s, Slot<E>::get(p + i));
   return block_sum_all<E>(s);
 }
 template <typename M>
@@ -180,23 +202,22 @@ __device__ __forceinline__ void scene_sums(const double* partials, int pstride, 
   for (int q = 0; q < NQ; ++q) s[q] = E(0);
   for (int i = threadIdx.x; i < count; i += blockDim.x)
 #pragma unroll
-    for (int q = 0; q < NQ; ++q) s[q] = s[q] + Slot<E>::get(partials + (size_t)(q0 + q) * pstride + first + i);
+    for (int q = 0; q < NQ; ++q) s[q] = radd(s[q], Slot<E>::get(partials + (size_t)(q0 + q) * pstride + first + i));
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
 #pragma unroll
   for (int q = 0; q < NQ; ++q)
 #pragma unroll
-    for (int off = 16; off > 0; off >>= 1) s[q] = s[q] + shfl_down(s[q], off);
+    for (int off = 16; off > 0; off >>= 1) s[q] = radd(s[q], shfl_down(s[q], off));
   __syncthreads();
   if (lane == 0)
 #pragma unroll
     for (int q = 0; q < NQ; ++q) Slot<E>::put(&red[warp][q], s[q]);
   __syncthreads();
-  if (threadIdx.x == 0)
+  if (warp == 0)
 #pragma unroll
     for (int q = 0; q < NQ; ++q) {
-      E a = Slot<E>::sget(&red[0][q]);
-      for (int w = 1; w < nw; ++w) a = a + Slot<E>::sget(&red[w][q]);
-      Slot<E>::put(&res[q], a);
+      const E a = warp0_combine<E, true>(&red[0][q], NQ, nw);
+      if (lane == 0) Slot<E>::put(&res[q], a);
     }
   __syncthreads();
 #pragma unroll
@@ -220,10 +241,21 @@ template <> struct Fin<double> {
   __device__ static double sqrt_ratio(double a, double b) { return ::sqrt(a / b); }
 };
 
+// Atomic add with acquire-release semantics at GPU scope: orders this
+// thread's earlier writes (the tile's partials) before the ticket, and the
+// last arrival sees every other tile's partials, without a separate fence.
+__device__ __forceinline__ unsigned int atom_add_acq_rel(unsigned int* p, unsigned int v) {
+  unsigned int old;
+  asm volatile("atom.add.acq_rel.gpu.u32 %0, [%1], %2;" : "=r"(old) : "l"(p), "r"(v) : "memory");
+  return old;
+}
+
 // True in every thread of the block that finished a scene's tile set last.
 // No thread waits: the last arrival is decided by atomic tickets, first per
 // group of kTicketGroup tiles (distinct addresses, so the increments do not
 // serialise on one L2 line), then per scene by the last tile of each group.
+// Thread 0 wrote the tile's partials, so its acquire-release tickets carry
+// them; the block barrier then extends what thread 0 acquired to the block.
 __device__ __forceinline__ bool last_tile(const SceneDev& sd, int table, int tix) {
   __shared__ int s_last;
   __syncthreads();
@@ -234,13 +266,11 @@ __device__ __forceinline__ bool last_tile(const SceneDev& sd, int table, int tix
     const int ngrp = (count + kTicketGroup - 1) / kTicketGroup;
     const int in_grp = min(kTicketGroup, count - grp * kTicketGroup);
     unsigned int* gc = sd.gctr + (size_t)table * sd.gmax + grp;
-    __threadfence();
     int last = 0;
-    if (atomicAdd(gc, 1u) + 1u == (unsigned int)in_grp) {
+    if (atom_add_acq_rel(gc, 1u) + 1u == (unsigned int)in_grp) {
       *gc = 0u;
-      __threadfence();
       unsigned int* sc = &sd.sc->ctr[table];
-      if (atomicAdd(sc, 1u) + 1u == (unsigned int)ngrp) {
+      if (atom_add_acq_rel(sc, 1u) + 1u == (unsigned int)ngrp) {
         *sc = 0u;
         last = 1;
       }
