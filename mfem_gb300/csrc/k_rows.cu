@@ -81,6 +81,56 @@ __device__ __forceinline__ double2 ld_pair(const double* ell, size_t pair) {
   const double2* p = reinterpret_cast<const double2*>(ell) + pair;
   return kCo ? __ldcg(p) : *p;
 }
+// L2 policies for the PCG's SpMV: the matrix is streamed once per iteration
+// (evict first, no L1 allocation, read-only path), while the vectors the
+// SpMV gathers at neighbouring rows are kept (evict last).  Without them the
+// 115 MB matrix stream of a 1M-tet scene pushes the 4 MB vectors out of L2.
+__device__ __forceinline__ unsigned long long l2_evict_first() {
+  unsigned long long p;
+  asm volatile("createpolicy.fractional.L2::evict_first.b64 %0, 1.0;" : "=l"(p));
+  return p;
+}
+__device__ __forceinline__ unsigned long long l2_evict_last() {
+  unsigned long long p;
+  asm volatile("createpolicy.fractional.L2::evict_last.b64 %0, 1.0;" : "=l"(p));
+  return p;
+}
+__device__ __forceinline__ float2 ld_stream(const float* ell, size_t pair, unsigned long long pol) {
+  float2 v;
+  asm volatile("ld.global.nc.L1::no_allocate.L2::cache_hint.v2.f32 {%0, %1}, [%2], %3;"
+               : "=f"(v.x), "=f"(v.y) : "l"(reinterpret_cast<const float2*>(ell) + pair), "l"(pol));
+  return v;
+}
+__device__ __forceinline__ double2 ld_stream(const double* ell, size_t pair, unsigned long long pol) {
+  double2 v;
+  asm volatile("ld.global.nc.L1::no_allocate.L2::cache_hint.v2.f64 {%0, %1}, [%2], %3;"
+               : "=d"(v.x), "=d"(v.y) : "l"(reinterpret_cast<const double2*>(ell) + pair), "l"(pol));
+  return v;
+}
+// Gather of a row's three components with the keep policy (between
+// launches only: the persistent form bypasses L1 instead).
+__device__ __forceinline__ void ld3_keep(const float* p, float v[3], unsigned long long pol) {
+  float4 t;
+  asm volatile("ld.global.L2::cache_hint.v4.f32 {%0, %1, %2, %3}, [%4], %5;"
+               : "=f"(t.x), "=f"(t.y), "=f"(t.z), "=f"(t.w) : "l"(p), "l"(pol));
+  v[0] = t.x;
+  v[1] = t.y;
+  v[2] = t.z;
+}
+__device__ __forceinline__ void ld3_keep(const double* p, double v[3], unsigned long long pol) {
+  double2 a, b;
+  asm volatile("ld.global.L2::cache_hint.v2.f64 {%0, %1}, [%2], %3;" : "=d"(a.x), "=d"(a.y) : "l"(p), "l"(pol));
+  asm volatile("ld.global.L2::cache_hint.v2.f64 {%0, %1}, [%2], %3;" : "=d"(b.x), "=d"(b.y) : "l"(p + 2), "l"(pol));
+  v[0] = a.x;
+  v[1] = a.y;
+  v[2] = b.x;
+}
+template <bool kCo, typename Real>
+__device__ __forceinline__ void ld3_gather(const Real* p, Real v[3], unsigned long long pol) {
+  if constexpr (kCo) ld3<true>(p, v);
+  else ld3_keep(p, v, pol);
+}
+
 __device__ __forceinline__ int pair_col(float2 w) { return __float_as_int(w.x); }
 __device__ __forceinline__ int pair_col(double2 w) { return (int)__double_as_longlong(w.x); }
 
@@ -389,19 +439,20 @@ __device__ __forceinline__ void cg_spmv_tile(int tix, const Tile* tiles, const S
   if (row < t.end) {
     const int slice = row >> 5, rs = row & 31;
     const int soff = sd.slice_off[slice], slen = (sd.slice_off[slice + 1] - soff) >> 5;
+    const unsigned long long pol_s = l2_evict_first(), pol_k = l2_evict_last();
     Real acc0 = 0, acc1 = 0, acc2 = 0;
 #pragma unroll 4
     for (int k = 0; k < slen; ++k) {
       const size_t q = ell_pair(soff, k, rs, 0);
-      const auto w0 = ld_pair<false>(ell, q), w1 = ld_pair<false>(ell, q + 32),
-                 w2 = ld_pair<false>(ell, q + 64), w3 = ld_pair<false>(ell, q + 96),
-                 w4 = ld_pair<false>(ell, q + 128);
+      const auto w0 = ld_stream(ell, q, pol_s), w1 = ld_stream(ell, q + 32, pol_s),
+                 w2 = ld_stream(ell, q + 64, pol_s), w3 = ld_stream(ell, q + 96, pol_s),
+                 w4 = ld_stream(ell, q + 128, pol_s);
       const int col = pair_col(w0);
       Real p[3];
-      ld3<kCo>(z + 4 * (size_t)col, p);
+      ld3_gather<kCo>(z + 4 * (size_t)col, p, pol_k);
       if (!first) {
         Real pp[3];
-        ld3<kCo>(pin + 4 * (size_t)col, pp);
+        ld3_gather<kCo>(pin + 4 * (size_t)col, pp, pol_k);
 #pragma unroll
         for (int c = 0; c < 3; ++c) p[c] += beta * pp[c];
       }
@@ -700,25 +751,26 @@ __device__ __forceinline__ void cgf_tile(int tix, const Tile* tiles, const Scene
     // w_{i+1} = A u_{i+1}
     const int slice = row >> 5, rs = row & 31;
     const int soff = sd.slice_off[slice], slen = (sd.slice_off[slice + 1] - soff) >> 5;
+    const unsigned long long pol_s = l2_evict_first(), pol_k = l2_evict_last();
     Real acc0 = 0, acc1 = 0, acc2 = 0;
 #pragma unroll 2
     for (int k = 0; k < slen; ++k) {
       const size_t q = ell_pair(soff, k, rs, 0);
-      const auto w0 = ld_pair<false>(ell, q), w1 = ld_pair<false>(ell, q + 32),
-                 w2 = ld_pair<false>(ell, q + 64), w3 = ld_pair<false>(ell, q + 96),
-                 w4 = ld_pair<false>(ell, q + 128);
+      const auto w0 = ld_stream(ell, q, pol_s), w1 = ld_stream(ell, q + 32, pol_s),
+                 w2 = ld_stream(ell, q + 64, pol_s), w3 = ld_stream(ell, q + 96, pol_s),
+                 w4 = ld_stream(ell, q + 128, pol_s);
       const int col = pair_col(w0);
       const size_t c4 = 4 * (size_t)col;
       Real uc[3];
       if (kInit) {
         Real bc[3];
-        ld3<false>(r_old + c4, bc);
+        ld3_keep(r_old + c4, bc, pol_k);
         apply_prec<Real>(sd, col, bc, uc);
       } else {
         Real rc[3], wc[3], spc[3], sc_[3], rnc[3];
-        ld3<false>(r_old + c4, rc);
-        ld3<false>(w_old + c4, wc);
-        ld3<false>(s_old + c4, spc);
+        ld3_keep(r_old + c4, rc, pol_k);
+        ld3_keep(w_old + c4, wc, pol_k);
+        ld3_keep(s_old + c4, spc, pol_k);
         cgf_next<Real>(sd, col, rc, wc, spc, a, b, sc_, rnc, uc);
       }
       acc0 += w0.y * uc[0] + w1.x * uc[1] + w1.y * uc[2];
