@@ -489,6 +489,7 @@ struct mfem_batch {
   BatchCounters* d_ctr = nullptr;
   BatchCounters* h_ctr = nullptr;   // pinned
   BatchCounters* h_ctr_pipe = nullptr;  // pinned, 2 slots: PCG chunk checks in flight
+  cudaGraphExec_t cg_graph = nullptr;   // one chunk of PCG iterations, captured once
   cudaEvent_t ev_pipe[2] = {nullptr, nullptr};
   SceneScalars* h_sc = nullptr;     // pinned, one per scene
   int max_newton = 0, max_ls = 0, max_cg = 0;
@@ -786,6 +787,63 @@ int worst_status(const SceneScalars& sc) {
 // PCG iterations after k_cg_init: one cooperative launch for the whole solve,
 // or SpMV/update launch pairs in chunks with a host check of the active
 // count after each chunk.
+// The same chunked loop with each chunk a CUDA graph captured once per batch
+// (the kernels' arguments are fixed for the batch's lifetime): one graph
+// launch replaces 8 (single-reduction) or 50-75 (two-reduction) kernel
+// launches.  A two-reduction chunk is kCgReplace iterations long, so that the
+// residual replacement keeps its period.
+int run_pcg_graph(mfem_batch* b, const Launch& Lcg, bool fused) {
+  const int len = fused ? 8 : kCgReplace;
+  if (!b->cg_graph) {
+    cudaGraph_t g = nullptr;
+    CUDA_OR(cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal), MFEM_ERR_CUDA);
+    for (int k = 0; k < len; ++k) {
+      if (fused) {
+        launch_cgf_iter(Lcg);
+      } else {
+        launch_cg_spmv(Lcg);
+        launch_cg_update(Lcg);
+        if (!b->fp64 && k + 1 == kCgReplace) launch_cg_replace(Lcg);
+      }
+    }
+    const cudaError_t ec = cudaStreamEndCapture(b->stream, &g);
+    if (ec != cudaSuccess) {
+      if (g) cudaGraphDestroy(g);
+      CUDA_OR(ec, MFEM_ERR_CUDA);
+    }
+    const cudaError_t ei = cudaGraphInstantiate(&b->cg_graph, g, 0);
+    cudaGraphDestroy(g);
+    CUDA_OR(ei, MFEM_ERR_CUDA);
+  }
+  int it = 0, nchunk = 0;
+  int reps = std::max(1, (b->cg_hint + len - 1) / len);
+  while (it < b->max_cg) {
+    for (int r = 0; r < reps && it < b->max_cg; ++r, it += len) {
+      CUDA_OR(cudaGraphLaunch(b->cg_graph, b->stream), MFEM_ERR_CUDA);
+      if (fused) {
+        b->k_launches[MFEM_K_CGF_ITER] += len;
+      } else {
+        b->k_launches[MFEM_K_CG_SPMV] += len;
+        b->k_launches[MFEM_K_CG_UPDATE] += len;
+        if (!b->fp64) b->k_launches[MFEM_K_CG_REPLACE] += 1;
+      }
+    }
+    const int slot = nchunk & 1;
+    CUDA_OR(cudaMemcpyAsync(&b->h_ctr_pipe[slot], b->d_ctr, sizeof(BatchCounters), cudaMemcpyDeviceToHost,
+                            b->stream),
+            MFEM_ERR_CUDA);
+    CUDA_OR(cudaEventRecord(b->ev_pipe[slot], b->stream), MFEM_ERR_CUDA);
+    if (nchunk > 0) {
+      CUDA_OR(cudaEventSynchronize(b->ev_pipe[slot ^ 1]), MFEM_ERR_CUDA);
+      if (b->h_ctr_pipe[slot ^ 1].cg_active == 0) break;
+    }
+    ++nchunk;
+    reps = 1;
+  }
+  b->cg_hint = std::max(4, (it * 3) / 4);
+  return MFEM_OK;
+}
+
 int run_pcg(mfem_batch* b, const Launch& Lcg) {
   int rc;
   const bool fused = b->pcg_kernel == MFEM_PCG_KERNEL_FUSED;
@@ -805,6 +863,7 @@ int run_pcg(mfem_batch* b, const Launch& Lcg) {
   // recorded; the host waits for the PREVIOUS chunk's copy, so the GPU
   // always has the current chunk queued while the host reads.  Iterations
   // launched after convergence return at once.
+  if (!b->profiling) return run_pcg_graph(b, Lcg, fused);
   int it = 0, nchunk = 0;
   int chunk = std::max(4, b->cg_hint);
   while (it < b->max_cg) {
@@ -997,6 +1056,7 @@ void batch_free(mfem_batch* b) {
   if (b->dmem) cudaFree(b->dmem);
   if (b->h_ctr) cudaFreeHost(b->h_ctr);
   if (b->h_ctr_pipe) cudaFreeHost(b->h_ctr_pipe);
+  if (b->cg_graph) cudaGraphExecDestroy(b->cg_graph);
   for (int k = 0; k < 2; ++k)
     if (b->ev_pipe[k]) cudaEventDestroy(b->ev_pipe[k]);
   if (b->h_sc) cudaFreeHost(b->h_sc);
