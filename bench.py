@@ -50,7 +50,10 @@ def parse():
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--config", default="c2", choices=["c1", "c2", "c3", "c4"])
+    ap.add_argument("--config", default="c2", choices=["c1", "c2", "c3", "c5"])
+    ap.add_argument("--c5-duration", type=float, default=5.0,
+                    help="seconds of Poisson arrivals (lambda = 20/s) in the served stream")
+    ap.add_argument("--c5-steps", type=int, default=20, help="timesteps per served request")
     ap.add_argument("--size", type=int, default=60, help="cubes per axis for c2")
     ap.add_argument("--precision", default="mixed", choices=["mixed", "fp64"])
     ap.add_argument("--solver", default="eigen-pcg-diag", choices=["eigen-pcg-diag", "gpu-pcg-block"])
@@ -508,8 +511,60 @@ def run_batch_mix(args, gpu, abi, configs):
             "batched_vs_plain": batched / plain}
 
 
+def run_served(args):
+    """The served stream (C5 shape, scaled in time): Poisson arrivals at 20/s,
+    cube-grid scenes of 1e3..5e5 tets (log-uniform), random materials and one
+    pinned face, admitted against a 150 GB budget and stepped by continuous
+    batching.  Aggregate timesteps/s, per-timestep and per-request latency;
+    beside it the same requests' first timesteps stepped one scene at a time."""
+    ws, rank, _, pg = dist_setup()
+    from mfem_gb300 import abi, configs, gpu, server
+    from mfem_gb300.build import build
+    if rank == 0:
+        build()
+    barrier(pg)
+    kern = {"persistent": abi.PCG_KERNEL_PERSISTENT, "split": abi.PCG_KERNEL_SPLIT,
+            "fused": abi.PCG_KERNEL_FUSED}[args.pcg_kernel]
+    stream = configs.stream_c5(duration=args.c5_duration, steps=args.c5_steps)
+    for _, sp, _ in stream:
+        sp.pcg_kernel = kern
+    srv = server.Server(budget_bytes=150e9)
+    for t, sp, n in stream:
+        srv.submit(sp, n, arrival=t)
+    t0 = time.perf_counter()
+    out = srv.run(realtime=True)
+    wall = time.perf_counter() - t0
+    summ = server.summary(out, srv.ticks, wall)
+    # plain: each request's first timesteps alone, one scene at a time
+    sample = out[: min(len(out), 16)]
+    plain_ms, plain_n = 0.0, 0
+    for r in sample:
+        s = gpu.Scene(r.spec)
+        for _ in range(2):
+            plain_ms += s.step().device_ms
+            plain_n += 1
+        s.close()
+    plain = plain_n / (plain_ms / 1e3)
+    line = {"metric": METRIC, "value": summ["timesteps_per_s"], "unit": UNIT, "n_gpus": ws,
+            "steps": args.c5_steps, "warmup": 0, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32+f64" if args.precision == "mixed" else "f64",
+            "data": "synthetic",
+            "config": {"workload": f"served_stream_c5_{args.c5_duration:g}s_{args.c5_steps}steps",
+                       "arrival_rate_per_s": 20.0, "tets_range": [1e3, 5e5],
+                       "budget_bytes": 150e9, "pcg_kernel": args.pcg_kernel},
+            "served": summ,
+            "plain": {"value": plain, "unit": UNIT, "sample": f"first 2 timesteps of {len(sample)} requests, alone"},
+            "served_vs_plain": summ["timesteps_per_s"] / plain if plain else None,
+            "tets_total": int(sum(r.spec.n_tets for r in out))}
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    return 0
+
+
 def main():
     args = parse()
+    if args.impl == "ours" and args.config == "c5":
+        return run_served(args)
     if args.impl == "reference":
         return run_reference(args)
     return run_ours(args)

@@ -493,7 +493,9 @@ __global__ void __launch_bounds__(kElemTile) k_local_solve(const Tile* tiles, co
       const E e1 = Ext<Real>::c(sd.h2, sd.h2x) * E(in.vol) * psiE;
       const Real e2 = in.vol * con;
       sums[0] = e1 - E(e2);
-      sums[1] = E(Real(fabs(Ext<Real>::to_real(e1)))) + E(Real(fabs(e2)));
+      // rounding bound of the line-search comparison: e2 is a Real sum, e1
+      // and the vertex energies are Ext (relative error far below 1e-7 eps)
+      sums[1] = E(Real(fabs(e2))) + E(Real(1e-7) * Real(fabs(Ext<Real>::to_real(e1))));
       Real m = 0;
 #pragma unroll
       for (int i = 0; i < 6; ++i) m = fmax(m, Real(fabs(ds[i])));
@@ -590,7 +592,9 @@ __global__ void __launch_bounds__(kElemTile) k_ls_energy(const Tile* tiles, cons
       const E e1 = Ext<Real>::c(sd.h2, sd.h2x) * E(in.vol) * psiE;
       const Real e2 = in.vol * con;
       sums[0] = e1 - E(e2);
-      sums[1] = E(Real(fabs(Ext<Real>::to_real(e1)))) + E(Real(fabs(e2)));
+      // rounding bound of the line-search comparison: e2 is a Real sum, e1
+      // and the vertex energies are Ext (relative error far below 1e-7 eps)
+      sums[1] = E(Real(fabs(e2))) + E(Real(1e-7) * Real(fabs(Ext<Real>::to_real(e1))));
     }
   } else if (idx < t.end) {
     sums[0] = vertex_energy<Real>(sd, idx, cgx, alpha);

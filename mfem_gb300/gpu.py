@@ -175,8 +175,12 @@ class Batch:
     def handle(self):
         return self._h
 
-    def step(self):
+    def step(self, raise_on_error=True):
+        """One timestep of every scene; per-scene stats (their .status says
+        how each scene's step ended).  With raise_on_error=False a scene's
+        numerical failure is left to the caller (the batch itself stays
+        usable); a CUDA error still raises."""
         rc = load().mfem_gpu_batch_step(self._h, self._stats)
-        if rc != abi.OK:
+        if rc != abi.OK and (raise_on_error or rc in (abi.ERR_CUDA, abi.ERR_TIMEOUT, abi.ERR_INVALID)):
             check(rc, "batch_step")
         return list(self._stats)

@@ -1,0 +1,153 @@
+"""Serving loop: continuous batching of simulation instances on one GPU.
+
+Requests (a SceneSpec and a number of timesteps) arrive over time.  The loop
+admits them in arrival order while their device footprint
+(mfem_gpu_scene_footprint) fits the memory budget, keeps every admitted
+instance's state resident (positions, velocities, stretch variables,
+rotations, BDF history and solver state live in the scene's device arena),
+and at every tick steps ALL admitted instances together: one batch, one
+launch per kernel phase for all of them (mfem_gpu_batch_step).  An instance
+that has taken its timesteps leaves the batch, its memory is freed and the
+next queued request takes its place at the next tick, so requests that
+arrive while others are on the GPU join them there.
+
+Scenes are built on a worker thread (the host mesh build and the arena
+upload), overlapping the GPU ticks.  A scene's arithmetic does not depend on
+which other scenes share its batch (per-scene tiles and fixed-order
+reductions), so every result is bitwise the one the request would get alone.
+
+No counterpart in the reference, which steps one scene per process.
+"""
+import concurrent.futures as cf
+import time
+from dataclasses import dataclass, field
+
+import numpy as np
+
+from . import abi, gpu
+
+
+@dataclass
+class Request:
+    spec: object
+    steps: int
+    arrival: float = 0.0           # seconds after the server starts
+    rid: int = -1
+    footprint: int = 0
+    # filled by the server
+    admitted_at: float = None
+    done_at: float = None
+    steps_done: int = 0
+    step_ms: list = field(default_factory=list)    # device time of each tick it took part in
+    newton: list = field(default_factory=list)
+    cg: list = field(default_factory=list)
+    status: int = abi.OK
+    result: dict = None
+
+
+class Server:
+    """Continuous-batching loop over one GPU.
+
+    budget_bytes  device memory the admitted scenes may hold together
+    keep_state    which final state arrays to return ("x", "v", "s", "R")
+    """
+
+    def __init__(self, budget_bytes, keep_state=("x",), max_scenes=4096):
+        self.budget = int(budget_bytes)
+        self.keep = tuple(keep_state)
+        self.max_scenes = max_scenes
+        self.queue = []
+        self.ticks = []
+
+    def submit(self, spec, steps, arrival=0.0):
+        r = Request(spec=spec, steps=int(steps), arrival=float(arrival), rid=len(self.queue))
+        r.footprint = gpu.footprint(spec)
+        if r.footprint > self.budget:
+            raise ValueError(f"request {r.rid} needs {r.footprint} bytes, over the budget")
+        self.queue.append(r)
+        return r.rid
+
+    def run(self, realtime=True):
+        """Serves every submitted request; returns them with their results.
+        realtime: arrivals follow the wall clock (else all are due at once)."""
+        pending = sorted(self.queue, key=lambda r: (r.arrival, r.rid))
+        building = {}          # rid -> future(Scene)
+        active = {}            # rid -> (Request, Scene)
+        used = 0
+        batch, members = None, ()
+        pool = cf.ThreadPoolExecutor(max_workers=1)
+        t0 = time.perf_counter()
+        now = lambda: time.perf_counter() - t0
+        try:
+            while pending or building or active:
+                # admit what has arrived and fits
+                while (pending and (not realtime or pending[0].arrival <= now())
+                       and used + pending[0].footprint <= self.budget
+                       and len(active) + len(building) < self.max_scenes):
+                    r = pending.pop(0)
+                    used += r.footprint
+                    building[r.rid] = (r, pool.submit(gpu.Scene, r.spec))
+                # scenes whose build finished join the next tick
+                for rid in [k for k, (_, f) in building.items() if f.done() or not active]:
+                    r, f = building.pop(rid)
+                    active[rid] = (r, f.result())
+                    r.admitted_at = now()
+                if not active:
+                    if pending and realtime:
+                        time.sleep(max(0.0, min(0.01, pending[0].arrival - now())))
+                    continue
+                key = tuple(sorted(active))
+                if key != members:
+                    if batch is not None:
+                        batch.close()
+                    batch = gpu.Batch([active[k][1] for k in key])
+                    members = key
+                stats = batch.step(raise_on_error=False)
+                tick_ms = stats[0].device_ms
+                self.ticks.append((now(), len(key), tick_ms))
+                finished = []
+                for k, st in zip(key, stats):
+                    r, _ = active[k]
+                    r.steps_done += 1
+                    r.step_ms.append(tick_ms)
+                    r.newton.append(st.newton_iterations)
+                    r.cg.append(st.cg_iterations)
+                    if st.status not in (abi.OK, abi.ERR_CG_MAXITER, abi.ERR_LS_FAILED):
+                        r.status = st.status
+                    # a scene whose state is no longer finite leaves with its status
+                    if r.steps_done >= r.steps or st.status in (abi.ERR_NONFINITE, abi.ERR_PROCRUSTES):
+                        finished.append(k)
+                for k in finished:
+                    r, sc = active.pop(k)
+                    if r.status in (abi.ERR_NONFINITE, abi.ERR_PROCRUSTES):
+                        r.result = None
+                    else:
+                        state = sc.get_state()
+                        r.result = {name: state[name] for name in self.keep}
+                    r.done_at = now()
+                    sc.close()
+                    used -= r.footprint
+                if finished:
+                    batch.close()
+                    batch, members = None, ()
+        finally:
+            if batch is not None:
+                batch.close()
+            for r, sc in active.values():
+                sc.close()
+            pool.shutdown(wait=True)
+        return sorted(self.queue, key=lambda r: r.rid)
+
+
+def summary(requests, ticks, wall_s):
+    """Aggregate timesteps/s and per-timestep latency percentiles."""
+    steps = sum(r.steps_done for r in requests)
+    lat = np.array([ms for r in requests for ms in r.step_ms]) if steps else np.zeros(1)
+    req = np.array([r.done_at - r.arrival for r in requests if r.done_at is not None])
+    failed = sum(1 for r in requests if r.status in (abi.ERR_NONFINITE, abi.ERR_PROCRUSTES))
+    return {"requests": len(requests), "failed_requests": failed, "timesteps": int(steps), "wall_s": wall_s,
+            "timesteps_per_s": steps / wall_s if wall_s > 0 else None,
+            "step_latency_ms": {"p50": float(np.percentile(lat, 50)), "p99": float(np.percentile(lat, 99))},
+            "request_latency_s": {"p50": float(np.percentile(req, 50)) if len(req) else None,
+                                  "p99": float(np.percentile(req, 99)) if len(req) else None},
+            "ticks": len(ticks), "max_batch": max((n for _, n, _ in ticks), default=0)}

@@ -1,0 +1,42 @@
+"""The serving loop on the GPU: every result equals the request served alone."""
+import numpy as np
+import pytest
+
+from mfem_gb300 import abi
+from mfem_gb300.desc import SceneSpec
+from mfem_gb300.meshgen import cube_grid, enu_to_lame, face_mask
+
+
+def _spec(dims, E, axis, prec):
+    V, T = cube_grid(*dims, 0.05)
+    lam, mu = enu_to_lame(E, 0.35)
+    return SceneSpec(V_rest=V, tets=T, mu=np.full(len(T), mu), lam=np.full(len(T), lam),
+                     is_fixed=face_mask(V, axis, "min"), dt=1 / 60, max_newton_iterations=8,
+                     iterative_solver_tolerance=1e-6, newton_residual_tolerance=1e-5,
+                     precision=prec, pcg_kernel=abi.PCG_KERNEL_FUSED)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("prec", [abi.PRECISION_FP64, abi.PRECISION_MIXED])
+def test_served_results_equal_alone(gpu_lib, prec):
+    from mfem_gb300 import gpu, server
+    reqs = [((5, 3, 2), 2e5, 0, 3), ((3, 4, 4), 4e5, 1, 5), ((7, 2, 3), 1e5, 2, 2),
+            ((4, 4, 4), 3e5, 0, 4)]
+    specs = [_spec(d, E, ax, prec) for d, E, ax, _ in reqs]
+    alone = []
+    for sp, (_, _, _, n) in zip(specs, reqs):
+        s = gpu.Scene(sp)
+        for _ in range(n):
+            s.step()
+        alone.append(s.get_state()["x"])
+        s.close()
+    # a budget for about two scenes at a time: the others wait and join later
+    budget = int(1.5 * max(gpu.footprint(sp) for sp in specs))
+    srv = server.Server(budget_bytes=budget)
+    for i, (sp, (_, _, _, n)) in enumerate(zip(specs, reqs)):
+        srv.submit(sp, n, arrival=0.0)
+    out = srv.run(realtime=False)
+    assert max(n for _, n, _ in srv.ticks) >= 2        # scenes did share ticks
+    for r, ref in zip(out, alone):
+        assert r.status in (abi.OK, abi.ERR_CG_MAXITER)
+        assert np.array_equal(r.result["x"], ref)
