@@ -43,7 +43,7 @@ class _FakeGpu:
         used = sum(s.spec["bytes"] for s in scenes)
 
         class B:
-            def step(self):
+            def step(self, raise_on_error=True):
                 assert used <= 100
                 for s in scenes:
                     s.x += 1.0
