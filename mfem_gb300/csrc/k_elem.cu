@@ -611,7 +611,9 @@ __global__ void __launch_bounds__(kElemTile) k_ls_energy(const Tile* tiles, cons
       // energies a difference below their rounding bound is not a decision
       // the arithmetic can make; such a step is accepted.
       const double noise = sd.fp64 ? 0.0 : 8.0 * 1.1920929e-7 * (eab + sc->E_abs);
-      if (fx < sc->fx0 + noise) {
+      // A trial point whose energy terms overflowed makes the bound
+      // infinite; it is rejected, not accepted.
+      if (isfinite(fx) && isfinite(noise) && fx < sc->fx0 + noise) {
         sc->ls_active = 0;
         sc->ls_ok = 1;
         atomicSub(&ctrs->ls_active, 1);

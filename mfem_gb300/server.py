@@ -16,9 +16,21 @@ upload), overlapping the GPU ticks.  A scene's arithmetic does not depend on
 which other scenes share its batch (per-scene tiles and fixed-order
 reductions), so every result is bitwise the one the request would get alone.
 
+Precision escalation: a mixed-precision scene whose line search fails in a
+timestep (every trial step size rejected, MFEM_ERR_LS_FAILED) or whose FP32
+rotation iteration did not converge (MFEM_ERR_PROCRUSTES) has reached what
+FP32 matrices and directions can resolve -- in very soft bodies at large
+deformation the clamped Hessian eigenvalues (1e-6 h^2 against O(10)) are
+below FP32 rounding, and later steps diverge.  Its state is still finite at
+that point (a failed line search moves nothing), so the server rebuilds the
+scene in FP64 from that state and it continues there; a scene that fails
+again in FP64 leaves with its status, as the reference would stop.  Scenes
+of one precision share a batch; a tick steps both batches.
+
 No counterpart in the reference, which steps one scene per process.
 """
 import concurrent.futures as cf
+import copy
 import time
 from dataclasses import dataclass, field
 
@@ -42,6 +54,7 @@ class Request:
     newton: list = field(default_factory=list)
     cg: list = field(default_factory=list)
     status: int = abi.OK
+    escalated_at: int = None       # timesteps taken in mixed precision before FP64
     result: dict = None
 
 
@@ -50,12 +63,15 @@ class Server:
 
     budget_bytes  device memory the admitted scenes may hold together
     keep_state    which final state arrays to return ("x", "v", "s", "R")
+    escalate      continue a mixed-precision scene in FP64 after a failed
+                  line search
     """
 
-    def __init__(self, budget_bytes, keep_state=("x",), max_scenes=4096):
+    def __init__(self, budget_bytes, keep_state=("x",), max_scenes=4096, escalate=True):
         self.budget = int(budget_bytes)
         self.keep = tuple(keep_state)
         self.max_scenes = max_scenes
+        self.escalate = escalate
         self.queue = []
         self.ticks = []
 
@@ -67,17 +83,36 @@ class Server:
         self.queue.append(r)
         return r.rid
 
+    @staticmethod
+    def _in_fp64(r, sc):
+        """The scene rebuilt in FP64 from its current state, or None when that
+        state is no longer finite."""
+        st = sc.get_state()
+        if not all(np.isfinite(st[k]).all() for k in ("x", "v", "s", "R")):
+            return None
+        spec = copy.copy(r.spec)
+        spec.precision = abi.PRECISION_FP64
+        sc64 = gpu.Scene(spec)
+        sc64.set_state(x=st["x"], v=st["v"], s=st["s"], R=st["R"])
+        return spec, sc64
+
     def run(self, realtime=True):
         """Serves every submitted request; returns them with their results.
         realtime: arrivals follow the wall clock (else all are due at once)."""
         pending = sorted(self.queue, key=lambda r: (r.arrival, r.rid))
         building = {}          # rid -> future(Scene)
         active = {}            # rid -> (Request, Scene)
+        groups = {}            # precision -> (Batch, member rids)
         used = 0
-        batch, members = None, ()
         pool = cf.ThreadPoolExecutor(max_workers=1)
         t0 = time.perf_counter()
         now = lambda: time.perf_counter() - t0
+
+        def close_batches():
+            for b, _ in groups.values():
+                b.close()
+            groups.clear()
+
         try:
             while pending or building or active:
                 # admit what has arrived and fits
@@ -96,27 +131,43 @@ class Server:
                     if pending and realtime:
                         time.sleep(max(0.0, min(0.01, pending[0].arrival - now())))
                     continue
-                key = tuple(sorted(active))
-                if key != members:
-                    if batch is not None:
-                        batch.close()
-                    batch = gpu.Batch([active[k][1] for k in key])
-                    members = key
-                stats = batch.step(raise_on_error=False)
-                tick_ms = stats[0].device_ms
-                self.ticks.append((now(), len(key), tick_ms))
-                finished = []
-                for k, st in zip(key, stats):
-                    r, _ = active[k]
+                by_prec = {}
+                for k in sorted(active):
+                    by_prec.setdefault(active[k][1].spec.precision, []).append(k)
+                for p in [p for p in groups if p not in by_prec]:
+                    groups.pop(p)[0].close()
+                results, tick_ms = [], 0.0
+                for p in sorted(by_prec):
+                    key = tuple(by_prec[p])
+                    b, members = groups.get(p, (None, ()))
+                    if key != members:
+                        if b is not None:
+                            b.close()
+                        b = gpu.Batch([active[k][1] for k in key])
+                        groups[p] = (b, key)
+                    stats = b.step(raise_on_error=False)
+                    tick_ms += stats[0].device_ms
+                    results += list(zip(key, stats))
+                self.ticks.append((now(), len(active), tick_ms))
+                finished, escalate = [], []
+                for k, st in results:
+                    r, sc = active[k]
                     r.steps_done += 1
                     r.step_ms.append(tick_ms)
                     r.newton.append(st.newton_iterations)
                     r.cg.append(st.cg_iterations)
+                    if (self.escalate and r.steps_done < r.steps
+                            and sc.spec.precision == abi.PRECISION_MIXED
+                            and st.status in (abi.ERR_LS_FAILED, abi.ERR_PROCRUSTES)):
+                        escalate.append(k)
+                        continue
                     if st.status not in (abi.OK, abi.ERR_CG_MAXITER, abi.ERR_LS_FAILED):
                         r.status = st.status
                     # a scene whose state is no longer finite leaves with its status
                     if r.steps_done >= r.steps or st.status in (abi.ERR_NONFINITE, abi.ERR_PROCRUSTES):
                         finished.append(k)
+                if finished or escalate:
+                    close_batches()      # before any of their scenes is freed
                 for k in finished:
                     r, sc = active.pop(k)
                     if r.status in (abi.ERR_NONFINITE, abi.ERR_PROCRUSTES):
@@ -127,12 +178,22 @@ class Server:
                     r.done_at = now()
                     sc.close()
                     used -= r.footprint
-                if finished:
-                    batch.close()
-                    batch, members = None, ()
+                for k in escalate:
+                    r, sc = active[k]
+                    moved = self._in_fp64(r, sc)
+                    sc.close()
+                    if moved is None:
+                        active.pop(k)
+                        r.status, r.result, r.done_at = abi.ERR_NONFINITE, None, now()
+                        used -= r.footprint
+                        continue
+                    spec, sc64 = moved
+                    fp = gpu.footprint(spec)
+                    used += fp - r.footprint
+                    r.footprint, r.escalated_at = fp, r.steps_done
+                    active[k] = (r, sc64)
         finally:
-            if batch is not None:
-                batch.close()
+            close_batches()
             for r, sc in active.values():
                 sc.close()
             pool.shutdown(wait=True)
@@ -145,7 +206,9 @@ def summary(requests, ticks, wall_s):
     lat = np.array([ms for r in requests for ms in r.step_ms]) if steps else np.zeros(1)
     req = np.array([r.done_at - r.arrival for r in requests if r.done_at is not None])
     failed = sum(1 for r in requests if r.status in (abi.ERR_NONFINITE, abi.ERR_PROCRUSTES))
-    return {"requests": len(requests), "failed_requests": failed, "timesteps": int(steps), "wall_s": wall_s,
+    escalated = sum(1 for r in requests if r.escalated_at is not None)
+    return {"requests": len(requests), "failed_requests": failed, "escalated_to_fp64": escalated,
+            "timesteps": int(steps), "wall_s": wall_s,
             "timesteps_per_s": steps / wall_s if wall_s > 0 else None,
             "step_latency_ms": {"p50": float(np.percentile(lat, 50)), "p99": float(np.percentile(lat, 99))},
             "request_latency_s": {"p50": float(np.percentile(req, 50)) if len(req) else None,

@@ -40,3 +40,20 @@ def test_served_results_equal_alone(gpu_lib, prec):
     for r, ref in zip(out, alone):
         assert r.status in (abi.OK, abi.ERR_CG_MAXITER)
         assert np.array_equal(r.result["x"], ref)
+
+
+@pytest.mark.gpu
+def test_soft_scene_escalates_to_fp64_and_stays_finite(gpu_lib):
+    """A very soft body (E = 3e4 Pa, hanging from one face) at large sag: in
+    mixed precision its line search fails at step 18 and, left in mixed, the
+    state diverges by step 20; served, it continues in FP64 and stays finite."""
+    from mfem_gb300 import configs, gpu, server
+    _, spec, _ = configs.stream_c5(duration=5.0, steps=20)[84]
+    spec.pcg_kernel = abi.PCG_KERNEL_FUSED
+    srv = server.Server(budget_bytes=8 * gpu.footprint(spec))
+    srv.submit(spec, 20)
+    (r,) = srv.run(realtime=False)
+    assert r.escalated_at is not None and 10 <= r.escalated_at < 20
+    assert r.steps_done == 20 and r.status in (abi.OK, abi.ERR_CG_MAXITER)
+    x = r.result["x"]
+    assert np.isfinite(x).all() and x[:, 1].min() > -0.3

@@ -1,24 +1,35 @@
-"""Admission and batching logic of the serving loop, with fake scenes (no GPU)."""
+"""Admission, batching and precision escalation of the serving loop, with
+fake scenes (no GPU)."""
+from types import SimpleNamespace
+
 import numpy as np
 
 from mfem_gb300 import abi, server
 
 
+def _spec(name, nbytes, precision=abi.PRECISION_MIXED, ls_fail_at=None, fail=abi.ERR_LS_FAILED):
+    return SimpleNamespace(name=name, bytes=nbytes, precision=precision, ls_fail_at=ls_fail_at,
+                           fail=fail)
+
+
 class _Stats:
-    def __init__(self):
+    def __init__(self, status=abi.OK):
         self.device_ms = 1.0
         self.newton_iterations = 2
         self.cg_iterations = 10
-        self.status = abi.OK
+        self.status = status
 
 
 class _FakeGpu:
+    """Scenes carry a step counter in x; an FP64 scene needs twice the bytes.
+    A mixed scene with ls_fail_at reports a failed line search at that step."""
+
     def __init__(self):
         self.batches = []
         self.live = set()
 
     def footprint(self, spec):
-        return spec["bytes"]
+        return spec.bytes * (2 if spec.precision == abi.PRECISION_FP64 else 1)
 
     def Scene(self, spec):
         gpu = self
@@ -27,27 +38,39 @@ class _FakeGpu:
             def __init__(self):
                 self.spec = spec
                 self.x = np.zeros((1, 3))
-                gpu.live.add(spec["name"])
+                self.key = (spec.name, spec.precision)
+                assert self.key not in gpu.live
+                gpu.live.add(self.key)
 
             def get_state(self):
-                return {"x": self.x.copy()}
+                z = np.zeros(1)
+                return {"x": self.x.copy(), "v": z, "s": z, "R": z}
+
+            def set_state(self, x=None, v=None, s=None, R=None):
+                self.x = np.array(x, dtype=float)
 
             def close(self):
-                gpu.live.discard(spec["name"])
+                gpu.live.discard(self.key)
         return S()
 
     def Batch(self, scenes):
         gpu = self
-        names = tuple(s.spec["name"] for s in scenes)
-        gpu.batches.append(names)
-        used = sum(s.spec["bytes"] for s in scenes)
+        assert len({s.spec.precision for s in scenes}) == 1
+        names = tuple(s.spec.name for s in scenes)
+        gpu.batches.append((scenes[0].spec.precision, names))
 
         class B:
             def step(self, raise_on_error=True):
-                assert used <= 100
+                used = sum(gpu.footprint(s.spec) for s in scenes if s.key in gpu.live)
+                assert all(s.key in gpu.live for s in scenes)
+                assert used <= 200
+                out = []
                 for s in scenes:
                     s.x += 1.0
-                return [_Stats() for _ in scenes]
+                    fail = (s.spec.precision == abi.PRECISION_MIXED
+                            and s.spec.ls_fail_at == int(s.x[0, 0]))
+                    out.append(_Stats(s.spec.fail if fail else abi.OK))
+                return out
 
             def close(self):
                 pass
@@ -58,22 +81,56 @@ def test_admission_by_budget_and_leaving_batches(monkeypatch):
     fake = _FakeGpu()
     monkeypatch.setattr(server, "gpu", fake)
     srv = server.Server(budget_bytes=100)
-    specs = [dict(name="a", bytes=60), dict(name="b", bytes=30), dict(name="c", bytes=50),
-             dict(name="d", bytes=10)]
+    specs = [_spec("a", 60), _spec("b", 30), _spec("c", 50), _spec("d", 10)]
     steps = [3, 1, 2, 2]
     for sp, n in zip(specs, steps):
         srv.submit(sp, n)
     out = srv.run(realtime=False)
     # every request took its own number of steps, and its state shows it
     for r, n in zip(out, steps):
-        assert r.steps_done == n and r.result["x"][0, 0] == n
-    # the budget held at every tick (asserted in the fake) and nothing leaked
+        assert r.steps_done == n and r.result["x"][0, 0] == n and r.escalated_at is None
+    # nothing leaked
     assert not fake.live
     # c waited for memory: it only joined after a and b left
-    first_c = next(i for i, b in enumerate(fake.batches) if "c" in b)
-    assert all("a" not in b for b in fake.batches[first_c:])
+    first_c = next(i for i, (_, b) in enumerate(fake.batches) if "c" in b)
+    assert all("a" not in b for _, b in fake.batches[first_c:])
     s = server.summary(out, srv.ticks, 1.0)
-    assert s["timesteps"] == sum(steps) and s["requests"] == 4
+    assert s["timesteps"] == sum(steps) and s["requests"] == 4 and s["escalated_to_fp64"] == 0
+
+
+def test_failed_line_search_continues_in_fp64(monkeypatch):
+    fake = _FakeGpu()
+    monkeypatch.setattr(server, "gpu", fake)
+    srv = server.Server(budget_bytes=200)
+    srv.submit(_spec("soft", 40, ls_fail_at=2), 5)
+    srv.submit(_spec("stiff", 40), 4)
+    srv.submit(_spec("last", 40, ls_fail_at=3), 3)   # fails on its final step: no move
+    srv.submit(_spec("rot", 20, ls_fail_at=1, fail=abi.ERR_PROCRUSTES), 2)
+    out = srv.run(realtime=False)
+    soft, stiff, last, rot = out
+    assert rot.escalated_at == 1 and rot.status == abi.OK and rot.result["x"][0, 0] == 2
+    # the soft scene took 2 steps in mixed, then 3 in FP64 from the carried state
+    assert soft.escalated_at == 2 and soft.steps_done == 5 and soft.result["x"][0, 0] == 5
+    assert soft.footprint == 80
+    assert stiff.escalated_at is None and last.escalated_at is None
+    assert last.result["x"][0, 0] == 3
+    # after the failure the two precisions ran as two batches in the same ticks
+    precs = [p for p, names in fake.batches if "soft" in names]
+    assert precs[0] == abi.PRECISION_MIXED and precs[-1] == abi.PRECISION_FP64
+    assert any(p == abi.PRECISION_MIXED and "stiff" in names for p, names in fake.batches[-2:])
+    assert not fake.live
+    s = server.summary(out, srv.ticks, 1.0)
+    assert s["escalated_to_fp64"] == 2 and s["failed_requests"] == 0
+
+
+def test_escalation_off_keeps_mixed(monkeypatch):
+    fake = _FakeGpu()
+    monkeypatch.setattr(server, "gpu", fake)
+    srv = server.Server(budget_bytes=200, escalate=False)
+    srv.submit(_spec("soft", 40, ls_fail_at=2), 4)
+    (r,) = srv.run(realtime=False)
+    assert r.escalated_at is None and r.steps_done == 4
+    assert all(p == abi.PRECISION_MIXED for p, _ in fake.batches)
 
 
 def test_oversize_request_is_refused(monkeypatch):
@@ -81,7 +138,7 @@ def test_oversize_request_is_refused(monkeypatch):
     monkeypatch.setattr(server, "gpu", fake)
     srv = server.Server(budget_bytes=10)
     try:
-        srv.submit(dict(name="big", bytes=11), 1)
+        srv.submit(_spec("big", 11), 1)
     except ValueError:
         return
     raise AssertionError("oversize request accepted")
