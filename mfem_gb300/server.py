@@ -17,15 +17,16 @@ which other scenes share its batch (per-scene tiles and fixed-order
 reductions), so every result is bitwise the one the request would get alone.
 
 Precision escalation: a mixed-precision scene whose line search fails in a
-timestep (every trial step size rejected, MFEM_ERR_LS_FAILED) or whose FP32
-rotation iteration did not converge (MFEM_ERR_PROCRUSTES) has reached what
-FP32 matrices and directions can resolve -- in very soft bodies at large
-deformation the clamped Hessian eigenvalues (1e-6 h^2 against O(10)) are
-below FP32 rounding, and later steps diverge.  Its state is still finite at
-that point (a failed line search moves nothing), so the server rebuilds the
-scene in FP64 from that state and it continues there; a scene that fails
-again in FP64 leaves with its status, as the reference would stop.  Scenes
-of one precision share a batch; a tick steps both batches.
+timestep (every trial step size rejected, MFEM_ERR_LS_FAILED) has reached
+what FP32 matrices and directions can resolve -- in very soft bodies at
+large deformation the clamped Hessian eigenvalues (1e-6 h^2 against O(10))
+are below FP32 rounding, and later steps diverge.  Its state is still finite
+at that point (a failed line search moves nothing), so the server rebuilds
+the scene in FP64 from that state and it continues there.  A singular
+rotation Hessian (MFEM_ERR_PROCRUSTES, where the reference exits) ends the
+request: by then inverted elements are in the state, and continuing from it
+in FP64 costs seconds per step in the 100-iteration rotation solves.
+Scenes of one precision share a batch; a tick steps both batches.
 
 No counterpart in the reference, which steps one scene per process.
 """
@@ -158,7 +159,7 @@ class Server:
                     r.cg.append(st.cg_iterations)
                     if (self.escalate and r.steps_done < r.steps
                             and sc.spec.precision == abi.PRECISION_MIXED
-                            and st.status in (abi.ERR_LS_FAILED, abi.ERR_PROCRUSTES)):
+                            and st.status == abi.ERR_LS_FAILED):
                         escalate.append(k)
                         continue
                     if st.status not in (abi.OK, abi.ERR_CG_MAXITER, abi.ERR_LS_FAILED):

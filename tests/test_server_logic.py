@@ -108,7 +108,8 @@ def test_failed_line_search_continues_in_fp64(monkeypatch):
     srv.submit(_spec("rot", 20, ls_fail_at=1, fail=abi.ERR_PROCRUSTES), 2)
     out = srv.run(realtime=False)
     soft, stiff, last, rot = out
-    assert rot.escalated_at == 1 and rot.status == abi.OK and rot.result["x"][0, 0] == 2
+    # a singular rotation Hessian ends the request (the reference exits there)
+    assert rot.escalated_at is None and rot.status == abi.ERR_PROCRUSTES and rot.result is None
     # the soft scene took 2 steps in mixed, then 3 in FP64 from the carried state
     assert soft.escalated_at == 2 and soft.steps_done == 5 and soft.result["x"][0, 0] == 5
     assert soft.footprint == 80
@@ -120,7 +121,7 @@ def test_failed_line_search_continues_in_fp64(monkeypatch):
     assert any(p == abi.PRECISION_MIXED and "stiff" in names for p, names in fake.batches[-2:])
     assert not fake.live
     s = server.summary(out, srv.ticks, 1.0)
-    assert s["escalated_to_fp64"] == 2 and s["failed_requests"] == 0
+    assert s["escalated_to_fp64"] == 1 and s["failed_requests"] == 1
 
 
 def test_escalation_off_keeps_mixed(monkeypatch):
