@@ -495,6 +495,7 @@ struct mfem_batch {
   int max_newton = 0, max_ls = 0, max_cg = 0;
   int cg_hint = 16;
   int pcg_kernel = MFEM_PCG_KERNEL_PERSISTENT;
+  int minres = 0;  // every scene uses "minres-indefinite-block"
   int coop_grid = 0;  // blocks of the persistent PCG (all co-resident)
   int pstride = 0;  // tiles per partials quantity
   // instrumentation
@@ -611,6 +612,16 @@ void layout_scene(mfem_scene* s, Arena& A) {
       D.cgf_w[k] = A.take_bytes(n4 * r);
       D.cgf_s[k] = A.take_bytes(n4 * r);
     }
+  }
+  if (s->cfg.linear_solver == MFEM_SOLVER_MINRES_ID) {
+    D.mr_len = 4 * (size_t)std::max(M.nf, 1) + 12 * ntp;
+    D.mr_B = A.take_bytes(72 * ntp * r);
+    D.mr_H = A.take_bytes(21 * ntp * r);
+    D.mr_vec = A.take<double>(8 * D.mr_len);
+    D.mr_y = A.take<double>(12 * ntp);
+    D.mr_hinv = A.take<double>(21 * ntp);
+    D.mr_sinv = A.take<double>(21 * ntp);
+    D.mr_mlinv = A.take<double>(std::max(M.nf, 1));
   }
   s->d_sc = A.take<SceneScalars>(1);
   D.sc = s->d_sc;
@@ -897,6 +908,40 @@ int run_pcg(mfem_batch* b, const Launch& Lcg) {
   return MFEM_OK;
 }
 
+// MINRES on the (x, s, lambda) system: init, then chunks of iterations
+// (three launches each) with the convergence check one chunk behind as in
+// run_pcg, then one more A1/A2 pair that applies the last pending update,
+// and the export of dx.
+int run_minres(mfem_batch* b, const Launch& Lev) {
+  { KTimer t(b, MFEM_K_MR_INIT); launch_mr_init(Lev); }
+  int it = 0, nchunk = 0;
+  int chunk = std::max(4, b->cg_hint);
+  while (it < b->max_cg) {
+    const int c = std::min(chunk, b->max_cg - it);
+    for (int k = 0; k < c; ++k, ++it) {
+      { KTimer t(b, MFEM_K_MR_ELEM); launch_mr_elem(Lev); }
+      { KTimer t(b, MFEM_K_MR_VERT); launch_mr_vert(Lev); }
+      { KTimer t(b, MFEM_K_MR_UPDATE); launch_mr_update(Lev); }
+    }
+    const int slot = nchunk & 1;
+    CUDA_OR(cudaMemcpyAsync(&b->h_ctr_pipe[slot], b->d_ctr, sizeof(BatchCounters), cudaMemcpyDeviceToHost,
+                            b->stream),
+            MFEM_ERR_CUDA);
+    CUDA_OR(cudaEventRecord(b->ev_pipe[slot], b->stream), MFEM_ERR_CUDA);
+    if (nchunk > 0) {
+      CUDA_OR(cudaEventSynchronize(b->ev_pipe[slot ^ 1]), MFEM_ERR_CUDA);
+      if (b->h_ctr_pipe[slot ^ 1].cg_active == 0) break;
+    }
+    ++nchunk;
+    chunk = 8;
+  }
+  { KTimer t(b, MFEM_K_MR_ELEM); launch_mr_elem(Lev); }
+  { KTimer t(b, MFEM_K_MR_VERT); launch_mr_vert(Lev); }
+  { KTimer t(b, MFEM_K_MR_EXPORT); launch_mr_export(Lev); }
+  b->cg_hint = std::max(4, (it * 3) / 4);
+  return MFEM_OK;
+}
+
 // The Newton loop of NewtonOptimizer::step for every scene of the batch.
 int batch_newton(mfem_batch* b) {
   const int n = (int)b->scenes.size();
@@ -907,7 +952,11 @@ int batch_newton(mfem_batch* b) {
   for (int newton = 0; newton <= b->max_newton + 1; ++newton) {
     { KTimer t(b, MFEM_K_ELEM_UPDATE); launch_elem_update(make_launch(b, TB_ELEM), nullptr); }
     { KTimer t(b, MFEM_K_ASSEMBLE); launch_assemble(make_launch(b, TB_ROW)); }
-    if ((rc = run_pcg(b, make_launch(b, TB_CG)))) return rc;
+    if (b->minres) {
+      if ((rc = run_minres(b, Lev))) return rc;
+    } else if ((rc = run_pcg(b, make_launch(b, TB_CG)))) {
+      return rc;
+    }
     { KTimer t(b, MFEM_K_LOCAL_SOLVE); launch_local_solve(Lev); }
     for (int l = 0; l < b->max_ls; ++l) {
       { KTimer t(b, MFEM_K_LS_ENERGY); launch_ls_energy(Lev); }
@@ -1007,8 +1056,10 @@ int batch_build(mfem_scene* const* scenes, int n, mfem_batch** out) {
     maxt = std::max(maxt, tabs[tb].size());
   }
   b->pcg_kernel = scenes[0]->cfg.pcg_kernel;
+  b->minres = scenes[0]->dev.minres;
   for (int i = 1; i < n; ++i)
-    if (scenes[i]->cfg.pcg_kernel != b->pcg_kernel) return MFEM_ERR_INVALID;
+    if (scenes[i]->cfg.pcg_kernel != b->pcg_kernel || scenes[i]->dev.minres != b->minres)
+      return MFEM_ERR_INVALID;
   if (b->pcg_kernel == MFEM_PCG_KERNEL_PERSISTENT) {
     int dev = 0, sms = 0;
     CUDA_OR(cudaGetDevice(&dev), MFEM_ERR_CUDA);
@@ -1092,6 +1143,7 @@ int scene_init_device(mfem_scene* s) {
   D.npin = M.npin;
   D.material_uniform = M.material_uniform;
   D.block_jacobi = s->cfg.linear_solver == MFEM_SOLVER_GPU_PCG_BLOCK ? 1 : 0;
+  D.minres = s->cfg.linear_solver == MFEM_SOLVER_MINRES_ID ? 1 : 0;
   D.fp64 = s->fp64;
   D.h2 = s->h2;
   D.h2x = split_df(D.h2);
@@ -1153,6 +1205,20 @@ int scene_init_device(mfem_scene* s) {
   rc |= put(D.slice_off, M.slice_off.data(), sizeof(int) * M.slice_off.size());
   rc |= put(D.inc_ptr, M.inc_ptr.data(), sizeof(int) * M.inc_ptr.size());
   rc |= put(D.inc, M.inc.data(), sizeof(int2) * M.inc.size());
+  std::vector<double> mlinv;
+  if (D.minres) {
+    // inverse lumped projected mass per free row: 1 / sum_{b free} m_ab
+    mlinv.assign(std::max(M.nf, 1), 1.0);
+    for (int v = 0; v < M.nv; ++v) {
+      const int f = M.free_map[v];
+      if (f < 0) continue;
+      double m = 0;
+      for (int q = M.m_ptr[v]; q < M.m_ptr[v + 1]; ++q)
+        if (M.free_map[M.m_col[q]] >= 0) m += M.m_val[q];
+      mlinv[f] = 1.0 / m;
+    }
+    rc |= put(D.mr_mlinv, mlinv.data(), sizeof(double) * mlinv.size());
+  }
   if (rc) return MFEM_ERR_CUDA;
   CUDA_OR(cudaStreamSynchronize(st), MFEM_ERR_CUDA);
   rc = s->fp64 ? upload_scene_reals<double>(s, st) : upload_scene_reals<float>(s, st);
@@ -1300,7 +1366,7 @@ static int scene_prepare(const mfem_scene_desc* desc, std::unique_ptr<mfem_scene
   if (desc->precision != MFEM_PRECISION_FP64 && desc->precision != MFEM_PRECISION_MIXED)
     return MFEM_ERR_INVALID;
   if (desc->linear_solver != MFEM_SOLVER_EIGEN_CG_DIAG &&
-      desc->linear_solver != MFEM_SOLVER_GPU_PCG_BLOCK)
+      desc->linear_solver != MFEM_SOLVER_GPU_PCG_BLOCK && desc->linear_solver != MFEM_SOLVER_MINRES_ID)
     return MFEM_ERR_UNSUPPORTED;
   if (desc->max_newton_iterations < 0 || desc->max_linesearch_iterations < 0 ||
       desc->max_iterative_solver_iters < 0)
@@ -1510,7 +1576,8 @@ int mfem_gpu_kernel_name(int kernel, char* name, int name_len) {
   static const char* names[MFEM_K_COUNT] = {
       "k_elem_update", "k_assemble", "k_cg_init", "k_cg_spmv", "k_cg_update", "k_local_solve",
       "k_ls_energy", "k_apply", "k_step_begin", "k_step_end", "k_scalars_begin",
-      "k_cg_solve", "k_cgf_iter", "k_cg_replace"};
+      "k_cg_solve", "k_cgf_iter", "k_cg_replace", "k_mr_init", "k_mr_elem", "k_mr_vert",
+      "k_mr_update", "k_mr_export"};
   if (kernel < 0 || kernel >= MFEM_K_COUNT || !name || name_len <= 0) return MFEM_ERR_INVALID;
   strncpy(name, names[kernel], name_len - 1);
   name[name_len - 1] = 0;

@@ -338,6 +338,18 @@ __global__ void __launch_bounds__(kElemTile)
           for (int r = 0; r < 9; ++r) dbg.dSdF[54 * (size_t)e + r + 9 * i] = sym[i] * double(G[9 * i + r]);
       }
     }
+    if (sd.minres) {
+      // ds/dx and the Hessian for the matrix-free (x, s, lambda) product
+      Real* Bo = static_cast<Real*>(sd.mr_B);
+#pragma unroll
+      for (int k = 0; k < 72; ++k) Bo[(size_t)k * sd.ntp + e] = B[k];
+      Real* Ho = static_cast<Real*>(sd.mr_H);
+      int k = 0;
+#pragma unroll
+      for (int i = 0; i < 6; ++i)
+#pragma unroll
+        for (int j = i; j < 6; ++j, ++k) Ho[(size_t)k * sd.ntp + e] = H[i + 6 * j];
+    }
     // ---- upper 3x3 blocks of Aloc = vol * B^T H B  (mixed_stretch.cpp:174-175)
 #pragma unroll
     for (int b = 0; b < 4; ++b) {
@@ -448,38 +460,48 @@ __global__ void __launch_bounds__(kElemTile) k_local_solve(const Tile* tiles, co
         sv[i] = Real(Ext<Real>::to_real(sE[i]));
         S6[i] = Real(Ext<Real>::to_real(sE[i] + E(d[i])));
       }
-      const int v[4] = {in.tv.x, in.tv.y, in.tv.z, in.tv.w};
-      Real dd[4][3];
+      Real ds[6], la[6];
+      if (sd.minres) {
+        // MINRES solved for ds and lambda with dx (SystemMatrixIndefinite::
+        // post_solve, linear_system.h:88-99)
+        const double* X = sd.mr_vec + 7 * sd.mr_len + 4 * (size_t)sd.nf;
 #pragma unroll
-      for (int k = 0; k < 4; ++k) {
-        const int f = sd.free_map[v[k]];
+        for (int i = 0; i < 6; ++i) {
+          ds[i] = Real(X[(size_t)i * sd.ntp + e]);
+          la[i] = Real(X[(size_t)(6 + i) * sd.ntp + e]);
+        }
+      } else {
+        const int v[4] = {in.tv.x, in.tv.y, in.tv.z, in.tv.w};
+        Real dd[4][3];
 #pragma unroll
-        for (int c = 0; c < 3; ++c) dd[k][c] = f >= 0 ? cgx[4 * f + c] : Real(0);
-      }
-      Real dF[9];
+        for (int k = 0; k < 4; ++k) {
+          const int f = sd.free_map[v[k]];
 #pragma unroll
-      for (int c = 0; c < 3; ++c)
+          for (int c = 0; c < 3; ++c) dd[k][c] = f >= 0 ? cgx[4 * f + c] : Real(0);
+        }
+        Real dF[9];
 #pragma unroll
-        for (int r = 0; r < 3; ++r)
-          dF[r + 3 * c] = (dd[1][r] - dd[0][r]) * in.dp[c] + (dd[2][r] - dd[0][r]) * in.dp[3 + c] +
-                          (dd[3][r] - dd[0][r]) * in.dp[6 + c];
-      Real dFh[9];
-      mulAtB(R, dF, dFh);
-      Real u[18], delta[6];
-      stretch_derivative_u(S6, u);
-      ds_dot(u, dFh, delta);
-      Real ds[6];
+        for (int c = 0; c < 3; ++c)
 #pragma unroll
-      for (int i = 0; i < 6; ++i) ds[i] = d[i] + delta[i];
-      Real g[6], H[36];
-      material_gH(in, sv, h2, g, H);
-      Real la[6];
+          for (int r = 0; r < 3; ++r)
+            dF[r + 3 * c] = (dd[1][r] - dd[0][r]) * in.dp[c] + (dd[2][r] - dd[0][r]) * in.dp[3 + c] +
+                            (dd[3][r] - dd[0][r]) * in.dp[6 + c];
+        Real dFh[9];
+        mulAtB(R, dF, dFh);
+        Real u[18], delta[6];
+        stretch_derivative_u(S6, u);
+        ds_dot(u, dFh, delta);
 #pragma unroll
-      for (int i = 0; i < 6; ++i) {
-        Real acc = g[i];
+        for (int i = 0; i < 6; ++i) ds[i] = d[i] + delta[i];
+        Real g[6], H[36];
+        material_gH(in, sv, h2, g, H);
 #pragma unroll
-        for (int j = 0; j < 6; ++j) acc += H[i + 6 * j] * ds[j];
-        la[i] = -(i < 3 ? Real(1) : Real(0.5)) * acc;
+        for (int i = 0; i < 6; ++i) {
+          Real acc = g[i];
+#pragma unroll
+          for (int j = 0; j < 6; ++j) acc += H[i + 6 * j] * ds[j];
+          la[i] = -(i < 3 ? Real(1) : Real(0.5)) * acc;
+        }
       }
       store6(sd.ds, sd.ntp, e, ds);
       store6(sd.la, sd.ntp, e, la);

@@ -90,6 +90,13 @@ struct SceneScalars {
   // float copies of the step lengths every thread reads (the mixed path
   // converts nothing per thread); alpha_ls is a power of two, exact in float
   float alpha_f, beta_f, alpha_ls_f, pad_f;
+  // MINRES (cg_active / cg_iter / cg_total / cg_status / cg_err shared with
+  // the PCG): Lanczos beta, Givens state, the pending p / x update of
+  // iteration mr_slot (r1, r2, r3 and coef = beta_one c eta), and the
+  // recursive squared residual estimate against its threshold
+  double mr_beta, mr_beta_one, mr_alpha, mr_c, mr_c_old, mr_s, mr_s_old, mr_eta;
+  double mr_r1, mr_r2, mr_r3, mr_coef, mr_resid2, mr_thr2;
+  int mr_pending, mr_slot;
 };
 
 // Counters of a batch: scenes still active in each loop.
@@ -180,6 +187,21 @@ struct SceneDev {
   void* cgf_r[2];
   void* cgf_w[2];
   void* cgf_s[2];
+  // "minres-indefinite-block" (null unless the scene uses it): per element
+  // ds/dx (72: [12 i + 3 a + l] = d s_i / d x_{a,l}) and the upper triangle
+  // of h^2 hess psi (21) from K1, Real SoA; eight FP64 (x, s, lambda)
+  // vectors of mr_len doubles (v, vn, wn, w, p0..p2, x); the x-row shares
+  // of each element (12 x ntp); the preconditioner blocks (vol H)^-1 and
+  // S_ee^-1 (21 x ntp each) and the inverse lumped free mass (nf).
+  int minres;
+  void* mr_B;
+  void* mr_H;
+  double* mr_vec;
+  size_t mr_len;
+  double* mr_y;
+  double* mr_hinv;
+  double* mr_sinv;
+  double* mr_mlinv;
   // tiles of this scene in each table
   int tile_first[TB_COUNT];
   int tile_count[TB_COUNT];
@@ -232,6 +254,12 @@ void launch_cg_replace(const Launch& L);  // r = b - A x in df64 (mixed path)
 void launch_cgf_init(const Launch& L);
 void launch_cgf_iter(const Launch& L);
 int cg_solve_blocks_per_sm(int fp64);
+// MINRES on the (x, s, lambda) system (k_minres.cu, all TB_EV)
+void launch_mr_init(const Launch& L);    // rhs, preconditioner blocks, v1, w1
+void launch_mr_elem(const Launch& L);    // A1: pending update, element rows of K w
+void launch_mr_vert(const Launch& L);    // A2: vertex rows of K w, alpha
+void launch_mr_update(const Launch& L);  // B: vn, wn = P vn, Givens, convergence
+void launch_mr_export(const Launch& L);  // dx -> the PCG solution vector
 
 // Maximum dynamic shared memory the element kernels need.
 int elem_update_smem_bytes(int fp64);

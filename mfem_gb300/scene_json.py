@@ -224,7 +224,7 @@ def load_scene(src, base_dir=None, direct_solver="pcg", precision=abi.PRECISION_
         if direct_solver != "pcg":
             raise SceneError(f"direct solver {args.get('linear_solver')} has no GPU form")
         solver, tol, iters = abi.SOLVER_EIGEN_CG_DIAG, 1e-10, max(iters, 10000)
-    elif solver not in (abi.SOLVER_EIGEN_CG_DIAG, abi.SOLVER_GPU_PCG_BLOCK):
+    elif solver not in (abi.SOLVER_EIGEN_CG_DIAG, abi.SOLVER_GPU_PCG_BLOCK, abi.SOLVER_MINRES_ID):
         raise SceneError(f"linear solver {args.get('linear_solver')} is not on the GPU path")
 
     rho_all = np.concatenate(rho)

@@ -54,6 +54,12 @@ def lib():
         L.oracle_scene_energy.argtypes = [C.c_void_p, C.c_double]
         L.oracle_scene_energy.restype = C.c_double
         L.oracle_scene_pcg.argtypes = [C.c_void_p, _dp, _dp, _ip, _dp]
+        L.oracle_scene_kkt_size.argtypes = [C.c_void_p]
+        L.oracle_scene_kkt_rhs.argtypes = [C.c_void_p, _dp]
+        L.oracle_scene_kkt_mul.argtypes = [C.c_void_p, _dp, _dp]
+        L.oracle_scene_minres.argtypes = [C.c_void_p, _dp, _dp, _ip, _dp]
+        L.oracle_scene_schur_solve.argtypes = [C.c_void_p, _dp, _ip, _dp]
+        L.oracle_scene_update_system.argtypes = [C.c_void_p]
         _lib = L
     return _lib
 
@@ -197,4 +203,37 @@ class OracleScene:
         it = C.c_int32()
         err = C.c_double()
         lib().oracle_scene_pcg(self._h, _p(b), _p(x), C.byref(it), C.byref(err))
+        return x, it.value, err.value
+
+    # ---- the (x, s, lambda) system of "minres-indefinite-block" ----------
+    # at the state of the last update_system(): KKT vectors are
+    # [x: 3 n_free][s: 6 n_tets][lambda: 6 n_tets]
+    def update_system(self):
+        return lib().oracle_scene_update_system(self._h)
+
+    def kkt_rhs(self):
+        r = np.zeros(lib().oracle_scene_kkt_size(self._h))
+        lib().oracle_scene_kkt_rhs(self._h, _p(r))
+        return r
+
+    def kkt_mul(self, w):
+        w = np.ascontiguousarray(w, dtype=np.float64)
+        out = np.zeros_like(w)
+        lib().oracle_scene_kkt_mul(self._h, _p(w), _p(out))
+        return out
+
+    def minres(self, b):
+        b = np.ascontiguousarray(b, dtype=np.float64)
+        x = np.zeros_like(b)
+        it = C.c_int32()
+        err = C.c_double()
+        st = lib().oracle_scene_minres(self._h, _p(b), _p(x), C.byref(it), C.byref(err))
+        return x, it.value, err.value, st
+
+    def schur_solve(self):
+        """PCG on the Schur system then the local solve: [dx; ds; lambda]."""
+        x = np.zeros(lib().oracle_scene_kkt_size(self._h))
+        it = C.c_int32()
+        err = C.c_double()
+        lib().oracle_scene_schur_solve(self._h, _p(x), C.byref(it), C.byref(err))
         return x, it.value, err.value

@@ -1000,6 +1000,238 @@ void local_solve(Scene& sc) {
   }
 }
 
+// ---------------------------------------------------------------------------
+// "minres-indefinite-block" (linear_solver_factory.cpp:116-133): MINRES on the
+// full (x, s, lambda) system of SystemMatrixIndefinite (linear_system.h:61-99)
+// whose product is BlockMatrix (block_matrix.h:63-126).  KKT vectors are
+// [x: 3 nfree (free order)][s: 6 nt][lambda: 6 nt], 6-vectors per element.
+inline int kkt_size(const Scene& sc) { return 3 * sc.nfree + 12 * sc.nt; }
+
+// K w: x rows PMP w_x - PJW (dSdF w_la); s rows vol H w_s + vol Sym w_la;
+// lambda rows -dSdF^T (PJW^T w_x) + vol Sym w_s  (Displacement::product_hessian,
+// MixedStretch::product_hessian / product_jacobian_x / product_jacobian_mixed,
+// mixed_stretch.cpp:373-435).
+void kkt_mul(const Scene& sc, const std::vector<double>& w, std::vector<double>& out) {
+  const int nx = 3 * sc.nfree, ns = 6 * sc.nt;
+  out.assign(kkt_size(sc), 0.0);
+  for (int r = 0; r < sc.nfree; ++r)
+    for (int d = 0; d < 3; ++d) {
+      double acc = 0;
+      for (int q = sc.b_ptr[r]; q < sc.b_ptr[r + 1]; ++q) acc += sc.b_mass[q] * w[3 * sc.b_col[q] + d];
+      out[3 * r + d] = acc;
+    }
+  std::vector<double> xs(12 * size_t(sc.nt));  // per element: vol Jloc^T dSdF w_la, 4 vertices x 3
+#pragma omp parallel for schedule(static)
+  for (int e = 0; e < sc.nt; ++e) {
+    const double vol = sc.vol[e];
+    const double* D = &sc.dSdF[54 * size_t(e)];
+    const double* H = &sc.Hm[36 * size_t(e)];
+    const double* ws = &w[nx + 6 * size_t(e)];
+    const double* wl = &w[nx + ns + 6 * size_t(e)];
+    double Jw[9] = {0};
+    for (int k = 0; k < 4; ++k) {
+      const int f = sc.free_map[sc.T[4 * e + k]];
+      if (f < 0) continue;
+      for (int c = 0; c < 3; ++c)
+        for (int r = 0; r < 3; ++r) Jw[3 * c + r] += vol * sc.dX[12 * e + 3 * k + c] * w[3 * f + r];
+    }
+    for (int i = 0; i < 6; ++i) {
+      double hs = 0, dj = 0;
+      for (int j = 0; j < 6; ++j) hs += H[i + 6 * j] * ws[j];
+      for (int r = 0; r < 9; ++r) dj += D[r + 9 * i] * Jw[r];
+      out[nx + 6 * size_t(e) + i] = vol * hs + vol * kSym[i] * wl[i];
+      out[nx + ns + 6 * size_t(e) + i] = -dj + vol * kSym[i] * ws[i];
+    }
+    double t9[9];
+    for (int r = 0; r < 9; ++r) {
+      double v = 0;
+      for (int i = 0; i < 6; ++i) v += D[r + 9 * i] * wl[i];
+      t9[r] = v;
+    }
+    for (int k = 0; k < 4; ++k) {
+      double o[3];
+      jloc_t(&sc.dX[12 * e], k, t9, o);
+      for (int d = 0; d < 3; ++d) xs[12 * size_t(e) + 3 * k + d] = vol * o[d];
+    }
+  }
+  for (int e = 0; e < sc.nt; ++e)
+    for (int k = 0; k < 4; ++k) {
+      const int f = sc.free_map[sc.T[4 * e + k]];
+      if (f < 0) continue;
+      for (int d = 0; d < 3; ++d) out[3 * f + d] -= xs[12 * size_t(e) + 3 * k + d];
+    }
+}
+
+// Block-diagonal preconditioner P = diag(A^-1, S^-1) with A = diag(PMP, Hs)
+// the (x, s) block and S = Gx^T PMP^-1 Gx + Gs Hs^-1 Gs its Schur complement
+// (Hs = vol H, Gs = vol Sym, Gx = jacobian_x = -PJW C, mixed_stretch.cpp:335-371),
+// each block reduced to what is local: PMP by its lumped (row-sum)
+// diagonal, S by its 6x6 diagonal block per element.  The reference's
+// BlockDiagonalPreconditioner (preconditioners.h:64-208) factors PMP and
+// L = Gx^T Mlump^-1 Gx + 1e-8 I with sparse direct solvers, scales the s
+// block as vol Hinv, and leaves out Gs Hs^-1 Gs; with those blocks MINRES's
+// recursive estimate falls below 1e-4 while the direction is still wrong
+// (a 6x3x3 beam: 17 iterations, dx 100% off; 7949 iterations to 1e-8),
+// whereas this one reaches 1e-4 with dx within 1e-4 in a few hundred.
+struct MinresPrecond {
+  std::vector<double> mlinv;  // 3 per free vertex
+  std::vector<double> sinv;   // 36 per element
+};
+
+void minres_precond_build(const Scene& sc, MinresPrecond& P) {
+  P.mlinv.assign(3 * size_t(sc.nfree), 0.0);
+  for (int r = 0; r < sc.nfree; ++r) {
+    double m = 0;
+    for (int q = sc.b_ptr[r]; q < sc.b_ptr[r + 1]; ++q) m += sc.b_mass[q];
+    for (int d = 0; d < 3; ++d) P.mlinv[3 * r + d] = 1.0 / m;
+  }
+  P.sinv.assign(36 * size_t(sc.nt), 0.0);
+#pragma omp parallel for schedule(static)
+  for (int e = 0; e < sc.nt; ++e) {
+    const double vol = sc.vol[e];
+    const double* D = &sc.dSdF[54 * size_t(e)];
+    const double* Hi = &sc.Hinv[36 * size_t(e)];
+    double S[36];
+    for (int i = 0; i < 6; ++i)
+      for (int j = 0; j < 6; ++j) S[i + 6 * j] = vol * kSym[i] * Hi[i + 6 * j] * kSym[j];
+    for (int k = 0; k < 4; ++k) {
+      const int f = sc.free_map[sc.T[4 * e + k]];
+      if (f < 0) continue;
+      double G[18];  // G(:, i) = vol Jloc_k^T dSdF(:, i)
+      for (int i = 0; i < 6; ++i) jloc_t(&sc.dX[12 * e], k, &D[9 * i], &G[3 * i]);
+      for (int i = 0; i < 18; ++i) G[i] *= vol;
+      const double mi = P.mlinv[3 * f];
+      for (int i = 0; i < 6; ++i)
+        for (int j = 0; j < 6; ++j)
+          S[i + 6 * j] += mi * (G[3 * i] * G[3 * j] + G[3 * i + 1] * G[3 * j + 1] + G[3 * i + 2] * G[3 * j + 2]);
+    }
+    inverse(6, S, &P.sinv[36 * size_t(e)]);
+  }
+}
+
+void minres_precond_apply(const Scene& sc, const MinresPrecond& P, const std::vector<double>& b,
+                          std::vector<double>& x) {
+  const int nx = 3 * sc.nfree, ns = 6 * sc.nt;
+  x.assign(b.size(), 0.0);
+  for (int i = 0; i < nx; ++i) x[i] = P.mlinv[i] * b[i];
+#pragma omp parallel for schedule(static)
+  for (int e = 0; e < sc.nt; ++e) {
+    const double* Hi = &sc.Hinv[36 * size_t(e)];
+    const double* Si = &P.sinv[36 * size_t(e)];
+    for (int i = 0; i < 6; ++i) {
+      double a = 0, c = 0;
+      for (int j = 0; j < 6; ++j) {
+        a += Hi[i + 6 * j] * b[nx + 6 * size_t(e) + j];
+        c += Si[i + 6 * j] * b[nx + ns + 6 * size_t(e) + j];
+      }
+      x[nx + 6 * size_t(e) + i] = a / sc.vol[e];
+      x[nx + ns + 6 * size_t(e) + i] = c;
+    }
+  }
+}
+
+// Preconditioned MINRES (Paige & Saunders 1975) in the form of Eigen 3.4's
+// unsupported MINRES (Eigen/src/IterativeSolvers/MINRES.h, no source here):
+// zero initial guess, Lanczos on the preconditioned operator, Givens
+// updates, and the stopping test on the recursive estimate
+// |r0|^2 prod s_k^2 < tol^2 |b|^2 with |r0| the unpreconditioned norm.
+int minres(const Scene& sc, const MinresPrecond& P, const std::vector<double>& rhs,
+           std::vector<double>& x, int max_iter, double tol, int* iters, double* err) {
+  const int n = kkt_size(sc);
+  x.assign(n, 0.0);
+  const double rhsNorm2 = dot(rhs, rhs);
+  if (rhsNorm2 == 0) {
+    *iters = 0;
+    *err = 0;
+    return MFEM_OK;
+  }
+  const double threshold2 = tol * tol * rhsNorm2;
+  std::vector<double> v_old(n), v(n, 0.0), v_new = rhs, w(n), w_new, p_oold(n), p_old(n, 0.0),
+      p(n, 0.0), Kw;
+  double residualNorm2 = rhsNorm2;
+  minres_precond_apply(sc, P, v_new, w_new);
+  double beta_new2 = dot(v_new, w_new);
+  double beta_new = std::sqrt(beta_new2);
+  const double beta_one = beta_new;
+  double c = 1.0, c_old = 1.0, s = 0.0, s_old = 0.0, eta = 1.0;
+  int it = 0;
+  while (it < max_iter) {
+    const double beta = beta_new;
+    v_old = v;
+    for (int i = 0; i < n; ++i) {
+      v_new[i] /= beta_new;
+      w_new[i] /= beta_new;
+    }
+    v = v_new;
+    w = w_new;
+    kkt_mul(sc, w, Kw);
+    for (int i = 0; i < n; ++i) v_new[i] = Kw[i] - beta * v_old[i];
+    const double alpha = dot(v_new, w);
+    for (int i = 0; i < n; ++i) v_new[i] -= alpha * v[i];
+    minres_precond_apply(sc, P, v_new, w_new);
+    beta_new2 = dot(v_new, w_new);
+    beta_new = std::sqrt(beta_new2);
+    const double r2 = s * alpha + c * c_old * beta;
+    const double r3 = s_old * beta;
+    const double r1_hat = c * alpha - c_old * s * beta;
+    const double r1 = std::sqrt(r1_hat * r1_hat + beta_new * beta_new);
+    c_old = c;
+    s_old = s;
+    c = r1_hat / r1;
+    s = beta_new / r1;
+    p_oold = p_old;
+    p_old = p;
+    for (int i = 0; i < n; ++i) p[i] = (w[i] - r2 * p_old[i] - r3 * p_oold[i]) / r1;
+    for (int i = 0; i < n; ++i) x[i] += beta_one * c * eta * p[i];
+    residualNorm2 *= s * s;
+    if (residualNorm2 < threshold2) break;
+    eta = -s * eta;
+    ++it;
+  }
+  *iters = it;
+  *err = std::sqrt(residualNorm2 / rhsNorm2);
+  return it >= max_iter ? MFEM_ERR_CG_MAXITER : MFEM_OK;
+}
+
+// SystemMatrixIndefinite::pre_solve (linear_system.h:67-86): rhs =
+// [-grad_x of Displacement; -vol g; vol Sym (S - s)], the last being
+// -gradient_dual = evaluate_constraint (mixed_stretch.cpp:126-131, 306-333).
+void kkt_rhs(Scene& sc, std::vector<double>& rhs) {
+  const int nx = 3 * sc.nfree, ns = 6 * sc.nt;
+  rhs.assign(kkt_size(sc), 0.0);
+  std::vector<double> full;
+  sc.unproject(sc.x, full);
+  const double dt = sc.dt();
+  std::vector<double> xt = sc.xtilde(), diff(3 * sc.nv), Md;
+  for (int i = 0; i < 3 * sc.nv; ++i) diff[i] = full[i] - xt[i] - dt * dt * sc.fext[i];
+  mass_mul(sc, diff, Md);
+  for (int v = 0; v < sc.nv; ++v)
+    if (sc.free_map[v] >= 0)
+      for (int d = 0; d < 3; ++d) rhs[3 * sc.free_map[v] + d] = -Md[3 * v + d];
+  for (int e = 0; e < sc.nt; ++e)
+    for (int i = 0; i < 6; ++i) {
+      rhs[nx + 6 * size_t(e) + i] = -sc.vol[e] * sc.g[6 * e + i];
+      rhs[nx + ns + 6 * size_t(e) + i] = sc.vol[e] * kSym[i] * (sc.Sv[6 * e + i] - sc.s[6 * e + i]);
+    }
+}
+
+// SystemMatrixIndefinite::post_solve (linear_system.h:88-99): dx, ds and
+// lambda straight from the solution.
+int minres_solve(Scene& sc, int* iters, double* err) {
+  MinresPrecond P;
+  minres_precond_build(sc, P);
+  std::vector<double> rhs, sol;
+  kkt_rhs(sc, rhs);
+  const int st = minres(sc, P, rhs, sol, sc.cg_iters, sc.cg_tol, iters, err);
+  const int nx = 3 * sc.nfree, ns = 6 * sc.nt;
+  sc.dx.assign(sol.begin(), sol.begin() + nx);
+  for (int i = 0; i < ns; ++i) {
+    sc.ds[i] = sol[nx + i];
+    sc.lam[i] = sol[nx + ns + i];
+  }
+  return st;
+}
+
 // energy_func(alpha) of newton_optimizer.cpp:34-49.
 double energy(Scene& sc, double a) {
   double dt = sc.dt(), h2 = dt * dt;
@@ -1054,11 +1286,16 @@ int step(Scene& sc, mfem_step_stats* stats) {
       break;
     int iters = 0;
     double err = 0;
-    int s2 = pcg(sc, sc.rhs, sc.dx, sc.cg_iters, sc.cg_tol, &iters, &err);
-    if (s2 != MFEM_OK && status == MFEM_OK) status = s2;
+    if (sc.solver == MFEM_SOLVER_MINRES_ID) {
+      int s2 = minres_solve(sc, &iters, &err);
+      if (s2 != MFEM_OK && status == MFEM_OK) status = s2;
+    } else {
+      int s2 = pcg(sc, sc.rhs, sc.dx, sc.cg_iters, sc.cg_tol, &iters, &err);
+      if (s2 != MFEM_OK && status == MFEM_OK) status = s2;
+      local_solve(sc);
+    }
     st.cg_iterations += iters;
     st.cg_error = err;
-    local_solve(sc);
     decrement = std::max(inf_norm(sc.dx), inf_norm(sc.ds));
     E = energy(sc, 0.0);
     res = std::fabs((E - E_prev) / (E + 1e-6));
@@ -1487,6 +1724,52 @@ int oracle_scene_pcg(void* scene, const double* b, double* x, int* iters,
   int st = pcg(sc, rhs, xo, sc.cg_iters, sc.cg_tol, iters, rel_residual);
   std::memcpy(x, xo.data(), 8 * xo.size());
   return st;
+}
+
+// The (x, s, lambda) system of "minres-indefinite-block" at the state of the
+// last update_system / elem_update: rhs (kkt_size), and out = K w.
+int oracle_scene_kkt_size(void* scene) { return kkt_size(*static_cast<Scene*>(scene)); }
+int oracle_scene_kkt_rhs(void* scene, double* rhs) {
+  Scene& sc = *static_cast<Scene*>(scene);
+  std::vector<double> r;
+  kkt_rhs(sc, r);
+  std::memcpy(rhs, r.data(), 8 * r.size());
+  return MFEM_OK;
+}
+int oracle_scene_kkt_mul(void* scene, const double* w, double* out) {
+  Scene& sc = *static_cast<Scene*>(scene);
+  std::vector<double> wi(w, w + kkt_size(sc)), o;
+  kkt_mul(sc, wi, o);
+  std::memcpy(out, o.data(), 8 * o.size());
+  return MFEM_OK;
+}
+// MINRES on that system; x = [dx; ds; lambda].
+int oracle_scene_minres(void* scene, const double* b, double* x, int* iters, double* rel) {
+  Scene& sc = *static_cast<Scene*>(scene);
+  MinresPrecond P;
+  minres_precond_build(sc, P);
+  std::vector<double> rhs(b, b + kkt_size(sc)), xo;
+  int st = minres(sc, P, rhs, xo, sc.cg_iters, sc.cg_tol, iters, rel);
+  std::memcpy(x, xo.data(), 8 * xo.size());
+  return st;
+}
+// The reduced path on the same state: PCG on the Schur system then
+// MixedStretch::solve; x = [dx; ds; lambda].
+int oracle_scene_schur_solve(void* scene, double* x, int* iters, double* rel) {
+  Scene& sc = *static_cast<Scene*>(scene);
+  int st = pcg(sc, sc.rhs, sc.dx, sc.cg_iters, sc.cg_tol, iters, rel);
+  local_solve(sc);
+  const int nx = 3 * sc.nfree, ns = 6 * sc.nt;
+  std::memcpy(x, sc.dx.data(), 8 * nx);
+  std::memcpy(x + nx, sc.ds.data(), 8 * ns);
+  std::memcpy(x + nx + ns, sc.lam.data(), 8 * ns);
+  return st;
+}
+// update_system at the current positions (K1-K3 of one Newton iteration).
+int oracle_scene_update_system(void* scene) {
+  Scene& sc = *static_cast<Scene*>(scene);
+  std::vector<double> full;
+  return update_system(sc, full);
 }
 
 }  // extern "C"

@@ -67,6 +67,12 @@ double oracle_scene_energy(void* scene, double alpha);
 /* PCG on the last assembled LHS (Eigen ConjugateGradient semantics). */
 int oracle_scene_pcg(void* scene, const double* b, double* x, int* iters,
                      double* rel_residual);
+int oracle_scene_kkt_size(void* scene);
+int oracle_scene_kkt_rhs(void* scene, double* rhs);
+int oracle_scene_kkt_mul(void* scene, const double* w, double* out);
+int oracle_scene_minres(void* scene, const double* b, double* x, int* iters, double* rel);
+int oracle_scene_schur_solve(void* scene, double* x, int* iters, double* rel);
+int oracle_scene_update_system(void* scene);
 
 #ifdef __cplusplus
 }

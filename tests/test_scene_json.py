@@ -94,7 +94,9 @@ def test_rejections(tmp_path):
     with pytest.raises(SceneError):
         load_scene(_scene(mixed_variables=["stretch"]), base_dir=str(tmp_path))
     with pytest.raises(SceneError):
-        load_scene(_scene(linear_solver="minres-indefinite-block"), base_dir=str(tmp_path))
+        load_scene(_scene(linear_solver="minres-indefinite-admm"), base_dir=str(tmp_path))
+    s = load_scene(_scene(linear_solver="minres-indefinite-block"), base_dir=str(tmp_path))
+    assert s.linear_solver == abi.SOLVER_MINRES_ID
     two = _scene()
     two["objects"] = [{"path": "beam.mesh", "boundary_condition": {"type": "hang"}},
                       {"path": "beam.mesh", "boundary_condition": {"type": "twist"}}]
