@@ -173,6 +173,27 @@ int mfem_gpu_scene_get_state(mfem_scene* scene, double* x, double* v,
 int mfem_gpu_scene_set_state(mfem_scene* scene, const double* x,
                              const double* v, const double* s, const double* R);
 
+/* ---- snapshots (resume): the whole dynamic state of a scene between steps --
+ * positions, the BDF history of positions and velocities (bdf_order slots,
+ * most recent first), the stretch variable s, the rotations (as unit
+ * quaternions) and the scripted pin positions -- the state a run carries
+ * from one NewtonOptimizer::step to the next (SimState x_, mixed_vars_ and
+ * the BDF integrator, src/simulation_state.cpp:263-308, BDF.cpp:6-93).
+ * Positions, history and s are stored as the scene holds them (8 bytes a
+ * value: an FP64 number or the mixed path's float pair), so a restore into
+ * a scene of the same precision is bitwise, and one into the other
+ * precision converts them (same mesh, BDF order and pins).
+ * snapshot_bytes gives the size; restore checks the header and returns
+ * MFEM_ERR_INVALID for a snapshot of another mesh.                        */
+int mfem_gpu_scene_snapshot_bytes(mfem_scene* scene, int64_t* bytes);
+int mfem_gpu_scene_snapshot(mfem_scene* scene, void* buf, int64_t bytes);
+int mfem_gpu_scene_restore(mfem_scene* scene, const void* buf, int64_t bytes);
+/* Device-resident checkpoint of the same state (raw copies inside device
+ * memory, allocated on first use): rollback returns the scene to its last
+ * checkpoint.  No counterpart in the reference.                          */
+int mfem_gpu_scene_checkpoint(mfem_scene* scene);
+int mfem_gpu_scene_rollback(mfem_scene* scene);
+
 /* ---- batches: many independent scenes stepped by one launch per phase ----- */
 int mfem_gpu_batch_create(mfem_scene* const* scenes, int32_t n, mfem_batch** out);
 int mfem_gpu_batch_destroy(mfem_batch* batch);

@@ -31,6 +31,11 @@ SIGNATURES = {
     "mfem_gpu_scene_sizes": (C.c_int, [_vp, _ip, _ip, _ip]),
     "mfem_gpu_scene_get_state": (C.c_int, [_vp, _dp, _dp, _dp, _dp, _dp]),
     "mfem_gpu_scene_set_state": (C.c_int, [_vp, _dp, _dp, _dp, _dp]),
+    "mfem_gpu_scene_snapshot_bytes": (C.c_int, [_vp, C.POINTER(C.c_int64)]),
+    "mfem_gpu_scene_snapshot": (C.c_int, [_vp, _vp, C.c_int64]),
+    "mfem_gpu_scene_restore": (C.c_int, [_vp, _vp, C.c_int64]),
+    "mfem_gpu_scene_checkpoint": (C.c_int, [_vp]),
+    "mfem_gpu_scene_rollback": (C.c_int, [_vp]),
     "mfem_gpu_batch_create": (C.c_int, [C.POINTER(_vp), C.c_int32, C.POINTER(_vp)]),
     "mfem_gpu_batch_destroy": (C.c_int, [_vp]),
     "mfem_gpu_batch_step": (C.c_int, [_vp, _vp]),

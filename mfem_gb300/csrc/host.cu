@@ -15,6 +15,7 @@
 #include <atomic>
 #include <cmath>
 #include <cstdio>
+#include <cstddef>
 #include <cstring>
 #include <limits>
 #include <memory>
@@ -473,6 +474,10 @@ struct mfem_scene {
   mfem_batch* solo = nullptr;
   int nnzb = 0;
   bool pins_driven = false;  // pins set by the caller for the next step
+  // device checkpoint (mfem_gpu_scene_checkpoint): raw copies of the state
+  char* ckpt = nullptr;
+  int ckpt_head = 0;
+  std::vector<double> ckpt_pins;
 };
 
 struct mfem_batch {
@@ -1439,6 +1444,7 @@ int mfem_gpu_scene_destroy(mfem_scene* scene) {
   if (!scene) return MFEM_ERR_INVALID;
   batch_free(scene->solo);
   if (scene->dmem) cudaFree(scene->dmem);
+  if (scene->ckpt) cudaFree(scene->ckpt);
   delete scene;
   return MFEM_OK;
 }
@@ -1490,6 +1496,193 @@ int mfem_gpu_scene_get_state(mfem_scene* s, double* x, double* v, double* sv, do
     else download_soa<float>(s->dev.quat, M.nt, s->ntp, 4, q.data(), st);
     for (int e = 0; e < M.nt; ++e) quat_to_rot_h(&q[4 * (size_t)e], &R[9 * (size_t)e]);
   }
+  return MFEM_OK;
+}
+
+// ---- snapshots ----------------------------------------------------------
+namespace {
+struct SnapHeader {
+  char magic[4];  // "MFSN"
+  int32_t version, nv, nt, bdf_order, npin, reserved[2];
+};
+size_t snapshot_doubles(const mfem_scene* s) {
+  const HostMesh& M = s->M;
+  const size_t I = s->cfg.bdf_order;
+  return 3 * (size_t)M.nv * (1 + 2 * I) + 10 * (size_t)M.nt + 3 * (size_t)M.npin;
+}
+int read_head(mfem_scene* s, int* head) {
+  CUDA_OR(cudaMemcpy(head, reinterpret_cast<char*>(s->d_sc) + offsetof(SceneScalars, hist_head), sizeof(int),
+                     cudaMemcpyDeviceToHost),
+          MFEM_ERR_CUDA);
+  return MFEM_OK;
+}
+int write_head(mfem_scene* s, int head) {
+  CUDA_OR(cudaMemcpy(reinterpret_cast<char*>(s->d_sc) + offsetof(SceneScalars, hist_head), &head, sizeof(int),
+                     cudaMemcpyHostToDevice),
+          MFEM_ERR_CUDA);
+  return MFEM_OK;
+}
+// byte sizes of the raw state buffers: x, one history slot, s, quat
+void state_sizes(const mfem_scene* s, size_t* bx, size_t* bslot, size_t* bs, size_t* bq) {
+  *bx = 24 * (size_t)s->M.nv;
+  *bslot = 24 * (size_t)s->M.nv;
+  *bs = 6 * (size_t)s->ntp * 8;
+  *bq = 4 * (size_t)s->ntp * s->rsz;
+}
+}  // namespace
+
+int mfem_gpu_scene_snapshot_bytes(mfem_scene* s, int64_t* bytes) {
+  if (!s || !bytes) return MFEM_ERR_INVALID;
+  *bytes = (int64_t)(sizeof(SnapHeader) + 8 * snapshot_doubles(s));
+  return MFEM_OK;
+}
+
+// Positions, history and s are stored as the scene holds them (an FP64
+// value, or a float pair in the mixed path: 8 bytes either way), so that a
+// restore into a scene of the same precision is bitwise; a restore into the
+// other precision converts them.  Quaternions are stored as doubles.
+int mfem_gpu_scene_snapshot(mfem_scene* s, void* buf, int64_t bytes) {
+  int64_t need = 0;
+  if (!s || !buf || mfem_gpu_scene_snapshot_bytes(s, &need) || bytes < need) return MFEM_ERR_INVALID;
+  CUDA_OR(cudaStreamSynchronize(s->solo->stream), MFEM_ERR_CUDA);
+  const HostMesh& M = s->M;
+  const int I = s->cfg.bdf_order;
+  SnapHeader h{};
+  std::memcpy(h.magic, "MFSN", 4);
+  h.version = 1;
+  h.nv = M.nv;
+  h.nt = M.nt;
+  h.bdf_order = I;
+  h.npin = M.npin;
+  h.reserved[0] = s->fp64;
+  std::memcpy(buf, &h, sizeof(h));
+  double* out = reinterpret_cast<double*>(static_cast<char*>(buf) + sizeof(h));
+  int head = 0, rc;
+  if ((rc = read_head(s, &head))) return rc;
+  const size_t n3 = 3 * (size_t)M.nv;
+  CUDA_OR(cudaMemcpy(out, s->dev.x, 8 * n3, cudaMemcpyDeviceToHost), MFEM_ERR_CUDA);
+  out += n3;
+  for (int i = 0; i < I; ++i, out += n3)
+    CUDA_OR(cudaMemcpy(out, byte_ptr(s->dev.xhist, 8 * n3 * ((head + i) % I)), 8 * n3, cudaMemcpyDeviceToHost),
+            MFEM_ERR_CUDA);
+  for (int i = 0; i < I; ++i, out += n3)
+    CUDA_OR(cudaMemcpy(out, byte_ptr(s->dev.vhist, 8 * n3 * ((head + i) % I)), 8 * n3, cudaMemcpyDeviceToHost),
+            MFEM_ERR_CUDA);
+  {
+    std::vector<double> t(6 * (size_t)s->ntp);
+    CUDA_OR(cudaMemcpy(t.data(), s->dev.s, 8 * t.size(), cudaMemcpyDeviceToHost), MFEM_ERR_CUDA);
+    for (int e = 0; e < M.nt; ++e)
+      for (int k = 0; k < 6; ++k) out[6 * (size_t)e + k] = t[(size_t)k * s->ntp + e];
+    out += 6 * (size_t)M.nt;
+  }
+  if (s->fp64) download_soa<double>(s->dev.quat, M.nt, s->ntp, 4, out, s->solo->stream);
+  else download_soa<float>(s->dev.quat, M.nt, s->ntp, 4, out, s->solo->stream);
+  out += 4 * (size_t)M.nt;
+  std::memcpy(out, s->pin_pos.data(), 8 * s->pin_pos.size());
+  return MFEM_OK;
+}
+
+int mfem_gpu_scene_restore(mfem_scene* s, const void* buf, int64_t bytes) {
+  int64_t need = 0;
+  if (!s || !buf || mfem_gpu_scene_snapshot_bytes(s, &need) || bytes < need) return MFEM_ERR_INVALID;
+  const HostMesh& M = s->M;
+  const int I = s->cfg.bdf_order;
+  SnapHeader h;
+  std::memcpy(&h, buf, sizeof(h));
+  if (std::memcmp(h.magic, "MFSN", 4) != 0 || h.version != 1 || h.nv != M.nv || h.nt != M.nt ||
+      h.bdf_order != I || h.npin != M.npin || (h.reserved[0] != 0 && h.reserved[0] != 1))
+    return MFEM_ERR_INVALID;
+  CUDA_OR(cudaStreamSynchronize(s->solo->stream), MFEM_ERR_CUDA);
+  const double* in = reinterpret_cast<const double*>(static_cast<const char*>(buf) + sizeof(h));
+  const int src64 = h.reserved[0];
+  // an array of stored values into the scene's representation
+  auto put = [&](void* dst, const double* v, size_t n) -> int {
+    if (src64 == s->fp64) {
+      CUDA_OR(cudaMemcpy(dst, v, 8 * n, cudaMemcpyHostToDevice), MFEM_ERR_CUDA);
+      return MFEM_OK;
+    }
+    std::vector<double> t(n);
+    from_ext(v, n, src64, t.data());
+    return put_ext(dst, t.data(), n, s->fp64);
+  };
+  const size_t n3 = 3 * (size_t)M.nv;
+  int rc;
+  if ((rc = put(s->dev.x, in, n3))) return rc;
+  in += n3;
+  for (int i = 0; i < I; ++i, in += n3)
+    if ((rc = put(byte_ptr(s->dev.xhist, 8 * n3 * i), in, n3))) return rc;
+  for (int i = 0; i < I; ++i, in += n3)
+    if ((rc = put(byte_ptr(s->dev.vhist, 8 * n3 * i), in, n3))) return rc;
+  if ((rc = write_head(s, 0))) return rc;
+  {
+    std::vector<double> t(6 * (size_t)s->ntp, 0.0);
+    for (int e = 0; e < M.nt; ++e)
+      for (int k = 0; k < 6; ++k) t[(size_t)k * s->ntp + e] = in[6 * (size_t)e + k];
+    if ((rc = put(s->dev.s, t.data(), t.size()))) return rc;
+    in += 6 * (size_t)M.nt;
+  }
+  if (s->fp64) upload_soa<double>(s->dev.quat, M.nt, s->ntp, 4, in, s->solo->stream);
+  else upload_soa<float>(s->dev.quat, M.nt, s->ntp, 4, in, s->solo->stream);
+  in += 4 * (size_t)M.nt;
+  std::memcpy(s->pin_pos.data(), in, 8 * s->pin_pos.size());
+  if (M.npin)
+    CUDA_OR(cudaMemcpy(s->d_pin_pos, s->pin_pos.data(), 8 * s->pin_pos.size(), cudaMemcpyHostToDevice),
+            MFEM_ERR_CUDA);
+  s->pins_driven = false;
+  CUDA_OR(cudaGetLastError(), MFEM_ERR_CUDA);
+  return MFEM_OK;
+}
+
+int mfem_gpu_scene_checkpoint(mfem_scene* s) {
+  if (!s) return MFEM_ERR_INVALID;
+  size_t bx, bslot, bs, bq;
+  state_sizes(s, &bx, &bslot, &bs, &bq);
+  const size_t I = s->cfg.bdf_order;
+  if (!s->ckpt) CUDA_OR(cudaMalloc(&s->ckpt, bx + 2 * I * bslot + bs + bq), MFEM_ERR_OOM);
+  cudaStream_t st = s->solo->stream;
+  CUDA_OR(cudaStreamSynchronize(st), MFEM_ERR_CUDA);
+  int rc;
+  if ((rc = read_head(s, &s->ckpt_head))) return rc;
+  char* d = s->ckpt;
+  CUDA_OR(cudaMemcpyAsync(d, s->dev.x, bx, cudaMemcpyDeviceToDevice, st), MFEM_ERR_CUDA);
+  d += bx;
+  CUDA_OR(cudaMemcpyAsync(d, s->dev.xhist, I * bslot, cudaMemcpyDeviceToDevice, st), MFEM_ERR_CUDA);
+  d += I * bslot;
+  CUDA_OR(cudaMemcpyAsync(d, s->dev.vhist, I * bslot, cudaMemcpyDeviceToDevice, st), MFEM_ERR_CUDA);
+  d += I * bslot;
+  CUDA_OR(cudaMemcpyAsync(d, s->dev.s, bs, cudaMemcpyDeviceToDevice, st), MFEM_ERR_CUDA);
+  d += bs;
+  CUDA_OR(cudaMemcpyAsync(d, s->dev.quat, bq, cudaMemcpyDeviceToDevice, st), MFEM_ERR_CUDA);
+  CUDA_OR(cudaStreamSynchronize(st), MFEM_ERR_CUDA);
+  s->ckpt_pins = s->pin_pos;
+  return MFEM_OK;
+}
+
+int mfem_gpu_scene_rollback(mfem_scene* s) {
+  if (!s || !s->ckpt) return MFEM_ERR_INVALID;
+  size_t bx, bslot, bs, bq;
+  state_sizes(s, &bx, &bslot, &bs, &bq);
+  const size_t I = s->cfg.bdf_order;
+  cudaStream_t st = s->solo->stream;
+  CUDA_OR(cudaDeviceSynchronize(), MFEM_ERR_CUDA);
+  const char* d = s->ckpt;
+  CUDA_OR(cudaMemcpyAsync(s->dev.x, d, bx, cudaMemcpyDeviceToDevice, st), MFEM_ERR_CUDA);
+  d += bx;
+  CUDA_OR(cudaMemcpyAsync(s->dev.xhist, d, I * bslot, cudaMemcpyDeviceToDevice, st), MFEM_ERR_CUDA);
+  d += I * bslot;
+  CUDA_OR(cudaMemcpyAsync(s->dev.vhist, d, I * bslot, cudaMemcpyDeviceToDevice, st), MFEM_ERR_CUDA);
+  d += I * bslot;
+  CUDA_OR(cudaMemcpyAsync(s->dev.s, d, bs, cudaMemcpyDeviceToDevice, st), MFEM_ERR_CUDA);
+  d += bs;
+  CUDA_OR(cudaMemcpyAsync(s->dev.quat, d, bq, cudaMemcpyDeviceToDevice, st), MFEM_ERR_CUDA);
+  CUDA_OR(cudaStreamSynchronize(st), MFEM_ERR_CUDA);
+  int rc;
+  if ((rc = write_head(s, s->ckpt_head))) return rc;
+  s->pin_pos = s->ckpt_pins;
+  if (s->M.npin)
+    CUDA_OR(cudaMemcpy(s->d_pin_pos, s->pin_pos.data(), 8 * s->pin_pos.size(), cudaMemcpyHostToDevice),
+            MFEM_ERR_CUDA);
+  s->pins_driven = false;
   return MFEM_OK;
 }
 

@@ -99,6 +99,26 @@ class Scene:
         x, v, s, R = f(x), f(v), f(s), f(R)
         check(load().mfem_gpu_scene_set_state(self._h, _p(x), _p(v), _p(s), _p(R)), "set_state")
 
+    def snapshot(self):
+        """The scene's state between steps as bytes (x, BDF history, s, R,
+        pins); restores into a scene of the same mesh in either precision."""
+        n = C.c_int64()
+        check(load().mfem_gpu_scene_snapshot_bytes(self._h, C.byref(n)), "snapshot_bytes")
+        buf = (C.c_char * n.value)()
+        check(load().mfem_gpu_scene_snapshot(self._h, buf, n.value), "snapshot")
+        return bytes(buf)
+
+    def restore(self, snap):
+        buf = C.create_string_buffer(bytes(snap), len(snap))
+        check(load().mfem_gpu_scene_restore(self._h, buf, len(snap)), "restore")
+
+    def checkpoint(self):
+        """Device-resident copy of the state; rollback() returns to it."""
+        check(load().mfem_gpu_scene_checkpoint(self._h), "checkpoint")
+
+    def rollback(self):
+        check(load().mfem_gpu_scene_rollback(self._h), "rollback")
+
     def elem_update(self, x, h):
         nt = self.n_tets
         out = dict(R=np.zeros((nt, 9)), S=np.zeros((nt, 6)), dSdF=np.zeros((nt, 54)),

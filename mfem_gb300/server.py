@@ -16,17 +16,19 @@ upload), overlapping the GPU ticks.  A scene's arithmetic does not depend on
 which other scenes share its batch (per-scene tiles and fixed-order
 reductions), so every result is bitwise the one the request would get alone.
 
-Precision escalation: a mixed-precision scene whose line search fails in a
-timestep (every trial step size rejected, MFEM_ERR_LS_FAILED) has reached
-what FP32 matrices and directions can resolve -- in very soft bodies at
-large deformation the clamped Hessian eigenvalues (1e-6 h^2 against O(10))
-are below FP32 rounding, and later steps diverge.  Its state is still finite
-at that point (a failed line search moves nothing), so the server rebuilds
-the scene in FP64 from that state and it continues there.  A singular
-rotation Hessian (MFEM_ERR_PROCRUSTES, where the reference exits) ends the
-request: by then inverted elements are in the state, and continuing from it
-in FP64 costs seconds per step in the 100-iteration rotation solves.
-Scenes of one precision share a batch; a tick steps both batches.
+Precision escalation: before every tick each mixed-precision scene keeps a
+device-resident checkpoint of its state (positions, BDF history, s, R,
+pins; mfem_gpu_scene_checkpoint).  A mixed scene whose step ends with a
+failed line search (every trial step rejected, MFEM_ERR_LS_FAILED), a
+singular rotation Hessian (MFEM_ERR_PROCRUSTES) or a non-finite state has
+reached what FP32 matrices and directions can resolve -- in very soft
+bodies at large deformation the clamped Hessian eigenvalues (1e-6 h^2
+against O(10)) are below FP32 rounding, and later steps diverge.  The
+server rolls it back to the checkpoint, rebuilds it in FP64 from that state
+(mfem_gpu_scene_snapshot / restore) and the FP64 scene takes the failed
+step again.  A scene that fails in FP64 leaves with its status, as the
+reference would stop.  Scenes of one precision share a batch; a tick steps
+both batches.
 
 No counterpart in the reference, which steps one scene per process.
 """
@@ -86,15 +88,13 @@ class Server:
 
     @staticmethod
     def _in_fp64(r, sc):
-        """The scene rebuilt in FP64 from its current state, or None when that
-        state is no longer finite."""
-        st = sc.get_state()
-        if not all(np.isfinite(st[k]).all() for k in ("x", "v", "s", "R")):
-            return None
+        """The scene rolled back to its checkpoint and rebuilt in FP64 there."""
+        sc.rollback()
+        snap = sc.snapshot()
         spec = copy.copy(r.spec)
         spec.precision = abi.PRECISION_FP64
         sc64 = gpu.Scene(spec)
-        sc64.set_state(x=st["x"], v=st["v"], s=st["s"], R=st["R"])
+        sc64.restore(snap)
         return spec, sc64
 
     def run(self, realtime=True):
@@ -137,6 +137,9 @@ class Server:
                     by_prec.setdefault(active[k][1].spec.precision, []).append(k)
                 for p in [p for p in groups if p not in by_prec]:
                     groups.pop(p)[0].close()
+                if self.escalate:
+                    for k in by_prec.get(abi.PRECISION_MIXED, ()):
+                        active[k][1].checkpoint()
                 results, tick_ms = [], 0.0
                 for p in sorted(by_prec):
                     key = tuple(by_prec[p])
@@ -157,9 +160,11 @@ class Server:
                     r.step_ms.append(tick_ms)
                     r.newton.append(st.newton_iterations)
                     r.cg.append(st.cg_iterations)
-                    if (self.escalate and r.steps_done < r.steps
-                            and sc.spec.precision == abi.PRECISION_MIXED
-                            and st.status == abi.ERR_LS_FAILED):
+                    if (self.escalate and sc.spec.precision == abi.PRECISION_MIXED
+                            and st.status in (abi.ERR_LS_FAILED, abi.ERR_NONFINITE, abi.ERR_PROCRUSTES)):
+                        # undo the step: the FP64 scene takes it again
+                        r.steps_done -= 1
+                        del r.step_ms[-1], r.newton[-1], r.cg[-1]
                         escalate.append(k)
                         continue
                     if st.status not in (abi.OK, abi.ERR_CG_MAXITER, abi.ERR_LS_FAILED):
@@ -181,14 +186,8 @@ class Server:
                     used -= r.footprint
                 for k in escalate:
                     r, sc = active[k]
-                    moved = self._in_fp64(r, sc)
+                    spec, sc64 = self._in_fp64(r, sc)
                     sc.close()
-                    if moved is None:
-                        active.pop(k)
-                        r.status, r.result, r.done_at = abi.ERR_NONFINITE, None, now()
-                        used -= r.footprint
-                        continue
-                    spec, sc64 = moved
                     fp = gpu.footprint(spec)
                     used += fp - r.footprint
                     r.footprint, r.escalated_at = fp, r.steps_done

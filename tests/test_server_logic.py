@@ -46,8 +46,17 @@ class _FakeGpu:
                 z = np.zeros(1)
                 return {"x": self.x.copy(), "v": z, "s": z, "R": z}
 
-            def set_state(self, x=None, v=None, s=None, R=None):
-                self.x = np.array(x, dtype=float)
+            def checkpoint(self):
+                self.saved = self.x.copy()
+
+            def rollback(self):
+                self.x = self.saved.copy()
+
+            def snapshot(self):
+                return self.x.tobytes()
+
+            def restore(self, snap):
+                self.x = np.frombuffer(snap, dtype=float).reshape(1, 3).copy()
 
             def close(self):
                 gpu.live.discard(self.key)
@@ -104,24 +113,23 @@ def test_failed_line_search_continues_in_fp64(monkeypatch):
     srv = server.Server(budget_bytes=200)
     srv.submit(_spec("soft", 40, ls_fail_at=2), 5)
     srv.submit(_spec("stiff", 40), 4)
-    srv.submit(_spec("last", 40, ls_fail_at=3), 3)   # fails on its final step: no move
+    srv.submit(_spec("last", 40, ls_fail_at=3), 3)   # fails on its final step
     srv.submit(_spec("rot", 20, ls_fail_at=1, fail=abi.ERR_PROCRUSTES), 2)
     out = srv.run(realtime=False)
     soft, stiff, last, rot = out
-    # a singular rotation Hessian ends the request (the reference exits there)
-    assert rot.escalated_at is None and rot.status == abi.ERR_PROCRUSTES and rot.result is None
-    # the soft scene took 2 steps in mixed, then 3 in FP64 from the carried state
-    assert soft.escalated_at == 2 and soft.steps_done == 5 and soft.result["x"][0, 0] == 5
-    assert soft.footprint == 80
-    assert stiff.escalated_at is None and last.escalated_at is None
-    assert last.result["x"][0, 0] == 3
+    # the failed step is rolled back and taken again in FP64
+    assert soft.escalated_at == 1 and soft.steps_done == 5 and soft.result["x"][0, 0] == 5
+    assert len(soft.newton) == 5 and soft.footprint == 80
+    assert last.escalated_at == 2 and last.result["x"][0, 0] == 3
+    assert rot.escalated_at == 0 and rot.status == abi.OK and rot.result["x"][0, 0] == 2
+    assert stiff.escalated_at is None
     # after the failure the two precisions ran as two batches in the same ticks
     precs = [p for p, names in fake.batches if "soft" in names]
     assert precs[0] == abi.PRECISION_MIXED and precs[-1] == abi.PRECISION_FP64
     assert any(p == abi.PRECISION_MIXED and "stiff" in names for p, names in fake.batches[-2:])
     assert not fake.live
     s = server.summary(out, srv.ticks, 1.0)
-    assert s["escalated_to_fp64"] == 1 and s["failed_requests"] == 1
+    assert s["escalated_to_fp64"] == 3 and s["failed_requests"] == 0
 
 
 def test_escalation_off_keeps_mixed(monkeypatch):
