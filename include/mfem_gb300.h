@@ -77,6 +77,12 @@ enum {
 
 enum { MFEM_PRECISION_FP64 = 0, MFEM_PRECISION_MIXED = 1 };
 
+/* ---- the elastic variable: "mixed_variables": ["mixed-stretch"]
+ * (MixedStretch, src/variables/mixed_stretch.cpp) or "variables":
+ * ["stretch"] (standard FEM, Stretch, src/variables/stretch.cpp; materials
+ * with a 9-vector energy only: Stable-Neohookean, Neohookean) ------------ */
+enum { MFEM_FORMULATION_MIXED_STRETCH = 0, MFEM_FORMULATION_STRETCH = 1 };
+
 /* How the PCG runs.  PERSISTENT: one cooperative (co-resident,
  * grid-synchronised) launch per solve; SPLIT: two launches per iteration
  * with a host check for convergence every few iterations (same arithmetic
@@ -120,7 +126,8 @@ typedef struct mfem_scene_desc {
   int32_t precision;                  /* MFEM_PRECISION_*                         */
   int32_t pcg_kernel;                 /* MFEM_PCG_KERNEL_* (a batch uses the first
                                          scene's choice)                         */
-  int32_t reserved[7];
+  int32_t formulation;                /* MFEM_FORMULATION_*                       */
+  int32_t reserved[6];
 } mfem_scene_desc;
 
 /* Per-step statistics (the reference prints these as its per-iteration

@@ -46,6 +46,10 @@ SOLVER_MINRES_ADMM = 9
 SOLVER_ADMM = 10
 SOLVER_GPU_PCG_BLOCK = 100
 
+# the elastic variable: MixedStretch ("mixed-stretch") or Stretch ("stretch")
+FORMULATION_MIXED_STRETCH = 0
+FORMULATION_STRETCH = 1
+
 # BCScriptType (reference src/config.h:70-87) + additions
 BC_NULL, BC_SCALEF, BC_HANG, BC_HANGENDS, BC_STRETCH = 0, 1, 2, 3, 4
 BC_BEND, BC_TWIST, BC_ONEPOINT, BC_RANDOM = 7, 8, 13, 14
@@ -92,7 +96,8 @@ class SceneDesc(C.Structure):
         ("linear_solver", C.c_int32),
         ("precision", C.c_int32),
         ("pcg_kernel", C.c_int32),
-        ("reserved", C.c_int32 * 7),
+        ("formulation", C.c_int32),
+        ("reserved", C.c_int32 * 6),
     ]
 
 

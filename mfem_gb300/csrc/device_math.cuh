@@ -560,6 +560,161 @@ template <typename T> MI bool psd_fix(T* H, T tol) {
   return true;
 }
 
+// ---------------------------------------------------------------------------
+// Standard FEM (the "stretch" variable, src/variables/stretch.cpp:33-60):
+// psi on the flattened deformation gradient F (9, column-major, index r + 3c;
+// MaterialModel's Vector9d forms, stable_neohookean.cpp:97-234,
+// neohookean.cpp:96-231).  Both are psi = A(|F|^2) + B(det F), so with the
+// invariant coefficients of material_coef (A1 = dA/dQ, B1 = dB/dJ, B2 =
+// d2B/dJ2; A2 = 0 for both):
+//   d psi / dF   = 2 A1 F + B1 cof F
+//   d2 psi / dF2 = 2 A1 I + B2 cof cof^T + B1 d2J/dF2,
+//   d2J / dF_ij dF_kl = sum_mn eps_ikm eps_jln F_mn.
+template <typename T> MI void det_cof3(const T* F, T& J, T cof[9]) {
+  // cof(r, c) = dJ / dF(r, c), column-major
+  cof[0] = F[4] * F[8] - F[7] * F[5];
+  cof[1] = F[6] * F[5] - F[3] * F[8];
+  cof[2] = F[3] * F[7] - F[6] * F[4];
+  cof[3] = F[7] * F[2] - F[1] * F[8];
+  cof[4] = F[0] * F[8] - F[6] * F[2];
+  cof[5] = F[6] * F[1] - F[0] * F[7];
+  cof[6] = F[1] * F[5] - F[4] * F[2];
+  cof[7] = F[3] * F[2] - F[0] * F[5];
+  cof[8] = F[0] * F[4] - F[3] * F[1];
+  J = F[0] * cof[0] + F[1] * cof[1] + F[2] * cof[2];
+}
+
+template <typename T> MI T fem_psi(int type, T mu, T la, const T* F) {
+  T J, cof[9], Q = T(0);
+#pragma unroll
+  for (int i = 0; i < 9; ++i) Q = Q + F[i] * F[i];
+  det_cof3(F, J, cof);
+  return material_coef<T>(type, mu, la, Q, J, T(0), true).psi;
+}
+
+template <typename T> MI void fem_grad(int type, T mu, T la, const T* F, T g[9]) {
+  T J, cof[9], Q = T(0);
+#pragma unroll
+  for (int i = 0; i < 9; ++i) Q = Q + F[i] * F[i];
+  det_cof3(F, J, cof);
+  const MatCoef<T> c = material_coef<T>(type, mu, la, Q, J, T(0), false);
+#pragma unroll
+  for (int i = 0; i < 9; ++i) g[i] = T(2) * c.A1 * F[i] + c.B1 * cof[i];
+}
+
+// Gradient and Hessian (full 9x9, column-major; not psd-fixed).
+template <typename T> MI void fem_grad_hess(int type, T mu, T la, const T* F, T g[9], T H[81]) {
+  T J, cof[9], Q = T(0);
+#pragma unroll
+  for (int i = 0; i < 9; ++i) Q = Q + F[i] * F[i];
+  det_cof3(F, J, cof);
+  const MatCoef<T> c = material_coef<T>(type, mu, la, Q, J, T(0), false);
+#pragma unroll
+  for (int i = 0; i < 9; ++i) g[i] = T(2) * c.A1 * F[i] + c.B1 * cof[i];
+#pragma unroll
+  for (int a = 0; a < 9; ++a)
+#pragma unroll
+    for (int b = 0; b < 9; ++b) H[a + 9 * b] = c.B2 * cof[a] * cof[b] + (a == b ? T(2) * c.A1 : T(0));
+  // B1 d2J/dF2: for (i, j) = (a % 3, a / 3), (k, l) = (b % 3, b / 3), nonzero
+  // only for i != k and j != l, = +-F(m, n) with m, n the remaining indices
+#pragma unroll
+  for (int a = 0; a < 9; ++a)
+#pragma unroll
+    for (int b = 0; b < 9; ++b) {
+      const int i = a % 3, j = a / 3, k = b % 3, l = b / 3;
+      if (i == k || j == l) continue;
+      const int m = 3 - i - k, n = 3 - j - l;
+      // eps_ikm eps_jln: sign of the permutations (i, k, m) and (j, l, n)
+      const int si = ((k - i + 3) % 3 == 1) ? 1 : -1;
+      const int sj = ((l - j + 3) % 3 == 1) ? 1 : -1;
+      H[a + 9 * b] += T(si * sj) * c.B1 * F[m + 3 * n];
+    }
+}
+
+// In-place lower Cholesky of a symmetric N x N (column-major) with every
+// pivot required above floor_.
+template <int N, typename T> MI bool cholesky_n(T* A, T floor_) {
+  bool ok = true;
+#pragma unroll
+  for (int j = 0; j < N; ++j) {
+    T d = A[j + N * j];
+#pragma unroll
+    for (int k = 0; k < j; ++k) d -= A[j + N * k] * A[j + N * k];
+    ok = ok && (d > floor_);
+    T ljj = Prec<T>::sqrt_(d > floor_ ? d : (floor_ > T(0) ? floor_ : T(1)));
+    A[j + N * j] = ljj;
+    T inv = T(1) / ljj;
+#pragma unroll
+    for (int i = j + 1; i < N; ++i) {
+      T v = A[i + N * j];
+#pragma unroll
+      for (int k = 0; k < j; ++k) v -= A[i + N * k] * A[j + N * k];
+      A[i + N * j] = v * inv;
+    }
+  }
+  return ok;
+}
+
+// Cyclic Jacobi eigen-decomposition of a symmetric N x N: the diagonal of A
+// holds the eigenvalues and V (column-major) the eigenvectors on return.
+template <int N, typename T> MI void jacobi_eig_n(T* A, T* V) {
+  for (int i = 0; i < N * N; ++i) V[i] = (i % (N + 1) == 0) ? T(1) : T(0);
+  for (int sweep = 0; sweep < 15; ++sweep) {
+    T off = 0, tot = 0;
+    for (int j = 0; j < N; ++j)
+      for (int i = 0; i < N; ++i) {
+        const T a = A[i + N * j] * A[i + N * j];
+        tot += a;
+        if (i != j) off += a;
+      }
+    if (!(off > (Prec<T>::kFP64 ? T(1e-30) : T(1e-14)) * tot)) break;
+    for (int p = 0; p < N - 1; ++p)
+      for (int q = p + 1; q < N; ++q) {
+        const T apq = A[p + N * q];
+        if (apq == T(0)) continue;
+        const T theta = (A[q + N * q] - A[p + N * p]) / (T(2) * apq);
+        const T tt = (theta >= T(0) ? T(1) : T(-1)) / (fabs(theta) + Prec<T>::sqrt_(theta * theta + T(1)));
+        const T c = Prec<T>::rsqrt_(tt * tt + T(1)), sn = tt * c;
+        for (int k = 0; k < N; ++k) {
+          const T akp = A[k + N * p], akq = A[k + N * q];
+          A[k + N * p] = c * akp - sn * akq;
+          A[k + N * q] = sn * akp + c * akq;
+        }
+        for (int k = 0; k < N; ++k) {
+          const T apk = A[p + N * k], aqk = A[q + N * k];
+          A[p + N * k] = c * apk - sn * aqk;
+          A[q + N * k] = sn * apk + c * aqk;
+        }
+        for (int k = 0; k < N; ++k) {
+          const T vkp = V[k + N * p], vkq = V[k + N * q];
+          V[k + N * p] = c * vkp - sn * vkq;
+          V[k + N * q] = sn * vkp + c * vkq;
+        }
+      }
+  }
+}
+
+// sim::simple_psd_fix on an N x N: eigenvalues below tol raised to tol and H
+// rebuilt; unchanged when the Cholesky test (pivots above tol) passes.
+template <int N, typename T> MI bool psd_fix_n(T* H, T tol) {
+  T L[N * N];
+#pragma unroll
+  for (int i = 0; i < N * N; ++i) L[i] = H[i];
+  if (cholesky_n<N>(L, tol)) return false;
+  T V[N * N];
+  for (int i = 0; i < N * N; ++i) L[i] = H[i];
+  jacobi_eig_n<N>(L, V);
+  T lam[N];
+  for (int k = 0; k < N; ++k) lam[k] = L[k + N * k] < tol ? tol : L[k + N * k];
+  for (int j = 0; j < N; ++j)
+    for (int i = 0; i < N; ++i) {
+      T v = 0;
+      for (int k = 0; k < N; ++k) v += V[i + N * k] * lam[k] * V[j + N * k];
+      H[i + N * j] = v;
+    }
+  return true;
+}
+
 // Element force of the mixed residual, in the precision of T:
 //   f_a = -vol * P dphi_a,  P = sum_i q_i ds_i/dF = R (Q - [w]x),
 // Q = sum_i q_i E_i (symmetric), w = W sum_i q_i c_i (the u_i of

@@ -501,6 +501,7 @@ struct mfem_batch {
   int cg_hint = 16;
   int pcg_kernel = MFEM_PCG_KERNEL_PERSISTENT;
   int minres = 0;  // every scene uses "minres-indefinite-block"
+  int fem = 0;     // every scene uses the standard-FEM variable
   int coop_grid = 0;  // blocks of the persistent PCG (all co-resident)
   int pstride = 0;  // tiles per partials quantity
   // instrumentation
@@ -561,6 +562,7 @@ Launch make_launch(mfem_batch* b, int table) {
   L.pstride = b->pstride;
   L.counters = b->d_ctr;
   L.fp64 = b->fp64;
+  L.fem = b->fem;
   return L;
 }
 
@@ -1062,8 +1064,10 @@ int batch_build(mfem_scene* const* scenes, int n, mfem_batch** out) {
   }
   b->pcg_kernel = scenes[0]->cfg.pcg_kernel;
   b->minres = scenes[0]->dev.minres;
+  b->fem = scenes[0]->dev.fem;
   for (int i = 1; i < n; ++i)
-    if (scenes[i]->cfg.pcg_kernel != b->pcg_kernel || scenes[i]->dev.minres != b->minres)
+    if (scenes[i]->cfg.pcg_kernel != b->pcg_kernel || scenes[i]->dev.minres != b->minres ||
+        scenes[i]->dev.fem != b->fem)
       return MFEM_ERR_INVALID;
   if (b->pcg_kernel == MFEM_PCG_KERNEL_PERSISTENT) {
     int dev = 0, sms = 0;
@@ -1149,6 +1153,7 @@ int scene_init_device(mfem_scene* s) {
   D.material_uniform = M.material_uniform;
   D.block_jacobi = s->cfg.linear_solver == MFEM_SOLVER_GPU_PCG_BLOCK ? 1 : 0;
   D.minres = s->cfg.linear_solver == MFEM_SOLVER_MINRES_ID ? 1 : 0;
+  D.fem = s->cfg.formulation == MFEM_FORMULATION_STRETCH ? 1 : 0;
   D.fp64 = s->fp64;
   D.h2 = s->h2;
   D.h2x = split_df(D.h2);
@@ -1379,6 +1384,17 @@ static int scene_prepare(const mfem_scene_desc* desc, std::unique_ptr<mfem_scene
   if (desc->pcg_kernel != MFEM_PCG_KERNEL_PERSISTENT && desc->pcg_kernel != MFEM_PCG_KERNEL_SPLIT &&
       desc->pcg_kernel != MFEM_PCG_KERNEL_FUSED)
     return MFEM_ERR_INVALID;
+  if (desc->formulation != MFEM_FORMULATION_MIXED_STRETCH && desc->formulation != MFEM_FORMULATION_STRETCH)
+    return MFEM_ERR_INVALID;
+  if (desc->formulation == MFEM_FORMULATION_STRETCH) {
+    // the standard-FEM variable has no MINRES form, and only SNH and NH
+    // define the 9-vector energy (the others print "unimplemented")
+    if (desc->linear_solver == MFEM_SOLVER_MINRES_ID) return MFEM_ERR_UNSUPPORTED;
+    if (desc->material)
+      for (int e = 0; e < desc->n_tets; ++e)
+        if (desc->material[e] != MFEM_MATERIAL_SNH && desc->material[e] != MFEM_MATERIAL_NH)
+          return MFEM_ERR_UNSUPPORTED;
+  }
   s->cfg = *desc;
   // pointers in the copied descriptor are not kept
   s->cfg.V_rest = s->cfg.V_init = s->cfg.v_init = nullptr;

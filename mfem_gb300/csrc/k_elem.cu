@@ -396,6 +396,94 @@ __global__ void __launch_bounds__(kElemTile)
   }
 }
 
+// ------------------------------------------------------------- K1 (FEM) ---
+// The standard-FEM variable (Stretch::update, src/variables/stretch.cpp:33-60):
+// per element the 12x12 block h^2 vol Jloc^T d2psi/dF2 Jloc (psd-fixed:
+// tolerance 0 for Stable-Neohookean, stable_neohookean.cpp:232; the default
+// for Neohookean, neohookean.cpp:230) and the forces -h^2 vol Jloc^T dpsi/dF,
+// in the record layout of the mixed K1 so that the assembly, the solvers and
+// the line search are shared.  Forces in Ext, as in the mixed residual chain.
+template <typename Real, bool DBG>
+__global__ void __launch_bounds__(kElemTile)
+    k_elem_fem(const Tile* tiles, const SceneDev* sds, ElemDebug dbg) {
+  using E = typename Ext<Real>::T;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  unsigned int* words = reinterpret_cast<unsigned int*>(smem_raw);
+  constexpr int RB = sizeof(Real);
+  constexpr int kWords = rec_bytes(RB) / 4;
+  constexpr int kStride = kWords + 1;
+  constexpr int kRhsWord = rec_rhs_offset(RB) / 4;
+  const Tile t = tiles[blockIdx.x];
+  const SceneDev& sd = sds[t.scene];
+  if (!sd.sc->newton_active) return;
+  const int e = t.begin + threadIdx.x;
+  const Real h2 = Ext<Real>::r(sd.h2, sd.h2x);
+  if (e < t.end) {
+    unsigned int* out = words + threadIdx.x * kStride;
+    ElemIn<Real> in;
+    load_elem(sd, e, in);
+    E FE[9];
+    Real F[9];
+    deformation_gradients<Real>(sd, in, nullptr, E(0), FE, F);
+    Real dph[12];
+    dphi12(in, dph);
+    {
+      E gE[9];
+      fem_grad<E>(in.mat, E(in.mu), E(in.lam), FE, gE);
+      const E c = E(0) - Ext<Real>::c(sd.h2, sd.h2x) * E(in.vol);
+#pragma unroll
+      for (int a = 0; a < 4; ++a)
+#pragma unroll
+        for (int r = 0; r < 3; ++r) {
+          const E f = c * (gE[r] * E(dph[3 * a]) + gE[r + 3] * E(dph[3 * a + 1]) + gE[r + 6] * E(dph[3 * a + 2]));
+          put_word(out, kRhsWord + 2 * (3 * a + r), f);
+        }
+    }
+    Real g[9], H[81];
+    fem_grad_hess<Real>(in.mat, in.mu, in.lam, F, g, H);
+    psd_fix_n<9>(H, in.mat == kSNH ? Real(0) : Real(kPsdTol));
+    const Real w = h2 * in.vol;
+#pragma unroll
+    for (int b = 0; b < 4; ++b) {
+      // HB(p, m) = sum_c' H(p, m + 3c') dphi_b[c']
+      Real HB[27];
+#pragma unroll
+      for (int pp = 0; pp < 9; ++pp)
+#pragma unroll
+        for (int m = 0; m < 3; ++m)
+          HB[pp + 9 * m] = H[pp + 9 * m] * dph[3 * b] + H[pp + 9 * (m + 3)] * dph[3 * b + 1] +
+                           H[pp + 9 * (m + 6)] * dph[3 * b + 2];
+#pragma unroll
+      for (int a = 0; a <= b; ++a) {
+        const int base = rec_block_start(a) + (a == b ? 0 : 6 + 9 * (b - a - 1));
+#pragma unroll
+        for (int l = 0; l < 3; ++l)
+#pragma unroll
+          for (int m = 0; m < 3; ++m) {
+            if (a == b && m < l) continue;
+            const Real acc = dph[3 * a] * HB[l + 9 * m] + dph[3 * a + 1] * HB[l + 3 + 9 * m] +
+                             dph[3 * a + 2] * HB[l + 6 + 9 * m];
+            const int k = base + (a == b ? sym_idx(l, m) : 3 * l + m);
+            const Real v = w * acc;
+            put_word(out, k * (RB / 4), v);
+            if (DBG) {
+              const size_t Ei = e;
+              dbg.Aloc[144 * Ei + (3 * a + l) + 12 * (3 * b + m)] = double(v);
+              dbg.Aloc[144 * Ei + (3 * b + m) + 12 * (3 * a + l)] = double(v);
+            }
+          }
+      }
+    }
+  }
+  __syncthreads();
+  const int n = t.end - t.begin;
+  unsigned int* dst = reinterpret_cast<unsigned int*>(sd.rec + (size_t)t.begin * rec_bytes(RB));
+  for (int i = threadIdx.x; i < n * kWords; i += blockDim.x) {
+    const int el = i / kWords;
+    dst[i] = words[el * kStride + (i - el * kWords)];
+  }
+}
+
 // Vertex part of the energy: 1/2 diff^T M diff with diff = x + alpha dx - xt.
 template <typename Real>
 __device__ __forceinline__ typename Ext<Real>::T vertex_energy(const SceneDev& sd, int a,
@@ -446,7 +534,17 @@ __global__ void __launch_bounds__(kElemTile) k_local_solve(const Tile* tiles, co
   Real maxs[2] = {Real(0), Real(0)};
   const int idx = t.begin + threadIdx.x;
   if (t.kind == 0) {
-    if (idx < t.end) {
+    if (idx < t.end && sd.fem) {
+      // standard FEM: E(0) element term h^2 vol psi(F) (Stretch::energy), no s
+      ElemIn<Real> in;
+      load_elem(sd, idx, in);
+      E FE[9];
+      Real F[9];
+      deformation_gradients<Real>(sd, in, nullptr, E(0), FE, F);
+      const E e1 = Ext<Real>::c(sd.h2, sd.h2x) * E(in.vol) * fem_psi<E>(in.mat, E(in.mu), E(in.lam), FE);
+      sums[0] = e1;
+      sums[1] = E(Real(1e-7) * Real(fabs(Ext<Real>::to_real(e1))));
+    } else if (idx < t.end) {
       const int e = idx;
       ElemIn<Real> in;
       load_elem(sd, e, in);
@@ -584,7 +682,17 @@ __global__ void __launch_bounds__(kElemTile) k_ls_energy(const Tile* tiles, cons
   E sums[2] = {E(0), E(0)};
   const int idx = t.begin + threadIdx.x;
   if (t.kind == 0) {
-    if (idx < t.end) {
+    if (idx < t.end && sd.fem) {
+      // standard FEM: h^2 vol psi(F(x + alpha dx))
+      ElemIn<Real> in;
+      load_elem(sd, idx, in);
+      E FE[9];
+      Real F[9];
+      deformation_gradients<Real>(sd, in, cgx, alpha, FE, F);
+      const E e1 = Ext<Real>::c(sd.h2, sd.h2x) * E(in.vol) * fem_psi<E>(in.mat, E(in.mu), E(in.lam), FE);
+      sums[0] = e1;
+      sums[1] = E(Real(1e-7) * Real(fabs(Ext<Real>::to_real(e1))));
+    } else if (idx < t.end) {
       const int e = idx;
       ElemIn<Real> in;
       load_elem(sd, e, in);
@@ -785,6 +893,10 @@ void configure_kernels() {
   set_smem(k_elem_update<float, true>, elem_update_smem_bytes(0));
   set_smem(k_elem_update<double, false>, elem_update_smem_bytes(1));
   set_smem(k_elem_update<double, true>, elem_update_smem_bytes(1));
+  set_smem(k_elem_fem<float, false>, elem_update_smem_bytes(0));
+  set_smem(k_elem_fem<float, true>, elem_update_smem_bytes(0));
+  set_smem(k_elem_fem<double, false>, elem_update_smem_bytes(1));
+  set_smem(k_elem_fem<double, true>, elem_update_smem_bytes(1));
 }
 
 void launch_elem_init(const Launch& L) {
@@ -800,6 +912,16 @@ void launch_elem_update(const Launch& L, const ElemDebug* dbg) {
   ElemDebug d{};
   if (dbg) d = *dbg;
   const int sm = elem_update_smem_bytes(L.fp64);
+  if (L.fem) {
+    if (L.fp64) {
+      if (dbg) k_elem_fem<double, true><<<L.ntiles, kElemTile, sm, L.stream>>>(L.tiles, L.sds, d);
+      else k_elem_fem<double, false><<<L.ntiles, kElemTile, sm, L.stream>>>(L.tiles, L.sds, d);
+    } else {
+      if (dbg) k_elem_fem<float, true><<<L.ntiles, kElemTile, sm, L.stream>>>(L.tiles, L.sds, d);
+      else k_elem_fem<float, false><<<L.ntiles, kElemTile, sm, L.stream>>>(L.tiles, L.sds, d);
+    }
+    return;
+  }
   if (L.fp64) {
     if (dbg)
       k_elem_update<double, true><<<L.ntiles, kElemTile, sm, L.stream>>>(L.tiles, L.sds, d);

@@ -118,6 +118,7 @@ struct SceneDev {
   int material_uniform;  // material id when uniform, -1 when per element
   int block_jacobi;  // 0: Jacobi (eigen-pcg-diag), 1: 3x3 block Jacobi
   int fp64;          // 1: all-FP64 path, 0: FP32 element work
+  int fem;           // 1: the standard-FEM "stretch" variable, 0: mixed stretch
   // parameters
   double h2;         // (beta*h)^2
   double dt;         // beta*h
@@ -231,6 +232,7 @@ struct Launch {
   int pstride;
   BatchCounters* counters;
   int fp64;
+  int fem;  // the batch's scenes use the standard-FEM variable
 };
 
 // Element kernels (k_elem.cu)

@@ -44,6 +44,7 @@ class SceneSpec:
     linear_solver: int = abi.SOLVER_EIGEN_CG_DIAG
     precision: int = abi.PRECISION_FP64
     pcg_kernel: int = abi.PCG_KERNEL_PERSISTENT
+    formulation: int = abi.FORMULATION_MIXED_STRETCH
     name: str = ""
     extra: dict = field(default_factory=dict)
 
@@ -130,4 +131,5 @@ def make_desc(spec: SceneSpec) -> _Desc:
     d.linear_solver = int(spec.linear_solver)
     d.precision = int(spec.precision)
     d.pcg_kernel = int(spec.pcg_kernel)
+    d.formulation = int(spec.formulation)
     return _Desc(d, keep)

@@ -146,12 +146,21 @@ def load_scene(src, base_dir=None, direct_solver="pcg", precision=abi.PRECISION_
     def path_of(p):
         return p if os.path.isabs(p) else os.path.join(base_dir, p)
 
-    mixed = args.get("mixed_variables", ["mixed-stretch"])
-    if "mixed-stretch" not in mixed:
-        raise SceneError("the GPU path runs the mixed-stretch variable; the scene names "
-                         f"{mixed}")
-    if args.get("variables"):
-        raise SceneError(f"variables {args['variables']} are not on the GPU path")
+    # "mixed_variables": ["mixed-stretch"] (MixedStretch) or "variables":
+    # ["stretch"] (standard FEM, Stretch); a scene naming neither gets the
+    # mixed-stretch variable (the reference would simulate no elasticity)
+    mixed = args.get("mixed_variables")
+    plain = args.get("variables") or []
+    if plain:
+        if list(plain) != ["stretch"] or mixed:
+            raise SceneError(f"variables {plain} with mixed_variables {mixed} are not on the GPU path")
+        formulation = abi.FORMULATION_STRETCH
+    else:
+        mixed = ["mixed-stretch"] if mixed is None else mixed
+        if "mixed-stretch" not in mixed:
+            raise SceneError("the GPU path runs the mixed-stretch or the stretch variable; the scene "
+                             f"names {mixed}")
+        formulation = abi.FORMULATION_MIXED_STRETCH
 
     # materials (MaterialConfig defaults, src/config.h:127-135)
     mats = []
@@ -240,7 +249,7 @@ def load_scene(src, base_dir=None, direct_solver="pcg", precision=abi.PRECISION_
         max_newton_iterations=int(args.get("max_newton_iterations", 5)),
         max_linesearch_iterations=int(args.get("max_linesearch_iterations", 20)),
         max_iterative_solver_iters=iters, iterative_solver_tolerance=tol,
-        linear_solver=solver, precision=precision,
+        linear_solver=solver, precision=precision, formulation=formulation,
         name=os.path.basename(src) if isinstance(src, str) and not src.lstrip().startswith("{") else "scene")
     for k, v in overrides.items():
         setattr(spec, k, v)

@@ -41,6 +41,8 @@ def lib():
         L.oracle_material_gradient.argtypes = [C.c_int, C.c_double, C.c_double, _dp, _dp]
         L.oracle_material_hessian.argtypes = [C.c_int, C.c_double, C.c_double, _dp, C.c_int, _dp]
         L.oracle_psd_fix.argtypes = [_dp, C.c_int, C.c_double]
+        L.oracle_material9.argtypes = [C.c_int, C.c_double, C.c_double, _dp, _dp, _dp, C.c_int]
+        L.oracle_material9.restype = C.c_double
         L.oracle_scene_create.argtypes = [C.c_void_p, _ip]
         L.oracle_scene_create.restype = C.c_void_p
         L.oracle_scene_destroy.argtypes = [C.c_void_p]
@@ -121,6 +123,16 @@ def material_hessian(mtype, mu, lam, s, psd_fix=True):
     H = np.zeros((6, 6), order="F")
     lib().oracle_material_hessian(mtype, mu, lam, _p(s), int(psd_fix), _p(H))
     return H
+
+
+def material9(mtype, mu, lam, F, psd_fix=True):
+    """psi, dpsi/dF (9) and d2psi/dF2 (9x9) on the column-major flattened F
+    (the standard-FEM variable's Vector9d forms)."""
+    f = np.asfortranarray(F, dtype=np.float64).ravel(order="F").copy()
+    g = np.zeros(9)
+    H = np.zeros((9, 9), order="F")
+    psi = lib().oracle_material9(mtype, mu, lam, _p(f), _p(g), _p(H), int(psd_fix))
+    return psi, g, H
 
 
 def psd_fix(H, tol=1e-6):

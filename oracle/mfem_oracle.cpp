@@ -266,9 +266,7 @@ void invariants(const double* s, double& Q, double& J, double& t, double dJ[6]) 
   dJ[5] = 2 * (s[3] * s[4] - s[0] * s[5]);
 }
 
-MatCoef material_coef(int type, double mu, double la, const double* s) {
-  double Q, J, t, dJ[6];
-  invariants(s, Q, J, t, dJ);
+MatCoef material_coef_qjt(int type, double mu, double la, double Q, double J, double t) {
   MatCoef c{0, 0, 0, 0, 0, 0, 0, false};
   switch (type) {
     case MFEM_MATERIAL_SNH:  // stable_neohookean.cpp:8-95
@@ -322,6 +320,12 @@ MatCoef material_coef(int type, double mu, double la, const double* s) {
       break;
   }
   return c;
+}
+
+MatCoef material_coef(int type, double mu, double la, const double* s) {
+  double Q, J, t, dJ[6];
+  invariants(s, Q, J, t, dJ);
+  return material_coef_qjt(type, mu, la, Q, J, t);
 }
 
 void material_gradient(int type, double mu, double la, const double* s, double* g) {
@@ -421,6 +425,49 @@ void material_hessian(int type, double mu, double la, const double* s, bool fix,
   if (fix && c.psd) psd_fix(H, 6, kPsdTol);
 }
 
+// MaterialModel's Vector9d forms (the standard-FEM "stretch" variable) for
+// the two materials that define them: Stable-Neohookean
+// (stable_neohookean.cpp:97-234) psi = mu (1 - J) + la/2 (1 - J)^2 +
+// mu/2 (|F|^2 - 3), and Neohookean (neohookean.cpp:96-231) psi =
+// la/2 log(J)^2 - mu log J + mu/2 (|F|^2 - 3), J = det F, F flattened
+// column-major.  Derivatives by the chain rule through |F|^2 and det F
+// (the reference's are generated code; FD-checked in the tests).  The
+// Hessian's psd fix uses tolerance 0 for SNH (stable_neohookean.cpp:232)
+// and the default for NH (neohookean.cpp:230).
+void material9(int type, double mu, double la, const double* F, double* psi, double* g, double* H,
+               bool fix) {
+  double cof[9];
+  cof[0] = F[4] * F[8] - F[7] * F[5];
+  cof[1] = F[6] * F[5] - F[3] * F[8];
+  cof[2] = F[3] * F[7] - F[6] * F[4];
+  cof[3] = F[7] * F[2] - F[1] * F[8];
+  cof[4] = F[0] * F[8] - F[6] * F[2];
+  cof[5] = F[6] * F[1] - F[0] * F[7];
+  cof[6] = F[1] * F[5] - F[4] * F[2];
+  cof[7] = F[3] * F[2] - F[0] * F[5];
+  cof[8] = F[0] * F[4] - F[3] * F[1];
+  const double J = F[0] * cof[0] + F[1] * cof[1] + F[2] * cof[2];
+  double Q = 0;
+  for (int i = 0; i < 9; ++i) Q += F[i] * F[i];
+  const MatCoef c = material_coef_qjt(type, mu, la, Q, J, 0.0);
+  if (psi) *psi = c.psi;
+  if (g)
+    for (int i = 0; i < 9; ++i) g[i] = 2 * c.A1 * F[i] + c.B1 * cof[i];
+  if (!H) return;
+  static const int eps[3][3][3] = {{{0, 0, 0}, {0, 0, 1}, {0, -1, 0}},
+                                   {{0, 0, -1}, {0, 0, 0}, {1, 0, 0}},
+                                   {{0, 1, 0}, {-1, 0, 0}, {0, 0, 0}}};
+  for (int a = 0; a < 9; ++a)
+    for (int b = 0; b < 9; ++b) {
+      const int i = a % 3, j = a / 3, k = b % 3, l = b / 3;
+      double d2 = 0;  // d2 det / dF_ij dF_kl = sum_mn eps_ikm eps_jln F_mn
+      for (int m = 0; m < 3; ++m)
+        for (int n = 0; n < 3; ++n) d2 += eps[i][k][m] * eps[j][l][n] * F[m + 3 * n];
+      H[a + 9 * b] = c.B2 * cof[a] * cof[b] + c.B1 * d2 + (a == b ? 2 * c.A1 : 0.0);
+    }
+  if (fix) psd_fix(H, 9, type == MFEM_MATERIAL_SNH ? 0.0 : kPsdTol);
+}
+
 // ---------------------------------------------------------------------------
 // Scene: Mesh::init (src/mesh/mesh.cpp:124-175), Displacement
 // (src/variables/displacement.cpp), MixedStretch (mixed_stretch.cpp),
@@ -454,6 +501,8 @@ struct Scene {
   // config
   double h = 0.034, ext[3] = {0, -9.8, 0};
   int bdf = 1, max_newton = 5, ls_iters = 20, cg_iters = 500, solver = 5;
+  int fem = 0;  // the standard-FEM "stretch" variable instead of MixedStretch
+  std::vector<double> fforce;  // fem: per element 12 forces -h^2 vol Jloc^T dpsi/dF
   double cg_tol = 1e-4, newton_tol = 1e-10, res_tol = 0, load_norm = 0;
   // state
   std::vector<double> x, dx, b, fext;  // x, dx: free (3*nfree); b, fext: full
@@ -824,6 +873,31 @@ int update_system(Scene& sc, std::vector<double>& full) {
   double dt = sc.dt();
   int status = MFEM_OK;
   std::vector<double> Aloc(144 * size_t(sc.nt));
+  if (sc.fem) {
+    // Stretch::update (stretch.cpp:33-60): Jloc^T H Jloc vol h^2 and the forces
+    sc.fforce.assign(12 * size_t(sc.nt), 0.0);
+#pragma omp parallel for schedule(static)
+    for (int e = 0; e < sc.nt; ++e) {
+      const M3 F = sc.defgrad(full, e);
+      double g[9], H[81];
+      material9(sc.mat[e], sc.mu[e], sc.la[e], F.data(), nullptr, g, H, true);
+      const double w = dt * dt * sc.vol[e];
+      const double* dX = &sc.dX[12 * size_t(e)];
+      for (int a = 0; a < 4; ++a)
+        for (int l = 0; l < 3; ++l) {
+          double f = 0;
+          for (int c = 0; c < 3; ++c) f += dX[3 * a + c] * g[l + 3 * c];
+          sc.fforce[12 * size_t(e) + 3 * a + l] = -w * f;
+          for (int b = 0; b < 4; ++b)
+            for (int m = 0; m < 3; ++m) {
+              double v = 0;
+              for (int c = 0; c < 3; ++c)
+                for (int cc = 0; cc < 3; ++cc) v += dX[3 * a + c] * dX[3 * b + cc] * H[(l + 3 * c) + 9 * (m + 3 * cc)];
+              Aloc[144 * size_t(e) + (3 * a + l) + 12 * (3 * b + m)] = w * v;
+            }
+        }
+    }
+  } else {
 #pragma omp parallel for schedule(static)
   for (int e = 0; e < sc.nt; ++e) {
     int st = elem_update(sc, e, full, dt, &Aloc[144 * size_t(e)]);
@@ -831,6 +905,7 @@ int update_system(Scene& sc, std::vector<double>& full) {
 #pragma omp critical
       status = st;
     }
+  }
   }
   // Assembler::update_matrix: gather each block's contributions in sorted order.
   std::fill(sc.A.begin(), sc.A.end(), 0.0);
@@ -853,6 +928,11 @@ int update_system(Scene& sc, std::vector<double>& full) {
   std::vector<double> rfull(3 * sc.nv);
   for (int i = 0; i < 3 * sc.nv; ++i) rfull[i] = -Md[i];
   for (int e = 0; e < sc.nt; ++e) {
+    if (sc.fem) {
+      for (int k = 0; k < 4; ++k)
+        for (int d = 0; d < 3; ++d) rfull[3 * sc.T[4 * e + k] + d] += sc.fforce[12 * size_t(e) + 3 * k + d];
+      continue;
+    }
     double tmp[9];
     const double* D = &sc.dSdF[54 * e];
     for (int r = 0; r < 9; ++r) {
@@ -1244,6 +1324,16 @@ double energy(Scene& sc, double a) {
   mass_mul(sc, diff, Md);
   double val = 0.5 * dot(diff, Md);
   std::vector<double> epsi(sc.nt), econ(sc.nt);
+  if (sc.fem) {  // Stretch::energy (stretch.cpp:15-28), weighted by h^2 in energy_func
+#pragma omp parallel for schedule(static)
+    for (int e = 0; e < sc.nt; ++e) {
+      double psi;
+      const M3 F = sc.defgrad(full, e);
+      material9(sc.mat[e], sc.mu[e], sc.la[e], F.data(), &psi, nullptr, nullptr, false);
+      epsi[e] = psi * sc.vol[e];
+    }
+    return val + h2 * det_sum(sc.nt, [&](long e) { return epsi[e]; });
+  }
 #pragma omp parallel for schedule(static)
   for (int e = 0; e < sc.nt; ++e) {
     double si[6];
@@ -1292,7 +1382,7 @@ int step(Scene& sc, mfem_step_stats* stats) {
     } else {
       int s2 = pcg(sc, sc.rhs, sc.dx, sc.cg_iters, sc.cg_tol, &iters, &err);
       if (s2 != MFEM_OK && status == MFEM_OK) status = s2;
-      local_solve(sc);
+      if (!sc.fem) local_solve(sc);
     }
     st.cg_iterations += iters;
     st.cg_error = err;
@@ -1383,6 +1473,7 @@ Scene* create(const mfem_scene_desc* d, int* status) {
   sc->newton_tol = d->newton_tol;
   sc->res_tol = d->newton_residual_tolerance;
   sc->solver = d->linear_solver;
+  sc->fem = d->formulation == MFEM_FORMULATION_STRETCH ? 1 : 0;
   // Mesh::init_bcs
   bc_init(*sc, d->is_fixed);
   sc->free_map.assign(sc->nv, -1);
@@ -1617,6 +1708,11 @@ void oracle_material_hessian(int type, double mu, double la, const double* s, in
   material_hessian(type, mu, la, s, fix != 0, H);
 }
 void oracle_psd_fix(double* H, int n, double tol) { psd_fix(H, n, tol); }
+double oracle_material9(int type, double mu, double la, const double* F, double* g, double* H, int fix) {
+  double psi = 0;
+  material9(type, mu, la, F, &psi, g, H, fix != 0);
+  return psi;
+}
 
 void* oracle_scene_create(const mfem_scene_desc* desc, int* status) {
   int st = MFEM_OK;

@@ -67,6 +67,7 @@ double oracle_scene_energy(void* scene, double alpha);
 /* PCG on the last assembled LHS (Eigen ConjugateGradient semantics). */
 int oracle_scene_pcg(void* scene, const double* b, double* x, int* iters,
                      double* rel_residual);
+double oracle_material9(int type, double mu, double la, const double* F, double* g, double* H, int fix);
 int oracle_scene_kkt_size(void* scene);
 int oracle_scene_kkt_rhs(void* scene, double* rhs);
 int oracle_scene_kkt_mul(void* scene, const double* w, double* out);

@@ -94,6 +94,11 @@ def test_rejections(tmp_path):
     with pytest.raises(SceneError):
         load_scene(_scene(mixed_variables=["stretch"]), base_dir=str(tmp_path))
     with pytest.raises(SceneError):
+        load_scene(_scene(variables=["stretch"]), base_dir=str(tmp_path))  # both variables
+    fem = _scene(variables=["stretch"])
+    del fem["mixed_variables"]
+    assert load_scene(fem, base_dir=str(tmp_path)).formulation == abi.FORMULATION_STRETCH
+    with pytest.raises(SceneError):
         load_scene(_scene(linear_solver="minres-indefinite-admm"), base_dir=str(tmp_path))
     s = load_scene(_scene(linear_solver="minres-indefinite-block"), base_dir=str(tmp_path))
     assert s.linear_solver == abi.SOLVER_MINRES_ID
