@@ -56,7 +56,10 @@ def parse():
     ap.add_argument("--c5-steps", type=int, default=20, help="timesteps per served request")
     ap.add_argument("--size", type=int, default=60, help="cubes per axis for c2")
     ap.add_argument("--precision", default="mixed", choices=["mixed", "fp64"])
-    ap.add_argument("--solver", default="eigen-pcg-diag", choices=["eigen-pcg-diag", "gpu-pcg-block"])
+    ap.add_argument("--solver", default="eigen-pcg-diag",
+                    choices=["eigen-pcg-diag", "gpu-pcg-block", "minres-indefinite-block"])
+    ap.add_argument("--formulation", default="mixed-stretch", choices=["mixed-stretch", "stretch"],
+                    help="the elastic variable: MixedStretch or the standard-FEM Stretch")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-batch", action="store_true",
@@ -180,6 +183,22 @@ def kernel_bytes(kind, sizes, rsz, cg_per_launch=None):
         return nt * (16 + 9 * rsz + 3 * rsz + 4 * rsz + 6 * rsz * 4) + 3 * nf * rsz + nnz_m * 12 + 48 * nv
     if kind == "k_ls_energy":
         return nt * (16 + 9 * rsz + 3 * rsz + 4 * rsz + 6 * rsz * 3) + 3 * nf * rsz + nnz_m * 12 + 48 * nv
+    if kind == "k_elem_fem":
+        # tets, dphi, vol/mu/lam, x; element record (w)
+        return nt * (16 + 9 * rsz + 3 * rsz + 92 * rsz) + 24 * nv
+    if kind == "k_mr_elem":
+        # ds/dx (72) and H (21) in Real, vol, tets, free_map; FP64: wn (12 own
+        # + 12 gathered x), v (rw), vn (rw), w (w), the pending p / x update
+        # (w, p1, p2 read, p0 written, x rw: 72), shares y (12 w)
+        return nt * (94 * rsz + 32 + 8 * (24 + 24 + 24 + 12 + 72 + 12))
+    if kind == "k_mr_vert":
+        # mass row (col, value, neighbour wn), incidences and their shares;
+        # own x rows: v, vn (rw), wn (r), w (w), the pending update (6 x 3)
+        return nnz_m * (4 + rsz + 24) + n_inc * (8 + 24) + nf * 8 * 3 * (2 + 2 + 1 + 1 + 6)
+    if kind == "k_mr_update":
+        # vn (rw), v (r), wn (w) for 12 element and 3 row entries; (vol H)^-1
+        # and S_ee^-1 (42 doubles), 1/m per row
+        return nt * 8 * (12 * 4 + 42) + nf * 8 * (3 * 4 + 1)
     return None
 
 
@@ -214,16 +233,20 @@ def measured_peak():
 def make_spec(args, precision):
     from mfem_gb300 import abi, configs
     prec = abi.PRECISION_MIXED if precision == "mixed" else abi.PRECISION_FP64
-    solver = abi.SOLVER_EIGEN_CG_DIAG if args.solver == "eigen-pcg-diag" else abi.SOLVER_GPU_PCG_BLOCK
+    solver = {"eigen-pcg-diag": abi.SOLVER_EIGEN_CG_DIAG, "gpu-pcg-block": abi.SOLVER_GPU_PCG_BLOCK,
+              "minres-indefinite-block": abi.SOLVER_MINRES_ID}[args.solver]
     kern = {"persistent": abi.PCG_KERNEL_PERSISTENT, "split": abi.PCG_KERNEL_SPLIT,
             "fused": abi.PCG_KERNEL_FUSED}[args.pcg_kernel]
+    form = abi.FORMULATION_STRETCH if args.formulation == "stretch" else abi.FORMULATION_MIXED_STRETCH
+    kw = dict(precision=prec, linear_solver=solver, pcg_kernel=kern, formulation=form)
+    tag = ("_minres" if args.solver == "minres-indefinite-block" else "") + \
+          ("_stretch" if args.formulation == "stretch" else "")
     if args.config == "c1":
-        return configs.beam_c1(precision=prec, linear_solver=solver, pcg_kernel=kern), "beam_c1_200tets"
+        return configs.beam_c1(**kw), "beam_c1_200tets" + tag
     if args.config == "c3":
-        return configs.stress_c3(precision=prec, linear_solver=solver, pcg_kernel=kern), "stress_c3_135k"
+        return configs.stress_c3(**kw), "stress_c3_135k" + tag
     n = args.size
-    return configs.cube_c2(n=n, precision=prec, linear_solver=solver, pcg_kernel=kern), \
-        f"cube_c2_{n}^3_{5 * n ** 3}tets"
+    return configs.cube_c2(n=n, **kw), f"cube_c2_{n}^3_{5 * n ** 3}tets" + tag
 
 
 def scene_sizes(spec, scene):
@@ -439,7 +462,7 @@ def run_ours(args):
         "config": {"workload": workload, "tets": sizes["nt"], "vertices": sizes["nv"],
                    "free_dofs": 3 * sizes["nf"], "blocks": sizes["nnzb"],
                    "precision": args.precision, "solver": args.solver,
-                   "pcg_kernel": args.pcg_kernel,
+                   "formulation": args.formulation, "pcg_kernel": args.pcg_kernel,
                    "newton_residual_tolerance": spec.newton_residual_tolerance,
                    "pcg_tolerance": spec.iterative_solver_tolerance,
                    "l2": "working set > L2 (about 1 GB per step)",
