@@ -28,7 +28,7 @@ server rolls it back to the checkpoint, rebuilds it in FP64 from that state
 (mfem_gpu_scene_snapshot / restore) and the FP64 scene takes the failed
 step again.  A scene that fails in FP64 leaves with its status, as the
 reference would stop.  Scenes of one precision share a batch; a tick steps
-both batches.
+both batches concurrently, each on its own stream.
 
 No counterpart in the reference, which steps one scene per process.
 """
@@ -106,6 +106,7 @@ class Server:
         groups = {}            # precision -> (Batch, member rids)
         used = 0
         pool = cf.ThreadPoolExecutor(max_workers=1)
+        stepper = cf.ThreadPoolExecutor(max_workers=2)
         t0 = time.perf_counter()
         now = lambda: time.perf_counter() - t0
 
@@ -140,7 +141,6 @@ class Server:
                 if self.escalate:
                     for k in by_prec.get(abi.PRECISION_MIXED, ()):
                         active[k][1].checkpoint()
-                results, tick_ms = [], 0.0
                 for p in sorted(by_prec):
                     key = tuple(by_prec[p])
                     b, members = groups.get(p, (None, ()))
@@ -149,15 +149,22 @@ class Server:
                             b.close()
                         b = gpu.Batch([active[k][1] for k in key])
                         groups[p] = (b, key)
-                    stats = b.step(raise_on_error=False)
-                    tick_ms += stats[0].device_ms
-                    results += list(zip(key, stats))
+                # the precisions' batches step concurrently, each on its own
+                # stream (the library's calls on distinct batches are
+                # thread-safe and release the interpreter lock)
+                order = sorted(by_prec)
+                futs = [stepper.submit(groups[p][0].step, raise_on_error=False) for p in order]
+                results, tick_ms = [], 0.0
+                for p, f in zip(order, futs):
+                    stats = f.result()
+                    tick_ms = max(tick_ms, stats[0].device_ms)
+                    results += [(k, st, stats[0].device_ms) for k, st in zip(groups[p][1], stats)]
                 self.ticks.append((now(), len(active), tick_ms))
                 finished, escalate = [], []
-                for k, st in results:
+                for k, st, batch_ms in results:
                     r, sc = active[k]
                     r.steps_done += 1
-                    r.step_ms.append(tick_ms)
+                    r.step_ms.append(batch_ms)
                     r.newton.append(st.newton_iterations)
                     r.cg.append(st.cg_iterations)
                     if (self.escalate and sc.spec.precision == abi.PRECISION_MIXED
@@ -197,6 +204,7 @@ class Server:
             for r, sc in active.values():
                 sc.close()
             pool.shutdown(wait=True)
+            stepper.shutdown(wait=True)
         return sorted(self.queue, key=lambda r: r.rid)
 
 
