@@ -715,6 +715,124 @@ template <int N, typename T> MI bool psd_fix_n(T* H, T tol) {
   return true;
 }
 
+// The psd-fixed d2psi/dF2 of a psi = A(|F|^2) + B(det F) material from its
+// eigensystem in closed form (the structure used by Smith, de Goes and Kim,
+// "Stable Neo-Hookean Flesh Simulation", 2018), instead of a 9x9 Jacobi
+// eigen-decomposition.  With the signed SVD F = U diag(s) V^T (U, V
+// rotations), in the basis vec(U E V^T):
+//   twist (u_i v_j^T - u_j v_i^T)/sqrt2:  2 A1 + B1 s_m   (m the third index)
+//   flip  (u_i v_j^T + u_j v_i^T)/sqrt2:  2 A1 - B1 s_m
+//   scaling sum_i z_i u_i v_i^T, z an eigenvector of the 3x3
+//     2 A1 I + 4 A2 s s^T + B2 c c^T + B1 [[0 s2 s1] [s2 0 s0] [s1 s0 0]],
+//     c = (s1 s2, s0 s2, s0 s1)
+// Eigenvalues below tol are raised to tol and H rebuilt from the nine modes.
+// Returns false (H untouched) when the SVD is ill-conditioned (the two
+// largest singular values not well separated from zero); the caller then
+// takes the Jacobi route.
+template <typename T> MI bool fem_hess_projected(int type, T mu, T la, const T* F, T tol, T H[81]) {
+  T C[9], V[9];
+#pragma unroll
+  for (int i = 0; i < 3; ++i)
+#pragma unroll
+    for (int j = 0; j < 3; ++j)
+      C[i + 3 * j] = F[3 * i] * F[3 * j] + F[3 * i + 1] * F[3 * j + 1] + F[3 * i + 2] * F[3 * j + 2];
+  jacobi_eig_n<3>(C, V);
+  // order the eigenpairs by decreasing eigenvalue
+  int o[3] = {0, 1, 2};
+  if (C[4 * o[1]] > C[4 * o[0]]) { const int t = o[0]; o[0] = o[1]; o[1] = t; }
+  if (C[4 * o[2]] > C[4 * o[1]]) { const int t = o[1]; o[1] = o[2]; o[2] = t; }
+  if (C[4 * o[1]] > C[4 * o[0]]) { const int t = o[0]; o[0] = o[1]; o[1] = t; }
+  T Vs[9];
+#pragma unroll
+  for (int k = 0; k < 3; ++k)
+#pragma unroll
+    for (int r = 0; r < 3; ++r) Vs[r + 3 * k] = V[r + 3 * o[k]];
+  const T detV = Vs[0] * (Vs[4] * Vs[8] - Vs[7] * Vs[5]) - Vs[3] * (Vs[1] * Vs[8] - Vs[7] * Vs[2]) +
+                 Vs[6] * (Vs[1] * Vs[5] - Vs[4] * Vs[2]);
+  if (detV < T(0)) {
+#pragma unroll
+    for (int r = 0; r < 3; ++r) Vs[r + 6] = -Vs[r + 6];
+  }
+  T B[9];  // F V
+#pragma unroll
+  for (int k = 0; k < 3; ++k)
+#pragma unroll
+    for (int r = 0; r < 3; ++r) B[r + 3 * k] = F[r] * Vs[3 * k] + F[r + 3] * Vs[3 * k + 1] + F[r + 6] * Vs[3 * k + 2];
+  const T s0 = Prec<T>::sqrt_(B[0] * B[0] + B[1] * B[1] + B[2] * B[2]);
+  if (!(s0 > T(0)) || !isfinite(s0)) return false;
+  T U[9];
+#pragma unroll
+  for (int r = 0; r < 3; ++r) U[r] = B[r] / s0;
+  const T d01 = U[0] * B[3] + U[1] * B[4] + U[2] * B[5];
+  T b1[3] = {B[3] - d01 * U[0], B[4] - d01 * U[1], B[5] - d01 * U[2]};
+  const T s1 = Prec<T>::sqrt_(b1[0] * b1[0] + b1[1] * b1[1] + b1[2] * b1[2]);
+  if (!(s1 > T(Prec<T>::kFP64 ? 1e-10 : 1e-4) * s0)) return false;
+#pragma unroll
+  for (int r = 0; r < 3; ++r) U[3 + r] = b1[r] / s1;
+  U[6] = U[1] * U[5] - U[2] * U[4];
+  U[7] = U[2] * U[3] - U[0] * U[5];
+  U[8] = U[0] * U[4] - U[1] * U[3];
+  const T s2 = U[6] * B[6] + U[7] * B[7] + U[8] * B[8];  // signed: < 0 when inverted
+  const T sg[3] = {s0, s1, s2};
+  T Q = T(0);
+#pragma unroll
+  for (int i = 0; i < 9; ++i) Q += F[i] * F[i];
+  const MatCoef<T> c = material_coef<T>(type, mu, la, Q, s0 * s1 * s2, T(0), false);
+  const T cf[3] = {s1 * s2, s0 * s2, s0 * s1};
+  T M3[9], Z[9];
+#pragma unroll
+  for (int i = 0; i < 3; ++i)
+#pragma unroll
+    for (int j = 0; j < 3; ++j) {
+      T v = T(4) * c.A2 * sg[i] * sg[j] + c.B2 * cf[i] * cf[j];
+      if (i == j) v += T(2) * c.A1;
+      else v += c.B1 * sg[3 - i - j];
+      M3[i + 3 * j] = v;
+    }
+  jacobi_eig_n<3>(M3, Z);
+#pragma unroll
+  for (int i = 0; i < 81; ++i) H[i] = T(0);
+  // scaling modes
+#pragma unroll
+  for (int k = 0; k < 3; ++k) {
+    const T lam = M3[4 * k] < tol ? tol : M3[4 * k];
+    T q[9];
+#pragma unroll
+    for (int cc = 0; cc < 3; ++cc)
+#pragma unroll
+      for (int r = 0; r < 3; ++r)
+        q[r + 3 * cc] = Z[3 * k] * U[r] * Vs[cc] + Z[3 * k + 1] * U[3 + r] * Vs[3 + cc] +
+                        Z[3 * k + 2] * U[6 + r] * Vs[6 + cc];
+#pragma unroll
+    for (int a = 0; a < 9; ++a)
+#pragma unroll
+      for (int b = 0; b < 9; ++b) H[a + 9 * b] += lam * q[a] * q[b];
+  }
+  // twist and flip modes of each pair (i, j), m the third index
+  const T rs2 = T(0.70710678118654752440);
+#pragma unroll
+  for (int p = 0; p < 3; ++p) {
+    const int i = p == 2 ? 1 : 0, j = p == 0 ? 1 : 2, m = 3 - i - j;
+#pragma unroll
+    for (int sgn = 0; sgn < 2; ++sgn) {
+      const T e = sgn == 0 ? T(2) * c.A1 + c.B1 * sg[m] : T(2) * c.A1 - c.B1 * sg[m];
+      const T lam = e < tol ? tol : e;
+      const T pm = sgn == 0 ? T(-1) : T(1);
+      T q[9];
+#pragma unroll
+      for (int cc = 0; cc < 3; ++cc)
+#pragma unroll
+        for (int r = 0; r < 3; ++r)
+          q[r + 3 * cc] = rs2 * (U[3 * i + r] * Vs[3 * j + cc] + pm * U[3 * j + r] * Vs[3 * i + cc]);
+#pragma unroll
+      for (int a = 0; a < 9; ++a)
+#pragma unroll
+        for (int b = 0; b < 9; ++b) H[a + 9 * b] += lam * q[a] * q[b];
+    }
+  }
+  return true;
+}
+
 // Element force of the mixed residual, in the precision of T:
 //   f_a = -vol * P dphi_a,  P = sum_i q_i ds_i/dF = R (Q - [w]x),
 // Q = sum_i q_i E_i (symmetric), w = W sum_i q_i c_i (the u_i of

@@ -403,6 +403,8 @@ __global__ void __launch_bounds__(kElemTile)
 // for Neohookean, neohookean.cpp:230) and the forces -h^2 vol Jloc^T dpsi/dF,
 // in the record layout of the mixed K1 so that the assembly, the solvers and
 // the line search are shared.  Forces in Ext, as in the mixed residual chain.
+// The psd fix takes the closed-form eigensystem (fem_hess_projected), and
+// the 9x9 Jacobi only when the SVD of F is ill-conditioned.
 template <typename Real, bool DBG>
 __global__ void __launch_bounds__(kElemTile)
     k_elem_fem(const Tile* tiles, const SceneDev* sds, ElemDebug dbg) {
@@ -439,9 +441,13 @@ __global__ void __launch_bounds__(kElemTile)
           put_word(out, kRhsWord + 2 * (3 * a + r), f);
         }
     }
-    Real g[9], H[81];
-    fem_grad_hess<Real>(in.mat, in.mu, in.lam, F, g, H);
-    psd_fix_n<9>(H, in.mat == kSNH ? Real(0) : Real(kPsdTol));
+    Real H[81];
+    const Real tol = in.mat == kSNH ? Real(0) : Real(kPsdTol);
+    if (!fem_hess_projected<Real>(in.mat, in.mu, in.lam, F, tol, H)) {
+      Real g[9];
+      fem_grad_hess<Real>(in.mat, in.mu, in.lam, F, g, H);
+      psd_fix_n<9>(H, tol);
+    }
     const Real w = h2 * in.vol;
 #pragma unroll
     for (int b = 0; b < 4; ++b) {
