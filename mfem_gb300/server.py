@@ -208,6 +208,21 @@ class Server:
         return sorted(self.queue, key=lambda r: r.rid)
 
 
+def shard(weights, world_size, rank):
+    """Indices of the requests rank `rank` serves when world_size GPUs share a
+    stream: requests are independent, so they are dealt out with no exchange,
+    greedily by decreasing weight (a scene's footprint, or its tets x steps)
+    to the least-loaded rank, ties to the lower index and rank."""
+    load = [0.0] * world_size
+    mine = []
+    for i in sorted(range(len(weights)), key=lambda i: (-float(weights[i]), i)):
+        r = min(range(world_size), key=lambda k: (load[k], k))
+        load[r] += float(weights[i])
+        if r == rank:
+            mine.append(i)
+    return sorted(mine)
+
+
 def summary(requests, ticks, wall_s):
     """Aggregate timesteps/s and per-timestep latency percentiles."""
     steps = sum(r.steps_done for r in requests)
