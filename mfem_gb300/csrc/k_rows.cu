@@ -153,6 +153,7 @@ __device__ __forceinline__ void xe_store(void* base, int row, const X3& x) {
 }
 
 constexpr int kAsmWindow = 64;  // block slots per warp accumulated in shared memory per pass
+constexpr int kAsmUnroll = 4;   // incidences whose record entries are in flight together
 
 template <typename Real>
 __global__ void __launch_bounds__(256) k_assemble(const Tile* tiles, const SceneDev* sds,
@@ -226,21 +227,46 @@ __global__ void __launch_bounds__(256) k_assemble(const Tile* tiles, const Scene
       const int wn = min(kAsmWindow, nb - w0);
       for (int o = lane; o < 9 * wn; o += 32) acc_w[o] = Real(0);
       __syncwarp();
-      for (int k = ib; k < ie; ++k) {
-        const int2 ic = sd.inc[k];
-        const int i = ic.y & 3;
-        const Real* rp = reinterpret_cast<const Real*>(sd.rec + (size_t)ic.x * rec_bytes(RB));
+      // kAsmUnroll incidences per round: their record entries are loaded
+      // first (independent gathers in flight together), then added in
+      // incidence order with the warp synchronised between incidences, so
+      // every entry still sums its contributions in element order.
+      for (int k0 = ib; k0 < ie; k0 += kAsmUnroll) {
+        Real av[kAsmUnroll][2];
+        int sv[kAsmUnroll][2];
 #pragma unroll
-        for (int pass = 0; pass < 2; ++pass) {
-          const int l = lane + 32 * pass;
-          if (l < 36) {
-            const int j = l / 9, ent = l - 9 * j;
-            const int slot = (ic.y >> (2 + 7 * j)) & 127;
-            const int sl = slot - w0;
-            if (slot != 127 && sl >= 0 && sl < wn) acc_w[9 * sl + ent] += rp[offtab[i][j][ent]];
+        for (int u = 0; u < kAsmUnroll; ++u) {
+#pragma unroll
+          for (int pass = 0; pass < 2; ++pass) {
+            sv[u][pass] = -1;
+            av[u][pass] = Real(0);
+          }
+          if (k0 + u < ie) {
+            const int2 ic = sd.inc[k0 + u];
+            const int i = ic.y & 3;
+            const Real* rp = reinterpret_cast<const Real*>(sd.rec + (size_t)ic.x * rec_bytes(RB));
+#pragma unroll
+            for (int pass = 0; pass < 2; ++pass) {
+              const int l = lane + 32 * pass;
+              if (l < 36) {
+                const int j = l / 9, ent = l - 9 * j;
+                const int slot = (ic.y >> (2 + 7 * j)) & 127;
+                const int sl = slot - w0;
+                if (slot != 127 && sl >= 0 && sl < wn) {
+                  sv[u][pass] = 9 * sl + ent;
+                  av[u][pass] = rp[offtab[i][j][ent]];
+                }
+              }
+            }
           }
         }
-        __syncwarp();
+#pragma unroll
+        for (int u = 0; u < kAsmUnroll; ++u) {
+#pragma unroll
+          for (int pass = 0; pass < 2; ++pass)
+            if (sv[u][pass] >= 0) acc_w[sv[u][pass]] += av[u][pass];
+          __syncwarp();
+        }
       }
       for (int o = lane; o < 9 * wn; o += 32) {
         const int q = o / 9, ent = o - 9 * q;
