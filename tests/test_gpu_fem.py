@@ -77,3 +77,26 @@ def test_fem_refusals(gpu_lib):
         gpu.Batch([a, b])
     a.close()
     b.close()
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("bc", [abi.BC_STRETCH, abi.BC_TWIST])
+def test_fem_boundary_scripts_match_oracle(gpu_lib, bc):
+    import oracle
+    from mfem_gb300 import gpu
+    from mfem_gb300.desc import SceneSpec
+    from mfem_gb300.meshgen import cube_grid, enu_to_lame
+    V, T = cube_grid(6, 2, 2, 0.1)
+    lam, mu = enu_to_lame(1e5, 0.4)
+    sp = SceneSpec(V_rest=V, tets=T, mu=np.full(len(T), mu), lam=np.full(len(T), lam),
+                   bc_type=bc, bc_axis=0, bc_ratio=0.05, bc_velocity=0.2, dt=1 / 60,
+                   max_newton_iterations=30, iterative_solver_tolerance=1e-10,
+                   max_iterative_solver_iters=2000, newton_residual_tolerance=1e-9,
+                   precision=abi.PRECISION_FP64, formulation=abi.FORMULATION_STRETCH)
+    o, g = oracle.OracleScene(sp), gpu.Scene(sp)
+    for _ in range(4):
+        o.step()
+        g.step()
+    xo = o.get_state()["x"]
+    assert np.abs(g.get_state()["x"] - xo).max() <= 1e-6 * bbox_diag(xo)
+    g.close()

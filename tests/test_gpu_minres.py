@@ -87,3 +87,20 @@ def test_batch_rejects_mixed_solvers(gpu_lib):
         gpu.Batch([a, b])
     a.close()
     b.close()
+
+
+@pytest.mark.gpu
+def test_minres_neohookean_bdf2_matches_oracle(gpu_lib):
+    import oracle
+    from mfem_gb300 import gpu
+    sp = _spec(abi.SOLVER_MINRES_ID, 1e-10, 8000, abi.PRECISION_FP64, E=5e5)
+    sp.material = np.full(sp.n_tets, abi.MATERIAL_NH, dtype=np.int32)
+    sp.bdf_order = 2
+    o = oracle.OracleScene(sp)
+    g = gpu.Scene(sp)
+    for _ in range(3):
+        so, sg = o.step(), g.step()
+        assert sg.status == abi.OK and so.newton_iterations == sg.newton_iterations
+    xo = o.get_state()["x"]
+    assert np.abs(g.get_state()["x"] - xo).max() <= 1e-7 * np.abs(xo - sp.V_rest).max()
+    g.close()

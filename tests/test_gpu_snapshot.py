@@ -72,3 +72,31 @@ def test_snapshot_crosses_precision(gpu_lib):
         other.restore(m.snapshot())
     for s in (m, d, other):
         s.close()
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("bc", [abi.BC_TWIST, abi.BC_STRETCH])
+def test_resume_continues_the_boundary_script(gpu_lib, bc):
+    """The scripted pins move every step; their positions travel in the
+    snapshot, so a resumed scene keeps following the script bitwise."""
+    from mfem_gb300 import gpu
+    V, T = cube_grid(6, 2, 2, 0.1)
+    lam, mu = enu_to_lame(1e5, 0.4)
+    spec = SceneSpec(V_rest=V, tets=T, mu=np.full(len(T), mu), lam=np.full(len(T), lam),
+                     bc_type=bc, bc_axis=0, bc_ratio=0.05, bc_velocity=0.2, dt=1 / 60, bdf_order=2,
+                     max_newton_iterations=10, iterative_solver_tolerance=1e-8,
+                     precision=abi.PRECISION_MIXED, pcg_kernel=abi.PCG_KERNEL_FUSED)
+    a = gpu.Scene(spec)
+    for _ in range(3):
+        a.step()
+    snap = a.snapshot()
+    for _ in range(3):
+        a.step()
+    b = gpu.Scene(spec)
+    b.restore(snap)
+    for _ in range(3):
+        b.step()
+    assert np.array_equal(a.get_state()["x"], b.get_state()["x"])
+    assert np.abs(a.get_state()["x"] - V).max() > 1e-3       # the pins moved
+    a.close()
+    b.close()
