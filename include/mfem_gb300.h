@@ -156,6 +156,12 @@ int mfem_gpu_abi_version(void);
 int mfem_gpu_set_device(int device);
 /* Writes the device name and SM count; fails with MFEM_ERR_NO_DEVICE. */
 int mfem_gpu_device_info(char* name, int name_len, int* sm_count);
+/* Failure-detection self-test of the bounded device wait the persistent PCG
+ * uses between its phases: a two-block cooperative launch whose grid
+ * barrier misses one arrival.  The wait runs out after its limit (2 s),
+ * the kernel returns, and the call reports MFEM_ERR_TIMEOUT (the status a
+ * step returns in that case) with the time waited; the context stays usable. */
+int mfem_gpu_selftest_bounded_wait(double* waited_ms);
 const char* mfem_gpu_status_string(int status);
 
 /* ---- scenes ---------------------------------------------------------------

@@ -23,6 +23,7 @@ SIGNATURES = {
     "mfem_gpu_abi_version": (C.c_int, []),
     "mfem_gpu_set_device": (C.c_int, [C.c_int]),
     "mfem_gpu_device_info": (C.c_int, [C.c_char_p, C.c_int, _ip]),
+    "mfem_gpu_selftest_bounded_wait": (C.c_int, [_dp]),
     "mfem_gpu_status_string": (C.c_char_p, [C.c_int]),
     "mfem_gpu_scene_create": (C.c_int, [_vp, C.POINTER(_vp)]),
     "mfem_gpu_scene_destroy": (C.c_int, [_vp]),

@@ -1353,6 +1353,38 @@ const char* mfem_gpu_status_string(int status) {
   }
 }
 
+int mfem_gpu_selftest_bounded_wait(double* waited_ms) {
+  int n = 0;
+  if (cudaGetDeviceCount(&n) != cudaSuccess || n == 0) return MFEM_ERR_NO_DEVICE;
+  BatchCounters* d = nullptr;
+  CUDA_OR(cudaMalloc(&d, sizeof(BatchCounters)), MFEM_ERR_OOM);
+  cudaStream_t st = nullptr;
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  BatchCounters h{};
+  int rc = MFEM_OK;
+  float ms = 0.f;
+  if (cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking) != cudaSuccess || cudaEventCreate(&e0) != cudaSuccess ||
+      cudaEventCreate(&e1) != cudaSuccess || cudaMemsetAsync(d, 0, sizeof(BatchCounters), st) != cudaSuccess ||
+      cudaEventRecord(e0, st) != cudaSuccess || launch_barrier_selftest(d, st) != cudaSuccess ||
+      cudaEventRecord(e1, st) != cudaSuccess ||
+      cudaMemcpyAsync(&h, d, sizeof(h), cudaMemcpyDeviceToHost, st) != cudaSuccess ||
+      cudaStreamSynchronize(st) != cudaSuccess || cudaEventElapsedTime(&ms, e0, e1) != cudaSuccess) {
+    rc = MFEM_ERR_CUDA;
+  } else {
+    // the wait ran out as designed: the persistent PCG reports this status
+    rc = h.error ? MFEM_ERR_TIMEOUT : MFEM_OK;
+    // and the context stays usable
+    if (cudaMemsetAsync(d, 0, sizeof(BatchCounters), st) != cudaSuccess || cudaStreamSynchronize(st) != cudaSuccess)
+      rc = MFEM_ERR_CUDA;
+  }
+  if (waited_ms) *waited_ms = ms;
+  if (e0) cudaEventDestroy(e0);
+  if (e1) cudaEventDestroy(e1);
+  if (st) cudaStreamDestroy(st);
+  cudaFree(d);
+  return rc;
+}
+
 int mfem_gpu_device_info(char* name, int name_len, int* sm_count) {
   int n = 0;
   if (cudaGetDeviceCount(&n) != cudaSuccess || n == 0) return MFEM_ERR_NO_DEVICE;

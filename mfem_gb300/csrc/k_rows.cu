@@ -1029,6 +1029,19 @@ void launch_cg_replace(const Launch& L) {
 void launch_cgf_init(const Launch& L) { MFEM_LAUNCH_ROWS(k_cgf_init, kCgThreads); }
 void launch_cgf_iter(const Launch& L) { MFEM_LAUNCH_ROWS(k_cgf_iter, kCgThreads); }
 
+// Failure-detection check of the bounded grid barrier: a cooperative launch
+// of two blocks in which block 1 leaves without arriving (a lost peer), so
+// block 0's wait must run out, raise ctrs->error and return.
+__global__ void k_barrier_selftest(BatchCounters* ctrs) {
+  if (blockIdx.x == 1) return;
+  grid_barrier(ctrs);
+}
+
+cudaError_t launch_barrier_selftest(BatchCounters* ctrs, cudaStream_t st) {
+  void* args[] = {&ctrs};
+  return cudaLaunchCooperativeKernel((const void*)k_barrier_selftest, dim3(2), dim3(32), args, 0, st);
+}
+
 int cg_solve_blocks_per_sm(int fp64) {
   int nb = 0;
   cudaError_t e = fp64 ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_cg_solve<double>, kCgThreads, 0)

@@ -256,6 +256,8 @@ void launch_cg_replace(const Launch& L);  // r = b - A x in df64 (mixed path)
 void launch_cgf_init(const Launch& L);
 void launch_cgf_iter(const Launch& L);
 int cg_solve_blocks_per_sm(int fp64);
+// Two-block cooperative launch whose grid barrier has a missing arrival.
+cudaError_t launch_barrier_selftest(BatchCounters* ctrs, cudaStream_t st);
 // MINRES on the (x, s, lambda) system (k_minres.cu, all TB_EV)
 void launch_mr_init(const Launch& L);    // rhs, preconditioner blocks, v1, w1
 void launch_mr_elem(const Launch& L);    // A1: pending update, element rows of K w

@@ -70,3 +70,17 @@ def test_no_device_fails_loudly_without_gpu(gpu_lib):
     h = C.c_void_p()
     rc = gpu_lib.mfem_gpu_scene_create(C.addressof(d.struct), C.byref(h))
     assert rc == abi.ERR_NO_DEVICE
+
+
+@pytest.mark.gpu
+def test_bounded_wait_runs_out_and_the_context_stays_usable(gpu_lib):
+    """A grid barrier that misses an arrival (a lost peer block) ends after
+    its limit with MFEM_ERR_TIMEOUT instead of hanging; scenes still run."""
+    from mfem_gb300 import configs, gpu
+    ms = C.c_double(0.0)
+    rc = gpu_lib.mfem_gpu_selftest_bounded_wait(C.byref(ms))
+    assert rc == abi.ERR_TIMEOUT
+    assert 500.0 < ms.value < 10000.0
+    s = gpu.Scene(configs.beam_c1())
+    assert s.step().status in (abi.OK, abi.ERR_LS_FAILED)
+    s.close()
