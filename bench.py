@@ -66,7 +66,8 @@ def parse():
                     help="skip the batched-vs-plain measurement on the 64-scene mix")
     ap.add_argument("--batch-steps", type=int, default=3)
     ap.add_argument("--cpu-threads", type=int, default=0)
-    ap.add_argument("--pcg-kernel", default="fused", choices=["persistent", "split", "fused"])
+    ap.add_argument("--pcg-kernel", default="auto", choices=["persistent", "split", "fused", "auto"],
+                    help="auto: the batch picks fused or split by its PCG tile count")
     return ap.parse_args()
 
 
@@ -245,7 +246,7 @@ def make_spec(args, precision):
     solver = {"eigen-pcg-diag": abi.SOLVER_EIGEN_CG_DIAG, "gpu-pcg-block": abi.SOLVER_GPU_PCG_BLOCK,
               "minres-indefinite-block": abi.SOLVER_MINRES_ID}[args.solver]
     kern = {"persistent": abi.PCG_KERNEL_PERSISTENT, "split": abi.PCG_KERNEL_SPLIT,
-            "fused": abi.PCG_KERNEL_FUSED}[args.pcg_kernel]
+            "fused": abi.PCG_KERNEL_FUSED, "auto": abi.PCG_KERNEL_AUTO}[args.pcg_kernel]
     form = abi.FORMULATION_STRETCH if args.formulation == "stretch" else abi.FORMULATION_MIXED_STRETCH
     kw = dict(precision=prec, linear_solver=solver, pcg_kernel=kern, formulation=form)
     tag = ("_minres" if args.solver == "minres-indefinite-block" else "") + \
@@ -472,6 +473,9 @@ def run_ours(args):
                    "free_dofs": 3 * sizes["nf"], "blocks": sizes["nnzb"],
                    "precision": args.precision, "solver": args.solver,
                    "formulation": args.formulation, "pcg_kernel": args.pcg_kernel,
+                   "pcg_kernel_resolved": ("fused" if kstats.get("k_cgf_iter", (0, 0))[1] else
+                                           "split" if kstats.get("k_cg_spmv", (0, 0))[1] else
+                                           "persistent" if kstats.get("k_cg_solve", (0, 0))[1] else None),
                    "newton_residual_tolerance": spec.newton_residual_tolerance,
                    "pcg_tolerance": spec.iterative_solver_tolerance,
                    "l2": "working set > L2 (about 1 GB per step)",
@@ -506,7 +510,7 @@ def run_batch_mix(args, gpu, abi, configs):
     other.  Both from rest after the same warm-up; timesteps/s counts
     scene-steps; device time from CUDA events around each step."""
     kern = {"persistent": abi.PCG_KERNEL_PERSISTENT, "split": abi.PCG_KERNEL_SPLIT,
-            "fused": abi.PCG_KERNEL_FUSED}[args.pcg_kernel]
+            "fused": abi.PCG_KERNEL_FUSED, "auto": abi.PCG_KERNEL_AUTO}[args.pcg_kernel]
     specs = configs.batch_c4(pcg_kernel=kern)
     n = len(specs)
     tets = int(sum(s.n_tets for s in specs))
@@ -556,7 +560,7 @@ def run_served(args):
         build()
     barrier(pg)
     kern = {"persistent": abi.PCG_KERNEL_PERSISTENT, "split": abi.PCG_KERNEL_SPLIT,
-            "fused": abi.PCG_KERNEL_FUSED}[args.pcg_kernel]
+            "fused": abi.PCG_KERNEL_FUSED, "auto": abi.PCG_KERNEL_AUTO}[args.pcg_kernel]
     stream = configs.stream_c5(duration=args.c5_duration, steps=args.c5_steps)
     for _, sp, _ in stream:
         sp.pcg_kernel = kern

@@ -61,6 +61,7 @@ PRECISION_MIXED = 1
 PCG_KERNEL_PERSISTENT = 0
 PCG_KERNEL_SPLIT = 1
 PCG_KERNEL_FUSED = 2
+PCG_KERNEL_AUTO = 3
 
 _dp = C.POINTER(C.c_double)
 _ip = C.POINTER(C.c_int32)

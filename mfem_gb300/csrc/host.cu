@@ -613,7 +613,7 @@ void layout_scene(mfem_scene* s, Arena& A) {
   D.cg_p[0] = A.take_bytes(n4 * r);
   D.cg_p[1] = A.take_bytes(n4 * r);
   D.cg_Ap = A.take_bytes(n4 * r);
-  if (s->cfg.pcg_kernel == MFEM_PCG_KERNEL_FUSED) {
+  if (s->cfg.pcg_kernel == MFEM_PCG_KERNEL_FUSED || s->cfg.pcg_kernel == MFEM_PCG_KERNEL_AUTO) {
     for (int k = 0; k < 2; ++k) {
       D.cgf_r[k] = A.take_bytes(n4 * r);
       D.cgf_w[k] = A.take_bytes(n4 * r);
@@ -1069,10 +1069,16 @@ int batch_build(mfem_scene* const* scenes, int n, mfem_batch** out) {
     if (scenes[i]->cfg.pcg_kernel != b->pcg_kernel || scenes[i]->dev.minres != b->minres ||
         scenes[i]->dev.fem != b->fem)
       return MFEM_ERR_INVALID;
-  if (b->pcg_kernel == MFEM_PCG_KERNEL_PERSISTENT) {
-    int dev = 0, sms = 0;
+  int sms = 0;
+  {
+    int dev = 0;
     CUDA_OR(cudaGetDevice(&dev), MFEM_ERR_CUDA);
     CUDA_OR(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev), MFEM_ERR_CUDA);
+  }
+  if (b->pcg_kernel == MFEM_PCG_KERNEL_AUTO)
+    b->pcg_kernel = (b->ntiles[TB_CG] >= 2 * sms || b->ntiles[TB_CG] <= 4) ? MFEM_PCG_KERNEL_FUSED
+                                                                          : MFEM_PCG_KERNEL_SPLIT;
+  if (b->pcg_kernel == MFEM_PCG_KERNEL_PERSISTENT) {
     const int per_sm = cg_solve_blocks_per_sm(b->fp64);
     if (per_sm <= 0) return MFEM_ERR_CUDA;
     b->coop_grid = std::min(b->ntiles[TB_CG], per_sm * sms);
@@ -1414,7 +1420,7 @@ static int scene_prepare(const mfem_scene_desc* desc, std::unique_ptr<mfem_scene
       desc->max_iterative_solver_iters < 0)
     return MFEM_ERR_INVALID;
   if (desc->pcg_kernel != MFEM_PCG_KERNEL_PERSISTENT && desc->pcg_kernel != MFEM_PCG_KERNEL_SPLIT &&
-      desc->pcg_kernel != MFEM_PCG_KERNEL_FUSED)
+      desc->pcg_kernel != MFEM_PCG_KERNEL_FUSED && desc->pcg_kernel != MFEM_PCG_KERNEL_AUTO)
     return MFEM_ERR_INVALID;
   if (desc->formulation != MFEM_FORMULATION_MIXED_STRETCH && desc->formulation != MFEM_FORMULATION_STRETCH)
     return MFEM_ERR_INVALID;

@@ -304,3 +304,30 @@ def test_fused_pcg_matches_two_reduction_pcg(gpu_lib, prec):
         # one every few iterations (the single-reduction form does not), so
         # their PCG counts differ on an ill-conditioned beam
         assert abs(na - nb) <= 0.25 * na + 2
+
+
+@pytest.mark.gpu
+def test_auto_pcg_form_by_tile_count(gpu_lib):
+    """AUTO runs the fused form for a one-tile beam and the split form for a
+    mid-size cube, bitwise like choosing that form directly."""
+    from mfem_gb300 import gpu
+
+    def run(spec):
+        s = gpu.Scene(spec)
+        b = s.solo_batch_handle()
+        gpu.set_profiling(b, True)
+        for _ in range(2):
+            s.step()
+        ks = gpu.kernel_stats(b)
+        x = s.get_state()["x"]
+        s.close()
+        return x, ks["k_cgf_iter"][1], ks["k_cg_spmv"][1]
+
+    beam = lambda k: configs.beam_c1(precision=abi.PRECISION_MIXED, pcg_kernel=k)
+    xa, fa, sa = run(beam(abi.PCG_KERNEL_AUTO))
+    xf, _, _ = run(beam(abi.PCG_KERNEL_FUSED))
+    assert fa > 0 and sa == 0 and np.array_equal(xa, xf)
+    cube = lambda k: configs.cube_c2(n=20, pcg_kernel=k)   # 40,000 tets: 36 PCG tiles
+    xa, fa, sa = run(cube(abi.PCG_KERNEL_AUTO))
+    xs, _, _ = run(cube(abi.PCG_KERNEL_SPLIT))
+    assert fa == 0 and sa > 0 and np.array_equal(xa, xs)
