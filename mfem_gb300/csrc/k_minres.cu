@@ -324,29 +324,43 @@ __global__ void __launch_bounds__(kElemTile) k_mr_elem(const Tile* tiles, const 
         V[j] = v;
         W[j] = w[i];
       }
-      const double vol = double(static_cast<const Real*>(sd.vol)[e]);
-      double H[36];
-      load_sym21<Real>(sd.mr_H, ntp, e, H);
+      // The element products run in the element data's precision (FP32 in
+      // the mixed path: GB300's FP64 rate is 1/64 of FP32's, and these are
+      // most of the iteration's arithmetic); the Lanczos vectors and the
+      // inner products stay FP64.
+      const Real vol = static_cast<const Real*>(sd.vol)[e];
+      const Real* Hp = static_cast<const Real*>(sd.mr_H);
+      Real H[36];
+#pragma unroll
+      for (int i = 0; i < 6; ++i)
+#pragma unroll
+        for (int j = i; j < 6; ++j) {
+          const Real v = Hp[(size_t)sym6(i, j) * ntp + e];
+          H[i + 6 * j] = v;
+          H[j + 6 * i] = v;
+        }
       const Real* Bp = static_cast<const Real*>(sd.mr_B);
       const int4 tv = sd.tets[e];
       const int v4[4] = {tv.x, tv.y, tv.z, tv.w};
-      double wx[12];
+      Real wx[12], wr[12];
 #pragma unroll
       for (int a = 0; a < 4; ++a) {
         const int f = sd.free_map[v4[a]];
 #pragma unroll
-        for (int l = 0; l < 3; ++l) wx[3 * a + l] = f >= 0 ? WN[4 * (size_t)f + l] * ib : 0.0;
+        for (int l = 0; l < 3; ++l) wx[3 * a + l] = f >= 0 ? Real(WN[4 * (size_t)f + l] * ib) : Real(0);
       }
+#pragma unroll
+      for (int i = 0; i < 12; ++i) wr[i] = Real(w[i]);
       double tkw[12];
 #pragma unroll
       for (int i = 0; i < 6; ++i) {
-        double hs = 0.0, bw = 0.0;
+        Real hs = Real(0), bw = Real(0);
 #pragma unroll
-        for (int j = 0; j < 6; ++j) hs += H[i + 6 * j] * w[j];
+        for (int j = 0; j < 6; ++j) hs += H[i + 6 * j] * wr[j];
 #pragma unroll
-        for (int q = 0; q < 12; ++q) bw += double(Bp[(size_t)(12 * i + q) * ntp + e]) * wx[q];
-        tkw[i] = vol * hs + vol * symv(i) * w[6 + i];
-        tkw[6 + i] = -vol * symv(i) * bw + vol * symv(i) * w[i];
+        for (int q = 0; q < 12; ++q) bw += Bp[(size_t)(12 * i + q) * ntp + e] * wx[q];
+        tkw[i] = double(vol * hs + vol * Real(symv(i)) * wr[6 + i]);
+        tkw[6 + i] = double(-vol * Real(symv(i)) * bw + vol * Real(symv(i)) * wr[i]);
       }
 #pragma unroll
       for (int i = 0; i < 12; ++i) {
@@ -357,10 +371,10 @@ __global__ void __launch_bounds__(kElemTile) k_mr_elem(const Tile* tiles, const 
       // x-row shares of this element: -vol B_a^T Sym w_lambda
 #pragma unroll
       for (int q = 0; q < 12; ++q) {
-        double acc = 0.0;
+        Real acc = Real(0);
 #pragma unroll
-        for (int i = 0; i < 6; ++i) acc += double(Bp[(size_t)(12 * i + q) * ntp + e]) * symv(i) * w[6 + i];
-        sd.mr_y[(size_t)q * ntp + e] = -vol * acc;
+        for (int i = 0; i < 6; ++i) acc += Bp[(size_t)(12 * i + q) * ntp + e] * Real(symv(i)) * wr[6 + i];
+        sd.mr_y[(size_t)q * ntp + e] = double(-vol * acc);
       }
     }
   }
