@@ -1442,6 +1442,18 @@ Scene* create(const mfem_scene_desc* d, int* status) {
     *status = MFEM_ERR_INVALID;
     return nullptr;
   }
+  if (d->formulation == MFEM_FORMULATION_STRETCH) {
+    // Stretch has no MINRES form, and only SNH and NH define the 9-vector
+    // energy (MaterialModel's default prints "unimplemented")
+    bool ok = d->linear_solver != MFEM_SOLVER_MINRES_ID;
+    if (d->material)
+      for (int e = 0; e < d->n_tets && ok; ++e)
+        ok = d->material[e] == MFEM_MATERIAL_SNH || d->material[e] == MFEM_MATERIAL_NH;
+    if (!ok) {
+      *status = MFEM_ERR_UNSUPPORTED;
+      return nullptr;
+    }
+  }
   auto sc = std::make_unique<Scene>();
   sc->nv = d->n_vertices;
   sc->nt = d->n_tets;

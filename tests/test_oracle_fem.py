@@ -97,3 +97,14 @@ def test_fem_steps_converge_and_sag():
         st = sc.step()
         assert st.status == abi.OK
     assert sc.get_state()["x"][:, 1].min() < y0
+
+
+def test_fem_refusals_in_the_oracle():
+    import oracle
+    s = _fem_spec(linear_solver=abi.SOLVER_MINRES_ID)
+    with pytest.raises(RuntimeError):
+        oracle.OracleScene(s)
+    s = _fem_spec()
+    s.material = np.full(s.n_tets, abi.MATERIAL_ARAP, dtype=np.int32)
+    with pytest.raises(RuntimeError):
+        oracle.OracleScene(s)
