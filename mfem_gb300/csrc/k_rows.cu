@@ -779,17 +779,12 @@ __device__ __forceinline__ void cgf_tile(int tix, const Tile* tiles, const Scene
     const int soff = sd.slice_off[slice], slen = (sd.slice_off[slice + 1] - soff) >> 5;
     const unsigned long long pol_s = l2_evict_first(), pol_k = l2_evict_last();
     Real acc0 = 0, acc1 = 0, acc2 = 0;
-    // The word carrying block k+1's column is requested one block ahead: a
-    // warp issues in order, and block k's gathers wait on block k's column,
-    // so without it the next block's stream was not requested until then.
-    auto n0 = slen > 0 ? ld_stream(ell, ell_pair(soff, 0, rs, 0), pol_s) : decltype(ld_stream(ell, 0, pol_s)){};
 #pragma unroll 2
     for (int k = 0; k < slen; ++k) {
       const size_t q = ell_pair(soff, k, rs, 0);
-      const auto w0 = n0;
-      const auto w1 = ld_stream(ell, q + 32, pol_s), w2 = ld_stream(ell, q + 64, pol_s),
-                 w3 = ld_stream(ell, q + 96, pol_s), w4 = ld_stream(ell, q + 128, pol_s);
-      if (k + 1 < slen) n0 = ld_stream(ell, q + 160, pol_s);
+      const auto w0 = ld_stream(ell, q, pol_s), w1 = ld_stream(ell, q + 32, pol_s),
+                 w2 = ld_stream(ell, q + 64, pol_s), w3 = ld_stream(ell, q + 96, pol_s),
+                 w4 = ld_stream(ell, q + 128, pol_s);
       const int col = pair_col(w0);
       const size_t c4 = 4 * (size_t)col;
       Real uc[3];
