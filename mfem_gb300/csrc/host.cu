@@ -502,6 +502,7 @@ struct mfem_batch {
   int pcg_kernel = MFEM_PCG_KERNEL_PERSISTENT;
   int minres = 0;  // every scene uses "minres-indefinite-block"
   int fem = 0;     // every scene uses the standard-FEM variable
+  int jacobi = 1;  // no scene uses the 3x3 block-Jacobi preconditioner
   int coop_grid = 0;  // blocks of the persistent PCG (all co-resident)
   int pstride = 0;  // tiles per partials quantity
   // instrumentation
@@ -563,6 +564,7 @@ Launch make_launch(mfem_batch* b, int table) {
   L.counters = b->d_ctr;
   L.fp64 = b->fp64;
   L.fem = b->fem;
+  L.jacobi = b->jacobi;
   return L;
 }
 
@@ -1065,6 +1067,9 @@ int batch_build(mfem_scene* const* scenes, int n, mfem_batch** out) {
   b->pcg_kernel = scenes[0]->cfg.pcg_kernel;
   b->minres = scenes[0]->dev.minres;
   b->fem = scenes[0]->dev.fem;
+  b->jacobi = 1;
+  for (int i = 0; i < n; ++i)
+    if (scenes[i]->dev.block_jacobi) b->jacobi = 0;
   for (int i = 1; i < n; ++i)
     if (scenes[i]->cfg.pcg_kernel != b->pcg_kernel || scenes[i]->dev.minres != b->minres ||
         scenes[i]->dev.fem != b->fem)

@@ -720,7 +720,13 @@ __device__ __forceinline__ void cgf_next(const SceneDev& sd, int row, const Real
 // One launch of the single-reduction PCG (init: r0 = b, x = 0, p = 0,
 // s_{-1} = 0, u0 = M^{-1} b, w0 = A u0).  The scene's last tile reduces the
 // three inner products and sets a, b of the next iteration.
-template <typename Real, bool kInit>
+//
+// kScaled (Jacobi preconditioner, M = diag(A)): r, w and s are kept scaled
+// by M^{-1} (r~ = M^{-1} r, ...).  The recurrences are linear, so
+// s~ = w~ + b s~_prev and u = r~ - a s~: a neighbour's u needs three
+// gathers and no preconditioner gather, and u is r~ itself (no u vector).
+// The own row unscales r = r~ / M^{-1} for the inner products.
+template <typename Real, bool kInit, bool kScaled>
 __device__ __forceinline__ void cgf_tile(int tix, const Tile* tiles, const SceneDev* sds,
                                          double* partials, int pstride, BatchCounters* ctrs) {
   const Tile t = tiles[tix];
@@ -746,7 +752,8 @@ __device__ __forceinline__ void cgf_tile(int tix, const Tile* tiles, const Scene
   const int row = t.begin + threadIdx.x;
   if (row < t.end) {
     const size_t k4 = 4 * (size_t)row;
-    Real un[3], rn[3];
+    Real un[3], rn[3], dv[3];
+    if (kScaled) ld3<false>(static_cast<const Real*>(sd.dinv) + k4, dv);
     if (kInit) {
       ld3<false>(r_old + k4, rn);
       apply_prec<Real>(sd, row, rn, un);
@@ -759,8 +766,18 @@ __device__ __forceinline__ void cgf_tile(int tix, const Tile* tiles, const Scene
       ld3<false>(r_old + k4, rv);
       ld3<false>(w_old + k4, wv);
       ld3<false>(s_old + k4, sp);
-      cgf_next<Real>(sd, row, rv, wv, sp, a, b, sv, rn, un);
-      ld3<false>(u + k4, uv);
+      if (kScaled) {
+#pragma unroll
+        for (int c = 0; c < 3; ++c) {
+          sv[c] = fma(b, sp[c], wv[c]);
+          un[c] = fma(-a, sv[c], rv[c]);
+          rn[c] = un[c] / dv[c];
+          uv[c] = rv[c];  // u_i = r~_i
+        }
+      } else {
+        cgf_next<Real>(sd, row, rv, wv, sp, a, b, sv, rn, un);
+        ld3<false>(u + k4, uv);
+      }
       ld3<false>(p + k4, pv);
       ld3<false>(x + k4, xv);
 #pragma unroll
@@ -772,8 +789,12 @@ __device__ __forceinline__ void cgf_tile(int tix, const Tile* tiles, const Scene
       st3(x + k4, xv);
       st3(s_new + k4, sv);
     }
-    st3(r_new + k4, rn);
-    st3(u + k4, un);
+    if (kScaled) {
+      st3(r_new + k4, un);
+    } else {
+      st3(r_new + k4, rn);
+      st3(u + k4, un);
+    }
     // w_{i+1} = A u_{i+1}
     const int slice = row >> 5, rs = row & 31;
     const int soff = sd.slice_off[slice], slen = (sd.slice_off[slice + 1] - soff) >> 5;
@@ -797,14 +818,26 @@ __device__ __forceinline__ void cgf_tile(int tix, const Tile* tiles, const Scene
         ld3_keep(r_old + c4, rc, pol_k);
         ld3_keep(w_old + c4, wc, pol_k);
         ld3_keep(s_old + c4, spc, pol_k);
-        cgf_next<Real>(sd, col, rc, wc, spc, a, b, sc_, rnc, uc);
+        if (kScaled) {
+#pragma unroll
+          for (int c = 0; c < 3; ++c) uc[c] = fma(-a, fma(b, spc[c], wc[c]), rc[c]);
+        } else {
+          cgf_next<Real>(sd, col, rc, wc, spc, a, b, sc_, rnc, uc);
+        }
       }
       acc0 += w0.y * uc[0] + w1.x * uc[1] + w1.y * uc[2];
       acc1 += w2.x * uc[0] + w2.y * uc[1] + w3.x * uc[2];
       acc2 += w3.y * uc[0] + w4.x * uc[1] + w4.y * uc[2];
     }
     const Real wn[3] = {acc0, acc1, acc2};
-    st3(w_new + k4, wn);
+    if (kScaled) {
+      // the row's M^{-1} again (an L1/L2 hit) rather than held across the loop
+      ld3<false>(static_cast<const Real*>(sd.dinv) + k4, dv);
+      const Real ws[3] = {dv[0] * acc0, dv[1] * acc1, dv[2] * acc2};
+      st3(w_new + k4, ws);
+    } else {
+      st3(w_new + k4, wn);
+    }
 #pragma unroll
     for (int c = 0; c < 3; ++c) {
       dots[0] = dots[0] + exact_prod(rn[c], rn[c]);
@@ -872,17 +905,18 @@ __device__ __forceinline__ void cgf_tile(int tix, const Tile* tiles, const Scene
   }
 }
 
-template <typename Real>
+// kScaled: every scene of the batch uses the Jacobi preconditioner.
+template <typename Real, bool kScaled>
 __global__ void __launch_bounds__(kCgThreads) k_cgf_init(const Tile* tiles, const SceneDev* sds,
                                                          double* partials, int pstride,
                                                          BatchCounters* ctrs) {
-  cgf_tile<Real, true>(blockIdx.x, tiles, sds, partials, pstride, ctrs);
+  cgf_tile<Real, true, kScaled>(blockIdx.x, tiles, sds, partials, pstride, ctrs);
 }
 
-template <typename Real>
+template <typename Real, bool kScaled>
 __global__ void __launch_bounds__(kCgThreads, sizeof(Real) == 4 ? 6 : 4) k_cgf_iter(
     const Tile* tiles, const SceneDev* sds, double* partials, int pstride, BatchCounters* ctrs) {
-  cgf_tile<Real, false>(blockIdx.x, tiles, sds, partials, pstride, ctrs);
+  cgf_tile<Real, false, kScaled>(blockIdx.x, tiles, sds, partials, pstride, ctrs);
 }
 
 // Nanoseconds of the GPU's global timer.
@@ -1021,8 +1055,23 @@ void launch_cg_replace(const Launch& L) {
   if (L.ntiles == 0 || L.fp64) return;
   k_cg_replace<<<L.ntiles, kCgThreads, 0, L.stream>>>(L.tiles, L.sds, L.partials, L.pstride, L.counters);
 }
-void launch_cgf_init(const Launch& L) { MFEM_LAUNCH_ROWS(k_cgf_init, kCgThreads); }
-void launch_cgf_iter(const Launch& L) { MFEM_LAUNCH_ROWS(k_cgf_iter, kCgThreads); }
+#define MFEM_LAUNCH_CGF(kern)                                                                \
+  do {                                                                                       \
+    if (L.ntiles == 0) return;                                                               \
+    const auto args = [&](auto k) {                                                          \
+      k<<<L.ntiles, kCgThreads, 0, L.stream>>>(L.tiles, L.sds, L.partials, L.pstride, L.counters); \
+    };                                                                                       \
+    if (L.fp64) {                                                                            \
+      if (L.jacobi) args(kern<double, true>);                                                \
+      else args(kern<double, false>);                                                        \
+    } else {                                                                                 \
+      if (L.jacobi) args(kern<float, true>);                                                 \
+      else args(kern<float, false>);                                                         \
+    }                                                                                        \
+  } while (0)
+
+void launch_cgf_init(const Launch& L) { MFEM_LAUNCH_CGF(k_cgf_init); }
+void launch_cgf_iter(const Launch& L) { MFEM_LAUNCH_CGF(k_cgf_iter); }
 
 // Failure-detection check of the bounded grid barrier: a cooperative launch
 // of two blocks in which block 1 leaves without arriving (a lost peer), so

@@ -232,7 +232,8 @@ struct Launch {
   int pstride;
   BatchCounters* counters;
   int fp64;
-  int fem;  // the batch's scenes use the standard-FEM variable
+  int fem;     // the batch's scenes use the standard-FEM variable
+  int jacobi;  // no scene of the batch uses the 3x3 block-Jacobi preconditioner
 };
 
 // Element kernels (k_elem.cu)
