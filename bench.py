@@ -177,9 +177,10 @@ def kernel_bytes(kind, sizes, rsz, cg_per_launch=None):
         # values + block cols + row ptr, z and p_prev read, Ap and p written
         return nnzb * (9 * rsz + 4) + 4 * (nf + 1) + 4 * 3 * nf * rsz
     if kind == "k_cgf_iter":
-        # one pass of the matrix; own rows: r, w, s, u, p, x read and r, w, s,
-        # u, p, x written (neighbour values come from caches)
-        return nnzb * (9 * rsz + 4) + 4 * (nf + 1) + 12 * 3 * nf * rsz
+        # one pass of the matrix; own rows (Jacobi, scaled form): r, w, s, p,
+        # x and the preconditioner read, r, w, s, p, x written (neighbour
+        # values come from caches)
+        return nnzb * (9 * rsz + 4) + 4 * (nf + 1) + 11 * 3 * nf * rsz
     if kind == "k_cg_update":
         # x (rw), r (rw), p, Ap, z (w), Jacobi diagonal
         return 8 * 3 * nf * rsz
