@@ -331,3 +331,21 @@ def test_auto_pcg_form_by_tile_count(gpu_lib):
     xa, fa, sa = run(cube(abi.PCG_KERNEL_AUTO))
     xs, _, _ = run(cube(abi.PCG_KERNEL_SPLIT))
     assert fa == 0 and sa > 0 and np.array_equal(xa, xs)
+
+
+@pytest.mark.parametrize("prec", PRECS)
+def test_fused_pcg_with_block_jacobi(gpu_lib, prec):
+    """The fused form keeps r, w, s unscaled under the 3x3 block-Jacobi
+    preconditioner (the scaled form is for Jacobi); both reach the split
+    form's states."""
+    res = {}
+    for kern in (abi.PCG_KERNEL_SPLIT, abi.PCG_KERNEL_FUSED):
+        spec = configs.beam_c1(precision=prec, pcg_kernel=kern, linear_solver=abi.SOLVER_GPU_PCG_BLOCK)
+        s = gpu.Scene(spec)
+        for _ in range(5):
+            assert s.step().status in (abi.OK, abi.ERR_LS_FAILED)
+        res[kern] = s.get_state()["x"]
+        s.close()
+    xa, xb = res[abi.PCG_KERNEL_SPLIT], res[abi.PCG_KERNEL_FUSED]
+    tol = 1e-7 if prec == abi.PRECISION_FP64 else 1e-5
+    assert np.abs(xa - xb).max() <= tol * bbox_diag(xa)
