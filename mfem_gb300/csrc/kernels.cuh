@@ -25,7 +25,6 @@ enum TableKind {
 constexpr int kElemTile = 128;   // elements per element tile (one thread each)
 constexpr int kVertTile = 128;   // vertices per vertex tile (TB_EV: same block size)
 constexpr int kRowTile = 32;     // rows per assembly tile (8 warps, 4 rows each)
-constexpr int kCgTpr = 8;        // threads per row in the PCG SpMV
 constexpr int kCgThreads = 256;  // threads per PCG tile
 constexpr int kCgRows = 256;     // rows per PCG tile
 constexpr int kTicketGroup = 32; // tiles per first-level ticket counter
@@ -184,7 +183,8 @@ struct SceneDev {
   void* cg_p[2];
   void* cg_Ap;
   // single-reduction PCG (Chronopoulos-Gear): r, w = A u and s by
-  // iteration parity; x, u (= cg_z) and p (= cg_p[0]) single
+  // iteration parity (scaled by the Jacobi M^-1 when every scene of the
+  // batch uses it); x, p (= cg_p[0]) and, unscaled, u (= cg_z) single
   void* cgf_r[2];
   void* cgf_w[2];
   void* cgf_s[2];
