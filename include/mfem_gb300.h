@@ -91,10 +91,10 @@ enum { MFEM_FORMULATION_MIXED_STRETCH = 0, MFEM_FORMULATION_STRETCH = 1 };
  * 1989), one launch per iteration; equal to the others in exact arithmetic,
  * not bitwise.  AUTO: the batch picks FUSED when its PCG tiles (256 rows
  * each) fill at least two per SM or fit in a few blocks, SPLIT in between,
- * where FUSED's one thread per row leaves SMs without enough warps (a
- * 30^3 cube: 117 tiles, SPLIT 20% faster; a 60^3 cube: 873 tiles, FUSED
- * faster; a 200-tet beam: one tile, FUSED's single launch per iteration
- * faster). */
+ * where the system sits in L2 and FUSED's extra gathers per neighbour set
+ * the pace (a 30^3 cube: 117 tiles, SPLIT 20% faster; a 60^3 cube: 873
+ * tiles, FUSED faster; a 200-tet beam: one tile, FUSED's single launch per
+ * iteration faster). */
 enum { MFEM_PCG_KERNEL_PERSISTENT = 0, MFEM_PCG_KERNEL_SPLIT = 1, MFEM_PCG_KERNEL_FUSED = 2,
        MFEM_PCG_KERNEL_AUTO = 3 };
 
