@@ -1,7 +1,7 @@
 """TEST INFRASTRUCTURE ONLY: ctypes loader for the FP64 CPU oracle.
 
 Only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline legs may
-import this package, as the checker or the timed CPU baseline.  See
+import this package, to check results or as the timed CPU baseline.  See
 mfem_oracle.h for what the oracle restates and how far parity is pinned.
 """
 import ctypes as C

@@ -1,8 +1,9 @@
 /*
  * TEST INFRASTRUCTURE ONLY — the FP64 CPU oracle of the mixed-FEM Newton
  * timestep of tytrusty/mfem.  Only tests/, __graft_entry__.smoke() and the
- * cpu_baseline / --impl reference legs of bench.py may load it, and only as
- * the checker or the timed CPU baseline, never as the product path.
+ * cpu_baseline / --impl reference legs of bench.py may load it, and only to
+ * check the GPU path's results or as the timed CPU baseline, never as the
+ * product path.
  *
  * Parity status: the reference (C++17 on Eigen/libigl/Bartels/CHOLMOD) cannot
  * be built here — those libraries are absent — so this is a restatement.
