@@ -800,7 +800,7 @@ __device__ __forceinline__ void cgf_tile(int tix, const Tile* tiles, const Scene
     const int soff = sd.slice_off[slice], slen = (sd.slice_off[slice + 1] - soff) >> 5;
     const unsigned long long pol_s = l2_evict_first(), pol_k = l2_evict_last();
     Real acc0 = 0, acc1 = 0, acc2 = 0;
-#pragma unroll 2
+#pragma unroll 1
     for (int k = 0; k < slen; ++k) {
       const size_t q = ell_pair(soff, k, rs, 0);
       const auto w0 = ld_stream(ell, q, pol_s), w1 = ld_stream(ell, q + 32, pol_s),
