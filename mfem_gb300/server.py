@@ -79,6 +79,8 @@ class Server:
         self.ticks = []
 
     def submit(self, spec, steps, arrival=0.0):
+        if int(steps) < 1:
+            raise ValueError("a request takes at least one timestep")
         r = Request(spec=spec, steps=int(steps), arrival=float(arrival), rid=len(self.queue))
         r.footprint = gpu.footprint(spec)
         if r.footprint > self.budget:

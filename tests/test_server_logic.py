@@ -151,3 +151,27 @@ def test_oversize_request_is_refused(monkeypatch):
     except ValueError:
         return
     raise AssertionError("oversize request accepted")
+
+
+def test_empty_stream_and_bad_requests(monkeypatch):
+    fake = _FakeGpu()
+    monkeypatch.setattr(server, "gpu", fake)
+    srv = server.Server(budget_bytes=100)
+    assert srv.run(realtime=False) == []
+    for bad in (0, -3):
+        try:
+            srv.submit(_spec("z", 10), bad)
+        except ValueError:
+            continue
+        raise AssertionError("a request without timesteps was accepted")
+    s = server.summary([], [], 1.0)
+    assert s["timesteps"] == 0 and s["requests"] == 0
+
+
+def test_shard_is_balanced_and_deterministic():
+    w = [9, 1, 8, 2, 7, 3, 6, 4, 5]
+    parts = [server.shard(w, 3, r) for r in range(3)]
+    assert sorted(i for p in parts for i in p) == list(range(9))
+    loads = [sum(w[i] for i in p) for p in parts]
+    assert max(loads) - min(loads) <= max(w)
+    assert parts == [server.shard(w, 3, r) for r in range(3)]
