@@ -498,7 +498,17 @@ struct mfem_batch {
   cudaEvent_t ev_pipe[2] = {nullptr, nullptr};
   SceneScalars* h_sc = nullptr;     // pinned, one per scene
   int max_newton = 0, max_ls = 0, max_cg = 0;
-  int cg_hint = 16;
+  // Iterations to launch before the first convergence check of a linear
+  // solve, per Newton iteration index (3/4 of the previous step's count at
+  // that index): the first Newton iteration of a step needs several times
+  // the iterations of the last, so one shared hint made the early solves
+  // check too often and the late ones launch dozens of finished iterations.
+  std::vector<int> cg_hints;
+  int newton_index = 0;
+  int& cg_hint() {
+    if (cg_hints.empty()) cg_hints.assign(64, 16);
+    return cg_hints[std::min(newton_index, (int)cg_hints.size() - 1)];
+  }
   int pcg_kernel = MFEM_PCG_KERNEL_PERSISTENT;
   int minres = 0;  // every scene uses "minres-indefinite-block"
   int fem = 0;     // every scene uses the standard-FEM variable
@@ -836,7 +846,7 @@ int run_pcg_graph(mfem_batch* b, const Launch& Lcg, bool fused) {
     CUDA_OR(ei, MFEM_ERR_CUDA);
   }
   int it = 0, nchunk = 0;
-  int reps = std::max(1, (b->cg_hint + len - 1) / len);
+  int reps = std::max(1, (b->cg_hint() + len - 1) / len);
   while (it < b->max_cg) {
     for (int r = 0; r < reps && it < b->max_cg; ++r, it += len) {
       CUDA_OR(cudaGraphLaunch(b->cg_graph, b->stream), MFEM_ERR_CUDA);
@@ -860,7 +870,7 @@ int run_pcg_graph(mfem_batch* b, const Launch& Lcg, bool fused) {
     ++nchunk;
     reps = 1;
   }
-  b->cg_hint = std::max(4, (it * 3) / 4);
+  b->cg_hint() = std::max(4, (it * 3) / 4);
   return MFEM_OK;
 }
 
@@ -885,7 +895,7 @@ int run_pcg(mfem_batch* b, const Launch& Lcg) {
   // launched after convergence return at once.
   if (!b->profiling) return run_pcg_graph(b, Lcg, fused);
   int it = 0, nchunk = 0;
-  int chunk = std::max(4, b->cg_hint);
+  int chunk = std::max(4, b->cg_hint());
   while (it < b->max_cg) {
     const int c = std::min(chunk, b->max_cg - it);
     for (int k = 0; k < c; ++k, ++it) {
@@ -913,7 +923,7 @@ int run_pcg(mfem_batch* b, const Launch& Lcg) {
     ++nchunk;
     chunk = 8;
   }
-  b->cg_hint = std::max(4, (it * 3) / 4);
+  b->cg_hint() = std::max(4, (it * 3) / 4);
   return MFEM_OK;
 }
 
@@ -924,7 +934,7 @@ int run_pcg(mfem_batch* b, const Launch& Lcg) {
 int run_minres(mfem_batch* b, const Launch& Lev) {
   { KTimer t(b, MFEM_K_MR_INIT); launch_mr_init(Lev); }
   int it = 0, nchunk = 0;
-  int chunk = std::max(4, b->cg_hint);
+  int chunk = std::max(4, b->cg_hint());
   while (it < b->max_cg) {
     const int c = std::min(chunk, b->max_cg - it);
     for (int k = 0; k < c; ++k, ++it) {
@@ -947,7 +957,7 @@ int run_minres(mfem_batch* b, const Launch& Lev) {
   { KTimer t(b, MFEM_K_MR_ELEM); launch_mr_elem(Lev); }
   { KTimer t(b, MFEM_K_MR_VERT); launch_mr_vert(Lev); }
   { KTimer t(b, MFEM_K_MR_EXPORT); launch_mr_export(Lev); }
-  b->cg_hint = std::max(4, (it * 3) / 4);
+  b->cg_hint() = std::max(4, (it * 3) / 4);
   return MFEM_OK;
 }
 
@@ -959,6 +969,7 @@ int batch_newton(mfem_batch* b) {
   { KTimer t(b, MFEM_K_STEP_BEGIN); launch_step_begin(Lev); }
   int rc;
   for (int newton = 0; newton <= b->max_newton + 1; ++newton) {
+    b->newton_index = newton;
     { KTimer t(b, MFEM_K_ELEM_UPDATE); launch_elem_update(make_launch(b, TB_ELEM), nullptr); }
     { KTimer t(b, MFEM_K_ASSEMBLE); launch_assemble(make_launch(b, TB_ROW)); }
     if (b->minres) {
