@@ -82,11 +82,22 @@ class Server:
         if int(steps) < 1:
             raise ValueError("a request takes at least one timestep")
         r = Request(spec=spec, steps=int(steps), arrival=float(arrival), rid=len(self.queue))
-        r.footprint = gpu.footprint(spec)
+        r.footprint = gpu.footprint(spec) + self._checkpoint_bytes(spec)
         if r.footprint > self.budget:
             raise ValueError(f"request {r.rid} needs {r.footprint} bytes, over the budget")
         self.queue.append(r)
         return r.rid
+
+    def _checkpoint_bytes(self, spec):
+        """Device bytes of the per-tick checkpoint a mixed scene keeps when
+        escalation is on (positions and the BDF history of x and v at 24
+        bytes a vertex each, s and the quaternions at 64 bytes a tet)."""
+        if not self.escalate or getattr(spec, "precision", None) != abi.PRECISION_MIXED:
+            return 0
+        nv = getattr(spec, "n_vertices", 0)
+        nt = getattr(spec, "n_tets", 0)
+        bdf = getattr(spec, "bdf_order", 1)
+        return 24 * nv * (1 + 2 * bdf) + 64 * nt
 
     @staticmethod
     def _in_fp64(r, sc):

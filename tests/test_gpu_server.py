@@ -31,7 +31,9 @@ def test_served_results_equal_alone(gpu_lib, prec):
         alone.append(s.get_state()["x"])
         s.close()
     # a budget for about two scenes at a time: the others wait and join later
-    budget = int(1.5 * max(gpu.footprint(sp) for sp in specs))
+    probe = server.Server(budget_bytes=1)
+    need = [gpu.footprint(sp) + probe._checkpoint_bytes(sp) for sp in specs]
+    budget = int(1.5 * max(need))
     srv = server.Server(budget_bytes=budget)
     for i, (sp, (_, _, _, n)) in enumerate(zip(specs, reqs)):
         srv.submit(sp, n, arrival=0.0)
