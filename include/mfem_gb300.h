@@ -294,6 +294,78 @@ int mfem_gpu_bsr_pcg_noalloc(int32_t n_block_rows, int32_t nnzb,
                              int32_t max_iters, double tol, void* stream,
                              int32_t* iterations, double* rel_residual);
 
+/* ---- 2-D scenes: triangle meshes in the plane -----------------------------
+ * The DIM = 2 instantiation of the same timestep: Tri2DMesh
+ * (src/mesh/tri2d_mesh.cpp), MixedStretch<2> with polar_svd<2>
+ * (src/variables/mixed_stretch.cpp:43-78, dsvd src/svd/dsvd.cpp:140-189),
+ * the 3-vector materials (Stable-Neohookean, Corot, FixedCorot, ARAP:
+ * the Vector3d sections of the src/energies files), Displacement<2>, BDF<2>,
+ * NewtonOptimizer<2> with "eigen-pcg-diag".  FP64 throughout.
+ * s per triangle is [S00, S11, (S10+S01)/2]; R is 2x2 column-major.
+ * "Volumes" are igl::doublearea, twice the triangle area, as in
+ * Tri2DMesh::volumes (tri2d_mesh.cpp:30-32); triangles must be
+ * counter-clockwise (a clockwise one has a negative doublearea and is
+ * rejected with MFEM_ERR_INVALID).  Every BC script of the 3-D path
+ * applies, with BEND and TWIST turning by Rotation2D (about the group's
+ * last vertex and the bounding-box centre, bend_boundary_condition.h:45,
+ * twist_boundary_condition.h:45).  Neohookean and Fung (no Vector3d energy
+ * in the reference) and solvers other than MFEM_SOLVER_EIGEN_CG_DIAG
+ * return MFEM_ERR_UNSUPPORTED.                                             */
+typedef struct mfem_tri2d_desc {
+  int32_t n_vertices;
+  int32_t n_tris;
+  const double*  V_rest;       /* 2*n_vertices rest positions                  */
+  const double*  V_init;       /* 2*n_vertices initial positions (NULL = rest) */
+  const double*  v_init;       /* 2*n_vertices initial velocities (NULL = 0)   */
+  const int32_t* tris;         /* 3*n_tris, counter-clockwise                  */
+  const double*  mu;           /* n_tris                                        */
+  const double*  lambda;       /* n_tris                                        */
+  const int32_t* material;     /* n_tris MFEM_MATERIAL_* (NULL = all SNH)      */
+  const double*  density;      /* n_tris (NULL = density_const)                */
+  double         density_const;
+  const int32_t* is_fixed;     /* n_vertices 0/1 override (NULL = from BC)     */
+  int32_t bc_type;
+  int32_t bc_axis;             /* 0 or 1                                        */
+  double  bc_ratio;
+  double  bc_velocity;
+  double  dt;
+  double  body_force[2];
+  int32_t bdf_order;           /* 1..6 */
+  int32_t max_newton_iterations;
+  int32_t max_linesearch_iterations;
+  int32_t max_iterative_solver_iters;
+  double  iterative_solver_tolerance;
+  double  newton_tol;
+  double  newton_residual_tolerance;
+  int32_t linear_solver;       /* MFEM_SOLVER_EIGEN_CG_DIAG */
+  int32_t reserved[7];
+} mfem_tri2d_desc;
+
+typedef struct mfem_tri2d mfem_tri2d;
+
+/* SimState<2>::load + NewtonOptimizer<2>::reset. */
+int mfem_gpu_tri2d_create(const mfem_tri2d_desc* desc, mfem_tri2d** out);
+int mfem_gpu_tri2d_destroy(mfem_tri2d* scene);
+/* NewtonOptimizer<2>::step. */
+int mfem_gpu_tri2d_step(mfem_tri2d* scene, mfem_step_stats* stats);
+int mfem_gpu_tri2d_sizes(const mfem_tri2d* scene, int32_t* n_vertices,
+                         int32_t* n_tris, int32_t* n_free, int32_t* nnzb);
+/* x, v: 2*n_vertices; s, la: 3*n_tris; R: 4*n_tris.  Any may be NULL. */
+int mfem_gpu_tri2d_get_state(mfem_tri2d* scene, double* x, double* v,
+                             double* s, double* R, double* la);
+/* MixedStretch<2>::update_rotations + update_derivatives at positions x
+ * (2*n_vertices) and step h.  Per triangle: R[4], S[3], dSdF[12] (4x3
+ * column-major), g[3], H[9], Hinv[9], Aloc[36] (6x6 column-major), gl[3]. */
+int mfem_gpu_tri2d_elem_update(mfem_tri2d* scene, const double* x, double h,
+                               double* R, double* S, double* dSdF, double* g,
+                               double* H, double* Hinv, double* Aloc,
+                               double* gl);
+/* LHS = PMP + A as 2x2 BCSR over free vertices (row_ptr n_free+1, col nnzb,
+ * val 4*nnzb row-major blocks) and the RHS (2*n_free) of the last
+ * elem_update or Newton iteration. */
+int mfem_gpu_tri2d_get_system(mfem_tri2d* scene, int32_t* row_ptr,
+                              int32_t* col, double* val, double* rhs);
+
 #ifdef __cplusplus
 }
 #endif

@@ -52,6 +52,13 @@ SIGNATURES = {
     "mfem_gpu_kernel_name": (C.c_int, [C.c_int, C.c_char_p, C.c_int]),
     "mfem_gpu_bsr_pcg_noalloc": (C.c_int, [C.c_int32, C.c_int32, _vp, _vp, _vp, _vp, _vp, C.c_int32,
                                            C.c_double, _vp, _ip, _dp]),
+    "mfem_gpu_tri2d_create": (C.c_int, [_vp, C.POINTER(_vp)]),
+    "mfem_gpu_tri2d_destroy": (C.c_int, [_vp]),
+    "mfem_gpu_tri2d_step": (C.c_int, [_vp, _vp]),
+    "mfem_gpu_tri2d_sizes": (C.c_int, [_vp, _ip, _ip, _ip, _ip]),
+    "mfem_gpu_tri2d_get_state": (C.c_int, [_vp, _dp, _dp, _dp, _dp, _dp]),
+    "mfem_gpu_tri2d_elem_update": (C.c_int, [_vp, _dp, C.c_double] + [_dp] * 8),
+    "mfem_gpu_tri2d_get_system": (C.c_int, [_vp, _ip, _ip, _dp, _dp]),
 }
 
 

@@ -120,3 +120,36 @@ class StepStats(C.Structure):
 
     def as_dict(self):
         return {name: getattr(self, name) for name, _ in self._fields_}
+
+
+class Tri2dDesc(C.Structure):
+    """mfem_tri2d_desc: a triangle mesh in the plane (the DIM = 2 path)."""
+    _fields_ = [
+        ("n_vertices", C.c_int32),
+        ("n_tris", C.c_int32),
+        ("V_rest", _dp),
+        ("V_init", _dp),
+        ("v_init", _dp),
+        ("tris", _ip),
+        ("mu", _dp),
+        ("lam", _dp),
+        ("material", _ip),
+        ("density", _dp),
+        ("density_const", C.c_double),
+        ("is_fixed", _ip),
+        ("bc_type", C.c_int32),
+        ("bc_axis", C.c_int32),
+        ("bc_ratio", C.c_double),
+        ("bc_velocity", C.c_double),
+        ("dt", C.c_double),
+        ("body_force", C.c_double * 2),
+        ("bdf_order", C.c_int32),
+        ("max_newton_iterations", C.c_int32),
+        ("max_linesearch_iterations", C.c_int32),
+        ("max_iterative_solver_iters", C.c_int32),
+        ("iterative_solver_tolerance", C.c_double),
+        ("newton_tol", C.c_double),
+        ("newton_residual_tolerance", C.c_double),
+        ("linear_solver", C.c_int32),
+        ("reserved", C.c_int32 * 7),
+    ]

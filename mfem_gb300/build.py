@@ -13,7 +13,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 OUT_DIR = os.path.join(HERE, "_build")
 LIB_NAME = "libmfem_gb300.so"
-SOURCES = ["k_elem.cu", "k_rows.cu", "k_minres.cu", "k_noalloc.cu", "host.cu"]
+SOURCES = ["k_elem.cu", "k_rows.cu", "k_minres.cu", "k_noalloc.cu", "tri2d.cu", "host.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 

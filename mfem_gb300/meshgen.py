@@ -69,3 +69,21 @@ def enu_to_lame(E, nu):
     mu = E / (2.0 * (1.0 + nu))
     lam = (E * nu) / ((1.0 + nu) * (1.0 - 2.0 * nu))
     return lam, mu
+
+
+def square_grid(nx, ny, spacing=0.1, origin=(0.0, 0.0)):
+    """Returns (V, T) of an nx*ny grid of squares in the plane, each split
+    into two counter-clockwise triangles along a diagonal that alternates
+    with the parity of i+j.  Vertex (i, j) has index i + (nx+1)*j."""
+    jj, ii = np.meshgrid(np.arange(ny + 1), np.arange(nx + 1), indexing="ij")
+    V = np.stack([origin[0] + spacing * ii.ravel(), origin[1] + spacing * jj.ravel()],
+                 axis=1).astype(np.float64)
+    cj, ci = np.meshgrid(np.arange(ny), np.arange(nx), indexing="ij")
+    ci, cj = ci.ravel(), cj.ravel()
+    v00 = ci + (nx + 1) * cj
+    v10, v01, v11 = v00 + 1, v00 + (nx + 1), v00 + nx + 2
+    even = ((ci + cj) & 1) == 0
+    t1 = np.where(even[:, None], np.stack([v00, v10, v11], 1), np.stack([v00, v10, v01], 1))
+    t2 = np.where(even[:, None], np.stack([v00, v11, v01], 1), np.stack([v10, v11, v01], 1))
+    T = np.stack([t1, t2], axis=1).reshape(-1, 3)
+    return V, T.astype(np.int32)

@@ -20,9 +20,10 @@ _ip = C.POINTER(C.c_int32)
 
 def build(force=False):
     """Compiles the oracle with the Makefile beside this file."""
-    src = os.path.join(_HERE, "mfem_oracle.cpp")
+    srcs = [os.path.join(_HERE, f) for f in ("mfem_oracle.cpp", "mfem_oracle2d.cpp",
+                                             "mfem_oracle.h", "Makefile")]
     if force or not os.path.exists(_LIB_PATH) or \
-            os.path.getmtime(_LIB_PATH) < os.path.getmtime(src):
+            os.path.getmtime(_LIB_PATH) < max(os.path.getmtime(s) for s in srcs):
         subprocess.run(["make", "-s", "-C", _HERE], check=True)
     return _LIB_PATH
 
@@ -62,6 +63,20 @@ def lib():
         L.oracle_scene_minres.argtypes = [C.c_void_p, _dp, _dp, _ip, _dp]
         L.oracle_scene_schur_solve.argtypes = [C.c_void_p, _dp, _ip, _dp]
         L.oracle_scene_update_system.argtypes = [C.c_void_p]
+        L.oracle2d_polar.argtypes = [_dp, _dp, _dp, _dp]
+        L.oracle2d_svd.argtypes = [_dp, _dp, _dp, _dp]
+        L.oracle2d_material.argtypes = [C.c_int, C.c_double, C.c_double, _dp, _dp, _dp, C.c_int]
+        L.oracle2d_material.restype = C.c_double
+        L.oracle2d_create.argtypes = [C.c_void_p, _ip]
+        L.oracle2d_create.restype = C.c_void_p
+        L.oracle2d_destroy.argtypes = [C.c_void_p]
+        L.oracle2d_step.argtypes = [C.c_void_p, C.c_void_p]
+        L.oracle2d_sizes.argtypes = [C.c_void_p, _ip, _ip, _ip, _ip]
+        L.oracle2d_get_state.argtypes = [C.c_void_p] + [_dp] * 5
+        L.oracle2d_elem_update.argtypes = [C.c_void_p, _dp, C.c_double] + [_dp] * 8
+        L.oracle2d_get_system.argtypes = [C.c_void_p, _ip, _ip, _dp, _dp]
+        L.oracle2d_energy.argtypes = [C.c_void_p, C.c_double]
+        L.oracle2d_energy.restype = C.c_double
         _lib = L
     return _lib
 
@@ -249,3 +264,93 @@ class OracleScene:
         err = C.c_double()
         lib().oracle_scene_schur_solve(self._h, _p(x), C.byref(it), C.byref(err))
         return x, it.value, err.value
+
+
+# ---- the 2-D path (mfem_oracle2d.cpp) --------------------------------------
+
+def polar2(F, compute_gradients=True):
+    """polar_svd<2>: (R 2x2, s[3], ds/dF 3x4 on the column-major vec(F), status)."""
+    F = np.asfortranarray(F, dtype=np.float64)
+    R = np.zeros((2, 2), order="F")
+    s = np.zeros(3)
+    dsdF = np.zeros((3, 4), order="F")
+    st = lib().oracle2d_polar(_p(R), _p(F), _p(s), _p(dsdF) if compute_gradients else None)
+    return R, s, dsdF, st
+
+
+def svd2(F):
+    F = np.asfortranarray(F, dtype=np.float64)
+    sig = np.zeros(2)
+    U = np.zeros((2, 2), order="F")
+    V = np.zeros((2, 2), order="F")
+    lib().oracle2d_svd(_p(F), _p(sig), _p(U), _p(V))
+    return sig, U, V
+
+
+def material2(mtype, mu, lam, s, psd_fix=True):
+    """psi, gradient (3) and Hessian (3x3) of a 3-vector material."""
+    s = np.ascontiguousarray(s, dtype=np.float64)
+    g = np.zeros(3)
+    H = np.zeros((3, 3), order="F")
+    psi = lib().oracle2d_material(mtype, mu, lam, _p(s), _p(g), _p(H), int(psd_fix))
+    return psi, g, H
+
+
+class OracleTri2d:
+    """FP64 CPU 2-D scene with the same descriptor as the GPU library."""
+
+    def __init__(self, spec):
+        from mfem_gb300.desc import make_tri2d_desc
+        self._desc = make_tri2d_desc(spec)
+        st = C.c_int32(0)
+        self._h = lib().oracle2d_create(C.addressof(self._desc.struct), C.byref(st))
+        self.create_status = st.value
+        if not self._h:
+            raise RuntimeError(f"oracle 2-D scene create failed: status {st.value}")
+        nv, nt, nf, nb = (C.c_int32() for _ in range(4))
+        lib().oracle2d_sizes(self._h, C.byref(nv), C.byref(nt), C.byref(nf), C.byref(nb))
+        self.n_vertices, self.n_tris, self.n_free, self.nnzb = nv.value, nt.value, nf.value, nb.value
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h:
+            lib().oracle2d_destroy(h)
+            self._h = None
+
+    def step(self):
+        from mfem_gb300.abi import StepStats
+        st = StepStats()
+        lib().oracle2d_step(self._h, C.byref(st))
+        return st
+
+    def get_state(self):
+        x = np.zeros(2 * self.n_vertices)
+        v = np.zeros(2 * self.n_vertices)
+        s = np.zeros(3 * self.n_tris)
+        R = np.zeros(4 * self.n_tris)
+        la = np.zeros(3 * self.n_tris)
+        lib().oracle2d_get_state(self._h, _p(x), _p(v), _p(s), _p(R), _p(la))
+        return dict(x=x.reshape(-1, 2), v=v.reshape(-1, 2), s=s.reshape(-1, 3),
+                    R=R.reshape(-1, 4), la=la.reshape(-1, 3))
+
+    def elem_update(self, x, h):
+        nt = self.n_tris
+        out = dict(R=np.zeros((nt, 4)), S=np.zeros((nt, 3)), dSdF=np.zeros((nt, 12)),
+                   g=np.zeros((nt, 3)), H=np.zeros((nt, 9)), Hinv=np.zeros((nt, 9)),
+                   Aloc=np.zeros((nt, 36)), gl=np.zeros((nt, 3)))
+        x = np.ascontiguousarray(x, dtype=np.float64).ravel()
+        lib().oracle2d_elem_update(self._h, _p(x), h, *(_p(out[k]) for k in
+                                   ("R", "S", "dSdF", "g", "H", "Hinv", "Aloc", "gl")))
+        return out
+
+    def get_system(self):
+        rp = np.zeros(self.n_free + 1, dtype=np.int32)
+        col = np.zeros(self.nnzb, dtype=np.int32)
+        val = np.zeros(4 * self.nnzb)
+        rhs = np.zeros(2 * self.n_free)
+        lib().oracle2d_get_system(self._h, rp.ctypes.data_as(_ip), col.ctypes.data_as(_ip),
+                                  _p(val), _p(rhs))
+        return rp, col, val.reshape(-1, 2, 2), rhs
+
+    def energy(self, alpha):
+        return lib().oracle2d_energy(self._h, alpha)

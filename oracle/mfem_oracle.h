@@ -76,6 +76,27 @@ int oracle_scene_minres(void* scene, const double* b, double* x, int* iters, dou
 int oracle_scene_schur_solve(void* scene, double* x, int* iters, double* rel);
 int oracle_scene_update_system(void* scene);
 
+/* ---- the 2-D path (mfem_oracle2d.cpp): triangle meshes, DIM = 2 ---------- */
+/* polar_svd<2,3> (mixed_stretch.cpp:43-78): R 2x2 column-major, s[3], dsdF
+ * 3x4 column-major (NULL: no derivative).  Returns MFEM_ERR_PROCRUSTES when
+ * sig0 + sig1 = 0 (no unique nearest rotation). */
+int oracle2d_polar(double* R, const double* F, double* s, double* dsdF);
+/* svd<double,2> with the sign fix (svd_eigen.h:7-32). */
+int oracle2d_svd(const double* F, double* sig, double* U, double* V);
+/* psi of a 3-vector material; g[3], H[9] (may be NULL); fix: psd projection. */
+double oracle2d_material(int type, double mu, double la, const double* s, double* g,
+                         double* H, int fix);
+void* oracle2d_create(const mfem_tri2d_desc* desc, int* status);
+void oracle2d_destroy(void* scene);
+int oracle2d_step(void* scene, mfem_step_stats* stats);
+int oracle2d_sizes(void* scene, int* nv, int* nt, int* nfree, int* nnzb);
+int oracle2d_get_state(void* scene, double* x, double* v, double* s, double* R, double* la);
+int oracle2d_elem_update(void* scene, const double* x, double h, double* R, double* S,
+                         double* dSdF, double* g, double* H, double* Hinv, double* Aloc,
+                         double* gl);
+int oracle2d_get_system(void* scene, int* row_ptr, int* col, double* val, double* rhs);
+double oracle2d_energy(void* scene, double alpha);
+
 #ifdef __cplusplus
 }
 #endif
