@@ -56,13 +56,24 @@ def _rel(a, b):
 def test_elem_update_matches_oracle(gpu_lib, mtype):
     import oracle
     from mfem_gb300.tri2d import Tri2dScene
-    sp = spec2(6, 3, material=np.full(36, mtype, np.int32))
+    # a perturbed initial state, so that s (= polar(F(V_init))) is away
+    # from the rest value and g = h^2 grad psi(s) is not rounding noise
+    sp = spec2(6, 3, seed=11, material=np.full(36, mtype, np.int32))
     o, g = oracle.OracleTri2d(sp), Tri2dScene(sp)
     rng = np.random.default_rng(7)
     x = sp.V_rest * np.array([1.1, 0.95]) + 0.03 * rng.uniform(-1, 1, sp.V_rest.shape)
     ro, rg = o.elem_update(x, 0.02), g.elem_update(x, 0.02)
-    for k in ("R", "S", "dSdF", "g", "H", "Hinv", "Aloc", "gl"):
+    for k in ("R", "S", "dSdF", "g", "H", "Aloc", "gl"):
         assert _rel(rg[k], ro[k]) < 1e-10, k
+    # Where the psd projection clamps two eigenvalues of an SNH Hessian to
+    # 1e-6 next to one near 1e6 (condition 1e12), the cofactor 3x3 inverse
+    # (Eigen's Matrix3d::inverse, which both sides restate) returns rounding
+    # noise on either side; H^-1 is compared where H's condition is below
+    # 1e8, with that condition times rounding as the tolerance.
+    Ho = ro["H"].reshape(-1, 3, 3)
+    ok = np.linalg.cond(Ho) < 1e8
+    assert ok.sum() >= len(ok) // 2
+    assert _rel(rg["Hinv"][ok], ro["Hinv"][ok]) < 1e-7
     g.close()
 
 
