@@ -50,7 +50,10 @@ def parse():
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--config", default="c2", choices=["c1", "c2", "c3", "c5"])
+    ap.add_argument("--config", default="c2", choices=["c1", "c2", "c3", "c5", "tri2d"],
+                    help="tri2d: the 2-D path on a hanging sheet (scenes/2D/square.json settings)")
+    ap.add_argument("--sheet", type=int, default=128,
+                    help="squares along x of the tri2d sheet (x/4 along y, 2 triangles each)")
     ap.add_argument("--c5-duration", type=float, default=5.0,
                     help="seconds of Poisson arrivals (lambda = 20/s) in the served stream")
     ap.add_argument("--c5-steps", type=int, default=20, help="timesteps per served request")
@@ -613,8 +616,204 @@ def run_served(args):
     return 0
 
 
+# ------------------------------------------------------------------ 2-D --
+def tri2d_workload(nx):
+    """A hanging sheet with the settings of the reference's 2-D scene
+    (scenes/2D/square.json: dt 0.0333, hangends ratio 0.01 on x, SNH
+    E = 1e5 Pa, nu = 0.45, rho = 1e3, cholmod, i.e. the Jacobi PCG at 1e-10,
+    30 Newton and 20 line-search iterations): nx x nx/4 squares of side 1/nx."""
+    from mfem_gb300 import abi
+    from mfem_gb300.desc import Tri2dSpec
+    from mfem_gb300.meshgen import enu_to_lame, square_grid
+    ny = max(nx // 4, 1)
+    V, T = square_grid(nx, ny, 1.0 / nx)
+    lam, mu = enu_to_lame(1e5, 0.45)
+    spec = Tri2dSpec(V_rest=V, tris=T, mu=np.full(len(T), float(mu)), lam=np.full(len(T), float(lam)),
+                     density_const=1000.0, bc_type=abi.BC_HANGENDS, bc_ratio=0.01, bc_axis=0,
+                     dt=0.0333, body_force=(0.0, float(np.float32(-9.8))), max_newton_iterations=30,
+                     max_linesearch_iterations=20, max_iterative_solver_iters=10000,
+                     iterative_solver_tolerance=1e-10)
+    return spec, f"sheet2d_{nx}x{ny}_{len(T)}tris"
+
+
+def tri2d_kernel_bytes(name, spec, n_free, nnzb, cg_per_launch):
+    """Algorithmic bytes per launch of the 2-D kernels (FP64, each array read
+    or written once; positions gathered once per vertex)."""
+    nt, nv, nf = spec.n_tris, spec.n_vertices, n_free
+    if name == "t2_elem":      # corners, dphi/dX, vol/mu/lambda/material, s, positions; 94 doubles out
+        return nt * (12 + 48 + 28 + 24) + nv * 20 + nt * 94 * 8
+    if name == "t2_pcg":       # per iteration: BCSR values + columns + row pointers, ~28 vector passes
+        return (cg_per_launch or 0) * (36 * nnzb + 4 * nf + 224 * nf) + 64 * nf
+    if name == "t2_local":
+        return nt * (12 + 48 + 8 + 96 + 72 + 72 + 24 + 24 + 48) + nf * 16
+    if name == "t2_energy":
+        return nt * (12 + 48 + 8 + 16 + 24 + 24 + 24 + 8) + nv * 68 + nt * 16
+    if name == "t2_rows":
+        return 9 * nt * 36 + nnzb * 44 + nf * 48 + nv * 16
+    return None
+
+
+def run_tri2d(args):
+    """The 2-D path's bench line: the same contract as the 3-D line on the
+    tri2d sheet (FP64; replicas for N > 1)."""
+    import ctypes
+    ws, rank, local, pg = dist_setup()
+    from mfem_gb300.build import build
+    if rank == 0:
+        build()
+    barrier(pg)
+    from mfem_gb300 import abi
+    from mfem_gb300._lib import check, load
+    from mfem_gb300.tri2d import Tri2dScene
+    L = load()
+    if ws > 1:
+        check(L.mfem_gpu_set_device(local), "set_device")
+    spec, workload = tri2d_workload(args.sheet)
+
+    # timed: resident state, CUDA-event time of every step
+    sc = Tri2dScene(spec)
+    for _ in range(args.warmup):
+        sc.step()
+    before = sc.kernel_stats()
+    barrier(pg)
+    sampler = ClockSampler(local)
+    sampler.start()
+    ms, stats = [], []
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        st = sc.step()
+        ms.append(st.device_ms)
+        stats.append(st.as_dict())
+    wall = time.perf_counter() - t0
+    clocks = sampler.stop()
+    after = sc.kernel_stats()
+    launches = int(sum(after[k][1] - before[k][1] for k in after))
+    dev_s_max = allmax(pg, sum(ms) / 1000.0)
+    value = ws * args.steps / dev_s_max
+
+    # end to end: the same steps on a fresh scene through the C ABI, each
+    # step's positions read into a pinned host buffer
+    e2e = None
+    if not args.no_e2e:
+        import torch
+        s2 = Tri2dScene(spec)
+        for _ in range(args.warmup):
+            s2.step()
+        x_host = torch.zeros((spec.n_vertices, 2), dtype=torch.float64).pin_memory()
+        xp = ctypes.cast(x_host.data_ptr(), ctypes.POINTER(ctypes.c_double))
+        st2 = abi.StepStats()
+        barrier(pg)
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            L.mfem_gpu_tri2d_step(s2._h, ctypes.byref(st2))
+            L.mfem_gpu_tri2d_get_state(s2._h, xp, None, None, None, None)
+        e2e_s = allmax(pg, time.perf_counter() - t0)
+        e2e = {"value": ws * args.steps / e2e_s, "unit": UNIT,
+               "h2d_bytes_per_step": 16 * spec.n_vertices,
+               "d2h_bytes_per_step": int(x_host.numel() * 8),
+               "note": "h2d: the pinned vertices' positions the step uploads (the whole 2 x n "
+                       "vector); d2h: all positions, read by the caller after each step"}
+        s2.close()
+
+    # per-kernel CUDA events in a replay on a fresh scene
+    s3 = Tri2dScene(spec)
+    for _ in range(args.warmup):
+        s3.step()
+    pre = s3.kernel_stats()
+    s3.set_profiling(True)
+    prof_ms, prof_stats = [], []
+    for _ in range(args.steps):
+        st3 = s3.step()
+        prof_ms.append(st3.device_ms)
+        prof_stats.append(st3)
+    kst = s3.kernel_stats()
+    s3.close()
+    n_rep = {k: kst[k][1] - pre[k][1] for k in kst}   # launches of the replay
+    cg_total = float(sum(t.cg_iterations for t in prof_stats))
+    cg_per_launch = cg_total / max(n_rep.get("t2_pcg", 0), 1)
+    timed = {k: v for k, v in kst.items() if v[0] > 0}
+    dom = max(timed, key=lambda k: timed[k][0]) if timed else None
+    peak, peak_src = measured_peak()
+    roof = None
+    per_kernel = {}
+    if dom:
+        for k, (kms, _) in timed.items():
+            per_kernel[k] = {"ms": round(kms, 3), "launches": int(n_rep[k]),
+                             "share": round(kms / max(sum(prof_ms), 1e-9), 4)}
+        dom_ms = timed[dom][0]
+        dom_n = max(int(n_rep[dom]), 1)
+        abytes = tri2d_kernel_bytes(dom, spec, sc.n_free, sc.nnzb, cg_per_launch)
+        achieved = abytes / (dom_ms / dom_n / 1e3) / 1e9 if abytes else None
+        roof = {"kernel": dom, "bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                "frac": achieved / peak if achieved else None, "traffic": None,
+                "algorithmic_bytes_per_launch": abytes, "avg_launch_us": 1e3 * dom_ms / dom_n,
+                "peak_source": f"{peak_src} (MEASURED_PEAKS.json hbm_gbs)",
+                "note": (f"{cg_per_launch:.1f} PCG iterations per launch; the sheet's system "
+                         "sits in L2, one thread block runs the solve")
+                        if dom == "t2_pcg" else None}
+    sc.close()
+    newton = float(np.mean([t["newton_iterations"] for t in stats]))
+    cgits = float(np.mean([t["cg_iterations"] for t in stats]))
+    line = {
+        "metric": "2-D timesteps/s (tri2d sheet)", "value": value, "unit": UNIT, "n_gpus": ws,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000.0 * dev_s_max / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic",
+        "config": {"workload": workload, "tris": spec.n_tris, "vertices": spec.n_vertices,
+                   "free_dofs": 2 * sc.n_free, "blocks": sc.nnzb, "precision": "fp64",
+                   "solver": "eigen-pcg-diag (1e-10)", "l2": "working set < L2 (resident)",
+                   "parallelism": f"replicas{ws}"},
+        "p50_ms": float(np.percentile(ms, 50)), "p99_ms": float(np.percentile(ms, 99)),
+        "wall_ms_per_step": 1000.0 * wall / args.steps,
+        "newton_iterations_per_step": newton, "cg_iterations_per_step": cgits,
+        "clocks": clocks, "e2e": e2e, "roofline": roof, "gpu_launches": launches,
+        "profiled_replay_ms_per_step": float(np.mean(prof_ms)), "kernels": per_kernel,
+    }
+    if rank == 0 and ws == 1 and not args.no_cpu_baseline:
+        line["cpu_baseline"] = tri2d_cpu_baseline(spec, workload, budget_s=20.0,
+                                                  max_steps=args.warmup + args.steps)
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    return 0
+
+
+def tri2d_cpu_baseline(spec, workload, budget_s, max_steps):
+    """The FP64 2-D oracle (one host thread) stepping the same sheet from its
+    initial state: seconds per step over a bounded sample."""
+    import oracle
+    o = oracle.OracleTri2d(spec)
+    t0 = time.perf_counter()
+    n = 0
+    while n < max_steps and (n == 0 or time.perf_counter() - t0 < budget_s):
+        o.step()
+        n += 1
+    t = (time.perf_counter() - t0) / n
+    return {"value": 1.0 / t, "unit": UNIT, "cores": 1, "kind": "port",
+            "sample": f"FP64 2-D oracle on 1 host thread, {workload}: {n} steps from the initial "
+                      f"state, {t:.3f} s per step"}
+
+
+def run_reference_tri2d(args):
+    ws, rank, _, _ = dist_setup()
+    if rank != 0:
+        return 0
+    spec, workload = tri2d_workload(args.sheet)
+    cb = tri2d_cpu_baseline(spec, workload, budget_s=120.0, max_steps=args.warmup + args.steps)
+    value = cb["value"]
+    line = {"impl": "reference", "metric": "2-D timesteps/s (tri2d sheet)", "value": value,
+            "unit": UNIT, "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": 1000.0 / value, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": workload, "precision": "fp64"}, "cpu_baseline": cb,
+            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
 def main():
     args = parse()
+    if args.config == "tri2d":
+        return run_reference_tri2d(args) if args.impl == "reference" else run_tri2d(args)
     if args.impl == "ours" and args.config == "c5":
         return run_served(args)
     if args.impl == "reference":

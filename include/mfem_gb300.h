@@ -365,6 +365,18 @@ int mfem_gpu_tri2d_elem_update(mfem_tri2d* scene, const double* x, double h,
  * elem_update or Newton iteration. */
 int mfem_gpu_tri2d_get_system(mfem_tri2d* scene, int32_t* row_ptr,
                               int32_t* col, double* val, double* rhs);
+/* Instrumentation of the 2-D kernels: launches are counted always; with
+ * profiling on, every launch is bracketed by CUDA events on the scene's
+ * stream and kernel_stats returns the summed device time since profiling
+ * was switched on (times are collected at the end of each step). */
+enum {
+  MFEM_T2_K_ELEM = 0, MFEM_T2_K_ROWS = 1, MFEM_T2_K_NORM = 2, MFEM_T2_K_PCG = 3,
+  MFEM_T2_K_LOCAL = 4, MFEM_T2_K_ENERGY = 5, MFEM_T2_K_ESUM = 6, MFEM_T2_K_APPLY = 7,
+  MFEM_T2_K_HISTORY = 8, MFEM_T2_K_COUNT = 9
+};
+int mfem_gpu_tri2d_set_profiling(mfem_tri2d* scene, int enable);
+int mfem_gpu_tri2d_kernel_stats(mfem_tri2d* scene, int kernel, double* total_ms,
+                                int64_t* launches);
 
 #ifdef __cplusplus
 }

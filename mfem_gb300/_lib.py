@@ -59,6 +59,8 @@ SIGNATURES = {
     "mfem_gpu_tri2d_get_state": (C.c_int, [_vp, _dp, _dp, _dp, _dp, _dp]),
     "mfem_gpu_tri2d_elem_update": (C.c_int, [_vp, _dp, C.c_double] + [_dp] * 8),
     "mfem_gpu_tri2d_get_system": (C.c_int, [_vp, _ip, _ip, _dp, _dp]),
+    "mfem_gpu_tri2d_set_profiling": (C.c_int, [_vp, C.c_int]),
+    "mfem_gpu_tri2d_kernel_stats": (C.c_int, [_vp, C.c_int, _dp, C.POINTER(C.c_int64)]),
 }
 
 

@@ -663,6 +663,14 @@ struct mfem_tri2d {
   double* vh = nullptr;
   double* xscratch = nullptr;  // 2 nv (parity entry point)
   int head = 0;
+  // launch counts (always) and CUDA-event times (profiling on) per kernel
+  int64_t launches[MFEM_T2_K_COUNT] = {};
+  double kernel_ms[MFEM_T2_K_COUNT] = {};
+  bool profiling = false;
+  std::vector<cudaEvent_t> ev_pool;
+  struct Pending { int kernel, a, b; };
+  std::vector<Pending> ev_pending;
+  size_t ev_used = 0;
   // configuration
   int bdf = 1, max_newton = 5, ls_iters = 20, cg_iters = 500;
   double h = 0.0333, cg_tol = 1e-4, newton_tol = 1e-10, res_tol = 0, load_norm = 0;
@@ -676,6 +684,7 @@ struct mfem_tri2d {
   double group_center[2][2] = {{0, 0}, {0, 0}};
 
   ~mfem_tri2d() {
+    for (cudaEvent_t e : ev_pool) cudaEventDestroy(e);
     if (dev) cudaFree(dev);
     if (ev0) cudaEventDestroy(ev0);
     if (ev1) cudaEventDestroy(ev1);
@@ -829,18 +838,64 @@ void bc_step(mfem_tri2d& sc, double dt) {
 
 int launch_status() { return cudaGetLastError() == cudaSuccess ? MFEM_OK : MFEM_ERR_CUDA; }
 
+// An event of the scene's pool (created on first use, reused after each
+// collection); -1 when none can be created.
+int take_event(mfem_tri2d& sc) {
+  if (sc.ev_used == sc.ev_pool.size()) {
+    cudaEvent_t e = nullptr;
+    if (cudaEventCreate(&e) != cudaSuccess) {
+      cudaGetLastError();
+      return -1;
+    }
+    sc.ev_pool.push_back(e);
+  }
+  return int(sc.ev_used++);
+}
+
+// Counts a launch of kernel k and, with profiling on, brackets it by events.
+template <typename F> void launch(mfem_tri2d& sc, int k, F&& f) {
+  ++sc.launches[k];
+  if (!sc.profiling) {
+    f();
+    return;
+  }
+  const int a = take_event(sc), b = take_event(sc);
+  if (a >= 0 && b >= 0) cudaEventRecord(sc.ev_pool[a], sc.stream);
+  f();
+  if (a >= 0 && b >= 0) {
+    cudaEventRecord(sc.ev_pool[b], sc.stream);
+    sc.ev_pending.push_back({k, a, b});
+  }
+}
+
+// Adds the bracketed launches' times (the stream has been synchronised).
+void collect_events(mfem_tri2d& sc) {
+  for (const auto& p : sc.ev_pending) {
+    float ms = 0;
+    if (cudaEventElapsedTime(&ms, sc.ev_pool[p.a], sc.ev_pool[p.b]) == cudaSuccess)
+      sc.kernel_ms[p.kernel] += ms;
+  }
+  sc.ev_pending.clear();
+  sc.ev_used = 0;
+}
+
 // elem + rows at the current state (update_system of the Newton loop).
 int t2_update(mfem_tri2d& sc, const double* xfull) {
   const double dt = sc.dt_bdf();
-  t2_elem<<<grid_of(sc.nt), kThreads, 0, sc.stream>>>(sc.d, dt * dt, xfull);
-  if (!xfull && sc.nf > 0) t2_rows<<<grid_of(sc.nf), kThreads, 0, sc.stream>>>(sc.d);
+  launch(sc, MFEM_T2_K_ELEM,
+         [&] { t2_elem<<<grid_of(sc.nt), kThreads, 0, sc.stream>>>(sc.d, dt * dt, xfull); });
+  if (!xfull && sc.nf > 0)
+    launch(sc, MFEM_T2_K_ROWS, [&] { t2_rows<<<grid_of(sc.nf), kThreads, 0, sc.stream>>>(sc.d); });
   return launch_status();
 }
 
 int t2_energy_at(mfem_tri2d& sc, double alpha, int with_dec, double* scal_host) {
   const double dt = sc.dt_bdf();
-  t2_energy<<<grid_of(std::max(sc.nt, sc.nv)), kThreads, 0, sc.stream>>>(sc.d, alpha);
-  t2_esum<<<1, kBlock, 0, sc.stream>>>(sc.d, dt * dt, SC_E, with_dec);
+  launch(sc, MFEM_T2_K_ENERGY, [&] {
+    t2_energy<<<grid_of(std::max(sc.nt, sc.nv)), kThreads, 0, sc.stream>>>(sc.d, alpha);
+  });
+  launch(sc, MFEM_T2_K_ESUM,
+         [&] { t2_esum<<<1, kBlock, 0, sc.stream>>>(sc.d, dt * dt, SC_E, with_dec); });
   if (launch_status() != MFEM_OK) return MFEM_ERR_CUDA;
   T2_CUDA(cudaMemcpyAsync(scal_host, sc.d.scal, sizeof(double) * SC_COUNT, cudaMemcpyDeviceToHost,
                           sc.stream));
@@ -865,7 +920,7 @@ int t2_step(mfem_tri2d& sc, mfem_step_stats* out) {
   do {
     T2_CUDA(cudaMemsetAsync(sc.d.status, 0, sizeof(int), sc.stream));
     if (t2_update(sc, nullptr) != MFEM_OK) return MFEM_ERR_CUDA;
-    t2_norm<<<1, kBlock, 0, sc.stream>>>(sc.d);
+    launch(sc, MFEM_T2_K_NORM, [&] { t2_norm<<<1, kBlock, 0, sc.stream>>>(sc.d); });
     if (launch_status() != MFEM_OK) return MFEM_ERR_CUDA;
     int kst = 0;
     T2_CUDA(cudaMemcpyAsync(scal, sc.d.scal, sizeof(scal), cudaMemcpyDeviceToHost, sc.stream));
@@ -876,8 +931,10 @@ int t2_step(mfem_tri2d& sc, mfem_step_stats* out) {
     st.residual = rn;
     if (sc.res_tol > 0 && ((i > 0 && rn <= sc.res_tol * st.residual0) || rn <= sc.res_tol * sc.load_norm))
       break;
-    if (sc.nf > 0) t2_pcg<<<1, kBlock, 0, sc.stream>>>(sc.d, sc.cg_iters, sc.cg_tol);
-    t2_local<<<grid_of(sc.nt), kThreads, 0, sc.stream>>>(sc.d);
+    if (sc.nf > 0)
+      launch(sc, MFEM_T2_K_PCG,
+             [&] { t2_pcg<<<1, kBlock, 0, sc.stream>>>(sc.d, sc.cg_iters, sc.cg_tol); });
+    launch(sc, MFEM_T2_K_LOCAL, [&] { t2_local<<<grid_of(sc.nt), kThreads, 0, sc.stream>>>(sc.d); });
     if (launch_status() != MFEM_OK) return MFEM_ERR_CUDA;
     if (t2_energy_at(sc, 0.0, 1, scal) != MFEM_OK) return MFEM_ERR_CUDA;
     const int iters = sc.nf > 0 ? int(scal[SC_CG_IT]) : 0;
@@ -900,7 +957,9 @@ int t2_step(mfem_tri2d& sc, mfem_step_stats* out) {
     }
     st.ls_iterations += it;
     if (it < sc.ls_iters) {
-      t2_apply<<<grid_of(std::max(2L * sc.nf, 3L * sc.nt)), kThreads, 0, sc.stream>>>(sc.d, alpha);
+      launch(sc, MFEM_T2_K_APPLY, [&] {
+        t2_apply<<<grid_of(std::max(2L * sc.nf, 3L * sc.nt)), kThreads, 0, sc.stream>>>(sc.d, alpha);
+      });
       if (launch_status() != MFEM_OK) return MFEM_ERR_CUDA;
     } else if (status == MFEM_OK) {
       status = MFEM_ERR_LS_FAILED;
@@ -923,7 +982,9 @@ int t2_step(mfem_tri2d& sc, mfem_step_stats* out) {
   const Bdf old_h = sc.bdf_at(sc.head);
   const int new_head = (sc.head + sc.bdf - 1) % sc.bdf;
   const Bdf new_h = sc.bdf_at(new_head);
-  t2_history<<<grid_of(sc.nv), kThreads, 0, sc.stream>>>(sc.d, sc.xh, sc.vh, old_h, new_h, 1);
+  launch(sc, MFEM_T2_K_HISTORY, [&] {
+    t2_history<<<grid_of(sc.nv), kThreads, 0, sc.stream>>>(sc.d, sc.xh, sc.vh, old_h, new_h, 1);
+  });
   if (launch_status() != MFEM_OK) return MFEM_ERR_CUDA;
   sc.head = new_head;
   T2_CUDA(cudaMemsetAsync(sc.d.lam, 0, sizeof(double) * 3 * sc.nt, sc.stream));
@@ -934,6 +995,7 @@ int t2_step(mfem_tri2d& sc, mfem_step_stats* out) {
   float ms = 0;
   T2_CUDA(cudaEventElapsedTime(&ms, sc.ev0, sc.ev1));
   st.device_ms = ms;
+  collect_events(sc);
   st.status = status;
   if (out) *out = st;
   return status;
@@ -1335,9 +1397,25 @@ int mfem_gpu_tri2d_get_system(mfem_tri2d* sc, int32_t* row_ptr, int32_t* col, do
     T2_CUDA(cudaMemcpyAsync(rhs, sc->d.rhs, 8 * 2 * size_t(sc->nf), cudaMemcpyDeviceToHost, sc->stream));
   int kst = 0;
   if (read_status(*sc, &kst) != MFEM_OK) return MFEM_ERR_CUDA;
+  collect_events(*sc);
   if (row_ptr) std::memcpy(row_ptr, sc->b_ptr.data(), 4 * sc->b_ptr.size());
   if (col) std::memcpy(col, sc->b_col.data(), 4 * sc->b_col.size());
   return kst;
+}
+
+int mfem_gpu_tri2d_set_profiling(mfem_tri2d* sc, int enable) {
+  if (!sc) return MFEM_ERR_INVALID;
+  if (enable && !sc->profiling)
+    for (int k = 0; k < MFEM_T2_K_COUNT; ++k) sc->kernel_ms[k] = 0.0;
+  sc->profiling = enable != 0;
+  return MFEM_OK;
+}
+
+int mfem_gpu_tri2d_kernel_stats(mfem_tri2d* sc, int kernel, double* total_ms, int64_t* launches) {
+  if (!sc || kernel < 0 || kernel >= MFEM_T2_K_COUNT) return MFEM_ERR_INVALID;
+  if (total_ms) *total_ms = sc->kernel_ms[kernel];
+  if (launches) *launches = sc->launches[kernel];
+  return MFEM_OK;
 }
 
 }  // extern "C"

@@ -17,6 +17,11 @@ def _p(a):
     return None if a is None else a.ctypes.data_as(_dp)
 
 
+# the 2-D kernels in the order of the MFEM_T2_K_* ids
+KERNELS = ["t2_elem", "t2_rows", "t2_norm", "t2_pcg", "t2_local", "t2_energy", "t2_esum",
+           "t2_apply", "t2_history"]
+
+
 class Tri2dScene:
     """One resident 2-D instance (SimState<2> + NewtonOptimizer<2>)."""
 
@@ -81,3 +86,16 @@ class Tri2dScene:
         check(load().mfem_gpu_tri2d_get_system(self._h, rp.ctypes.data_as(_ip), col.ctypes.data_as(_ip),
                                                _p(val), _p(rhs)), "tri2d_get_system")
         return rp, col, val.reshape(-1, 2, 2), rhs
+
+    def set_profiling(self, enable):
+        check(load().mfem_gpu_tri2d_set_profiling(self._h, int(bool(enable))), "tri2d_set_profiling")
+
+    def kernel_stats(self):
+        """{kernel name: (total ms with profiling on, launches)}."""
+        out = {}
+        for k, name in enumerate(KERNELS):
+            ms, n = C.c_double(), C.c_int64()
+            check(load().mfem_gpu_tri2d_kernel_stats(self._h, k, C.byref(ms), C.byref(n)),
+                  "tri2d_kernel_stats")
+            out[name] = (ms.value, n.value)
+        return out
