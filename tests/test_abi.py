@@ -84,3 +84,47 @@ def test_bounded_wait_runs_out_and_the_context_stays_usable(gpu_lib):
     s = gpu.Scene(configs.beam_c1())
     assert s.step().status in (abi.OK, abi.ERR_LS_FAILED)
     s.close()
+
+
+def test_c_caller_links_against_the_library(gpu_lib, tmp_path):
+    """A plain C99 program (the kind of caller the reference's build would
+    add) includes the header, links libmfem_gb300.so and calls through it:
+    the 2-D create reports MFEM_ERR_NO_DEVICE without a GPU, MFEM_OK with one."""
+    import shutil
+    src = tmp_path / "caller.c"
+    src.write_text(r'''
+#include <stdio.h>
+#include "mfem_gb300.h"
+int main(void) {
+  double V[6] = {0, 0, 1, 0, 0, 1};
+  int32_t T[3] = {0, 1, 2};
+  double mu = 1, la = 1;
+  mfem_tri2d_desc d = {0};
+  d.n_vertices = 3; d.n_tris = 1; d.V_rest = V; d.tris = T; d.mu = &mu; d.lambda = &la;
+  d.density_const = 1000; d.dt = 0.01; d.bdf_order = 1; d.max_newton_iterations = 1;
+  d.max_linesearch_iterations = 1; d.max_iterative_solver_iters = 10;
+  d.iterative_solver_tolerance = 1e-8; d.linear_solver = MFEM_SOLVER_EIGEN_CG_DIAG;
+  mfem_tri2d* s = 0;
+  int rc = mfem_gpu_tri2d_create(&d, &s);
+  if (rc == MFEM_OK) mfem_gpu_tri2d_destroy(s);
+  printf("%d %d\n", mfem_gpu_abi_version(), rc);
+  return 0;
+}
+''')
+    libdir = os.path.join(ROOT, "mfem_gb300", "_build")
+    nvcc = shutil.which("nvcc") or "/usr/local/cuda/bin/nvcc"
+    cudalib = os.path.join(os.path.dirname(os.path.dirname(os.path.realpath(nvcc))), "lib64")
+    exe = str(tmp_path / "caller")
+    subprocess.run(["gcc", "-std=c99", "-Wall", "-Werror", "-I", os.path.join(ROOT, "include"),
+                    str(src), "-L", libdir, "-lmfem_gb300", f"-Wl,-rpath,{libdir}",
+                    f"-Wl,-rpath-link,{cudalib}", "-o", exe], check=True)
+    ver, rc = (int(v) for v in subprocess.run([exe], capture_output=True, text=True,
+                                              check=True).stdout.split())
+    assert ver == abi.ABI_VERSION
+    assert rc in (abi.OK, abi.ERR_NO_DEVICE)
+    try:
+        import torch
+        if not torch.cuda.is_available():
+            assert rc == abi.ERR_NO_DEVICE
+    except ImportError:
+        pass
