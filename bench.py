@@ -771,16 +771,18 @@ def run_tri2d(args):
     }
     if rank == 0 and ws == 1 and not args.no_cpu_baseline:
         line["cpu_baseline"] = tri2d_cpu_baseline(spec, workload, budget_s=20.0,
-                                                  max_steps=args.warmup + args.steps)
+                                                  max_steps=args.warmup + args.steps,
+                                                  threads=args.cpu_threads)
     if rank == 0:
         print(json.dumps(line), flush=True)
     return 0
 
 
-def tri2d_cpu_baseline(spec, workload, budget_s, max_steps):
-    """The FP64 2-D oracle (one host thread) stepping the same sheet from its
-    initial state: seconds per step over a bounded sample."""
+def tri2d_cpu_baseline(spec, workload, budget_s, max_steps, threads=0):
+    """The FP64 2-D oracle (OpenMP over the host cores) stepping the same
+    sheet from its initial state: seconds per step over a bounded sample."""
     import oracle
+    threads = oracle.set_threads(threads or os.cpu_count())
     o = oracle.OracleTri2d(spec)
     t0 = time.perf_counter()
     n = 0
@@ -788,9 +790,9 @@ def tri2d_cpu_baseline(spec, workload, budget_s, max_steps):
         o.step()
         n += 1
     t = (time.perf_counter() - t0) / n
-    return {"value": 1.0 / t, "unit": UNIT, "cores": 1, "kind": "port",
-            "sample": f"FP64 2-D oracle on 1 host thread, {workload}: {n} steps from the initial "
-                      f"state, {t:.3f} s per step"}
+    return {"value": 1.0 / t, "unit": UNIT, "cores": threads, "kind": "port",
+            "sample": f"FP64 2-D oracle on {threads} host threads, {workload}: {n} steps from the "
+                      f"initial state, {t:.3f} s per step"}
 
 
 def run_reference_tri2d(args):
@@ -798,7 +800,8 @@ def run_reference_tri2d(args):
     if rank != 0:
         return 0
     spec, workload = tri2d_workload(args.sheet)
-    cb = tri2d_cpu_baseline(spec, workload, budget_s=120.0, max_steps=args.warmup + args.steps)
+    cb = tri2d_cpu_baseline(spec, workload, budget_s=120.0, max_steps=args.warmup + args.steps,
+                            threads=args.cpu_threads)
     value = cb["value"]
     line = {"impl": "reference", "metric": "2-D timesteps/s (tri2d sheet)", "value": value,
             "unit": UNIT, "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,

@@ -489,6 +489,7 @@ void build_assembler(Scene2& sc) {
 
 void mass_mul(const Scene2& sc, const std::vector<double>& xin, std::vector<double>& y) {
   y.assign(2 * sc.nv, 0.0);
+#pragma omp parallel for schedule(static)
   for (int a = 0; a < sc.nv; ++a) {
     double acc[2] = {0, 0};
     for (int q = sc.m_ptr[a]; q < sc.m_ptr[a + 1]; ++q)
@@ -498,10 +499,27 @@ void mass_mul(const Scene2& sc, const std::vector<double>& xin, std::vector<doub
   }
 }
 
-double dot(const std::vector<double>& a, const std::vector<double>& b) {
+// Sums f(i) over [0, n) in fixed chunks whose partials are added in order,
+// so the result does not depend on the thread count or schedule.
+template <typename Fn>
+double det_sum(long n, Fn f) {
+  const long chunk = 2048;
+  const long nc = (n + chunk - 1) / chunk;
+  std::vector<double> part(nc, 0.0);
+#pragma omp parallel for schedule(static)
+  for (long c = 0; c < nc; ++c) {
+    double s = 0;
+    const long e = std::min(n, (c + 1) * chunk);
+    for (long i = c * chunk; i < e; ++i) s += f(i);
+    part[c] = s;
+  }
   double s = 0;
-  for (size_t i = 0; i < a.size(); ++i) s += a[i] * b[i];
+  for (double p : part) s += p;
   return s;
+}
+
+double dot(const std::vector<double>& a, const std::vector<double>& b) {
+  return det_sum((long)a.size(), [&](long i) { return a[i] * b[i]; });
 }
 
 // MixedStretch<2>::update_rotations + update_derivatives + rhs for one
@@ -568,9 +586,13 @@ int update_system(Scene2& sc, std::vector<double>& full) {
   sc.unproject(sc.x, full);
   const double dt = sc.dt();
   int status = MFEM_OK;
+#pragma omp parallel for schedule(static)
   for (int e = 0; e < sc.nt; ++e) {
     const int st = elem_update(sc, e, full, dt);
-    if (st != MFEM_OK) status = st;
+    if (st != MFEM_OK) {
+#pragma omp critical
+      status = st;
+    }
   }
   std::fill(sc.A.begin(), sc.A.end(), 0.0);
   for (size_t i = 0; i < sc.pair_elem.size(); ++i) {
@@ -613,6 +635,7 @@ int update_system(Scene2& sc, std::vector<double>& full) {
 
 void bcsr_mul(const Scene2& sc, const std::vector<double>& p, std::vector<double>& y) {
   y.assign(2 * sc.nfree, 0.0);
+#pragma omp parallel for schedule(static)
   for (int r = 0; r < sc.nfree; ++r)
     for (int i = 0; i < 2; ++i) {
       double acc = 0;
@@ -651,16 +674,19 @@ int pcg(const Scene2& sc, const std::vector<double>& rhs, std::vector<double>& x
   while (it < sc.cg_iters) {
     bcsr_mul(sc, p, tmp);
     const double alpha = absNew / dot(p, tmp);
+#pragma omp parallel for schedule(static)
     for (int i = 0; i < n; ++i) {
       x[i] += alpha * p[i];
       r[i] -= alpha * tmp[i];
     }
     rn2 = dot(r, r);
     if (rn2 < threshold) break;
+#pragma omp parallel for schedule(static)
     for (int i = 0; i < n; ++i) z[i] = invdiag[i] * r[i];
     const double absOld = absNew;
     absNew = dot(r, z);
     const double beta = absNew / absOld;
+#pragma omp parallel for schedule(static)
     for (int i = 0; i < n; ++i) p[i] = z[i] + beta * p[i];
     ++it;
   }
@@ -674,6 +700,7 @@ void local_solve(Scene2& sc) {
   for (int v = 0; v < sc.nv; ++v)
     if (sc.free_map[v] >= 0)
       for (int d = 0; d < 2; ++d) dfull[2 * v + d] = sc.dx[2 * sc.free_map[v] + d];
+#pragma omp parallel for schedule(static)
   for (int e = 0; e < sc.nt; ++e) {
     double Jdx[4] = {0, 0, 0, 0};
     for (int k = 0; k < 3; ++k)
@@ -714,18 +741,21 @@ double energy(Scene2& sc, double a) {
   for (int i = 0; i < 2 * sc.nv; ++i) diff[i] = full[i] - xt[i] - h2 * sc.fext[i];
   mass_mul(sc, diff, Md);
   const double val = 0.5 * dot(diff, Md);
-  double sp = 0, sq = 0;
+  std::vector<double> epsi(sc.nt), econ(sc.nt);
+#pragma omp parallel for schedule(static)
   for (int e = 0; e < sc.nt; ++e) {
     double si[3];
     for (int i = 0; i < 3; ++i) si[i] = sc.s[3 * e + i] + a * sc.ds[3 * e + i];
-    sp += coef2(sc.mat[e], sc.mu[e], sc.la[e], si).psi * sc.vol[e];
+    epsi[e] = coef2(sc.mat[e], sc.mu[e], sc.la[e], si).psi * sc.vol[e];
     M2 R;
     double st[3];
     polar2(R, sc.defgrad(full, e), false, st, nullptr);
     double c = 0;
     for (int i = 0; i < 3; ++i) c += sc.lam[3 * e + i] * kSym[i] * (st[i] - si[i]);
-    sq += c * sc.vol[e];
+    econ[e] = c * sc.vol[e];
   }
+  const double sp = det_sum(sc.nt, [&](long e) { return epsi[e]; });
+  const double sq = det_sum(sc.nt, [&](long e) { return econ[e]; });
   return val + h2 * sp - sq;
 }
 

@@ -54,10 +54,16 @@ def test_tri2d_line_bookkeeping(monkeypatch):
     monkeypatch.setattr(mfem_gb300.build, "build", lambda *a, **k: None)
     monkeypatch.setattr(mfem_gb300.tri2d, "Tri2dScene", FakeScene)
     monkeypatch.setattr(mfem_gb300._lib, "load", lambda *a, **k: None)
-    args = argparse.Namespace(sheet=16, steps=4, warmup=3, no_e2e=True, no_cpu_baseline=False)
+    args = argparse.Namespace(sheet=16, steps=4, warmup=3, no_e2e=True, no_cpu_baseline=False,
+                              cpu_threads=2)
     out = io.StringIO()
-    with redirect_stdout(out):
-        assert bench.run_tri2d(args) == 0
+    try:
+        with redirect_stdout(out):
+            assert bench.run_tri2d(args) == 0
+    finally:
+        import os
+        import oracle
+        oracle.set_threads(os.cpu_count())
     line = json.loads(out.getvalue().strip().splitlines()[-1])
     assert line["config"]["workload"] == "sheet2d_16x4_128tris"
     assert line["value"] == pytest.approx(4 / (sum(2.0 + 0.01 * k for k in range(4, 8)) / 1e3))
@@ -67,4 +73,4 @@ def test_tri2d_line_bookkeeping(monkeypatch):
     assert roof["frac"] == pytest.approx(roof["achieved"] / roof["peak"])
     assert line["kernels"]["t2_pcg"]["launches"] == 12
     cb = line["cpu_baseline"]
-    assert cb["kind"] == "port" and cb["cores"] == 1 and cb["value"] > 0
+    assert cb["kind"] == "port" and cb["cores"] == 2 and cb["value"] > 0

@@ -7,6 +7,8 @@ The reference holds no 2-D test, so these pin the restatement by finite
 differences, by the reference's generated energy expressions written out
 again here, and by conservation laws of the whole step.
 """
+import os
+
 import numpy as np
 import pytest
 
@@ -245,3 +247,17 @@ def test_bc_scripts_step(bc):
         st = sc.step()
         assert st.status in (abi.OK, abi.ERR_CG_MAXITER, abi.ERR_LS_FAILED)
     assert np.isfinite(sc.get_state()["x"]).all()
+
+
+def test_results_do_not_depend_on_the_thread_count():
+    """Element loops run in parallel; every sum is a fixed-order chunked sum."""
+    out = []
+    for threads in (1, 4):
+        oracle.set_threads(threads)
+        sc = oracle.OracleTri2d(tri2d_spec(40, 10))
+        for _ in range(2):
+            sc.step()
+        out.append(sc.get_state())
+    oracle.set_threads(os.cpu_count())
+    for k in ("x", "v", "s", "R"):
+        assert np.array_equal(out[0][k], out[1][k]), k
