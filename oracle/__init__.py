@@ -77,6 +77,7 @@ def lib():
         L.oracle2d_get_system.argtypes = [C.c_void_p, _ip, _ip, _dp, _dp]
         L.oracle2d_energy.argtypes = [C.c_void_p, C.c_double]
         L.oracle2d_energy.restype = C.c_double
+        L.oracle2d_direction.argtypes = [C.c_void_p, _dp, _dp, _dp, _ip]
         _lib = L
     return _lib
 
@@ -354,3 +355,13 @@ class OracleTri2d:
 
     def energy(self, alpha):
         return lib().oracle2d_energy(self._h, alpha)
+
+    def direction(self):
+        """(dx per vertex, ds, lambda, PCG iterations) of one Newton
+        iteration at the current state, without stepping."""
+        dx = np.zeros(2 * self.n_vertices)
+        ds = np.zeros(3 * self.n_tris)
+        la = np.zeros(3 * self.n_tris)
+        it = C.c_int32()
+        lib().oracle2d_direction(self._h, _p(dx), _p(ds), _p(la), C.byref(it))
+        return dx.reshape(-1, 2), ds.reshape(-1, 3), la.reshape(-1, 3), it.value

@@ -96,6 +96,10 @@ int oracle2d_elem_update(void* scene, const double* x, double h, double* R, doub
                          double* gl);
 int oracle2d_get_system(void* scene, int* row_ptr, int* col, double* val, double* rhs);
 double oracle2d_energy(void* scene, double alpha);
+/* One Newton direction at the current state, without stepping: the system,
+ * its PCG solve and the local solve.  dx: 2*n_vertices (0 at pinned
+ * vertices), ds and la: 3*n_tris. */
+int oracle2d_direction(void* scene, double* dx, double* ds, double* la, int* iters);
 
 #ifdef __cplusplus
 }

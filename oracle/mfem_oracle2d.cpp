@@ -1055,5 +1055,23 @@ int oracle2d_get_system(void* scene, int* row_ptr, int* col, double* val, double
 double oracle2d_energy(void* scene, double alpha) {
   return energy(*static_cast<Scene2*>(scene), alpha);
 }
+int oracle2d_direction(void* scene, double* dx, double* ds, double* la, int* iters) {
+  Scene2& sc = *static_cast<Scene2*>(scene);
+  std::vector<double> full;
+  int st = update_system(sc, full);
+  int it = 0;
+  double err = 0;
+  const int s2 = pcg(sc, sc.rhs, sc.dx, &it, &err);
+  if (st == MFEM_OK) st = s2;
+  local_solve(sc);
+  if (dx)
+    for (int v = 0; v < sc.nv; ++v)
+      for (int d = 0; d < 2; ++d)
+        dx[2 * v + d] = sc.free_map[v] >= 0 ? sc.dx[2 * sc.free_map[v] + d] : 0.0;
+  if (ds) std::memcpy(ds, sc.ds.data(), 8 * sc.ds.size());
+  if (la) std::memcpy(la, sc.lam.data(), 8 * sc.lam.size());
+  if (iters) *iters = it;
+  return st;
+}
 
 }  // extern "C"

@@ -261,3 +261,71 @@ def test_results_do_not_depend_on_the_thread_count():
     oracle.set_threads(os.cpu_count())
     for k in ("x", "v", "s", "R"):
         assert np.array_equal(out[0][k], out[1][k]), k
+
+
+def test_newton_direction_solves_the_linearised_kkt_system():
+    """The direction that the Schur system and the local solve produce
+    satisfies the linearised KKT conditions of the mixed problem, checked
+    with D = ds/dF from central differences of polar_svd<2>'s s (not the
+    dsvd route), B = Jloc from dphi/dX, the material's H = h^2 hess psi and
+    g = h^2 grad psi, and the P1 mass written out again here:
+      M (x + dx - x~ - h^2 f) - sum_e vol_e B_e^T D_e^T Sym la_e = 0  (free rows)
+      Sym la_e + H_e ds_e + g_e = 0
+      ds_e = S_e(x) - s_e + D_e B_e dx_e."""
+    rng = np.random.default_rng(21)
+    V0, T = square_grid(6, 3, 0.1)
+    Vi = V0 + 0.015 * rng.uniform(-1, 1, V0.shape)
+    sp = tri2d_spec(6, 3, V_init=Vi, iterative_solver_tolerance=1e-13,
+                    max_iterative_solver_iters=20000)
+    sc = oracle.OracleTri2d(sp)
+    sc.step()                      # so that s differs from S(x) and v from 0
+    st = sc.get_state()
+    x, v, s = st["x"], st["v"], st["s"]
+    h = sp.dt
+    xt = x + h * v                 # BDF1: x~ = x + h v
+    dx, ds, la, _ = sc.direction()
+    sym = np.array([1.0, 1.0, 2.0])
+    nv, nt = len(V0), len(T)
+    M = np.zeros((nv, nv))
+    rhsA = np.zeros((nv, 2))
+    lam, mu = sp.lam[0], sp.mu[0]
+    f = np.array([0.0, float(np.float32(-9.8))])
+    worst_b = worst_c = 0.0
+    for e in range(nt):
+        X = V0[T[e]]
+        Dm = np.stack([X[1] - X[0], X[2] - X[0]], axis=1)
+        vol = np.linalg.det(Dm)
+        Di = np.linalg.inv(Dm)
+        dX = np.vstack([-Di.sum(axis=0), Di[0], Di[1]])        # dphi_k/dX_c
+        for a in range(3):
+            for b in range(3):
+                M[T[e, a], T[e, b]] += 1000.0 * vol / 12 * (2 if a == b else 1)
+        B = np.zeros((4, 6))
+        for k in range(3):
+            for c in range(2):
+                for r in range(2):
+                    B[r + 2 * c, 2 * k + r] = dX[k, c]
+        xe = x[T[e]].ravel()
+        Fv = B @ xe
+        D = np.zeros((3, 4))
+        eps = 1e-7
+        for c in range(4):
+            d = np.zeros(4)
+            d[c] = eps
+            sp_ = oracle.polar2((Fv + d).reshape(2, 2, order="F"), False)[1]
+            sm_ = oracle.polar2((Fv - d).reshape(2, 2, order="F"), False)[1]
+            D[:, c] = (sp_ - sm_) / (2 * eps)
+        S = oracle.polar2(Fv.reshape(2, 2, order="F"), False)[1]
+        _, g, H = oracle.material2(abi.MATERIAL_SNH, mu, lam, s[e])
+        g, H = h * h * g, h * h * H
+        rb = sym * la[e] + H @ ds[e] + g
+        worst_b = max(worst_b, np.abs(rb).max() / (np.abs(g).max() + np.abs(H @ ds[e]).max()))
+        rc = ds[e] - (S - s[e] + D @ B @ dx[T[e]].ravel())
+        worst_c = max(worst_c, np.abs(rc).max() / max(np.abs(ds[e]).max(), 1e-12))
+        rhsA[T[e]] -= vol * (B.T @ D.T @ (sym * la[e])).reshape(3, 2)
+    assert worst_b < 1e-9
+    assert worst_c < 1e-6
+    ra = M @ (x + dx - xt - h * h * f) + rhsA
+    free = V0[:, 0] <= V0[:, 0].max() - 0.01 * np.ptp(V0[:, 0])
+    scale = np.abs(M @ (x - xt - h * h * f)).max()
+    assert np.abs(ra[free]).max() < 1e-6 * scale
