@@ -12,6 +12,10 @@ kat_dsvd.json
 c1_oracle_fp64.npz
     Positions of the FP64 oracle on the 200-tet beam after 1, 10 and 100
     steps (a regression pin of the oracle itself).
+tri2d_oracle_fp64.npz
+    Positions of the FP64 2-D oracle on a 10 x 3 hanging sheet (60
+    triangles, the settings of scenes/2D/square.json) after 1 and 10 steps
+    (a regression pin of the 2-D oracle).
 
 Run from the repository root:  python tests/golden/make_golden.py
 """
@@ -36,6 +40,29 @@ def eigen_random3(libc):
     return m
 
 
+def tri2d_sheet_spec():
+    from mfem_gb300 import abi
+    from mfem_gb300.desc import Tri2dSpec
+    from mfem_gb300.meshgen import enu_to_lame, square_grid
+    V, T = square_grid(10, 3, 0.1)
+    lam, mu = enu_to_lame(1e5, 0.45)
+    return Tri2dSpec(V_rest=V, tris=T, mu=np.full(len(T), mu), lam=np.full(len(T), lam),
+                     density_const=1000.0, bc_type=abi.BC_HANGENDS, bc_ratio=0.01, bc_axis=0,
+                     dt=0.0333, max_newton_iterations=4, iterative_solver_tolerance=1e-12,
+                     max_iterative_solver_iters=10000)
+
+
+def write_tri2d():
+    import oracle
+    sc = oracle.OracleTri2d(tri2d_sheet_spec())
+    out = {}
+    for step in range(1, 11):
+        sc.step()
+        if step in (1, 10):
+            out[f"x_{step}"] = sc.get_state()["x"]
+    np.savez_compressed(os.path.join(HERE, "tri2d_oracle_fp64.npz"), **out)
+
+
 def main():
     libc = ctypes.CDLL("libc.so.6")
     libc.srand(1)
@@ -57,6 +84,7 @@ def main():
         if step in (1, 10, 100):
             out[f"x_{step}"] = sc.get_state()["x"]
     np.savez_compressed(os.path.join(HERE, "c1_oracle_fp64.npz"), **out)
+    write_tri2d()
     print("written")
 
 

@@ -329,3 +329,21 @@ def test_newton_direction_solves_the_linearised_kkt_system():
     free = V0[:, 0] <= V0[:, 0].max() - 0.01 * np.ptp(V0[:, 0])
     scale = np.abs(M @ (x - xt - h * h * f)).max()
     assert np.abs(ra[free]).max() < 1e-6 * scale
+
+
+def test_tri2d_golden_regression():
+    """The 2-D oracle against its committed fixture
+    (tests/golden/make_golden.py: write_tri2d)."""
+    import sys
+    gold_dir = os.path.join(os.path.dirname(__file__), "golden")
+    sys.path.insert(0, gold_dir)
+    try:
+        import make_golden
+    finally:
+        sys.path.remove(gold_dir)
+    gold = np.load(os.path.join(gold_dir, "tri2d_oracle_fp64.npz"))
+    sc = oracle.OracleTri2d(make_golden.tri2d_sheet_spec())
+    for step in range(1, 11):
+        sc.step()
+        if step in (1, 10):
+            assert np.allclose(sc.get_state()["x"], gold[f"x_{step}"], atol=1e-10, rtol=0)
