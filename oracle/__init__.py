@@ -21,7 +21,8 @@ _ip = C.POINTER(C.c_int32)
 def build(force=False):
     """Compiles the oracle with the Makefile beside this file."""
     srcs = [os.path.join(_HERE, f) for f in ("mfem_oracle.cpp", "mfem_oracle2d.cpp",
-                                             "mfem_oracle.h", "Makefile")]
+                                             "mfem_oracle.h", "Makefile",
+                                             os.path.join("..", "include", "mfem_gb300.h"))]
     if force or not os.path.exists(_LIB_PATH) or \
             os.path.getmtime(_LIB_PATH) < max(os.path.getmtime(s) for s in srcs):
         subprocess.run(["make", "-s", "-C", _HERE], check=True)
