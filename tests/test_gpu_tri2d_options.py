@@ -16,7 +16,7 @@ def test_density_velocity_and_pin_mask(gpu_lib):
     sp.density = 500.0 + 1000.0 * rng.uniform(size=nt)
     sp.v_init = 0.2 * rng.uniform(-1, 1, (nv, 2))
     fixed = np.zeros(nv, np.int32)
-    fixed[[0, 10]] = 1                      # two corners of the left edge
+    fixed[[0, 10]] = 1                      # the two bottom corners
     sp.is_fixed = fixed
     so, sg, g = _run_pair(sp, 4)
     assert np.abs(sg["x"] - so["x"]).max() < 1e-8 * _bbox(so["x"])
