@@ -17,11 +17,16 @@ One JSON line on rank 0:
               launch time (CUDA events around every launch, in a replay of the
               timed steps from the same state: the events slow the step, so
               `value` comes from the run without them)
-  cpu_baseline  the FP64 oracle port on the host cores (bounded sample): one
-              Newton iteration of the same scene without its PCG and one PCG
-              iteration, combined with this run's iterations per step
-  --impl reference  the same oracle port as the reference's CPU arm, with the
-              oracle's own iteration counts (oracle/calibration.json).
+  error_vs_fp64  (mixed path) max |x - x_fp64| / bbox diagonal per step
+              against the all-FP64 GPU path: each step retaken in FP64 from
+              the mixed state before it, and an FP64 trajectory alongside
+  residual_true_pcg  |b - A dx| / |b| of one solve of the PCG form the step
+              runs, beside the recursive estimate it stops on
+  cpu_baseline  the FP64 oracle port on the host cores: whole timesteps from
+              the GPU scene's warmed state, timed with the host clock
+              (about --cpu-budget seconds, at least 3 steps)
+  --impl reference  the same oracle port as the reference's CPU arm: W
+              untimed steps from rest, then K whole timesteps timed.
 
 Multi-GPU (torchrun): independent replicas, one scene per rank (the path has
 no exchange step); value = N * steps / max over ranks of the timed seconds.
@@ -68,6 +73,17 @@ def parse():
     ap.add_argument("--no-batch", action="store_true",
                     help="skip the batched-vs-plain measurement on the 64-scene mix")
     ap.add_argument("--batch-steps", type=int, default=3)
+    ap.add_argument("--no-error", action="store_true",
+                    help="skip the error-vs-FP64 replay and the true PCG residual")
+    ap.add_argument("--error-steps", type=int, default=10,
+                    help="steps of the error-vs-FP64 replay (at most --steps)")
+    ap.add_argument("--cpu-budget", type=float, default=25.0,
+                    help="seconds of whole CPU timesteps in the cpu_baseline leg (at least 3 steps)")
+    ap.add_argument("--ref-budget", type=float, default=300.0,
+                    help="seconds of timed steps in the reference arm before it stops early")
+    ap.add_argument("--c2-reading", default="jittered-rest", choices=["jittered-rest", "perturbed-initial"],
+                    help="C2's 'initial vertex positions perturbed': a jittered rest mesh starting "
+                         "at rest, or a regular rest grid with perturbed (pre-strained) initial positions")
     ap.add_argument("--cpu-threads", type=int, default=0)
     ap.add_argument("--pcg-kernel", default="auto", choices=["persistent", "split", "fused", "auto"],
                     help="auto: the batch picks fused or split by its PCG tile count")
@@ -260,7 +276,10 @@ def make_spec(args, precision):
     if args.config == "c3":
         return configs.stress_c3(**kw), "stress_c3_135k" + tag
     n = args.size
-    return configs.cube_c2(n=n, **kw), f"cube_c2_{n}^3_{5 * n ** 3}tets" + tag
+    literal = args.c2_reading == "perturbed-initial"
+    reading = "_perturbed_initial" if literal else "_jittered_rest"
+    return (configs.cube_c2(n=n, perturb_initial_only=literal, **kw),
+            f"cube_c2_{n}^3_{5 * n ** 3}tets{reading}" + tag)
 
 
 def scene_sizes(spec, scene):
@@ -277,66 +296,87 @@ def scene_sizes(spec, scene):
     return dict(nt=T.shape[0], nv=nv, nf=scene.n_free, nnzb=scene.nnzb, n_inc=n_inc, nnz_m=nnz_m)
 
 
-# ------------------------------------------------------------ CPU sample --
-def cpu_costs(spec, threads, samples, warmup, budget_s):
-    """FP64 oracle on the host cores: seconds of one Newton iteration without
-    its PCG (timed from the same state every sample) and of one PCG iteration
-    (one solve of that Newton system).  Sampling stops early once budget_s
-    has passed, keeping at least one timed sample."""
-    import copy
+# ------------------------------------------------------------ CPU steps --
+def cpu_steps(spec, threads, budget_s, min_steps, max_steps, warmup=0, state=None):
+    """Whole timesteps of the FP64 oracle on the host cores, each timed with
+    the host clock: `warmup` untimed steps, then timed steps until max_steps
+    have run or budget_s has passed (at least min_steps).  From `state` (x,
+    v, s, R of a scene, e.g. the GPU scene's warmed state) when given, else
+    from the workload's initial state."""
     import oracle
-    oracle.set_threads(threads)
-    s = copy.copy(spec)
-    s.max_newton_iterations = 1
-    sc = oracle.OracleScene(s)
-    state0 = sc.get_state()
-    _, _, _, rhs = sc.get_system()
-    t = time.perf_counter()
-    _, cg_its, _ = sc.pcg(rhs)
-    t_cg = (time.perf_counter() - t) / max(cg_its, 1)
-    t_start = time.perf_counter()
-    rest = []
-    for i in range(warmup + samples):
-        sc.set_state(**state0)
+    threads = oracle.set_threads(threads)
+    t_make = time.perf_counter()
+    sc = oracle.OracleScene(spec)
+    if state is not None:
+        sc.set_state(x=state["x"], v=state["v"], s=state["s"], R=state["R"])
+    make_s = time.perf_counter() - t_make
+    for _ in range(warmup):
+        sc.step()
+    secs, newton, cg = [], [], []
+    t0 = time.perf_counter()
+    while len(secs) < max_steps and (len(secs) < min_steps or time.perf_counter() - t0 < budget_s):
         t = time.perf_counter()
         st = sc.step()
-        dt = time.perf_counter() - t
-        if i >= warmup:
-            rest.append(max(dt - st.cg_iterations * t_cg, 0.0))
-        if rest and time.perf_counter() - t_start > budget_s:
-            break
-    return {"t_newton": float(np.mean(rest)), "t_cg": t_cg, "samples": len(rest),
-            "pcg_iterations_timed": cg_its, "threads": threads}
+        secs.append(time.perf_counter() - t)
+        newton.append(int(st.newton_iterations))
+        cg.append(int(st.cg_iterations))
+    return {"threads": threads, "steps": len(secs), "seconds": float(sum(secs)), "step_s": secs,
+            "newton_iterations": newton, "cg_iterations": cg, "warmup": warmup,
+            "scene_build_s": make_s, "n_free": sc.n_free, "nnzb": sc.nnzb}
 
 
-def cpu_line(costs, newton, cgits, workload, where):
-    t_step = newton * costs["t_newton"] + cgits * costs["t_cg"]
-    return {"value": 1.0 / t_step, "unit": UNIT, "cores": costs["threads"], "kind": "port",
-            "sample": (f"FP64 oracle on {costs['threads']} host threads, {workload}: one Newton "
-                       f"iteration without its PCG {costs['t_newton']:.3f} s (mean of "
-                       f"{costs['samples']} from the same state), one Jacobi-PCG iteration "
-                       f"{1e3 * costs['t_cg']:.2f} ms (from a {costs['pcg_iterations_timed']}-iteration "
-                       f"solve); per step = {newton:.2f} Newton x {costs['t_newton']:.3f} s + "
-                       f"{cgits:.0f} PCG x {1e3 * costs['t_cg']:.2f} ms ({where})")}
+def cpu_line(res, workload, start):
+    value = res["steps"] / res["seconds"]
+    return {"value": value, "unit": UNIT, "cores": res["threads"], "kind": "port",
+            "steps_timed": res["steps"],
+            "sample": (f"FP64 oracle (the project's C++/OpenMP restatement of the reference step) on "
+                       f"{res['threads']} host threads, {workload}: {res['steps']} whole timesteps from "
+                       f"{start}, {res['seconds']:.1f} s in all ({res['seconds'] / res['steps']:.2f} s a "
+                       f"step; {np.mean(res['newton_iterations']):.2f} Newton and "
+                       f"{np.mean(res['cg_iterations']):.0f} PCG iterations a step)"),
+            "newton_iterations": res["newton_iterations"], "cg_iterations": res["cg_iterations"],
+            "step_s": [round(t, 3) for t in res["step_s"]]}
+
+
+def workload_config(args, spec, workload, nf, nnzb, ws):
+    """The `config` object of both arms (the same workload, whatever the arm
+    computes in)."""
+    big = args.config == "c2" and args.size >= 40
+    return {"workload": workload, "tets": int(spec.n_tets), "vertices": int(spec.n_vertices),
+            "free_dofs": 3 * int(nf), "blocks": int(nnzb), "solver": args.solver,
+            "formulation": args.formulation,
+            "newton_residual_tolerance": spec.newton_residual_tolerance,
+            "pcg_tolerance": spec.iterative_solver_tolerance,
+            "l2": ("working set > L2 (about 1 GB per step); no flush" if big else
+                   "working set within L2; no flush"),
+            "parallelism": f"replicas{ws}"}
 
 
 def run_reference(args):
+    """The reference arm: the FP64 oracle port (the reference itself does not
+    build here) stepping the same workload on all host cores, W untimed
+    warm-up steps from the initial state, then K whole timesteps timed."""
     ws, rank, _, pg = dist_setup()
     if rank != 0:
         return 0
     import oracle  # noqa: F401  (the reference arm is the FP64 port on the host cores)
     threads = args.cpu_threads or os.cpu_count()
     spec, workload = make_spec(args, "fp64")
-    newton, cgits, where = _iteration_counts(args)
-    costs = cpu_costs(spec, threads, args.steps, min(args.warmup, 1), budget_s=150.0)
-    cb = cpu_line(costs, newton, cgits, workload, where)
+    res = cpu_steps(spec, threads, budget_s=args.ref_budget, min_steps=min(args.steps, 3),
+                    max_steps=args.steps, warmup=args.warmup)
+    cb = cpu_line(res, workload, f"the state after {args.warmup} untimed steps from rest")
     value = cb["value"]
     line = {
         "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws,
-        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000.0 / value,
-        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
-        "data": "synthetic", "config": {"workload": workload, "precision": "fp64",
-                                        "solver": args.solver},
+        "steps": res["steps"], "steps_requested": args.steps, "warmup": args.warmup,
+        "ms_per_step": 1000.0 / value, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": workload_config(args, spec, workload, res["n_free"], res["nnzb"], ws),
+        "precision": "fp64",
+        "p50_ms": 1000.0 * float(np.percentile(res["step_s"], 50)),
+        "p99_ms": 1000.0 * float(np.percentile(res["step_s"], 99)),
+        "newton_iterations_per_step": float(np.mean(res["newton_iterations"])),
+        "cg_iterations_per_step": float(np.mean(res["cg_iterations"])),
         "cpu_baseline": cb,
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
@@ -344,21 +384,55 @@ def run_reference(args):
     return 0
 
 
-def _iteration_counts(args):
-    """Newton and PCG iterations per step of the timed window (steps
-    warmup+1 .. warmup+steps), measured by the FP64 oracle
-    (oracle/calibration.json, made by oracle/calibrate.py)."""
-    p = os.path.join(ROOT, "oracle", "calibration.json")
-    key = f"{args.config}_{args.size}" if args.config == "c2" else args.config
-    if os.path.exists(p):
-        d = json.load(open(p)).get(key)
-        if d and "newton_iterations" in d:
-            its, cgs = d["newton_iterations"], d["cg_iterations"]
-            w = its[args.warmup:args.warmup + args.steps] or its
-            c = cgs[args.warmup:args.warmup + args.steps] or cgs
-            return (float(np.mean(w)), float(np.mean(c)),
-                    f"oracle counts of steps {args.warmup + 1}..{args.warmup + len(w)}")
-    return 4.0, 1000.0, "no calibration: assumed 4 Newton and 1000 PCG iterations per step"
+def error_vs_fp64(args, spec_fp64, scene, state0, steps):
+    """Error of the mixed path against the all-FP64 GPU path, outside the
+    timed region.  same_state: each step taken in FP64 from the mixed
+    path's state before it; trajectory: an FP64 scene stepped from the same
+    starting state alongside.  Both as max |x - x_fp64| over the bounding-box
+    diagonal of x_fp64, per step."""
+    from mfem_gb300 import gpu
+    f64 = gpu.Scene(spec_fp64)
+    traj = gpu.Scene(spec_fp64)
+    scene.set_state(x=state0["x"], v=state0["v"], s=state0["s"], R=state0["R"])
+    traj.set_state(x=state0["x"], v=state0["v"], s=state0["s"], R=state0["R"])
+    same, along, t64 = [], [], []
+    for _ in range(steps):
+        before = scene.get_state()
+        scene.step()
+        xm = scene.positions()
+        f64.set_state(x=before["x"], v=before["v"], s=before["s"], R=before["R"])
+        t = time.perf_counter()
+        f64.step()
+        t64.append(time.perf_counter() - t)
+        x64 = f64.positions()
+        diag = float(np.linalg.norm(np.ptp(x64, axis=0)))
+        same.append(float(np.abs(xm - x64).max()) / diag)
+        traj.step()
+        xt = traj.positions()
+        along.append(float(np.abs(xm - xt).max()) / float(np.linalg.norm(np.ptp(xt, axis=0))))
+    f64.close()
+    traj.close()
+    return {"metric": "max |x - x_fp64| / bbox diagonal", "steps": steps,
+            "same_state_max": max(same), "same_state": same,
+            "trajectory_max": max(along), "trajectory": along,
+            "fp64_gpu_step_s": float(np.mean(t64)),
+            "note": "same_state: one FP64 GPU step from the mixed state before each step; "
+                    "trajectory: FP64 GPU scene stepped from the same starting state"}
+
+
+def true_pcg_residual(scene):
+    """The true residual |b - A dx| / |b| of one solve of the scene's PCG form
+    on the system assembled at the scene's current state (A as the device
+    holds it), beside the recursive estimate the solver stops on."""
+    rp, col, val, rhs = scene.get_system()
+    dx, it, rec = scene.pcg(rhs)
+    n = len(rp) - 1
+    rows = np.repeat(np.arange(n), np.diff(rp))
+    y = np.zeros((n, 3))
+    np.add.at(y, rows, np.einsum("kij,kj->ki", val, dx.reshape(-1, 3)[col]))
+    true = float(np.linalg.norm(rhs - y.ravel()) / np.linalg.norm(rhs))
+    return {"true": true, "recursive": float(rec), "iterations": int(it),
+            "tolerance": float(scene.spec.iterative_solver_tolerance)}
 
 
 # ----------------------------------------------------------------- ours --
@@ -471,19 +545,16 @@ def run_ours(args):
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": 1000.0 * dev_s_max / args.steps,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-        "dtype": "f32+f64" if args.precision == "mixed" else "f64",
+        # mixed: FP32 element work, matrix and SpMV; positions, s, the residual
+        # chain and every reduction in float-float (df64, ~48-bit significand,
+        # FP32 exponent range)
+        "dtype": "f32+df64" if args.precision == "mixed" else "f64",
         "data": "synthetic",
-        "config": {"workload": workload, "tets": sizes["nt"], "vertices": sizes["nv"],
-                   "free_dofs": 3 * sizes["nf"], "blocks": sizes["nnzb"],
-                   "precision": args.precision, "solver": args.solver,
-                   "formulation": args.formulation, "pcg_kernel": args.pcg_kernel,
-                   "pcg_kernel_resolved": ("fused" if kstats.get("k_cgf_iter", (0, 0))[1] else
-                                           "split" if kstats.get("k_cg_spmv", (0, 0))[1] else
-                                           "persistent" if kstats.get("k_cg_solve", (0, 0))[1] else None),
-                   "newton_residual_tolerance": spec.newton_residual_tolerance,
-                   "pcg_tolerance": spec.iterative_solver_tolerance,
-                   "l2": "working set > L2 (about 1 GB per step)",
-                   "parallelism": f"replicas{ws}"},
+        "config": workload_config(args, spec, workload, sizes["nf"], sizes["nnzb"], ws),
+        "precision": args.precision, "pcg_kernel": args.pcg_kernel,
+        "pcg_kernel_resolved": ("fused" if kstats.get("k_cgf_iter", (0, 0))[1] else
+                                "split" if kstats.get("k_cg_spmv", (0, 0))[1] else
+                                "persistent" if kstats.get("k_cg_solve", (0, 0))[1] else None),
         "p50_ms": float(np.percentile(ms, 50)), "p99_ms": float(np.percentile(ms, 99)),
         "wall_ms_per_step": 1000.0 * wall / args.steps,
         "newton_iterations_per_step": newton, "cg_iterations_per_step": cgits,
@@ -492,12 +563,23 @@ def run_ours(args):
         "profiled_replay_ms_per_step": 1000.0 * prof_s / args.steps,
         "kernels": per_kernel,
     }
+    # ---- error against the all-FP64 GPU path and the true PCG residual
+    # (outside the timed region)
+    if args.precision == "mixed" and not args.no_error and args.formulation == "mixed-stretch" \
+            and args.solver != "minres-indefinite-block":
+        spec64, _ = make_spec(args, "fp64")
+        line["error_vs_fp64"] = error_vs_fp64(args, spec64, scene, state0,
+                                              min(args.steps, args.error_steps))
+    if not args.no_error and args.solver != "minres-indefinite-block":
+        line["residual_true_pcg"] = true_pcg_residual(scene)
     if rank == 0 and ws == 1 and not args.no_cpu_baseline:
+        # whole FP64 oracle timesteps from the GPU scene's warmed state (the
+        # state the timed region started from)
         threads = args.cpu_threads or os.cpu_count()
         ref_spec, _ = make_spec(args, "fp64")
-        costs = cpu_costs(ref_spec, threads, 1, 0, budget_s=60.0)
-        line["cpu_baseline"] = cpu_line(costs, newton, cgits, workload,
-                                        "this run's GPU iteration counts")
+        res = cpu_steps(ref_spec, threads, budget_s=args.cpu_budget, min_steps=min(3, args.steps),
+                        max_steps=args.steps, state=state0)
+        line["cpu_baseline"] = cpu_line(res, workload, f"the GPU scene's state after {args.warmup} steps")
     scene.close()
     if rank == 0 and ws == 1 and not args.no_batch and args.config == "c2":
         from mfem_gb300 import configs

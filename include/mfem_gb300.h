@@ -281,9 +281,12 @@ int mfem_gpu_scene_pcg(mfem_scene* scene, const double* b, double* dx,
  * from its own budget or pool, or a real-time loop where cudaMalloc's
  * implicit device synchronisation would stall other streams.
  * The first call on a device (with that device current) looks up the
- * scratch address with cudaGetSymbolAddress; make it before any stream
- * capture.  Calls on one device share the scratch, so they are serialised
- * by a process-wide lock held until the call's stream has drained.  All
+ * scratch address with cudaGetSymbolAddress; that first call should come
+ * before any stream capture.  Every call waits for its stream
+ * (cudaStreamSynchronize) and copies the solver's scalars to the host
+ * between chunks of iterations.  Calls on one device share the scratch,
+ * so overlapping calls would race: they are serialised by a per-device
+ * lock held until the call's stream has drained.  All
  * pointers must be device memory of the current device; `stream` is a
  * cudaStream_t (NULL: the legacy default stream).  Returns iterations and
  * |r|/|b| like mfem_gpu_scene_pcg. */

@@ -38,16 +38,24 @@ def beam_c1(precision=abi.PRECISION_FP64, **kw):
     return spec
 
 
-def cube_c2(n=60, spacing=0.01, precision=abi.PRECISION_MIXED, seed=SEED, **kw):
-    """The vertex perturbation jitters the mesh: rest and initial positions are
-    the perturbed grid, so the body starts undeformed and sags under gravity
-    from its pinned bottom layer (j = 0 of the grid)."""
+def cube_c2(n=60, spacing=0.01, precision=abi.PRECISION_MIXED, seed=SEED, perturb_initial_only=False,
+            **kw):
+    """By default the vertex perturbation jitters the mesh: rest and initial
+    positions are the perturbed grid, so the body starts undeformed and sags
+    under gravity from its pinned bottom layer (j = 0 of the grid).  With
+    perturb_initial_only the rest mesh is the regular grid and only the
+    initial positions are perturbed, so the body starts pre-strained."""
     V, T = cube_grid(n, n, n, spacing)
     pinned = face_mask(V, 1, "min")
     rng = np.random.default_rng(seed)
-    V = V + rng.uniform(-0.1 * spacing, 0.1 * spacing, size=V.shape)
+    Vp = V + rng.uniform(-0.1 * spacing, 0.1 * spacing, size=V.shape)
+    V_init = None
+    if perturb_initial_only:
+        V_init = Vp
+    else:
+        V = Vp
     lam, mu = enu_to_lame(1e5, 0.45)
-    spec = SceneSpec(V_rest=V, tets=T, mu=np.full(len(T), mu), lam=np.full(len(T), lam),
+    spec = SceneSpec(V_rest=V, tets=T, mu=np.full(len(T), mu), lam=np.full(len(T), lam), V_init=V_init,
                      is_fixed=pinned, density_const=1000.0, dt=1.0 / 60.0,
                      body_force=(0.0, -9.8, 0.0), max_newton_iterations=40,
                      iterative_solver_tolerance=1e-4, max_iterative_solver_iters=500,

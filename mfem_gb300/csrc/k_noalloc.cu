@@ -18,8 +18,9 @@
 // is written before it is read within a call.
 //
 // Calls on one device share that scratch, so two calls that overlapped on
-// one device would race.  The entry point therefore holds a process-wide
-// lock from its first launch until its stream has drained.
+// one device would race.  The entry point therefore holds that device's
+// lock from its first launch until its stream has drained; calls on
+// different devices use different scratch copies and different locks.
 #include <cuda_runtime.h>
 
 #include <cfloat>
@@ -199,6 +200,9 @@ __global__ void __launch_bounds__(kNaThreads) k_na_init(NaMatrix A, const double
     sc->thr = fmax(tol * tol * rr, DBL_MIN);
     sc->err = rr == 0.0 ? 0.0 : 1.0;
     sc->active = (na_status(sc) == 0 && rr != 0.0 && rr >= sc->thr && max_iters > 0) ? 1 : 0;
+    // No iteration allowed while the residual is above the threshold: the
+    // solve stops on max_iters, as Eigen's NoConvergence.
+    if (na_status(sc) == 0 && rr != 0.0 && rr >= sc->thr && max_iters == 0) sc->status = MFEM_ERR_CG_MAXITER;
     if (!(rr == rr) || !(rz == rz)) sc->status = MFEM_ERR_NONFINITE;
   }
 }
@@ -291,7 +295,7 @@ __global__ void __launch_bounds__(kNaThreads) k_na_update(int n, double* x, NaVi
   }
 }
 
-std::mutex g_na_mu;
+std::mutex g_na_mu[kNaMaxDevices];  // one per device: its scratch copy
 unsigned char* g_na_base[kNaMaxDevices] = {};
 
 bool na_device_pointer(const void* p, int dev) {
@@ -324,7 +328,7 @@ extern "C" int mfem_gpu_bsr_pcg_noalloc(int32_t n_block_rows, int32_t nnzb, cons
       (nnzb > 0 && (!na_device_pointer(col, dev) || !na_device_pointer(val, dev))))
     return MFEM_ERR_INVALID;
 
-  std::lock_guard<std::mutex> lock(g_na_mu);
+  std::lock_guard<std::mutex> lock(g_na_mu[dev]);
   if (!g_na_base[dev]) {  // once per device: the address of the static scratch
     void* p = nullptr;
     if (cudaGetSymbolAddress(&p, g_na_scratch) != cudaSuccess || !p) {
@@ -337,13 +341,17 @@ extern "C" int mfem_gpu_bsr_pcg_noalloc(int32_t n_block_rows, int32_t nnzb, cons
   const NaMatrix A{n_block_rows, nnzb, row_ptr, col, val};
   cudaStream_t st = static_cast<cudaStream_t>(stream);
   const int ntiles = (n_block_rows + kNaThreads - 1) / kNaThreads;
+  // Launch errors are read with cudaPeekAtLastError right after this call's
+  // own launches (it leaves any pending error of the caller's in place);
+  // faults while the kernels run come back from cudaStreamSynchronize.
   if (cudaMemsetAsync(v.sc, 0, sizeof(NaScalars), st) != cudaSuccess) return MFEM_ERR_CUDA;
   k_na_init<<<ntiles, kNaThreads, 0, st>>>(A, b, x, v, max_iters, tol);
+  if (cudaPeekAtLastError() != cudaSuccess) return MFEM_ERR_CUDA;
   NaScalars h{};
   int launched = 0;
   for (;;) {
     if (cudaMemcpyAsync(&h, v.sc, sizeof(h), cudaMemcpyDeviceToHost, st) != cudaSuccess ||
-        cudaStreamSynchronize(st) != cudaSuccess || cudaGetLastError() != cudaSuccess)
+        cudaStreamSynchronize(st) != cudaSuccess)
       return MFEM_ERR_CUDA;
     if (!h.active || launched >= max_iters) break;
     const int c = max_iters - launched < kNaChunk ? max_iters - launched : kNaChunk;
@@ -351,6 +359,7 @@ extern "C" int mfem_gpu_bsr_pcg_noalloc(int32_t n_block_rows, int32_t nnzb, cons
       k_na_spmv<<<ntiles, kNaThreads, 0, st>>>(A, v);
       k_na_update<<<ntiles, kNaThreads, 0, st>>>(n_block_rows, x, v);
     }
+    if (cudaPeekAtLastError() != cudaSuccess) return MFEM_ERR_CUDA;
     launched += c;
   }
   if (iterations) *iterations = h.iter;

@@ -457,6 +457,14 @@ __global__ void __launch_bounds__(kBlock) t2_pcg(T2 d, int max_iter, double tol)
   }
   const double thr = fmax(tol * tol * b2, DBL_MIN);
   double rn2 = b2;
+  if (b2 < thr) {  // Eigen's test before the first iteration: no iteration
+    if (t == 0) {
+      d.scal[SC_CG_IT] = 0;
+      d.scal[SC_CG_RN2] = b2;
+      d.scal[SC_CG_B2] = b2;
+    }
+    return;
+  }
   part = 0;
   for (int i = t; i < n; i += kBlock) {
     const double pi = d.dinv[i] * d.r[i];

@@ -94,6 +94,12 @@ class Scene:
         return dict(x=x.reshape(-1, 3), v=v.reshape(-1, 3), s=s.reshape(-1, 6),
                     R=R.reshape(-1, 9), la=la.reshape(-1, 6))
 
+    def positions(self):
+        """Vertex positions only (3 per vertex, FP64)."""
+        x = np.zeros(3 * self.n_vertices)
+        check(load().mfem_gpu_scene_get_state(self._h, _p(x), None, None, None, None), "get_state")
+        return x.reshape(-1, 3)
+
     def set_state(self, x=None, v=None, s=None, R=None):
         f = lambda a: None if a is None else np.ascontiguousarray(a, dtype=np.float64).ravel()
         x, v, s, R = f(x), f(v), f(s), f(R)

@@ -668,6 +668,11 @@ int pcg(const Scene2& sc, const std::vector<double>& rhs, std::vector<double>& x
   }
   const double threshold = std::max(sc.cg_tol * sc.cg_tol * rhsNorm2, std::numeric_limits<double>::min());
   double rn2 = rhsNorm2;
+  if (rn2 < threshold) {  // Eigen's test before the first iteration
+    *iters = 0;
+    *err = std::sqrt(rn2 / rhsNorm2);
+    return MFEM_OK;
+  }
   for (int i = 0; i < n; ++i) p[i] = invdiag[i] * r[i];
   double absNew = dot(r, p);
   int it = 0;

@@ -57,3 +57,19 @@ def test_all_pinned_scene_follows_its_script(gpu_lib):
         assert sg.status in (abi.OK, abi.ERR_LS_FAILED) and sg.cg_iterations == 0
     assert np.array_equal(g.get_state()["x"], o.get_state()["x"])
     g.close()
+
+
+@pytest.mark.gpu
+def test_pcg_tolerance_above_one_runs_no_iteration(gpu_lib):
+    """Eigen's test before the first iteration: with tol > 1 the threshold
+    tol^2 |b|^2 exceeds |b|^2, so the solve returns dx = 0 after 0
+    iterations, on both sides."""
+    import oracle
+    from mfem_gb300.tri2d import Tri2dScene
+    sp = spec2(6, 2, iterative_solver_tolerance=2.0, max_newton_iterations=2)
+    o, g = oracle.OracleTri2d(sp), Tri2dScene(sp)
+    so, sg = o.step(), g.step()
+    assert so.cg_iterations == 0 and sg.cg_iterations == 0
+    assert sg.status == so.status and sg.newton_iterations == so.newton_iterations
+    assert np.array_equal(g.get_state()["x"], o.get_state()["x"])
+    g.close()

@@ -80,10 +80,17 @@ def test_noalloc_pcg_matches_scene_pcg():
 
     bnorm = np.linalg.norm(rhs)
     xs = []
-    for _ in range(2):  # two calls in a row on the same scratch
+    for call in range(2):  # two calls in a row on the same scratch
+        free_before = torch.cuda.mem_get_info(dev)[0]
         rc, it, err = _noalloc(n, nnzb, d_rp.data_ptr(), d_col.data_ptr(), d_val.data_ptr(),
                                d_b.data_ptr(), d_x.data_ptr(), 3000, TOL)
         assert rc == abi.OK, rc
+        if call > 0:
+            # Nothing was allocated on the device by the call.  (On the first
+            # call the CUDA runtime may still be loading the library's device
+            # code and its static scratch, which is the library's fixed
+            # footprint, not an allocation of the call.)
+            assert torch.cuda.mem_get_info(dev)[0] == free_before
         x = d_x.cpu().numpy()
         assert np.isfinite(x).all()
         assert err <= TOL
@@ -114,6 +121,12 @@ def test_noalloc_pcg_maxiter_and_singular_block():
     rc, it, err = _noalloc(n, nnzb, d_rp.data_ptr(), d_col.data_ptr(), d_val.data_ptr(),
                            d_b.data_ptr(), d_x.data_ptr(), 3, TOL)
     assert rc == abi.ERR_CG_MAXITER and it == 3 and err > TOL
+    # No iteration allowed and b above the threshold: stopped on max_iters,
+    # with x = 0 (Eigen reports NoConvergence here)
+    rc, it, err = _noalloc(n, nnzb, d_rp.data_ptr(), d_col.data_ptr(), d_val.data_ptr(),
+                           d_b.data_ptr(), d_x.data_ptr(), 0, TOL)
+    assert rc == abi.ERR_CG_MAXITER and it == 0 and err == 1.0
+    assert not d_x.any().item()
     # A host pointer is rejected before any launch.
     host_b = np.ascontiguousarray(rhs)
     rc, _, _ = _noalloc(n, nnzb, d_rp.data_ptr(), d_col.data_ptr(), d_val.data_ptr(),
