@@ -244,6 +244,20 @@ int mfem_gpu_batch_kernel_stats(mfem_batch* batch, int kernel, double* total_ms,
                                 int64_t* launches);
 int mfem_gpu_kernel_name(int kernel, char* name, int name_len);
 
+/* ---- kernel shapes (no counterpart in the reference) ---------------------
+ * Shape of the batch's fused PCG iteration: stages = 0 streams the matrix
+ * through registers; 2..4 stage each warp's ELL slots through that many
+ * shared-memory buffers filled by bulk copies (FP64 batches use 2);
+ * keep = 1 marks half of the matrix's L2 lines evict-last, 0 all
+ * evict-first; unroll = 2 (with stages = 4) puts two slots' gathers in
+ * flight together, unroll = 1 one.  FP64 batches use stages <= 2 and
+ * unroll 1.  Every shape computes the same bits; the autotuner picks one
+ * per batch.  Changing the shape re-captures the batch's PCG graph. */
+int mfem_gpu_batch_set_pcg_shape(mfem_batch* batch, int32_t stages, int32_t keep,
+                                 int32_t unroll);
+int mfem_gpu_batch_get_pcg_shape(mfem_batch* batch, int32_t* stages, int32_t* keep,
+                                 int32_t* unroll);
+
 /* ---- per-kernel parity entry points (host buffers in, host buffers out) ----
  * elem_update: MixedStretch::update_rotations + update_derivatives for the
  * current state at positions x (3*n_vertices, full) and time step h
@@ -263,7 +277,11 @@ int mfem_gpu_scene_bcsr_sizes(mfem_scene* scene, int32_t* n_free, int32_t* nnzb)
 int mfem_gpu_scene_get_system(mfem_scene* scene, int32_t* row_ptr,
                               int32_t* col, double* val, double* rhs);
 /* Solves LHS * dx = b with the scene's PCG on the last assembled matrix.
- * b, dx: 3*n_free.  Returns iterations and |r|/|b|. */
+ * b, dx: 3*n_free.  Returns iterations and |r|/|b|.  In the mixed path dx
+ * is the solver's float-float (df64) solution and |r|/|b| the residual it
+ * stopped on: the single-reduction form verifies its recursive residual
+ * against b - A dx before it stops; the two-reduction forms replace the
+ * recursive residual by b - A dx every 25 iterations. */
 int mfem_gpu_scene_pcg(mfem_scene* scene, const double* b, double* dx,
                        int32_t* iterations, double* rel_residual);
 

@@ -510,6 +510,7 @@ struct mfem_batch {
     return cg_hints[std::min(newton_index, (int)cg_hints.size() - 1)];
   }
   int pcg_kernel = MFEM_PCG_KERNEL_PERSISTENT;
+  CgfShape cgf_shape{0, 0, 1};  // shape of the fused PCG iteration (same bits in every shape)
   int minres = 0;  // every scene uses "minres-indefinite-block"
   int fem = 0;     // every scene uses the standard-FEM variable
   int jacobi = 1;  // no scene uses the 3x3 block-Jacobi preconditioner
@@ -829,7 +830,7 @@ int run_pcg_graph(mfem_batch* b, const Launch& Lcg, bool fused) {
     CUDA_OR(cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal), MFEM_ERR_CUDA);
     for (int k = 0; k < len; ++k) {
       if (fused) {
-        launch_cgf_iter(Lcg);
+        launch_cgf_iter(Lcg, b->cgf_shape);
       } else {
         launch_cg_spmv(Lcg);
         launch_cg_update(Lcg);
@@ -845,10 +846,13 @@ int run_pcg_graph(mfem_batch* b, const Launch& Lcg, bool fused) {
     cudaGraphDestroy(g);
     CUDA_OR(ei, MFEM_ERR_CUDA);
   }
+  // the mixed single-reduction form verifies its stop in launches of its
+  // own (at most 4 rounds of two, and one to write the solution)
+  const int max_launch = b->max_cg + (fused && !b->fp64 ? 9 : 0);
   int it = 0, nchunk = 0;
   int reps = std::max(1, (b->cg_hint() + len - 1) / len);
-  while (it < b->max_cg) {
-    for (int r = 0; r < reps && it < b->max_cg; ++r, it += len) {
+  while (it < max_launch) {
+    for (int r = 0; r < reps && it < max_launch; ++r, it += len) {
       CUDA_OR(cudaGraphLaunch(b->cg_graph, b->stream), MFEM_ERR_CUDA);
       if (fused) {
         b->k_launches[MFEM_K_CGF_ITER] += len;
@@ -894,14 +898,15 @@ int run_pcg(mfem_batch* b, const Launch& Lcg) {
   // always has the current chunk queued while the host reads.  Iterations
   // launched after convergence return at once.
   if (!b->profiling) return run_pcg_graph(b, Lcg, fused);
+  const int max_launch = b->max_cg + (fused && !b->fp64 ? 9 : 0);
   int it = 0, nchunk = 0;
   int chunk = std::max(4, b->cg_hint());
-  while (it < b->max_cg) {
-    const int c = std::min(chunk, b->max_cg - it);
+  while (it < max_launch) {
+    const int c = std::min(chunk, max_launch - it);
     for (int k = 0; k < c; ++k, ++it) {
       if (fused) {
         KTimer t(b, MFEM_K_CGF_ITER);
-        launch_cgf_iter(Lcg);
+        launch_cgf_iter(Lcg, b->cgf_shape);
       } else {
         { KTimer t(b, MFEM_K_CG_SPMV); launch_cg_spmv(Lcg); }
         { KTimer t(b, MFEM_K_CG_UPDATE); launch_cg_update(Lcg); }
@@ -1075,6 +1080,10 @@ int batch_build(mfem_scene* const* scenes, int n, mfem_batch** out) {
     b->ntiles[tb] = (int)tabs[tb].size();
     maxt = std::max(maxt, tabs[tb].size());
   }
+  // the fused iteration's matrix staged through two shared-memory buffers
+  // per warp (measured fastest on the 1M-tet cube); the autotuner may
+  // choose another shape for the batch's size class
+  b->cgf_shape = b->fp64 ? CgfShape{0, 0, 1} : CgfShape{2, 0, 1};
   b->pcg_kernel = scenes[0]->cfg.pcg_kernel;
   b->minres = scenes[0]->dev.minres;
   b->fem = scenes[0]->dev.fem;
@@ -1828,6 +1837,30 @@ int mfem_gpu_batch_set_profiling(mfem_batch* b, int enable) {
   return MFEM_OK;
 }
 
+int mfem_gpu_batch_set_pcg_shape(mfem_batch* b, int32_t stages, int32_t keep, int32_t unroll) {
+  if (!b || stages < 0 || stages > 4 || stages == 1 || keep < 0 || keep > 1 || unroll < 1 || unroll > 2 ||
+      (unroll == 2 && stages != 4))
+    return MFEM_ERR_INVALID;
+  if (b->fp64 && stages > 2) stages = 2;
+  if (b->fp64) unroll = 1;
+  if (b->cgf_shape.stages == stages && b->cgf_shape.keep == keep && b->cgf_shape.unroll == unroll) return MFEM_OK;
+  b->cgf_shape = CgfShape{stages, keep, unroll};
+  if (b->cg_graph) {  // captured with the old shape
+    CUDA_OR(cudaStreamSynchronize(b->stream), MFEM_ERR_CUDA);
+    cudaGraphExecDestroy(b->cg_graph);
+    b->cg_graph = nullptr;
+  }
+  return MFEM_OK;
+}
+
+int mfem_gpu_batch_get_pcg_shape(mfem_batch* b, int32_t* stages, int32_t* keep, int32_t* unroll) {
+  if (!b) return MFEM_ERR_INVALID;
+  if (stages) *stages = b->cgf_shape.stages;
+  if (keep) *keep = b->cgf_shape.keep;
+  if (unroll) *unroll = b->cgf_shape.unroll;
+  return MFEM_OK;
+}
+
 int mfem_gpu_batch_kernel_stats(mfem_batch* b, int kernel, double* total_ms, int64_t* launches) {
   if (!b || kernel < 0 || kernel >= MFEM_K_COUNT) return MFEM_ERR_INVALID;
   if (total_ms) *total_ms = b->k_ms[kernel];
@@ -1929,6 +1962,19 @@ int mfem_gpu_scene_bcsr_sizes(mfem_scene* s, int32_t* nf, int32_t* nnzb) {
 
 // Real vector of the device (4 Real per free row, device row order) to
 // FP64 in the reference's free order (3 per row, vertex order).
+// The mixed path's df64 solution vector (4 float pairs per row, device row
+// order) to FP64 in the reference's free order.
+int fetch_rows_df64(const mfem_scene* s, const void* src, double* dst) {
+  const HostMesh& M = s->M;
+  const size_t n8 = 8 * (size_t)M.nf;
+  std::vector<float> f(n8);
+  CUDA_OR(cudaMemcpy(f.data(), src, n8 * 4, cudaMemcpyDeviceToHost), MFEM_ERR_CUDA);
+  for (int r = 0; r < M.nf; ++r)
+    for (int c = 0; c < 3; ++c)
+      dst[3 * (size_t)M.ref_of_row[r] + c] = double(f[8 * (size_t)r + 2 * c]) + double(f[8 * (size_t)r + 2 * c + 1]);
+  return MFEM_OK;
+}
+
 int fetch_rows(const mfem_scene* s, const void* src, double* dst) {
   const HostMesh& M = s->M;
   const size_t n4 = 4 * (size_t)M.nf;
@@ -2024,7 +2070,8 @@ int mfem_gpu_scene_pcg(mfem_scene* s, const double* bvec, double* dx, int32_t* i
   if ((rc = sync_counters(b))) return rc;
   if (b->h_ctr->error) return MFEM_ERR_TIMEOUT;
   CUDA_OR(cudaGetLastError(), MFEM_ERR_CUDA);
-  if ((rc = fetch_rows(s, s->dev.cg_x, dx))) return rc;
+  // the mixed path keeps the solution in df64 (x_e); FP64: x itself
+  if ((rc = s->dev.cg_xe ? fetch_rows_df64(s, s->dev.cg_xe, dx) : fetch_rows(s, s->dev.cg_x, dx))) return rc;
   SceneScalars sc;
   CUDA_OR(cudaMemcpy(&sc, s->d_sc, sizeof(sc), cudaMemcpyDeviceToHost), MFEM_ERR_CUDA);
   if (iterations) *iterations = sc.cg_total;

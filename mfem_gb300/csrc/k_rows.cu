@@ -15,6 +15,7 @@
 
 #include "device_math.cuh"
 #include "kernels.cuh"
+#include "async_copy.cuh"
 #include "reduce.cuh"
 
 namespace mfem_gpu {
@@ -703,6 +704,17 @@ __global__ void __launch_bounds__(kCgThreads) k_cg_update(const Tile* tiles, con
 // iteration parity, so no row is overwritten while another block reads it).
 // In exact arithmetic the iterates are those of the two-reduction PCG.
 
+// acc += B u for one packed ELL slot (pairs (col, a00) (a01, a02) (a10, a11)
+// (a12, a20) (a21, a22)), as explicit FMA chains: every form of the fused
+// iteration (registers or staged through shared memory) rounds alike.
+template <typename P, typename Real>
+__device__ __forceinline__ void ell_block_fma(const P& w0, const P& w1, const P& w2, const P& w3, const P& w4,
+                                              const Real u[3], Real& a0, Real& a1, Real& a2) {
+  a0 = fma(w1.y, u[2], fma(w1.x, u[1], fma(w0.y, u[0], a0)));
+  a1 = fma(w3.x, u[2], fma(w2.y, u[1], fma(w2.x, u[0], a1)));
+  a2 = fma(w4.y, u[2], fma(w4.x, u[1], fma(w3.y, u[0], a2)));
+}
+
 // u_{i+1} of a row from r_i, w_i, s_{i-1}: the same operations, in the same
 // order, wherever a row's value is formed.
 template <typename Real>
@@ -715,6 +727,290 @@ __device__ __forceinline__ void cgf_next(const SceneDev& sd, int row, const Real
     rn[c] = fma(-a, s[c], r[c]);
   }
   apply_prec<Real>(sd, row, rn, u);
+}
+
+__device__ __forceinline__ void cgf_verify_step(const SceneDev& sd, BatchCounters* ctrs, double rr, double g,
+                                                double d, double su, double ps, int it);
+
+// The three inner products of one tile as tile partials; the scene's last
+// tile reduces them and sets a, b of the next iteration and the stopping
+// test (Eigen's |r|^2 < tol^2 |b|^2).  A bounded wait that ran out in this
+// launch (ctrs->error) ends the solve.
+template <typename Real, bool kInit, int NQ = 3>
+__device__ __forceinline__ void cgf_finish(const SceneDev& sd, BatchCounters* ctrs,
+                                           typename Ext<Real>::T (&dots)[NQ], double* partials,
+                                           int pstride, int tix, int it) {
+  using E = typename Ext<Real>::T;
+  SceneScalars* sc = sd.sc;
+  tile_partials<E, Real, NQ, 0>(dots, nullptr, partials, pstride, 0, tix);
+  if (last_tile(sd, TB_CG, tix)) {
+    E v[NQ];
+    scene_sums<E, NQ>(partials, pstride, 0, sd.tile_first[TB_CG], sd.tile_count[TB_CG], v);
+    if (threadIdx.x == 0) {
+      const double rr = to_double_any(v[0]), g = to_double_any(v[1]), d = to_double_any(v[2]);
+      const double su = NQ > 3 ? to_double_any(v[NQ > 3 ? 3 : 0]) : 0.0;
+      const double ps = NQ > 4 ? to_double_any(v[NQ > 4 ? 4 : 0]) : 0.0;
+      if (kInit) {
+        sc->cg_rhs_norm2 = rr;
+        sc->cg_iter = 0;
+        sc->cg_err = 0.0;
+        sc->cgf_phase = 0;
+        sc->cgf_rounds = 0;
+        const double thr = fmax(sd.cg_tol * sd.cg_tol * rr, DBL_MIN);
+        sc->cg_threshold = thr;
+        if (rr == 0.0) {
+          sc->cg_active = 0;
+        } else if (rr < thr || sd.max_cg <= 0) {
+          sc->cg_active = 0;
+          sc->cg_err = 1.0;
+        } else {
+          sc->cg_active = 1;
+          atomicAdd(&ctrs->cg_active, 1);
+        }
+        const double a0 = Fin<Real>::div(g, d);
+        sc->cgf_gamma[0] = g;
+        sc->alpha = a0;
+        sc->alpha_f = float(a0);
+        sc->beta = 0.0;
+        sc->beta_f = 0.0f;
+      } else if (sizeof(Real) == 4 && sd.cg_xe) {
+        cgf_verify_step(sd, ctrs, rr, g, d, su, ps, it);
+      } else {
+        bool stop = false;
+        sc->cg_err = Fin<Real>::sqrt_ratio(rr, sc->cg_rhs_norm2);
+        if (rr < sc->cg_threshold) {
+          stop = true;
+        } else {
+          const double bn = Fin<Real>::div(g, sc->cgf_gamma[0]);
+          const double an = Fin<Real>::div(g, d - Fin<Real>::div(bn * g, sc->alpha));
+          sc->beta = bn;
+          sc->beta_f = float(bn);
+          sc->alpha = an;
+          sc->alpha_f = float(an);
+          sc->cgf_gamma[0] = g;
+          sc->cg_iter = it + 1;
+          if (it + 1 >= sd.max_cg) {
+            stop = true;
+            sc->cg_status = 5;  // MFEM_ERR_CG_MAXITER
+          }
+        }
+        if (!(rr == rr)) {
+          stop = true;
+          sc->status = 4;
+        }
+        if (*(volatile int*)&ctrs->error) stop = true;  // the host reports MFEM_ERR_TIMEOUT
+        if (stop) {
+          sc->cg_total += sc->cg_iter;
+          sc->cg_active = 0;
+          atomicSub(&ctrs->cg_active, 1);
+        }
+      }
+    }
+  }
+}
+
+// ---------------------------------------- verified stop (mixed path) ---
+// In FP32 the single-reduction recurrences drift: the recursive residual
+// meets the tolerance while the true |b - A x| / |b| sits several times
+// above it (x itself rounded to FP32 floors it near eps32 |A||x| / |b|).
+// So when the recursion says "converged", the mixed path verifies before it
+// stops, in three further launches of the same kernel (the scene's
+// cgf_phase selects the work; the iteration count does not move):
+//   1  r = b - A (x_e + x), with each FP32 matrix entry times the df64
+//      x_e + x as an exact product summed in df64 (the reliable residual);
+//      u = M^-1 r;
+//   2  x_e += x, x = 0 (the FP32 x restarts as a correction, so its
+//      rounding shrinks with what is left to solve); w = A u and s = A p
+//      (the recursions' drift starts again from zero); the inner products
+//      of the true residual.  If it meets the tolerance: phase 3.
+//      Otherwise the recursion continues from the replaced r, w and s:
+//      the next direction u + b p is made A-conjugate to p directly (b =
+//      -(A p, u) / (p, A p)), because the drifted recursion's
+//      gamma_prev no longer describes the true residual, and a from the
+//      exact (p_new, A p_new).  After kCgfRounds failed verifications the
+//      next recursive stop is accepted as it is;
+//   3  x_e += x, and x = round(x_e) for the readers of the solution; stop.
+// A stop on max_iterative_solver_iters or a non-finite residual also goes
+// through phase 3, so the solution is always x_e + x.
+
+// The finalizer's part for the mixed path (thread 0 of the scene's last tile).
+constexpr int kCgfRounds = 4;
+__device__ __forceinline__ void cgf_verify_step(const SceneDev& sd, BatchCounters* ctrs, double rr, double g,
+                                                double d, double su, double ps, int it) {
+  SceneScalars* sc = sd.sc;
+  const int ph = sc->cgf_phase;
+  if (ph == 1) {
+    sc->cgf_phase = 2;
+    return;
+  }
+  if (ph == 3 || *(volatile int*)&ctrs->error) {
+    sc->cg_total += sc->cg_iter;
+    sc->cg_active = 0;
+    atomicSub(&ctrs->cg_active, 1);
+    return;
+  }
+  sc->cg_err = Fin<float>::sqrt_ratio(rr, sc->cg_rhs_norm2);
+  if (!(rr == rr)) {
+    sc->status = 4;
+    sc->cgf_phase = 3;
+    return;
+  }
+  if (rr < sc->cg_threshold) {
+    // phase 0: the recursion's residual passes, verify it (unless the
+    // verifications are used up); phase 2: the true residual passes, write
+    // the solution
+    sc->cgf_phase = (ph == 0 && sc->cgf_rounds < kCgfRounds) ? 1 : 3;
+    return;
+  }
+  double bn, an;
+  if (ph == 2) {
+    // A failed verification.  The recursion's gamma had drifted below the
+    // true residual's, so b = gamma / gamma_prev would be far too large: the
+    // new direction is made A-conjugate to the last one directly,
+    // b = -(A p, u) / (p, A p), and (p_new, A p_new) = d + 2 b (A p, u) +
+    // b^2 (p, A p) from phase 2's exact A p.
+    sc->cgf_rounds += 1;
+    bn = -Fin<float>::div(su, ps);
+    an = Fin<float>::div(g, d + 2.0 * bn * su + bn * bn * ps);
+  } else {
+    bn = Fin<float>::div(g, sc->cgf_gamma[0]);
+    an = Fin<float>::div(g, d - Fin<float>::div(bn * g, sc->alpha));
+  }
+  sc->beta = bn;
+  sc->beta_f = float(bn);
+  sc->alpha = an;
+  sc->alpha_f = float(an);
+  sc->cgf_gamma[0] = g;
+  sc->cg_iter = it + 1;
+  sc->cgf_phase = 0;
+  if (it + 1 >= sd.max_cg) {
+    sc->cg_status = 5;  // MFEM_ERR_CG_MAXITER
+    sc->cgf_phase = 3;
+  }
+}
+
+// One launch of phases 1..3 for one tile (plain loads: these are a few
+// launches per solve).
+template <bool kScaled>
+__device__ __noinline__ void cgf_verify_tile(int ph, int tix, const Tile* tiles, const SceneDev* sds,
+                                             double* partials, int pstride, BatchCounters* ctrs) {
+  const Tile t = tiles[tix];
+  const SceneDev& sd = sds[t.scene];
+  SceneScalars* sc = sd.sc;
+  const int it = sc->cg_iter;
+  float* r_cur = static_cast<float*>(sd.cgf_r[(it + 1) & 1]);  // r_{it+1}, replaced in phase 1
+  float* w_cur = static_cast<float*>(sd.cgf_w[(it + 1) & 1]);  // w_{it+1}, replaced in phase 2
+  float* x = static_cast<float*>(sd.cg_x);
+  float* u = static_cast<float*>(sd.cg_z);
+  const float* ell = static_cast<const float*>(sd.ell);
+  // (r,r), (r,u), (w,u) and in phase 2 also (A p, u), (p, A p)
+  df64 dots[5] = {df64(0.f), df64(0.f), df64(0.f), df64(0.f), df64(0.f)};
+  const int row = t.begin + threadIdx.x;
+  if (row < t.end) {
+    const size_t k4 = 4 * (size_t)row;
+    const int slice = row >> 5, rs = row & 31;
+    const int soff = sd.slice_off[slice], slen = (sd.slice_off[slice + 1] - soff) >> 5;
+    if (ph == 1) {
+      df64 acc[3] = {df64(0.f), df64(0.f), df64(0.f)};
+      for (int k = 0; k < slen; ++k) {
+        const size_t q = ell_pair(soff, k, rs, 0);
+        const float2 w0 = ld_pair<false>(ell, q), w1 = ld_pair<false>(ell, q + 32),
+                     w2 = ld_pair<false>(ell, q + 64), w3 = ld_pair<false>(ell, q + 96),
+                     w4 = ld_pair<false>(ell, q + 128);
+        const int col = pair_col(w0);
+        X3 xc = xe_load<false>(sd.cg_xe, col);
+        float xf[3];
+        ld3<false>(x + 4 * (size_t)col, xf);
+#pragma unroll
+        for (int j = 0; j < 3; ++j) xc.v[j] = xc.v[j] + df64(xf[j]);
+        const float a[9] = {w0.y, w1.x, w1.y, w2.x, w2.y, w3.x, w3.y, w4.x, w4.y};
+#pragma unroll
+        for (int i = 0; i < 3; ++i)
+#pragma unroll
+          for (int j = 0; j < 3; ++j) {
+            const float aij = a[3 * i + j];
+            acc[i] = acc[i] + two_prod(aij, xc.v[j].hi) + df64(aij * xc.v[j].lo);
+          }
+      }
+      float bv[3], r[3], z[3];
+      ld3<false>(static_cast<const float*>(sd.rhs) + k4, bv);
+#pragma unroll
+      for (int c = 0; c < 3; ++c) r[c] = Ext<float>::to_real(df64(bv[c]) - acc[c]);
+      apply_prec<float>(sd, row, r, z);
+      st3(r_cur + k4, kScaled ? z : r);  // the scaled form keeps r~ = M^-1 r (= u)
+      if (!kScaled) st3(u + k4, z);
+    } else if (ph == 2) {
+      // fold x into x_e
+      X3 xe = xe_load<false>(sd.cg_xe, row);
+      float xf[3];
+      ld3<false>(x + k4, xf);
+#pragma unroll
+      for (int c = 0; c < 3; ++c) xe.v[c] = xe.v[c] + df64(xf[c]);
+      xe_store(sd.cg_xe, row, xe);
+      const float zero[3] = {0.f, 0.f, 0.f};
+      st3(x + k4, zero);
+      // w = A u with u of the neighbours as phase 1 stored it, and s = A p
+      // (the recursion's s_it, whose drift is what moves r away from b - A x)
+      const float* pv = static_cast<const float*>(sd.cg_p[0]);
+      float acc0 = 0.f, acc1 = 0.f, acc2 = 0.f, sa0 = 0.f, sa1 = 0.f, sa2 = 0.f;
+      for (int k = 0; k < slen; ++k) {
+        const size_t q = ell_pair(soff, k, rs, 0);
+        const float2 w0 = ld_pair<false>(ell, q), w1 = ld_pair<false>(ell, q + 32),
+                     w2 = ld_pair<false>(ell, q + 64), w3 = ld_pair<false>(ell, q + 96),
+                     w4 = ld_pair<false>(ell, q + 128);
+        const size_t c4 = 4 * (size_t)pair_col(w0);
+        float uc[3], pc[3];
+        ld3<false>((kScaled ? r_cur : u) + c4, uc);
+        ld3<false>(pv + c4, pc);
+        ell_block_fma(w0, w1, w2, w3, w4, uc, acc0, acc1, acc2);
+        ell_block_fma(w0, w1, w2, w3, w4, pc, sa0, sa1, sa2);
+      }
+      float* s_cur = static_cast<float*>(sd.cgf_s[it & 1]);  // s_it
+      float un[3], rn[3];
+      ld3<false>((kScaled ? r_cur : u) + k4, un);
+      if (kScaled) {
+        float dv[3];
+        ld3<false>(static_cast<const float*>(sd.dinv) + k4, dv);
+#pragma unroll
+        for (int c = 0; c < 3; ++c) rn[c] = un[c] / dv[c];
+        const float ws[3] = {dv[0] * acc0, dv[1] * acc1, dv[2] * acc2};
+        const float ss[3] = {dv[0] * sa0, dv[1] * sa1, dv[2] * sa2};
+        st3(w_cur + k4, ws);
+        st3(s_cur + k4, ss);
+      } else {
+        ld3<false>(r_cur + k4, rn);
+        const float wn[3] = {acc0, acc1, acc2};
+        const float sn[3] = {sa0, sa1, sa2};
+        st3(w_cur + k4, wn);
+        st3(s_cur + k4, sn);
+      }
+      const float wn[3] = {acc0, acc1, acc2};
+      const float san[3] = {sa0, sa1, sa2};
+      float po[3];
+      ld3<false>(pv + k4, po);
+#pragma unroll
+      for (int c = 0; c < 3; ++c) {
+        dots[0] = dots[0] + exact_prod(rn[c], rn[c]);
+        dots[1] = dots[1] + exact_prod(rn[c], un[c]);
+        dots[2] = dots[2] + exact_prod(wn[c], un[c]);
+        dots[3] = dots[3] + exact_prod(san[c], un[c]);
+        dots[4] = dots[4] + exact_prod(po[c], san[c]);
+      }
+    } else {
+      // the solution: x_e + x in x_e, and rounded to FP32 in x for its readers
+      X3 xe = xe_load<false>(sd.cg_xe, row);
+      float xf[3];
+      ld3<false>(x + k4, xf);
+#pragma unroll
+      for (int c = 0; c < 3; ++c) {
+        xe.v[c] = xe.v[c] + df64(xf[c]);
+        xf[c] = Ext<float>::to_real(xe.v[c]);
+      }
+      xe_store(sd.cg_xe, row, xe);
+      st3(x + k4, xf);
+    }
+  }
+  cgf_finish<float, false, 5>(sd, ctrs, dots, partials, pstride, tix, it);
 }
 
 // One launch of the single-reduction PCG (init: r0 = b, x = 0, p = 0,
@@ -733,6 +1029,12 @@ __device__ __forceinline__ void cgf_tile(int tix, const Tile* tiles, const Scene
   const SceneDev& sd = sds[t.scene];
   SceneScalars* sc = sd.sc;
   if (kInit ? !sc->newton_active : !sc->cg_active) return;
+  if constexpr (!kInit && sizeof(Real) == 4) {
+    if (const int ph = sc->cgf_phase) {
+      cgf_verify_tile<kScaled>(ph, tix, tiles, sds, partials, pstride, ctrs);
+      return;
+    }
+  }
   const int it = kInit ? 0 : sc->cg_iter;
   const Real a = kInit ? Real(0) : (sizeof(Real) == 4 ? Real(sc->alpha_f) : Real(sc->alpha));
   const Real b = kInit ? Real(0) : (sizeof(Real) == 4 ? Real(sc->beta_f) : Real(sc->beta));
@@ -761,6 +1063,7 @@ __device__ __forceinline__ void cgf_tile(int tix, const Tile* tiles, const Scene
       st3(x + k4, zero);
       st3(p + k4, zero);
       st3(s_new + k4, zero);
+      if (sizeof(Real) == 4 && sd.cg_xe) xe_store(sd.cg_xe, row, zero_x3());
     } else {
       Real rv[3], wv[3], sp[3], sv[3], uv[3], pv[3], xv[3];
       ld3<false>(r_old + k4, rv);
@@ -825,9 +1128,7 @@ __device__ __forceinline__ void cgf_tile(int tix, const Tile* tiles, const Scene
           cgf_next<Real>(sd, col, rc, wc, spc, a, b, sc_, rnc, uc);
         }
       }
-      acc0 += w0.y * uc[0] + w1.x * uc[1] + w1.y * uc[2];
-      acc1 += w2.x * uc[0] + w2.y * uc[1] + w3.x * uc[2];
-      acc2 += w3.y * uc[0] + w4.x * uc[1] + w4.y * uc[2];
+      ell_block_fma(w0, w1, w2, w3, w4, uc, acc0, acc1, acc2);
     }
     const Real wn[3] = {acc0, acc1, acc2};
     if (kScaled) {
@@ -845,64 +1146,7 @@ __device__ __forceinline__ void cgf_tile(int tix, const Tile* tiles, const Scene
       dots[2] = dots[2] + exact_prod(wn[c], un[c]);
     }
   }
-  tile_partials<E, Real, 3, 0>(dots, nullptr, partials, pstride, 0, tix);
-  if (last_tile(sd, TB_CG, tix)) {
-    E v[3];
-    scene_sums<E, 3>(partials, pstride, 0, sd.tile_first[TB_CG], sd.tile_count[TB_CG], v);
-    if (threadIdx.x == 0) {
-      const double rr = to_double_any(v[0]), g = to_double_any(v[1]), d = to_double_any(v[2]);
-      if (kInit) {
-        sc->cg_rhs_norm2 = rr;
-        sc->cg_iter = 0;
-        sc->cg_err = 0.0;
-        const double thr = fmax(sd.cg_tol * sd.cg_tol * rr, DBL_MIN);
-        sc->cg_threshold = thr;
-        if (rr == 0.0) {
-          sc->cg_active = 0;
-        } else if (rr < thr || sd.max_cg <= 0) {
-          sc->cg_active = 0;
-          sc->cg_err = 1.0;
-        } else {
-          sc->cg_active = 1;
-          atomicAdd(&ctrs->cg_active, 1);
-        }
-        const double a0 = Fin<Real>::div(g, d);
-        sc->cgf_gamma[0] = g;
-        sc->alpha = a0;
-        sc->alpha_f = float(a0);
-        sc->beta = 0.0;
-        sc->beta_f = 0.0f;
-      } else {
-        bool stop = false;
-        sc->cg_err = Fin<Real>::sqrt_ratio(rr, sc->cg_rhs_norm2);
-        if (rr < sc->cg_threshold) {
-          stop = true;
-        } else {
-          const double bn = Fin<Real>::div(g, sc->cgf_gamma[0]);
-          const double an = Fin<Real>::div(g, d - Fin<Real>::div(bn * g, sc->alpha));
-          sc->beta = bn;
-          sc->beta_f = float(bn);
-          sc->alpha = an;
-          sc->alpha_f = float(an);
-          sc->cgf_gamma[0] = g;
-          sc->cg_iter = it + 1;
-          if (it + 1 >= sd.max_cg) {
-            stop = true;
-            sc->cg_status = 5;  // MFEM_ERR_CG_MAXITER
-          }
-        }
-        if (!(rr == rr)) {
-          stop = true;
-          sc->status = 4;
-        }
-        if (stop) {
-          sc->cg_total += sc->cg_iter;
-          sc->cg_active = 0;
-          atomicSub(&ctrs->cg_active, 1);
-        }
-      }
-    }
-  }
+  cgf_finish<Real, kInit>(sd, ctrs, dots, partials, pstride, tix, it);
 }
 
 // kScaled: every scene of the batch uses the Jacobi preconditioner.
@@ -917,6 +1161,256 @@ template <typename Real, bool kScaled>
 __global__ void __launch_bounds__(kCgThreads, sizeof(Real) == 4 ? 6 : 4) k_cgf_iter(
     const Tile* tiles, const SceneDev* sds, double* partials, int pstride, BatchCounters* ctrs) {
   cgf_tile<Real, false, kScaled>(blockIdx.x, tiles, sds, partials, pstride, ctrs);
+}
+
+
+// ------------------------------------------- staged fused iteration ---
+// The same iteration as cgf_tile (not the init), with the matrix streamed
+// through shared memory: each warp owns one 32-row slice of the packed
+// sliced ELL, whose ELL slot k (the 32 rows' block k: 160 pairs, contiguous
+// in global memory) is one bulk copy (cp.async.bulk, the TMA engine) into a
+// ring of S stages, completed on one mbarrier per stage.  Lane 0 keeps S
+// slots in flight: a stage is refilled with slot k + S as soon as the warp
+// has read slot k out of it.  The column -> gather -> FMA chain of a slot
+// then starts from shared memory, and the DRAM latency of the matrix stream
+// is hidden behind the S - 1 slots ahead instead of sitting in every
+// slot's chain.  Arithmetic and its order are those of cgf_tile (bitwise
+// the same results).
+//
+// Shared memory: (blockDim / 32) warps x S stages x 160 pairs, then S
+// mbarriers per warp.  Every wait is bounded; one that runs out raises
+// ctrs->error, waits (bounded) for the warp's copies still in flight and
+// leaves the rest of the slice undone.
+template <typename Real> struct PairOf;
+template <> struct PairOf<float> { using T = float2; };
+template <> struct PairOf<double> { using T = double2; };
+
+constexpr int kSlotPairs = 160;  // pairs of one ELL slot of a 32-row slice
+
+template <typename Real, int S>
+constexpr size_t cgf_staged_smem_bytes(int warps) {
+  return (size_t)warps * S * kSlotPairs * sizeof(typename PairOf<Real>::T) + (size_t)warps * S * 8;
+}
+
+// L2 policy of the matrix stream: all lines evict-first (keep = 0), or half
+// of them evict-last (keep = 1), so that about half the matrix can stay in
+// L2 from one iteration to the next.
+template <int kKeep>
+__device__ __forceinline__ unsigned long long l2_matrix_policy() {
+  unsigned long long p;
+  if constexpr (kKeep == 0)
+    asm volatile("createpolicy.fractional.L2::evict_first.b64 %0, 1.0;" : "=l"(p));
+  else
+    asm volatile("createpolicy.fractional.L2::evict_last.L2::evict_first.b64 %0, 0.5;" : "=l"(p));
+  return p;
+}
+
+template <typename Real, bool kScaled, int S, int kKeep, int U>
+__device__ __forceinline__ void cgf_staged_tile(int tix, const Tile* tiles, const SceneDev* sds,
+                                                double* partials, int pstride, BatchCounters* ctrs,
+                                                unsigned char* smem) {
+  using P = typename PairOf<Real>::T;
+  constexpr uint32_t kSlotBytes = kSlotPairs * sizeof(P);
+  const Tile t = tiles[tix];
+  const SceneDev& sd = sds[t.scene];
+  SceneScalars* sc = sd.sc;
+  if (!sc->cg_active) return;
+  if constexpr (sizeof(Real) == 4) {
+    if (const int ph = sc->cgf_phase) {
+      cgf_verify_tile<kScaled>(ph, tix, tiles, sds, partials, pstride, ctrs);
+      return;
+    }
+  }
+  const int it = sc->cg_iter;
+  const Real a = sizeof(Real) == 4 ? Real(sc->alpha_f) : Real(sc->alpha);
+  const Real b = sizeof(Real) == 4 ? Real(sc->beta_f) : Real(sc->beta);
+  const Real* r_old = static_cast<const Real*>(sd.cgf_r[it & 1]);
+  const Real* w_old = static_cast<const Real*>(sd.cgf_w[it & 1]);
+  const Real* s_old = static_cast<const Real*>(sd.cgf_s[(it + 1) & 1]);
+  Real* r_new = static_cast<Real*>(sd.cgf_r[(it + 1) & 1]);
+  Real* w_new = static_cast<Real*>(sd.cgf_w[(it + 1) & 1]);
+  Real* s_new = static_cast<Real*>(sd.cgf_s[it & 1]);
+  Real* x = static_cast<Real*>(sd.cg_x);
+  Real* u = static_cast<Real*>(sd.cg_z);
+  Real* p = static_cast<Real*>(sd.cg_p[0]);
+  using E = typename Ext<Real>::T;
+  E dots[3] = {E(0), E(0), E(0)};  // (r,r), (r,u), (w,u) at it+1
+
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  // 32-bit shared addresses of this warp's stage ring and its mbarriers
+  const uint32_t stage0 = smem_addr(smem) + (uint32_t)(warp * S) * kSlotBytes;
+  const uint32_t bar0 = smem_addr(smem) + (uint32_t)((blockDim.x >> 5) * S) * kSlotBytes + (uint32_t)(warp * S) * 8u;
+  const int row0 = t.begin + 32 * warp;  // first row of the warp's slice
+  const int row = row0 + lane;
+  const bool live = row < t.end;
+  int slen = 0;
+  const P* gslice = nullptr;
+  if (row0 < t.end) {  // warp-uniform
+    const int slice = row0 >> 5;
+    const int soff = sd.slice_off[slice];
+    slen = (sd.slice_off[slice + 1] - soff) >> 5;
+    gslice = static_cast<const P*>(sd.ell) + 5 * (size_t)soff;  // slot k: + 160 k pairs
+    if (lane == 0) {
+#pragma unroll
+      for (int q = 0; q < S; ++q) mbar_init(bar0 + 8u * q, 1u);
+      fence_mbar_init();
+      const unsigned long long pol_m = l2_matrix_policy<kKeep>();
+      for (int k = 0; k < S && k < slen; ++k) {
+        mbar_arrive_expect_tx(bar0 + 8u * k, kSlotBytes);
+        bulk_g2s(stage0 + k * kSlotBytes, gslice + (size_t)k * kSlotPairs, kSlotBytes, bar0 + 8u * k, pol_m);
+      }
+    }
+    __syncwarp();
+  }
+
+  // own row: p, x, s, r (and u) of iteration it+1, while the first slots
+  // fly.  Nothing of it stays in registers across the slot loop (the 40
+  // registers of six resident blocks would spill): the dot products reload
+  // r and u afterwards (their lines are still in L1).
+  if (live) {
+    const size_t k4 = 4 * (size_t)row;
+    Real dv[3], rv[3], wv[3], sp[3], sv[3], uv[3], pv[3], xv[3], un[3], rn[3];
+    if (kScaled) ld3<false>(static_cast<const Real*>(sd.dinv) + k4, dv);
+    ld3<false>(r_old + k4, rv);
+    ld3<false>(w_old + k4, wv);
+    ld3<false>(s_old + k4, sp);
+    if (kScaled) {
+#pragma unroll
+      for (int c = 0; c < 3; ++c) {
+        sv[c] = fma(b, sp[c], wv[c]);
+        un[c] = fma(-a, sv[c], rv[c]);
+        uv[c] = rv[c];  // u_i = r~_i
+      }
+    } else {
+      cgf_next<Real>(sd, row, rv, wv, sp, a, b, sv, rn, un);
+      ld3<false>(u + k4, uv);
+    }
+    ld3<false>(p + k4, pv);
+    ld3<false>(x + k4, xv);
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+      pv[c] = fma(b, pv[c], uv[c]);
+      xv[c] = fma(a, pv[c], xv[c]);
+    }
+    st3(p + k4, pv);
+    st3(x + k4, xv);
+    st3(s_new + k4, sv);
+    if (kScaled) {
+      st3(r_new + k4, un);
+    } else {
+      st3(r_new + k4, rn);
+      st3(u + k4, un);
+    }
+  }
+
+  // w_{i+1} = A u_{i+1}, out of the stage ring: U slots at a time, whose
+  // gathers all go out before the first of them is consumed (the slots are
+  // still accumulated in order, so every U computes the same bits)
+  Real acc0 = 0, acc1 = 0, acc2 = 0;
+  int k = 0;
+  bool ok = true;
+  const uint32_t pb = (uint32_t)sizeof(P) * 32u;
+  const uint32_t lane_off = (uint32_t)lane * (uint32_t)sizeof(P);
+  auto fill = [&](int j) {  // lane 0: stage of slot j - S gets slot j
+    if (lane == 0 && j < slen) {
+      const int q = j % S;
+      fence_proxy_async_smem();
+      mbar_arrive_expect_tx(bar0 + 8u * q, kSlotBytes);
+      bulk_g2s(stage0 + (uint32_t)q * kSlotBytes, gslice + (size_t)j * kSlotPairs, kSlotBytes, bar0 + 8u * q,
+               l2_matrix_policy<kKeep>());
+    }
+  };
+  for (; ok && k < slen; k += U) {
+    const int n = min(U, slen - k);  // warp-uniform
+    P w0[U];
+    Real uc[U][3];
+#pragma unroll
+    for (int j = 0; j < U; ++j) {
+      if (j < n) {
+        const int q = (k + j) % S;
+        const bool got = mbar_wait(bar0 + 8u * q, (uint32_t)(((k + j) / S) & 1));
+        if (!__all_sync(0xffffffffu, got)) {
+          ok = false;
+          break;
+        }
+        // the column first: the gathers go out before the other pairs are read
+        w0[j] = lds_pair(stage0 + (uint32_t)q * kSlotBytes + lane_off, Real(0));
+        if (live) {
+          const unsigned long long pol_k = l2_evict_last();
+          const size_t c4 = 4 * (size_t)pair_col(w0[j]);
+          Real rc[3], wc[3], spc[3];
+          ld3_keep(r_old + c4, rc, pol_k);
+          ld3_keep(w_old + c4, wc, pol_k);
+          ld3_keep(s_old + c4, spc, pol_k);
+          if (kScaled) {
+#pragma unroll
+            for (int c = 0; c < 3; ++c) uc[j][c] = fma(-a, fma(b, spc[c], wc[c]), rc[c]);
+          } else {
+            Real sc_[3], rnc[3];
+            cgf_next<Real>(sd, pair_col(w0[j]), rc, wc, spc, a, b, sc_, rnc, uc[j]);
+          }
+        }
+      }
+    }
+    if (!ok) break;
+#pragma unroll
+    for (int j = 0; j < U; ++j) {
+      if (j < n) {
+        const uint32_t sp = stage0 + (uint32_t)((k + j) % S) * kSlotBytes + lane_off;
+        const P w1 = lds_pair(sp + pb, Real(0)), w2 = lds_pair(sp + 2 * pb, Real(0)),
+                w3 = lds_pair(sp + 3 * pb, Real(0)), w4 = lds_pair(sp + 4 * pb, Real(0));
+        __syncwarp();
+        fill(k + j + S);
+        if (live) ell_block_fma(w0[j], w1, w2, w3, w4, uc[j], acc0, acc1, acc2);
+      }
+    }
+  }
+  if (!ok) {
+    // a wait ran out: flag it, then let the copies still in flight land
+    // (bounded) before the block may exit
+    if (lane == 0) atomicExch(&ctrs->error, 1);
+    for (int j = k; j < slen && j < k + S; ++j) mbar_wait(bar0 + 8u * (j % S), (uint32_t)((j / S) & 1));
+    __syncwarp();
+  }
+  if (live) {
+    const size_t k4 = 4 * (size_t)row;
+    const Real wn[3] = {acc0, acc1, acc2};
+    Real un[3], rn[3];
+    if (kScaled) {
+      Real dv[3];
+      ld3<false>(static_cast<const Real*>(sd.dinv) + k4, dv);
+      ld3<false>(r_new + k4, un);
+#pragma unroll
+      for (int c = 0; c < 3; ++c) rn[c] = un[c] / dv[c];
+      const Real ws[3] = {dv[0] * acc0, dv[1] * acc1, dv[2] * acc2};
+      st3(w_new + k4, ws);
+    } else {
+      ld3<false>(r_new + k4, rn);
+      ld3<false>(u + k4, un);
+      st3(w_new + k4, wn);
+    }
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+      dots[0] = dots[0] + exact_prod(rn[c], rn[c]);
+      dots[1] = dots[1] + exact_prod(rn[c], un[c]);
+      dots[2] = dots[2] + exact_prod(wn[c], un[c]);
+    }
+  }
+  cgf_finish<Real, false>(sd, ctrs, dots, partials, pstride, tix, it);
+}
+
+// Resident blocks per SM: six (40 registers) in FP32 where the stages fit
+// six blocks' shared memory, five with four stages (41 KB a block), four
+// (64 registers) when two slots' gathers are in flight together.
+template <typename Real, int S, int U>
+constexpr int cgf_staged_min_blocks() {
+  return sizeof(Real) == 4 ? (U > 1 ? 4 : (S >= 4 ? 5 : 6)) : 4;
+}
+template <typename Real, bool kScaled, int S, int kKeep, int U>
+__global__ void __launch_bounds__(kCgThreads, cgf_staged_min_blocks<Real, S, U>()) k_cgf_iter_staged(
+    const Tile* tiles, const SceneDev* sds, double* partials, int pstride, BatchCounters* ctrs) {
+  extern __shared__ __align__(128) unsigned char cgf_smem[];
+  cgf_staged_tile<Real, kScaled, S, kKeep, U>(blockIdx.x, tiles, sds, partials, pstride, ctrs, cgf_smem);
 }
 
 // Nanoseconds of the GPU's global timer.
@@ -1071,7 +1565,46 @@ void launch_cg_replace(const Launch& L) {
   } while (0)
 
 void launch_cgf_init(const Launch& L) { MFEM_LAUNCH_CGF(k_cgf_init); }
-void launch_cgf_iter(const Launch& L) { MFEM_LAUNCH_CGF(k_cgf_iter); }
+
+namespace {
+template <typename Real, bool kScaled, int S, int kKeep, int U>
+void launch_staged(const Launch& L) {
+  const size_t smem = cgf_staged_smem_bytes<Real, S>(kCgThreads / 32);
+  k_cgf_iter_staged<Real, kScaled, S, kKeep, U>
+      <<<L.ntiles, kCgThreads, smem, L.stream>>>(L.tiles, L.sds, L.partials, L.pstride, L.counters);
+}
+template <typename Real, bool kScaled, int kKeep>
+void launch_staged_s(const Launch& L, int stages, int unroll) {
+  if constexpr (sizeof(Real) == 4) {
+    if (unroll > 1) launch_staged<Real, kScaled, 4, kKeep, 2>(L);
+    else if (stages == 2) launch_staged<Real, kScaled, 2, kKeep, 1>(L);
+    else if (stages == 3) launch_staged<Real, kScaled, 3, kKeep, 1>(L);
+    else launch_staged<Real, kScaled, 4, kKeep, 1>(L);
+  } else {
+    launch_staged<Real, kScaled, 2, kKeep, 1>(L);  // 2560-byte slots: two stages
+  }
+}
+template <typename Real, bool kScaled>
+void launch_staged_k(const Launch& L, const CgfShape& sh) {
+  if (sh.keep) launch_staged_s<Real, kScaled, 1>(L, sh.stages, sh.unroll);
+  else launch_staged_s<Real, kScaled, 0>(L, sh.stages, sh.unroll);
+}
+}  // namespace
+
+void launch_cgf_iter(const Launch& L, const CgfShape& sh) {
+  if (sh.stages <= 0) {
+    MFEM_LAUNCH_CGF(k_cgf_iter);
+    return;
+  }
+  if (L.ntiles == 0) return;
+  if (L.fp64) {
+    if (L.jacobi) launch_staged_k<double, true>(L, sh);
+    else launch_staged_k<double, false>(L, sh);
+  } else {
+    if (L.jacobi) launch_staged_k<float, true>(L, sh);
+    else launch_staged_k<float, false>(L, sh);
+  }
+}
 
 // Failure-detection check of the bounded grid barrier: a cooperative launch
 // of two blocks in which block 1 leaves without arriving (a lost peer), so

@@ -76,6 +76,10 @@ struct SceneScalars {
   // single-reduction PCG: (r, u) and alpha of iteration i in slot i & 1
   // (kernel i reads slot (i+1) & 1 and its first block writes slot i & 1)
   double cgf_gamma[2], cgf_alpha[2];
+  // mixed path: verification phase of the single-reduction PCG (0: iterate;
+  // 1: r = b - A (x_e + x) exactly; 2: fold x into x_e, w = A u and the
+  // inner products of the true residual; 3: write the rounded solution)
+  int cgf_phase, cgf_rounds;  // verifications that failed in this solve
   // line search (linesearch.h:80-129 with c = 0, p = 0.5)
   int ls_active, ls_iter, ls_ok, ls_total;
   double fx0, alpha_ls, E_trial;
@@ -254,8 +258,20 @@ void launch_scalars_begin(const Launch& L, int nscenes);        // reset Newton 
 cudaError_t launch_cg_solve(const Launch& L, int grid, int max_iters);
 void launch_cg_replace(const Launch& L);  // r = b - A x in df64 (mixed path)
 // Single-reduction PCG: init (r0, u0, w0 = A u0) and one launch per iteration.
+// The iteration's shape: stages = 0 streams the matrix through registers;
+// stages = 2..4 stages each warp's ELL slots through a ring of that many
+// shared-memory buffers filled by bulk copies (the FP64 path uses 2);
+// keep = 1 marks half of the matrix lines evict-last in L2 (0: all
+// evict-first); unroll = 2 puts two slots' gathers in flight together
+// (four stages, four resident blocks of 64 registers; FP32 only).  Every
+// shape computes the same bits.
+struct CgfShape {
+  int stages;
+  int keep;
+  int unroll;
+};
 void launch_cgf_init(const Launch& L);
-void launch_cgf_iter(const Launch& L);
+void launch_cgf_iter(const Launch& L, const CgfShape& sh);
 int cg_solve_blocks_per_sm(int fp64);
 // Two-block cooperative launch whose grid barrier has a missing arrival.
 cudaError_t launch_barrier_selftest(BatchCounters* ctrs, cudaStream_t st);

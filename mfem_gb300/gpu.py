@@ -165,6 +165,19 @@ def set_profiling(batch_handle, enable=True):
     check(load().mfem_gpu_batch_set_profiling(batch_handle, int(enable)), "set_profiling")
 
 
+def set_pcg_shape(batch_handle, stages, keep=0, unroll=1):
+    """Shape of the batch's fused PCG iteration (mfem_gpu_batch_set_pcg_shape)."""
+    check(load().mfem_gpu_batch_set_pcg_shape(batch_handle, int(stages), int(keep), int(unroll)),
+          "set_pcg_shape")
+
+
+def get_pcg_shape(batch_handle):
+    st, kp, un = C.c_int32(), C.c_int32(), C.c_int32()
+    check(load().mfem_gpu_batch_get_pcg_shape(batch_handle, C.byref(st), C.byref(kp), C.byref(un)),
+          "get_pcg_shape")
+    return st.value, kp.value, un.value
+
+
 def kernel_stats(batch_handle):
     """{kernel name: (total device ms, launches)} since profiling was enabled."""
     out = {}

@@ -1,0 +1,81 @@
+"""The single-reduction (fused) PCG: its verified stop in the mixed path and
+its kernel shapes.
+
+* Verified stop: in FP32 the recursive residual drifts from the true one
+  (on the 1M-tet cube the recursion reported 9.6e-5 while |b - A dx|/|b|
+  was 6.9e-4 at tol 1e-4).  The mixed path now checks b - A dx, computed
+  with exact products in float-float, before it stops, so the true residual
+  of the returned dx meets the tolerance (written below: 1.01 x tol, the
+  host's FP64 product against the device's float-float one).
+* Shapes: the matrix streamed through registers, or staged through 2, 3 or
+  4 shared-memory buffers per warp by bulk copies, with or without the L2
+  keep policy.  They change only how the data moves: the steps are bitwise
+  the same in every shape.
+"""
+import numpy as np
+import pytest
+
+from mfem_gb300 import abi, configs, gpu
+
+pytestmark = pytest.mark.gpu
+
+
+def bsr_mul(rp, col, val, x):
+    n = len(rp) - 1
+    rows = np.repeat(np.arange(n), np.diff(rp))
+    y = np.zeros((n, 3))
+    np.add.at(y, rows, np.einsum("kij,kj->ki", val, x.reshape(-1, 3)[col]))
+    return y.ravel()
+
+
+def cube(n, precision=abi.PRECISION_MIXED, **kw):
+    return configs.cube_c2(n=n, precision=precision, pcg_kernel=abi.PCG_KERNEL_FUSED, **kw)
+
+
+@pytest.mark.parametrize("tol", [1e-4, 1e-6])
+def test_fused_mixed_true_residual_meets_tolerance(gpu_lib, tol):
+    sc = gpu.Scene(cube(20, iterative_solver_tolerance=tol, max_iterative_solver_iters=5000))
+    st = sc.step()
+    assert st.status == abi.OK
+    rp, col, val, rhs = sc.get_system()
+    dx, it, err = sc.pcg(rhs)
+    assert 0 < it < 5000
+    true = np.linalg.norm(rhs - bsr_mul(rp, col, val, dx)) / np.linalg.norm(rhs)
+    assert err < tol                     # the reported residual is the verified one
+    assert true <= 1.01 * tol, (true, err, it)
+    sc.close()
+
+
+@pytest.mark.parametrize("prec", [abi.PRECISION_MIXED, abi.PRECISION_FP64])
+def test_fused_shapes_compute_the_same_bits(gpu_lib, prec):
+    sc = gpu.Scene(cube(20, precision=prec))
+    bh = sc.solo_batch_handle()
+    sc.step()
+    s0 = sc.get_state()
+    shapes = [(0, 0, 1), (2, 0, 1), (3, 0, 1), (4, 0, 1), (2, 1, 1), (4, 1, 1), (4, 0, 2), (4, 1, 2)]
+    fp64 = prec == abi.PRECISION_FP64
+    ref = None
+    for shape in shapes:
+        gpu.set_pcg_shape(bh, *shape)
+        got = gpu.get_pcg_shape(bh)
+        assert got == ((min(shape[0], 2), shape[1], 1) if fp64 else shape)
+        sc.set_state(x=s0["x"], v=s0["v"], s=s0["s"], R=s0["R"])
+        stats = [sc.step() for _ in range(2)]
+        assert all(s.status == abi.OK for s in stats)
+        out = (sc.positions(), [(s.newton_iterations, s.cg_iterations) for s in stats])
+        if ref is None:
+            ref = out
+        else:
+            assert np.array_equal(out[0], ref[0]), shape
+            assert out[1] == ref[1], shape
+    sc.close()
+
+
+def test_fused_shape_is_validated(gpu_lib):
+    sc = gpu.Scene(cube(6))
+    bh = sc.solo_batch_handle()
+    from mfem_gb300._lib import MfemError
+    for bad in ((1, 0, 1), (5, 0, 1), (-1, 0, 1), (2, 2, 1), (2, 0, 2), (4, 0, 3), (4, 0, 0)):
+        with pytest.raises(MfemError):
+            gpu.set_pcg_shape(bh, *bad)
+    sc.close()
