@@ -247,16 +247,17 @@ int mfem_gpu_kernel_name(int kernel, char* name, int name_len);
 /* ---- kernel shapes (no counterpart in the reference) ---------------------
  * Shape of the batch's fused PCG iteration: stages = 0 streams the matrix
  * through registers; 2..4 stage each warp's ELL slots through that many
- * shared-memory buffers filled by bulk copies (FP64 batches use 2);
- * keep = 1 marks half of the matrix's L2 lines evict-last, 0 all
- * evict-first; unroll = 2 (with stages = 4) puts two slots' gathers in
- * flight together, unroll = 1 one.  FP64 batches use stages <= 2 and
+ * shared-memory buffers filled by bulk copies; keep = 1 marks half of the
+ * matrix's L2 lines evict-last, 0 all evict-first; unroll = 2 (with
+ * stages = 4) puts two slots' gathers in flight together, unroll = 1 one;
+ * pdl = 1 (staged shapes only) launches each iteration as a programmatic
+ * dependent of the previous one.  FP64 batches use stages <= 2 and
  * unroll 1.  Every shape computes the same bits; the autotuner picks one
  * per batch.  Changing the shape re-captures the batch's PCG graph. */
 int mfem_gpu_batch_set_pcg_shape(mfem_batch* batch, int32_t stages, int32_t keep,
-                                 int32_t unroll);
+                                 int32_t unroll, int32_t pdl);
 int mfem_gpu_batch_get_pcg_shape(mfem_batch* batch, int32_t* stages, int32_t* keep,
-                                 int32_t* unroll);
+                                 int32_t* unroll, int32_t* pdl);
 
 /* ---- per-kernel parity entry points (host buffers in, host buffers out) ----
  * elem_update: MixedStretch::update_rotations + update_derivatives for the

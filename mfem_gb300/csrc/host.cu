@@ -510,7 +510,7 @@ struct mfem_batch {
     return cg_hints[std::min(newton_index, (int)cg_hints.size() - 1)];
   }
   int pcg_kernel = MFEM_PCG_KERNEL_PERSISTENT;
-  CgfShape cgf_shape{0, 0, 1};  // shape of the fused PCG iteration (same bits in every shape)
+  CgfShape cgf_shape{0, 0, 1, 0};  // shape of the fused PCG iteration (same bits in every shape)
   int minres = 0;  // every scene uses "minres-indefinite-block"
   int fem = 0;     // every scene uses the standard-FEM variable
   int jacobi = 1;  // no scene uses the 3x3 block-Jacobi preconditioner
@@ -1081,9 +1081,10 @@ int batch_build(mfem_scene* const* scenes, int n, mfem_batch** out) {
     maxt = std::max(maxt, tabs[tb].size());
   }
   // the fused iteration's matrix staged through two shared-memory buffers
-  // per warp (measured fastest on the 1M-tet cube); the autotuner may
-  // choose another shape for the batch's size class
-  b->cgf_shape = b->fp64 ? CgfShape{0, 0, 1} : CgfShape{2, 0, 1};
+  // per warp, each iteration a programmatic dependent launch (measured
+  // fastest on the 1M-tet cube); the autotuner may choose another shape for
+  // the batch's size class
+  b->cgf_shape = b->fp64 ? CgfShape{0, 0, 1, 0} : CgfShape{2, 0, 1, 1};
   b->pcg_kernel = scenes[0]->cfg.pcg_kernel;
   b->minres = scenes[0]->dev.minres;
   b->fem = scenes[0]->dev.fem;
@@ -1837,14 +1838,17 @@ int mfem_gpu_batch_set_profiling(mfem_batch* b, int enable) {
   return MFEM_OK;
 }
 
-int mfem_gpu_batch_set_pcg_shape(mfem_batch* b, int32_t stages, int32_t keep, int32_t unroll) {
+int mfem_gpu_batch_set_pcg_shape(mfem_batch* b, int32_t stages, int32_t keep, int32_t unroll, int32_t pdl) {
   if (!b || stages < 0 || stages > 4 || stages == 1 || keep < 0 || keep > 1 || unroll < 1 || unroll > 2 ||
-      (unroll == 2 && stages != 4))
+      (unroll == 2 && stages != 4) || pdl < 0 || pdl > 1 || (pdl && stages == 0))
     return MFEM_ERR_INVALID;
   if (b->fp64 && stages > 2) stages = 2;
   if (b->fp64) unroll = 1;
-  if (b->cgf_shape.stages == stages && b->cgf_shape.keep == keep && b->cgf_shape.unroll == unroll) return MFEM_OK;
-  b->cgf_shape = CgfShape{stages, keep, unroll};
+  const CgfShape sh{stages, keep, unroll, pdl};
+  if (b->cgf_shape.stages == sh.stages && b->cgf_shape.keep == sh.keep && b->cgf_shape.unroll == sh.unroll &&
+      b->cgf_shape.pdl == sh.pdl)
+    return MFEM_OK;
+  b->cgf_shape = sh;
   if (b->cg_graph) {  // captured with the old shape
     CUDA_OR(cudaStreamSynchronize(b->stream), MFEM_ERR_CUDA);
     cudaGraphExecDestroy(b->cg_graph);
@@ -1853,11 +1857,13 @@ int mfem_gpu_batch_set_pcg_shape(mfem_batch* b, int32_t stages, int32_t keep, in
   return MFEM_OK;
 }
 
-int mfem_gpu_batch_get_pcg_shape(mfem_batch* b, int32_t* stages, int32_t* keep, int32_t* unroll) {
+int mfem_gpu_batch_get_pcg_shape(mfem_batch* b, int32_t* stages, int32_t* keep, int32_t* unroll,
+                                 int32_t* pdl) {
   if (!b) return MFEM_ERR_INVALID;
   if (stages) *stages = b->cgf_shape.stages;
   if (keep) *keep = b->cgf_shape.keep;
   if (unroll) *unroll = b->cgf_shape.unroll;
+  if (pdl) *pdl = b->cgf_shape.pdl;
   return MFEM_OK;
 }
 

@@ -1205,7 +1205,15 @@ __device__ __forceinline__ unsigned long long l2_matrix_policy() {
   return p;
 }
 
-template <typename Real, bool kScaled, int S, int kKeep, int U>
+// Programmatic dependent launch: this grid lets the next one launch, and
+// waits for the previous one's completion (and its writes) before it reads
+// anything the previous iteration wrote.
+__device__ __forceinline__ void griddep_launch_dependents() {
+  asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+}
+__device__ __forceinline__ void griddep_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+
+template <typename Real, bool kScaled, int S, int kKeep, int U, bool kPdl>
 __device__ __forceinline__ void cgf_staged_tile(int tix, const Tile* tiles, const SceneDev* sds,
                                                 double* partials, int pstride, BatchCounters* ctrs,
                                                 unsigned char* smem) {
@@ -1214,28 +1222,19 @@ __device__ __forceinline__ void cgf_staged_tile(int tix, const Tile* tiles, cons
   const Tile t = tiles[tix];
   const SceneDev& sd = sds[t.scene];
   SceneScalars* sc = sd.sc;
-  if (!sc->cg_active) return;
-  if constexpr (sizeof(Real) == 4) {
-    if (const int ph = sc->cgf_phase) {
-      cgf_verify_tile<kScaled>(ph, tix, tiles, sds, partials, pstride, ctrs);
-      return;
+  if constexpr (!kPdl) {
+    if (!sc->cg_active) return;
+    if constexpr (sizeof(Real) == 4) {
+      if (const int ph = sc->cgf_phase) {
+        cgf_verify_tile<kScaled>(ph, tix, tiles, sds, partials, pstride, ctrs);
+        return;
+      }
     }
   }
-  const int it = sc->cg_iter;
-  const Real a = sizeof(Real) == 4 ? Real(sc->alpha_f) : Real(sc->alpha);
-  const Real b = sizeof(Real) == 4 ? Real(sc->beta_f) : Real(sc->beta);
-  const Real* r_old = static_cast<const Real*>(sd.cgf_r[it & 1]);
-  const Real* w_old = static_cast<const Real*>(sd.cgf_w[it & 1]);
-  const Real* s_old = static_cast<const Real*>(sd.cgf_s[(it + 1) & 1]);
-  Real* r_new = static_cast<Real*>(sd.cgf_r[(it + 1) & 1]);
-  Real* w_new = static_cast<Real*>(sd.cgf_w[(it + 1) & 1]);
-  Real* s_new = static_cast<Real*>(sd.cgf_s[it & 1]);
-  Real* x = static_cast<Real*>(sd.cg_x);
-  Real* u = static_cast<Real*>(sd.cg_z);
-  Real* p = static_cast<Real*>(sd.cg_p[0]);
-  using E = typename Ext<Real>::T;
-  E dots[3] = {E(0), E(0), E(0)};  // (r,r), (r,u), (w,u) at it+1
 
+  // prologue: the warp's slice and its first S slots in flight (the matrix
+  // does not change between iterations, so with kPdl this overlaps the
+  // previous iteration's tail)
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   // 32-bit shared addresses of this warp's stage ring and its mbarriers
   const uint32_t stage0 = smem_addr(smem) + (uint32_t)(warp * S) * kSlotBytes;
@@ -1262,6 +1261,36 @@ __device__ __forceinline__ void cgf_staged_tile(int tix, const Tile* tiles, cons
     }
     __syncwarp();
   }
+  if constexpr (kPdl) {
+    griddep_launch_dependents();
+    griddep_wait();
+    int ph = 0;
+    if constexpr (sizeof(Real) == 4) ph = sc->cgf_phase;
+    const bool active = sc->cg_active != 0;
+    if (!active || ph) {  // block-uniform
+      // the prefetched slots are not needed: let them land (bounded), leave
+      for (int k = 0; k < S && k < slen; ++k) mbar_wait(bar0 + 8u * k, 0u);
+      __syncwarp();
+      if constexpr (sizeof(Real) == 4) {
+        if (active) cgf_verify_tile<kScaled>(ph, tix, tiles, sds, partials, pstride, ctrs);
+      }
+      return;
+    }
+  }
+  const int it = sc->cg_iter;
+  const Real a = sizeof(Real) == 4 ? Real(sc->alpha_f) : Real(sc->alpha);
+  const Real b = sizeof(Real) == 4 ? Real(sc->beta_f) : Real(sc->beta);
+  const Real* r_old = static_cast<const Real*>(sd.cgf_r[it & 1]);
+  const Real* w_old = static_cast<const Real*>(sd.cgf_w[it & 1]);
+  const Real* s_old = static_cast<const Real*>(sd.cgf_s[(it + 1) & 1]);
+  Real* r_new = static_cast<Real*>(sd.cgf_r[(it + 1) & 1]);
+  Real* w_new = static_cast<Real*>(sd.cgf_w[(it + 1) & 1]);
+  Real* s_new = static_cast<Real*>(sd.cgf_s[it & 1]);
+  Real* x = static_cast<Real*>(sd.cg_x);
+  Real* u = static_cast<Real*>(sd.cg_z);
+  Real* p = static_cast<Real*>(sd.cg_p[0]);
+  using E = typename Ext<Real>::T;
+  E dots[3] = {E(0), E(0), E(0)};  // (r,r), (r,u), (w,u) at it+1
 
   // own row: p, x, s, r (and u) of iteration it+1, while the first slots
   // fly.  Nothing of it stays in registers across the slot loop (the 40
@@ -1406,11 +1435,11 @@ template <typename Real, int S, int U>
 constexpr int cgf_staged_min_blocks() {
   return sizeof(Real) == 4 ? (U > 1 ? 4 : (S >= 4 ? 5 : 6)) : 4;
 }
-template <typename Real, bool kScaled, int S, int kKeep, int U>
+template <typename Real, bool kScaled, int S, int kKeep, int U, bool kPdl>
 __global__ void __launch_bounds__(kCgThreads, cgf_staged_min_blocks<Real, S, U>()) k_cgf_iter_staged(
     const Tile* tiles, const SceneDev* sds, double* partials, int pstride, BatchCounters* ctrs) {
   extern __shared__ __align__(128) unsigned char cgf_smem[];
-  cgf_staged_tile<Real, kScaled, S, kKeep, U>(blockIdx.x, tiles, sds, partials, pstride, ctrs, cgf_smem);
+  cgf_staged_tile<Real, kScaled, S, kKeep, U, kPdl>(blockIdx.x, tiles, sds, partials, pstride, ctrs, cgf_smem);
 }
 
 // Nanoseconds of the GPU's global timer.
@@ -1567,27 +1596,49 @@ void launch_cg_replace(const Launch& L) {
 void launch_cgf_init(const Launch& L) { MFEM_LAUNCH_CGF(k_cgf_init); }
 
 namespace {
-template <typename Real, bool kScaled, int S, int kKeep, int U>
+template <typename Real, bool kScaled, int S, int kKeep, int U, bool kPdl>
 void launch_staged(const Launch& L) {
   const size_t smem = cgf_staged_smem_bytes<Real, S>(kCgThreads / 32);
-  k_cgf_iter_staged<Real, kScaled, S, kKeep, U>
-      <<<L.ntiles, kCgThreads, smem, L.stream>>>(L.tiles, L.sds, L.partials, L.pstride, L.counters);
+  if constexpr (kPdl) {
+    // the launch may start while the previous kernel of the stream runs; the
+    // kernel waits for it (griddepcontrol.wait) before reading its results
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(L.ntiles);
+    cfg.blockDim = dim3(kCgThreads);
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = L.stream;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    cudaLaunchKernelEx(&cfg, k_cgf_iter_staged<Real, kScaled, S, kKeep, U, true>, L.tiles, L.sds, L.partials,
+                       L.pstride, L.counters);
+  } else {
+    k_cgf_iter_staged<Real, kScaled, S, kKeep, U, false>
+        <<<L.ntiles, kCgThreads, smem, L.stream>>>(L.tiles, L.sds, L.partials, L.pstride, L.counters);
+  }
 }
-template <typename Real, bool kScaled, int kKeep>
+template <typename Real, bool kScaled, int kKeep, bool kPdl>
 void launch_staged_s(const Launch& L, int stages, int unroll) {
   if constexpr (sizeof(Real) == 4) {
-    if (unroll > 1) launch_staged<Real, kScaled, 4, kKeep, 2>(L);
-    else if (stages == 2) launch_staged<Real, kScaled, 2, kKeep, 1>(L);
-    else if (stages == 3) launch_staged<Real, kScaled, 3, kKeep, 1>(L);
-    else launch_staged<Real, kScaled, 4, kKeep, 1>(L);
+    if (unroll > 1) launch_staged<Real, kScaled, 4, kKeep, 2, kPdl>(L);
+    else if (stages == 2) launch_staged<Real, kScaled, 2, kKeep, 1, kPdl>(L);
+    else if (stages == 3) launch_staged<Real, kScaled, 3, kKeep, 1, kPdl>(L);
+    else launch_staged<Real, kScaled, 4, kKeep, 1, kPdl>(L);
   } else {
-    launch_staged<Real, kScaled, 2, kKeep, 1>(L);  // 2560-byte slots: two stages
+    launch_staged<Real, kScaled, 2, kKeep, 1, kPdl>(L);  // 2560-byte slots: two stages
   }
 }
 template <typename Real, bool kScaled>
 void launch_staged_k(const Launch& L, const CgfShape& sh) {
-  if (sh.keep) launch_staged_s<Real, kScaled, 1>(L, sh.stages, sh.unroll);
-  else launch_staged_s<Real, kScaled, 0>(L, sh.stages, sh.unroll);
+  if (sh.pdl) {
+    if (sh.keep) launch_staged_s<Real, kScaled, 1, true>(L, sh.stages, sh.unroll);
+    else launch_staged_s<Real, kScaled, 0, true>(L, sh.stages, sh.unroll);
+  } else {
+    if (sh.keep) launch_staged_s<Real, kScaled, 1, false>(L, sh.stages, sh.unroll);
+    else launch_staged_s<Real, kScaled, 0, false>(L, sh.stages, sh.unroll);
+  }
 }
 }  // namespace
 

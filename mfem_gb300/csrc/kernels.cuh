@@ -269,6 +269,9 @@ struct CgfShape {
   int stages;
   int keep;
   int unroll;
+  int pdl;  // 1 (staged shapes): each iteration a programmatic dependent
+            // launch of the previous one, its prologue (barriers, the first
+            // slots' copies) overlapping the previous iteration's tail
 };
 void launch_cgf_init(const Launch& L);
 void launch_cgf_iter(const Launch& L, const CgfShape& sh);

@@ -165,17 +165,16 @@ def set_profiling(batch_handle, enable=True):
     check(load().mfem_gpu_batch_set_profiling(batch_handle, int(enable)), "set_profiling")
 
 
-def set_pcg_shape(batch_handle, stages, keep=0, unroll=1):
+def set_pcg_shape(batch_handle, stages, keep=0, unroll=1, pdl=0):
     """Shape of the batch's fused PCG iteration (mfem_gpu_batch_set_pcg_shape)."""
-    check(load().mfem_gpu_batch_set_pcg_shape(batch_handle, int(stages), int(keep), int(unroll)),
+    check(load().mfem_gpu_batch_set_pcg_shape(batch_handle, int(stages), int(keep), int(unroll), int(pdl)),
           "set_pcg_shape")
 
 
 def get_pcg_shape(batch_handle):
-    st, kp, un = C.c_int32(), C.c_int32(), C.c_int32()
-    check(load().mfem_gpu_batch_get_pcg_shape(batch_handle, C.byref(st), C.byref(kp), C.byref(un)),
-          "get_pcg_shape")
-    return st.value, kp.value, un.value
+    v = [C.c_int32() for _ in range(4)]
+    check(load().mfem_gpu_batch_get_pcg_shape(batch_handle, *(C.byref(x) for x in v)), "get_pcg_shape")
+    return tuple(x.value for x in v)
 
 
 def kernel_stats(batch_handle):

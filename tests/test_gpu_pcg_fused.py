@@ -9,8 +9,9 @@ its kernel shapes.
   host's FP64 product against the device's float-float one).
 * Shapes: the matrix streamed through registers, or staged through 2, 3 or
   4 shared-memory buffers per warp by bulk copies, with or without the L2
-  keep policy.  They change only how the data moves: the steps are bitwise
-  the same in every shape.
+  keep policy, one or two slots' gathers in flight, with or without
+  programmatic dependent launch.  They change only how the data moves: the
+  steps are bitwise the same in every shape.
 """
 import numpy as np
 import pytest
@@ -52,13 +53,14 @@ def test_fused_shapes_compute_the_same_bits(gpu_lib, prec):
     bh = sc.solo_batch_handle()
     sc.step()
     s0 = sc.get_state()
-    shapes = [(0, 0, 1), (2, 0, 1), (3, 0, 1), (4, 0, 1), (2, 1, 1), (4, 1, 1), (4, 0, 2), (4, 1, 2)]
+    shapes = [(0, 0, 1, 0), (2, 0, 1, 0), (3, 0, 1, 0), (4, 0, 1, 0), (2, 1, 1, 0), (4, 1, 1, 0),
+              (4, 0, 2, 0), (4, 1, 2, 0), (2, 0, 1, 1), (4, 0, 2, 1), (3, 1, 1, 1)]
     fp64 = prec == abi.PRECISION_FP64
     ref = None
     for shape in shapes:
         gpu.set_pcg_shape(bh, *shape)
         got = gpu.get_pcg_shape(bh)
-        assert got == ((min(shape[0], 2), shape[1], 1) if fp64 else shape)
+        assert got == ((min(shape[0], 2), shape[1], 1, shape[3]) if fp64 else shape)
         sc.set_state(x=s0["x"], v=s0["v"], s=s0["s"], R=s0["R"])
         stats = [sc.step() for _ in range(2)]
         assert all(s.status == abi.OK for s in stats)
@@ -75,7 +77,8 @@ def test_fused_shape_is_validated(gpu_lib):
     sc = gpu.Scene(cube(6))
     bh = sc.solo_batch_handle()
     from mfem_gb300._lib import MfemError
-    for bad in ((1, 0, 1), (5, 0, 1), (-1, 0, 1), (2, 2, 1), (2, 0, 2), (4, 0, 3), (4, 0, 0)):
+    for bad in ((1, 0, 1, 0), (5, 0, 1, 0), (-1, 0, 1, 0), (2, 2, 1, 0), (2, 0, 2, 0), (4, 0, 3, 0),
+                (4, 0, 0, 0), (0, 0, 1, 1), (2, 0, 1, 2)):
         with pytest.raises(MfemError):
             gpu.set_pcg_shape(bh, *bad)
     sc.close()
