@@ -541,6 +541,7 @@ def run_ours(args):
 
     newton = float(np.mean([s["newton_iterations"] for s in stats]))
     cgits = float(np.mean([s["cg_iterations"] for s in stats]))
+    pcg_shape = dict(zip(("stages", "keep", "unroll", "pdl"), gpu.get_pcg_shape(batch_h)))
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": 1000.0 * dev_s_max / args.steps,
@@ -562,6 +563,8 @@ def run_ours(args):
         "clocks": clocks, "e2e": e2e, "roofline": roof, "gpu_launches": launches,
         "profiled_replay_ms_per_step": 1000.0 * prof_s / args.steps,
         "kernels": per_kernel,
+        "pcg_shape": pcg_shape,
+        "autotune": gpu.tune_report(batch_h),
     }
     # ---- error against the all-FP64 GPU path and the true PCG residual
     # (outside the timed region)

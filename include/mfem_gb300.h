@@ -258,6 +258,23 @@ int mfem_gpu_batch_set_pcg_shape(mfem_batch* batch, int32_t stages, int32_t keep
                                  int32_t unroll, int32_t pdl);
 int mfem_gpu_batch_get_pcg_shape(mfem_batch* batch, int32_t* stages, int32_t* keep,
                                  int32_t* unroll, int32_t* pdl);
+/* The autotuner's record for the batch as a JSON object: "source"
+ * ("tuned", "cache" or "default"), the cache key and, when tuned, for each
+ * tuned kernel the candidates' measured times per launch (per iteration for
+ * the PCG), the default's and the chosen one's.  At batch (and scene)
+ * creation the tuner times register-budget variants of K1, K5 and K6 and
+ * the fused PCG shapes on the batch's own system and keeps the fastest;
+ * every candidate computes the same bits.  MFEM_GB300_TUNE=0 keeps the
+ * built-in defaults, =force re-times on every creation;
+ * MFEM_GB300_TUNE_CACHE names the cache file.  MFEM_ERR_CAPACITY if len is
+ * too small. */
+int mfem_gpu_batch_tune_report(mfem_batch* batch, char* buf, int32_t len);
+/* Sets the register-budget variants of K1 (0..1; FP64 and the standard-FEM
+ * variable have only 0), K5 (0..2) and K6 (0..1) by hand, overriding the
+ * autotuner; 0 is the built-in default.  Every variant computes the same
+ * bits. */
+int mfem_gpu_batch_set_variants(mfem_batch* batch, int32_t elem_update, int32_t local_solve,
+                                int32_t ls_energy);
 
 /* ---- per-kernel parity entry points (host buffers in, host buffers out) ----
  * elem_update: MixedStretch::update_rotations + update_derivatives for the

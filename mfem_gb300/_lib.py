@@ -51,6 +51,8 @@ SIGNATURES = {
     "mfem_gpu_batch_kernel_stats": (C.c_int, [_vp, C.c_int, _dp, C.POINTER(C.c_int64)]),
     "mfem_gpu_batch_set_pcg_shape": (C.c_int, [_vp, C.c_int32, C.c_int32, C.c_int32, C.c_int32]),
     "mfem_gpu_batch_get_pcg_shape": (C.c_int, [_vp] + [C.POINTER(C.c_int32)] * 4),
+    "mfem_gpu_batch_tune_report": (C.c_int, [_vp, C.c_char_p, C.c_int32]),
+    "mfem_gpu_batch_set_variants": (C.c_int, [_vp, C.c_int32, C.c_int32, C.c_int32]),
     "mfem_gpu_kernel_name": (C.c_int, [C.c_int, C.c_char_p, C.c_int]),
     "mfem_gpu_bsr_pcg_noalloc": (C.c_int, [C.c_int32, C.c_int32, _vp, _vp, _vp, _vp, _vp, C.c_int32,
                                            C.c_double, _vp, _ip, _dp]),

@@ -16,10 +16,13 @@
 #include <cmath>
 #include <cstdio>
 #include <cstddef>
+#include <cstdlib>
 #include <cstring>
 #include <limits>
+#include <map>
 #include <memory>
 #include <mutex>
+#include <sys/stat.h>
 #include <new>
 #include <string>
 #include <vector>
@@ -511,6 +514,9 @@ struct mfem_batch {
   }
   int pcg_kernel = MFEM_PCG_KERNEL_PERSISTENT;
   CgfShape cgf_shape{0, 0, 1, 0};  // shape of the fused PCG iteration (same bits in every shape)
+  // register-budget variants of K1, K5, K6 chosen by the autotuner
+  int var_elem = 0, var_local = 0, var_ls = 0;
+  std::string tune_report = "{\"source\": \"default\"}";
   int minres = 0;  // every scene uses "minres-indefinite-block"
   int fem = 0;     // every scene uses the standard-FEM variable
   int jacobi = 1;  // no scene uses the 3x3 block-Jacobi preconditioner
@@ -823,28 +829,36 @@ int worst_status(const SceneScalars& sc) {
 // launch replaces 8 (single-reduction) or 50-75 (two-reduction) kernel
 // launches.  A two-reduction chunk is kCgReplace iterations long, so that the
 // residual replacement keeps its period.
+// One chunk of PCG iterations of the batch as an instantiated CUDA graph.
+int capture_cg_graph(mfem_batch* b, const Launch& Lcg, bool fused, cudaGraphExec_t* out) {
+  const int len = fused ? 8 : kCgReplace;
+  cudaGraph_t g = nullptr;
+  CUDA_OR(cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal), MFEM_ERR_CUDA);
+  for (int k = 0; k < len; ++k) {
+    if (fused) {
+      launch_cgf_iter(Lcg, b->cgf_shape);
+    } else {
+      launch_cg_spmv(Lcg);
+      launch_cg_update(Lcg);
+      if (!b->fp64 && k + 1 == kCgReplace) launch_cg_replace(Lcg);
+    }
+  }
+  const cudaError_t ec = cudaStreamEndCapture(b->stream, &g);
+  if (ec != cudaSuccess) {
+    if (g) cudaGraphDestroy(g);
+    CUDA_OR(ec, MFEM_ERR_CUDA);
+  }
+  const cudaError_t ei = cudaGraphInstantiate(out, g, 0);
+  cudaGraphDestroy(g);
+  CUDA_OR(ei, MFEM_ERR_CUDA);
+  return MFEM_OK;
+}
+
 int run_pcg_graph(mfem_batch* b, const Launch& Lcg, bool fused) {
   const int len = fused ? 8 : kCgReplace;
   if (!b->cg_graph) {
-    cudaGraph_t g = nullptr;
-    CUDA_OR(cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal), MFEM_ERR_CUDA);
-    for (int k = 0; k < len; ++k) {
-      if (fused) {
-        launch_cgf_iter(Lcg, b->cgf_shape);
-      } else {
-        launch_cg_spmv(Lcg);
-        launch_cg_update(Lcg);
-        if (!b->fp64 && k + 1 == kCgReplace) launch_cg_replace(Lcg);
-      }
-    }
-    const cudaError_t ec = cudaStreamEndCapture(b->stream, &g);
-    if (ec != cudaSuccess) {
-      if (g) cudaGraphDestroy(g);
-      CUDA_OR(ec, MFEM_ERR_CUDA);
-    }
-    const cudaError_t ei = cudaGraphInstantiate(&b->cg_graph, g, 0);
-    cudaGraphDestroy(g);
-    CUDA_OR(ei, MFEM_ERR_CUDA);
+    const int rc = capture_cg_graph(b, Lcg, fused, &b->cg_graph);
+    if (rc) return rc;
   }
   // the mixed single-reduction form verifies its stop in launches of its
   // own (at most 4 rounds of two, and one to write the solution)
@@ -879,7 +893,6 @@ int run_pcg_graph(mfem_batch* b, const Launch& Lcg, bool fused) {
 }
 
 int run_pcg(mfem_batch* b, const Launch& Lcg) {
-  int rc;
   const bool fused = b->pcg_kernel == MFEM_PCG_KERNEL_FUSED;
   {
     KTimer t(b, MFEM_K_CG_INIT);
@@ -975,16 +988,31 @@ int batch_newton(mfem_batch* b) {
   int rc;
   for (int newton = 0; newton <= b->max_newton + 1; ++newton) {
     b->newton_index = newton;
-    { KTimer t(b, MFEM_K_ELEM_UPDATE); launch_elem_update(make_launch(b, TB_ELEM), nullptr); }
+    {
+      KTimer t(b, MFEM_K_ELEM_UPDATE);
+      Launch l = make_launch(b, TB_ELEM);
+      l.variant = b->var_elem;
+      launch_elem_update(l, nullptr);
+    }
     { KTimer t(b, MFEM_K_ASSEMBLE); launch_assemble(make_launch(b, TB_ROW)); }
     if (b->minres) {
       if ((rc = run_minres(b, Lev))) return rc;
     } else if ((rc = run_pcg(b, make_launch(b, TB_CG)))) {
       return rc;
     }
-    { KTimer t(b, MFEM_K_LOCAL_SOLVE); launch_local_solve(Lev); }
+    {
+      KTimer t(b, MFEM_K_LOCAL_SOLVE);
+      Launch l = Lev;
+      l.variant = b->var_local;
+      launch_local_solve(l);
+    }
     for (int l = 0; l < b->max_ls; ++l) {
-      { KTimer t(b, MFEM_K_LS_ENERGY); launch_ls_energy(Lev); }
+      {
+        KTimer t(b, MFEM_K_LS_ENERGY);
+        Launch le = Lev;
+        le.variant = b->var_ls;
+        launch_ls_energy(le);
+      }
       if ((rc = sync_counters(b))) return rc;
       if (b->h_ctr->ls_active == 0) break;
     }
@@ -1045,6 +1073,311 @@ int upload_sds(mfem_batch* b) {
   CUDA_OR(cudaStreamSynchronize(b->stream), MFEM_ERR_CUDA);
   return MFEM_OK;
 }
+
+// ------------------------------------------------------------ autotuner ---
+// A batch picks, per kernel, the fastest of variants that compute the same
+// bits: the fused PCG iteration's shape (matrix through registers or
+// staged through 2-4 shared-memory buffers, L2 keep policy, two slots in
+// flight, programmatic dependent launch) and the register budgets of K1,
+// K5 and K6.  At batch creation every candidate is timed on the batch's
+// own system with CUDA events (a few launches each); the choice is cached
+// in memory and on disk, keyed by GPU, precision, solver and the size
+// class of the batch (half-octaves of its element and PCG tile counts), so
+// that later batches of that class skip the timing.
+//   MFEM_GB300_TUNE        "0": built-in defaults, no timing; "force":
+//                          always time; otherwise time on a cache miss
+//   MFEM_GB300_TUNE_CACHE  cache file (default
+//                          $XDG_CACHE_HOME or ~/.cache, mfem_gb300/tune-v1.txt)
+// Nothing the timing runs leaves a trace: the rotation warm starts K1
+// overwrites are saved and restored, and every other buffer it writes is
+// recomputed before it is read in a step.
+namespace {
+
+std::mutex g_tune_mu;
+std::map<std::string, std::string> g_tune_mem;
+bool g_tune_loaded = false;
+
+int tune_mode() {
+  const char* v = std::getenv("MFEM_GB300_TUNE");
+  if (!v) return 1;
+  if (!std::strcmp(v, "0") || !std::strcmp(v, "off")) return 0;
+  if (!std::strcmp(v, "force")) return 2;
+  return 1;
+}
+
+std::string tune_cache_path() {
+  if (const char* p = std::getenv("MFEM_GB300_TUNE_CACHE")) return p;
+  std::string base;
+  if (const char* x = std::getenv("XDG_CACHE_HOME")) base = x;
+  else if (const char* h = std::getenv("HOME")) base = std::string(h) + "/.cache";
+  else return std::string();
+  return base + "/mfem_gb300/tune-v1.txt";
+}
+
+void tune_load_locked() {
+  if (g_tune_loaded) return;
+  g_tune_loaded = true;
+  const std::string path = tune_cache_path();
+  if (path.empty()) return;
+  FILE* f = std::fopen(path.c_str(), "r");
+  if (!f) return;
+  char line[1024];
+  while (std::fgets(line, sizeof line, f)) {
+    char* tab = std::strchr(line, '\t');
+    if (!tab) continue;
+    *tab = 0;
+    std::string val(tab + 1);
+    while (!val.empty() && (val.back() == '\n' || val.back() == '\r')) val.pop_back();
+    g_tune_mem[line] = val;
+  }
+  std::fclose(f);
+}
+
+void tune_store_locked(const std::string& key, const std::string& val) {
+  g_tune_mem[key] = val;
+  const std::string path = tune_cache_path();
+  if (path.empty()) return;
+  const size_t slash = path.rfind('/');
+  if (slash != std::string::npos && slash > 0) {
+    const std::string dir = path.substr(0, slash);
+    const size_t up = dir.rfind('/');
+    if (up != std::string::npos && up > 0) mkdir(dir.substr(0, up).c_str(), 0755);
+    mkdir(dir.c_str(), 0755);
+  }
+  if (FILE* f = std::fopen(path.c_str(), "a")) {
+    std::fprintf(f, "%s\t%s\n", key.c_str(), val.c_str());
+    std::fclose(f);
+  }
+}
+
+int size_class(int n) {  // half-octaves of a tile count
+  return n <= 1 ? 0 : (int)std::lround(2.0 * std::log2((double)n));
+}
+
+std::string tune_key(const mfem_batch* b) {
+  int dev = 0, sms = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  cudaDeviceProp prop;
+  std::string name = "gpu";
+  if (cudaGetDeviceProperties(&prop, dev) == cudaSuccess) name = prop.name;
+  for (char& c : name)
+    if (c == ' ' || c == '\t' || c == '|' || c == '"' || c == '\\') c = '_';
+  char buf[512];
+  std::snprintf(buf, sizeof buf, "%s|%d|fp64=%d|jacobi=%d|fem=%d|minres=%d|pcg=%d|elem=%d|cg=%d", name.c_str(),
+                sms, b->fp64, b->jacobi, b->fem, b->minres, b->pcg_kernel, size_class(b->ntiles[TB_ELEM]),
+                size_class(b->ntiles[TB_CG]));
+  return buf;
+}
+
+// Mean device time of one call of `launch` (after one untimed call).
+template <typename F>
+int time_calls(mfem_batch* b, int reps, F&& launch, float* ms) {
+  launch();
+  CUDA_OR(cudaEventRecord(b->ev0, b->stream), MFEM_ERR_CUDA);
+  for (int r = 0; r < reps; ++r) launch();
+  CUDA_OR(cudaEventRecord(b->ev1, b->stream), MFEM_ERR_CUDA);
+  CUDA_OR(cudaEventSynchronize(b->ev1), MFEM_ERR_CUDA);
+  CUDA_OR(cudaGetLastError(), MFEM_ERR_CUDA);
+  float t = 0;
+  CUDA_OR(cudaEventElapsedTime(&t, b->ev0, b->ev1), MFEM_ERR_CUDA);
+  *ms = t / reps;
+  return MFEM_OK;
+}
+
+// Index of the fastest candidate; a variant replaces the default (index 0)
+// only if it is at least 2% faster.
+int pick(const std::vector<float>& t) {
+  int best = 0;
+  for (int i = 1; i < (int)t.size(); ++i)
+    if (t[i] < t[best]) best = i;
+  return (best != 0 && t[best] < 0.98f * t[0]) ? best : 0;
+}
+
+std::vector<CgfShape> cgf_candidates(int fp64) {
+  if (fp64) return {CgfShape{0, 0, 1, 0}, CgfShape{2, 0, 1, 0}, CgfShape{2, 0, 1, 1}};
+  return {CgfShape{2, 0, 1, 1}, CgfShape{0, 0, 1, 0}, CgfShape{2, 0, 1, 0}, CgfShape{3, 0, 1, 1},
+          CgfShape{2, 1, 1, 1}, CgfShape{4, 0, 2, 1}};
+}
+
+std::string shape_str(const CgfShape& c) {
+  char buf[96];
+  std::snprintf(buf, sizeof buf, "stages=%d keep=%d unroll=%d pdl=%d", c.stages, c.keep, c.unroll, c.pdl);
+  return buf;
+}
+
+// The cached form of a choice: "stages keep unroll pdl k1 k5 k6".
+std::string choice_str(const mfem_batch* b) {
+  char buf[96];
+  std::snprintf(buf, sizeof buf, "%d %d %d %d %d %d %d", b->cgf_shape.stages, b->cgf_shape.keep,
+                b->cgf_shape.unroll, b->cgf_shape.pdl, b->var_elem, b->var_local, b->var_ls);
+  return buf;
+}
+bool parse_choice(const std::string& v, mfem_batch* b) {
+  int a[7];
+  if (std::sscanf(v.c_str(), "%d %d %d %d %d %d %d", &a[0], &a[1], &a[2], &a[3], &a[4], &a[5], &a[6]) != 7)
+    return false;
+  if (a[4] < 0 || a[4] >= elem_update_variants(b->fp64, b->fem) || a[5] < 0 ||
+      a[5] >= local_solve_variants(b->fp64) || a[6] < 0 || a[6] >= ls_energy_variants(b->fp64))
+    return false;
+  b->cgf_shape = CgfShape{a[0], a[1], a[2], a[3]};
+  b->var_elem = a[4];
+  b->var_local = a[5];
+  b->var_ls = a[6];
+  return true;
+}
+
+void json_kernel(std::string& out, const char* name, const std::vector<std::string>& names,
+                 const std::vector<float>& t, int chosen) {
+  char buf[256];
+  std::snprintf(buf, sizeof buf,
+                "\"%s\": {\"chosen\": \"%s\", \"default_ms\": %.6f, \"tuned_ms\": %.6f, \"candidates\": {", name,
+                names[chosen].c_str(), t[0], t[chosen]);
+  out += buf;
+  for (size_t i = 0; i < t.size(); ++i) {
+    std::snprintf(buf, sizeof buf, "%s\"%s\": %.6f", i ? ", " : "", names[i].c_str(), t[i]);
+    out += buf;
+  }
+  out += "}}";
+}
+
+int batch_autotune(mfem_batch* b) {
+  const int mode = tune_mode();
+  if (mode == 0) return MFEM_OK;
+  const std::string key = tune_key(b);
+  {
+    std::lock_guard<std::mutex> lk(g_tune_mu);
+    tune_load_locked();
+    auto it = g_tune_mem.find(key);
+    if (mode == 1 && it != g_tune_mem.end() && parse_choice(it->second, b)) {
+      b->tune_report = "{\"source\": \"cache\", \"key\": \"" + key + "\", \"choice\": \"" + it->second + "\"}";
+      return MFEM_OK;
+    }
+  }
+  const int n = (int)b->scenes.size();
+  // the rotation warm starts that K1 overwrites
+  size_t qbytes = 0;
+  for (mfem_scene* s : b->scenes) qbytes += 4 * (size_t)s->ntp * s->rsz;
+  char* qsave = nullptr;
+  CUDA_OR(cudaMalloc(&qsave, std::max<size_t>(qbytes, 1)), MFEM_ERR_OOM);
+  struct Free {
+    char* p;
+    ~Free() { cudaFree(p); }
+  } free_q{qsave};
+  {
+    size_t off = 0;
+    for (mfem_scene* s : b->scenes) {
+      const size_t nb = 4 * (size_t)s->ntp * s->rsz;
+      CUDA_OR(cudaMemcpyAsync(qsave + off, s->dev.quat, nb, cudaMemcpyDeviceToDevice, b->stream), MFEM_ERR_CUDA);
+      off += nb;
+    }
+  }
+  // a PCG that never stops: tolerance 0, no iteration limit
+  std::vector<SceneDev> tsd = b->h_sds;
+  for (SceneDev& d : tsd) {
+    d.cg_tol = 0.0;
+    d.max_cg = 1 << 30;
+  }
+  CUDA_OR(cudaMemcpyAsync(b->d_sds, tsd.data(), sizeof(SceneDev) * n, cudaMemcpyHostToDevice, b->stream),
+          MFEM_ERR_CUDA);
+  const Launch Lev = make_launch(b, TB_EV);
+  launch_scalars_begin(Lev, n);
+  launch_step_begin(Lev);
+  int rc;
+  std::string rep = "{\"source\": \"tuned\", \"key\": \"" + key + "\", \"kernels\": {";
+  bool first = true;
+  auto sep = [&]() {
+    if (!first) rep += ", ";
+    first = false;
+  };
+  // K1
+  {
+    const int nv = elem_update_variants(b->fp64, b->fem);
+    std::vector<float> t(nv);
+    std::vector<std::string> names;
+    for (int v = 0; v < nv; ++v) {
+      Launch l = make_launch(b, TB_ELEM);
+      l.variant = v;
+      if ((rc = time_calls(b, 3, [&]() { launch_elem_update(l, nullptr); }, &t[v]))) return rc;
+      names.push_back(elem_update_variant_name(v));
+    }
+    b->var_elem = pick(t);
+    if (nv > 1) {
+      sep();
+      json_kernel(rep, "k_elem_update", names, t, b->var_elem);
+    }
+  }
+  launch_assemble(make_launch(b, TB_ROW));
+  // the fused PCG iteration: chunks of 8 launches as graphs, as a step runs them
+  bool have_dx = false;
+  if (b->pcg_kernel == MFEM_PCG_KERNEL_FUSED && !b->minres && b->ntiles[TB_CG] >= 8) {
+    const Launch Lcg = make_launch(b, TB_CG);
+    launch_cgf_init(Lcg);
+    const std::vector<CgfShape> cand = cgf_candidates(b->fp64);
+    std::vector<float> t(cand.size());
+    std::vector<std::string> names;
+    for (size_t c = 0; c < cand.size(); ++c) {
+      b->cgf_shape = cand[c];
+      cudaGraphExec_t g = nullptr;
+      if ((rc = capture_cg_graph(b, Lcg, true, &g))) return rc;
+      rc = time_calls(b, 3, [&]() { cudaGraphLaunch(g, b->stream); }, &t[c]);
+      cudaGraphExecDestroy(g);
+      if (rc) return rc;
+      t[c] /= 8.f;  // per iteration
+      names.push_back(shape_str(cand[c]));
+    }
+    const int best = pick(t);
+    b->cgf_shape = cand[best];
+    sep();
+    json_kernel(rep, "k_cgf_iter", names, t, best);
+    have_dx = true;
+  }
+  if (!have_dx) {
+    for (mfem_scene* s : b->scenes)
+      CUDA_OR(cudaMemsetAsync(s->dev.cg_x, 0, 4 * (size_t)std::max(s->M.nf, 1) * s->rsz, b->stream),
+              MFEM_ERR_CUDA);
+  }
+  if (!b->minres) {
+    std::vector<float> t5(local_solve_variants(b->fp64)), t6(ls_energy_variants(b->fp64));
+    std::vector<std::string> n5, n6;
+    for (int v = 0; v < (int)t5.size(); ++v) {
+      Launch l = Lev;
+      l.variant = v;
+      if ((rc = time_calls(b, 3, [&]() { launch_local_solve(l); }, &t5[v]))) return rc;
+      n5.push_back(local_solve_variant_name(v));
+    }
+    for (int v = 0; v < (int)t6.size(); ++v) {
+      Launch l = Lev;
+      l.variant = v;
+      if ((rc = time_calls(b, 3, [&]() { launch_ls_energy(l); }, &t6[v]))) return rc;
+      n6.push_back(ls_energy_variant_name(v));
+    }
+    b->var_local = pick(t5);
+    b->var_ls = pick(t6);
+    sep();
+    json_kernel(rep, "k_local_solve", n5, t5, b->var_local);
+    sep();
+    json_kernel(rep, "k_ls_energy", n6, t6, b->var_ls);
+  }
+  rep += "}}";
+  // restore: rotations, the real scene parameters, counters
+  {
+    size_t off = 0;
+    for (mfem_scene* s : b->scenes) {
+      const size_t nb = 4 * (size_t)s->ntp * s->rsz;
+      CUDA_OR(cudaMemcpyAsync(s->dev.quat, qsave + off, nb, cudaMemcpyDeviceToDevice, b->stream), MFEM_ERR_CUDA);
+      off += nb;
+    }
+  }
+  CUDA_OR(cudaMemsetAsync(b->d_ctr, 0, sizeof(BatchCounters), b->stream), MFEM_ERR_CUDA);
+  if ((rc = upload_sds(b))) return rc;  // synchronises the stream
+  b->tune_report = rep;
+  std::lock_guard<std::mutex> lk(g_tune_mu);
+  tune_store_locked(key, choice_str(b));
+  return MFEM_OK;
+}
+
+}  // namespace
 
 int batch_build(mfem_scene* const* scenes, int n, mfem_batch** out) {
   if (!scenes || n <= 0 || !out) return MFEM_ERR_INVALID;
@@ -1138,6 +1471,8 @@ int batch_build(mfem_scene* const* scenes, int n, mfem_batch** out) {
   CUDA_OR(cudaMemsetAsync(b->d_ctr, 0, sizeof(BatchCounters), b->stream), MFEM_ERR_CUDA);
   int rc = upload_sds(b.get());
   if (rc) return rc;
+  std::call_once(g_configured, configure_kernels);
+  if ((rc = batch_autotune(b.get()))) return rc;
   *out = b.release();
   return MFEM_OK;
 }
@@ -1864,6 +2199,23 @@ int mfem_gpu_batch_get_pcg_shape(mfem_batch* b, int32_t* stages, int32_t* keep, 
   if (keep) *keep = b->cgf_shape.keep;
   if (unroll) *unroll = b->cgf_shape.unroll;
   if (pdl) *pdl = b->cgf_shape.pdl;
+  return MFEM_OK;
+}
+
+int mfem_gpu_batch_set_variants(mfem_batch* b, int32_t elem_update, int32_t local_solve, int32_t ls_energy) {
+  if (!b || elem_update < 0 || elem_update >= elem_update_variants(b->fp64, b->fem) || local_solve < 0 ||
+      local_solve >= local_solve_variants(b->fp64) || ls_energy < 0 || ls_energy >= ls_energy_variants(b->fp64))
+    return MFEM_ERR_INVALID;
+  b->var_elem = elem_update;
+  b->var_local = local_solve;
+  b->var_ls = ls_energy;
+  return MFEM_OK;
+}
+
+int mfem_gpu_batch_tune_report(mfem_batch* b, char* buf, int32_t len) {
+  if (!b || !buf || len <= 0) return MFEM_ERR_INVALID;
+  if ((int32_t)b->tune_report.size() + 1 > len) return MFEM_ERR_CAPACITY;
+  std::memcpy(buf, b->tune_report.c_str(), b->tune_report.size() + 1);
   return MFEM_OK;
 }
 

@@ -243,8 +243,12 @@ __global__ void __launch_bounds__(kElemTile) k_elem_init(const Tile* tiles, cons
 // element forces are tens of times the net residual, so Real forces would
 // floor the Newton residual near 1e-4.  The Hessian, ds/dF and the element
 // block stay in Real.
-template <typename Real, bool DBG>
-__global__ void __launch_bounds__(kElemTile)
+// MB: resident blocks per SM the register allocation must allow (0: the
+// compiler's own choice).  The variants differ only in register allocation
+// (the autotuner picks one per batch); each one offered is tested to
+// compute the same bits as the default.
+template <typename Real, bool DBG, int MB = 0>
+__global__ void __launch_bounds__(kElemTile, MB)
     k_elem_update(const Tile* tiles, const SceneDev* sds, ElemDebug dbg) {
   using E = typename Ext<Real>::T;
   extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -524,8 +528,8 @@ __device__ __forceinline__ typename Ext<Real>::T vertex_energy(const SceneDev& s
 // ds = (S - s) + dS/dF : dF(dx)  (the closed form of -H^{-1}(Sym la + g),
 // MixedStretch::solve), la = -Syminv (H ds + g); E(0), max |ds|, max |dx|.
 // Tile partials: 0 E(0), 1 sum |terms|, 2 max|ds|, 3 max|dx|.
-template <typename Real>
-__global__ void __launch_bounds__(kElemTile) k_local_solve(const Tile* tiles, const SceneDev* sds,
+template <typename Real, int MB>
+__global__ void __launch_bounds__(kElemTile, MB) k_local_solve(const Tile* tiles, const SceneDev* sds,
                                                            double* partials, int pstride,
                                                            BatchCounters* ctrs) {
   using E = typename Ext<Real>::T;
@@ -672,8 +676,8 @@ __global__ void __launch_bounds__(kElemTile) k_local_solve(const Tile* tiles, co
 
 // ------------------------------------------------------------------ K6 ---
 // Tile partials: 0 E(alpha), 1 sum |terms|.
-template <typename Real>
-__global__ void __launch_bounds__(kElemTile) k_ls_energy(const Tile* tiles, const SceneDev* sds,
+template <typename Real, int MB>
+__global__ void __launch_bounds__(kElemTile, MB) k_ls_energy(const Tile* tiles, const SceneDev* sds,
                                                          double* partials, int pstride,
                                                          BatchCounters* ctrs) {
   using E = typename Ext<Real>::T;
@@ -896,6 +900,7 @@ int elem_update_smem_bytes(int fp64) { return kElemTile * (rec_bytes(fp64 ? 8 : 
 
 void configure_kernels() {
   set_smem(k_elem_update<float, false>, elem_update_smem_bytes(0));
+  set_smem(k_elem_update<float, false, 2>, elem_update_smem_bytes(0));
   set_smem(k_elem_update<float, true>, elem_update_smem_bytes(0));
   set_smem(k_elem_update<double, false>, elem_update_smem_bytes(1));
   set_smem(k_elem_update<double, true>, elem_update_smem_bytes(1));
@@ -936,10 +941,26 @@ void launch_elem_update(const Launch& L, const ElemDebug* dbg) {
   } else {
     if (dbg)
       k_elem_update<float, true><<<L.ntiles, kElemTile, sm, L.stream>>>(L.tiles, L.sds, d);
+    else if (L.variant == 1)
+      k_elem_update<float, false, 2><<<L.ntiles, kElemTile, sm, L.stream>>>(L.tiles, L.sds, d);
     else
       k_elem_update<float, false><<<L.ntiles, kElemTile, sm, L.stream>>>(L.tiles, L.sds, d);
   }
 }
+
+// The variants the autotuner may pick (Launch::variant; 0 is the default).
+// Only register budgets whose builds were measured to give the default's
+// bits are offered.
+int elem_update_variants(int fp64, int fem) { return (fp64 || fem) ? 1 : 2; }
+int local_solve_variants(int) { return 3; }
+int ls_energy_variants(int) { return 2; }
+const char* elem_update_variant_name(int v) {
+  return v == 1 ? "2 blocks/SM (255 registers)" : "default (168 registers in FP32)";
+}
+const char* local_solve_variant_name(int v) {
+  return v == 1 ? "4 blocks/SM (128 registers)" : v == 2 ? "5 blocks/SM (102 registers)" : "default";
+}
+const char* ls_energy_variant_name(int v) { return v == 1 ? "8 blocks/SM (64 registers)" : "default"; }
 
 #define MFEM_LAUNCH_EV(kern, ...)                                                     \
   do {                                                                                \
@@ -950,12 +971,27 @@ void launch_elem_update(const Launch& L, const ElemDebug* dbg) {
       kern<float><<<L.ntiles, kElemTile, 0, L.stream>>>(__VA_ARGS__);                 \
   } while (0)
 
-void launch_local_solve(const Launch& L) {
-  MFEM_LAUNCH_EV(k_local_solve, L.tiles, L.sds, L.partials, L.pstride, L.counters);
-}
-void launch_ls_energy(const Launch& L) {
-  MFEM_LAUNCH_EV(k_ls_energy, L.tiles, L.sds, L.partials, L.pstride, L.counters);
-}
+// Launch of a register-budget variant: v1, v2 are the blocks per SM of
+// variants 1 and 2 (0: no such variant), variant 0 the compiler's choice.
+#define MFEM_LAUNCH_EV_MB(kern, v1, v2)                                                   \
+  do {                                                                                  \
+    if (L.ntiles == 0) return;                                                          \
+    const auto go = [&](auto k) {                                                       \
+      k<<<L.ntiles, kElemTile, 0, L.stream>>>(L.tiles, L.sds, L.partials, L.pstride, L.counters); \
+    };                                                                                  \
+    if (L.fp64) {                                                                       \
+      if (L.variant == 1) go(kern<double, v1>);                                         \
+      else if (L.variant == 2) go(kern<double, v2>);                                    \
+      else go(kern<double, 0>);                                                         \
+    } else {                                                                            \
+      if (L.variant == 1) go(kern<float, v1>);                                          \
+      else if (L.variant == 2) go(kern<float, v2>);                                     \
+      else go(kern<float, 0>);                                                          \
+    }                                                                                   \
+  } while (0)
+
+void launch_local_solve(const Launch& L) { MFEM_LAUNCH_EV_MB(k_local_solve, 4, 5); }
+void launch_ls_energy(const Launch& L) { MFEM_LAUNCH_EV_MB(k_ls_energy, 8, 0); }
 void launch_apply(const Launch& L) {
   MFEM_LAUNCH_EV(k_apply, L.tiles, L.sds, L.partials, L.pstride, L.counters);
 }

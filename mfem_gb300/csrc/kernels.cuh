@@ -238,6 +238,7 @@ struct Launch {
   int fp64;
   int fem;     // the batch's scenes use the standard-FEM variable
   int jacobi;  // no scene of the batch uses the 3x3 block-Jacobi preconditioner
+  int variant = 0;  // kernel variant chosen by the autotuner (same bits in each)
 };
 
 // Element kernels (k_elem.cu)
@@ -284,6 +285,15 @@ void launch_mr_elem(const Launch& L);    // A1: pending update, element rows of 
 void launch_mr_vert(const Launch& L);    // A2: vertex rows of K w, alpha
 void launch_mr_update(const Launch& L);  // B: vn, wn = P vn, Givens, convergence
 void launch_mr_export(const Launch& L);  // dx -> the PCG solution vector
+
+// Register-budget variants of the element kernels the autotuner may pick
+// (Launch::variant, 0 the default); each computes the default's bits.
+int elem_update_variants(int fp64, int fem);
+int local_solve_variants(int fp64);
+int ls_energy_variants(int fp64);
+const char* elem_update_variant_name(int v);
+const char* local_solve_variant_name(int v);
+const char* ls_energy_variant_name(int v);
 
 // Maximum dynamic shared memory the element kernels need.
 int elem_update_smem_bytes(int fp64);

@@ -177,6 +177,20 @@ def get_pcg_shape(batch_handle):
     return tuple(x.value for x in v)
 
 
+def set_variants(batch_handle, elem_update=0, local_solve=0, ls_energy=0):
+    """Register-budget variants of K1, K5, K6 by hand (0: built-in default)."""
+    check(load().mfem_gpu_batch_set_variants(batch_handle, int(elem_update), int(local_solve), int(ls_energy)),
+          "set_variants")
+
+
+def tune_report(batch_handle):
+    """The autotuner's record for the batch (dict)."""
+    import json
+    buf = C.create_string_buffer(1 << 16)
+    check(load().mfem_gpu_batch_tune_report(batch_handle, buf, len(buf)), "tune_report")
+    return json.loads(buf.value.decode())
+
+
 def kernel_stats(batch_handle):
     """{kernel name: (total device ms, launches)} since profiling was enabled."""
     out = {}

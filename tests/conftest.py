@@ -10,6 +10,10 @@ if ROOT not in sys.path:
 
 def pytest_configure(config):
     config.addinivalue_line("markers", "gpu: needs a CUDA GPU (GB300); runs the CUDA library")
+    # the kernel autotuner's cache of this test session: a file of its own
+    import tempfile
+    os.environ.setdefault("MFEM_GB300_TUNE_CACHE",
+                          os.path.join(tempfile.mkdtemp(prefix="mfem_tune_"), "tune.txt"))
 
 
 @pytest.fixture(scope="session")
