@@ -1185,6 +1185,27 @@ int time_calls(mfem_batch* b, int reps, F&& launch, float* ms) {
   return MFEM_OK;
 }
 
+// Mean device time of `launch` alone, each call preceded by an untimed
+// `prep` that puts its input state back (the line search's energy runs
+// only while the local solve has opened a line search).
+template <typename P, typename F>
+int time_prepped(mfem_batch* b, int reps, P&& prep, F&& launch, float* ms) {
+  float total = 0;
+  for (int r = 0; r <= reps; ++r) {
+    prep();
+    CUDA_OR(cudaEventRecord(b->ev0, b->stream), MFEM_ERR_CUDA);
+    launch();
+    CUDA_OR(cudaEventRecord(b->ev1, b->stream), MFEM_ERR_CUDA);
+    CUDA_OR(cudaEventSynchronize(b->ev1), MFEM_ERR_CUDA);
+    CUDA_OR(cudaGetLastError(), MFEM_ERR_CUDA);
+    float t = 0;
+    CUDA_OR(cudaEventElapsedTime(&t, b->ev0, b->ev1), MFEM_ERR_CUDA);
+    if (r > 0) total += t;  // the first pair warms up
+  }
+  *ms = total / reps;
+  return MFEM_OK;
+}
+
 // Index of the fastest candidate; a variant replaces the default (index 0)
 // only if it is at least 2% faster.
 int pick(const std::vector<float>& t) {
@@ -1349,7 +1370,8 @@ int batch_autotune(mfem_batch* b) {
     for (int v = 0; v < (int)t6.size(); ++v) {
       Launch l = Lev;
       l.variant = v;
-      if ((rc = time_calls(b, 3, [&]() { launch_ls_energy(l); }, &t6[v]))) return rc;
+      if ((rc = time_prepped(b, 3, [&]() { launch_local_solve(Lev); }, [&]() { launch_ls_energy(l); }, &t6[v])))
+        return rc;
       n6.push_back(ls_energy_variant_name(v));
     }
     b->var_local = pick(t5);
