@@ -72,7 +72,10 @@ def parse():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-batch", action="store_true",
                     help="skip the batched-vs-plain measurement on the 64-scene mix")
-    ap.add_argument("--batch-steps", type=int, default=3)
+    ap.add_argument("--mix-plain-steps", type=int, default=3,
+                    help="timesteps per scene of the plain (one scene at a time) 64-scene mix")
+    ap.add_argument("--mix-steps", type=int, default=100,
+                    help="timesteps per scene of the batched 64-scene mix (its stated 100)")
     ap.add_argument("--no-error", action="store_true",
                     help="skip the error-vs-FP64 replay and the true PCG residual")
     ap.add_argument("--error-steps", type=int, default=10,
@@ -594,46 +597,88 @@ def run_ours(args):
 
 def run_batch_mix(args, gpu, abi, configs):
     """The 64-scene mix (cube grids 4..30 per axis, random materials and
-    pinned face, seeded): the batch stepped together (one launch per kernel
-    phase for all scenes) against each scene stepped alone, one after the
-    other.  Both from rest after the same warm-up; timesteps/s counts
-    scene-steps; device time from CUDA events around each step."""
+    pinned face, seeded).  After the same 2 warm-up steps:
+
+    batched    the stated 100 timesteps of every scene in one
+               mfem_gpu_batch_step_n call, each scene at its own pace
+    batched_3  the same form over 3 timesteps from the same state, beside
+    lockstep   the one-step batch form (every scene waits for the slowest
+               scene's Newton loop each step), 3 steps from that state, and
+    plain      each scene alone through mfem_gpu_scene_step, one after the
+               other, 3 steps per scene
+    timesteps/s counts scene-steps; device time from CUDA events.  Latency:
+    the device time between a scene's consecutive steps in the 100-step
+    call.  A scene whose step ends non-finite is retired (its remaining
+    steps are not taken and not counted)."""
     kern = {"persistent": abi.PCG_KERNEL_PERSISTENT, "split": abi.PCG_KERNEL_SPLIT,
             "fused": abi.PCG_KERNEL_FUSED, "auto": abi.PCG_KERNEL_AUTO}[args.pcg_kernel]
     specs = configs.batch_c4(pcg_kernel=kern)
     n = len(specs)
     tets = int(sum(s.n_tets for s in specs))
-    warm, steps = 2, max(1, args.batch_steps)
+    warm, steps, short = 2, args.mix_steps, 3
     scenes = [gpu.Scene(s) for s in specs]
     batch = gpu.Batch(scenes)
     for _ in range(warm):
-        batch.step()
-    ms, newton = [], []
-    for _ in range(steps):
-        stats = batch.step()
-        ms.append(stats[0].device_ms)
-        newton.append(max(st.newton_iterations for st in stats))
+        batch.step(raise_on_error=False)
+    snap = [s.snapshot() for s in scenes]
+
+    def restore():
+        for sc, sn in zip(scenes, snap):
+            sc.restore(sn)
+
+    st3, d3 = batch.step_n(short, raise_on_error=False)
+    b3 = int((d3 >= 0).sum()) / (st3[0].device_ms / 1e3)
+    restore()
+    ls_ms = [batch.step(raise_on_error=False)[0].device_ms for _ in range(short)]
+    lockstep = n / (float(np.mean(ls_ms)) / 1e3)
+    restore()
+    stats, done = batch.step_n(steps, raise_on_error=False)
+    batched_ms = stats[0].device_ms
     batch.close()
     for s in scenes:
         s.close()
-    batched = n * steps / (sum(ms) / 1e3)
-    plain_ms, plain_steps = 0.0, 1
+    taken = done >= 0
+    lat = np.diff(np.concatenate([np.zeros((n, 1)), np.where(taken, done, np.nan)], axis=1), axis=1)
+    lat = lat[np.isfinite(lat)]
+    scene_steps = int(taken.sum())
+    newton = float(np.sum([st.newton_iterations for st in stats])) / max(scene_steps, 1)
+    failed = [i for i, st in enumerate(stats) if st.status not in (abi.OK, abi.ERR_LS_FAILED, abi.ERR_CG_MAXITER)]
+    finish = np.array([float(d[t].max()) if t.any() else 0.0 for d, t in zip(done, taken)])
+    slowest = list(np.argsort(-finish)[:3])
+    batched = scene_steps / (batched_ms / 1e3)
+    plain_ms, plain_n, plain_steps = 0.0, 0, args.mix_plain_steps
     for sp in specs:
         s = gpu.Scene(sp)
         for _ in range(warm):
             s.step()
         for _ in range(plain_steps):
-            plain_ms += s.step().device_ms
+            st = s.step()
+            plain_ms += st.device_ms
+            plain_n += 1
+            if st.status in (abi.ERR_NONFINITE, abi.ERR_PROCRUSTES):
+                break  # retired, as in the batched form
         s.close()
-    plain = n * plain_steps / (plain_ms / 1e3)
+    plain = plain_n / (plain_ms / 1e3)
     return {"workload": f"batch_c4_{n}_scenes", "scenes": n, "tets_total": tets,
             "batched": {"value": batched, "unit": UNIT, "steps": steps, "warmup": warm,
-                        "ms_per_batch_step": float(np.mean(ms)),
-                        "p50_ms": float(np.percentile(ms, 50)), "p99_ms": float(np.percentile(ms, 99)),
-                        "newton_max_per_step": float(np.mean(newton))},
+                        "form": "mfem_gpu_batch_step_n (each scene at its own pace)",
+                        "ms_total": batched_ms, "scene_steps": scene_steps,
+                        "newton_per_scene_step": newton,
+                        "p50_ms": float(np.percentile(lat, 50)), "p99_ms": float(np.percentile(lat, 99)),
+                        "scenes_done_ms_p50_p90_max": [float(np.percentile(finish, 50)),
+                                                       float(np.percentile(finish, 90)), float(finish.max())],
+                        "failed_scenes": [{"scene": int(i), "tets": specs[i].n_tets, "status": int(stats[i].status),
+                                           "steps_done": int(taken[i].sum())} for i in failed],
+                        "slowest_scenes": [{"scene": int(i), "tets": specs[i].n_tets, "done_ms": float(finish[i]),
+                                            "newton": int(stats[i].newton_iterations),
+                                            "cg": int(stats[i].cg_iterations)} for i in slowest]},
+            "batched_3": {"value": b3, "unit": UNIT, "steps": short},
+            "lockstep": {"value": lockstep, "unit": UNIT, "steps": short,
+                         "ms_per_batch_step": float(np.mean(ls_ms))},
             "plain": {"value": plain, "unit": UNIT, "steps_per_scene": plain_steps, "warmup": warm,
-                      "ms_per_scene_step": plain_ms / (n * plain_steps)},
-            "batched_vs_plain": batched / plain}
+                      "scene_steps": plain_n, "ms_per_scene_step": plain_ms / max(plain_n, 1)},
+            "batched_vs_plain": batched / plain, "batched_3_vs_plain": b3 / plain,
+            "lockstep_vs_plain": lockstep / plain}
 
 
 def run_served(args):

@@ -218,6 +218,23 @@ int mfem_gpu_batch_create(mfem_scene* const* scenes, int32_t n, mfem_batch** out
 int mfem_gpu_batch_destroy(mfem_batch* batch);
 /* Steps every scene in the batch once; stats[i] belongs to scenes[i]. */
 int mfem_gpu_batch_step(mfem_batch* batch, mfem_step_stats* stats);
+/* Steps every scene `steps` timesteps (1..MFEM_BATCH_MAX_STEPS), each at its
+ * own pace: a scene whose Newton loop has ended turns over to its next
+ * timestep at once and joins the next round of launches, instead of waiting
+ * for the batch's slowest scene (no counterpart in the reference, where
+ * each scene is its own NewtonOptimizer::step loop).  The results are those
+ * of `steps` calls of mfem_gpu_batch_step, bitwise.  stats[i]: status the
+ * worst of scene i's steps, Newton / PCG / line-search iterations summed
+ * over them, energy and residuals of its last step, device_ms the call's
+ * time.  step_done_ms (optional; steps doubles per scene, scene-major): the
+ * device time from the call's start at which each step of each scene was
+ * done (-1 for a step not taken).  A scene whose step ends non-finite or
+ * with a singular rotation solve is retired: its remaining steps are not
+ * taken and its status is that step's.  Scripted boundary motion is
+ * precomputed on the host for the call's steps. */
+#define MFEM_BATCH_MAX_STEPS 1024
+int mfem_gpu_batch_step_n(mfem_batch* batch, int32_t steps, mfem_step_stats* stats,
+                          double* step_done_ms);
 
 /* Prescribed positions of the pinned vertices for the next step (3*n_pinned
  * doubles in the order of mfem_gpu_scene_pinned), replacing the scripted

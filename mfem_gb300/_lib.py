@@ -40,6 +40,7 @@ SIGNATURES = {
     "mfem_gpu_batch_create": (C.c_int, [C.POINTER(_vp), C.c_int32, C.POINTER(_vp)]),
     "mfem_gpu_batch_destroy": (C.c_int, [_vp]),
     "mfem_gpu_batch_step": (C.c_int, [_vp, _vp]),
+    "mfem_gpu_batch_step_n": (C.c_int, [_vp, C.c_int32, _vp, _dp]),
     "mfem_gpu_scene_elem_update": (C.c_int, [_vp, _dp, C.c_double] + [_dp] * 8),
     "mfem_gpu_scene_bcsr_sizes": (C.c_int, [_vp, _ip, _ip]),
     "mfem_gpu_scene_get_system": (C.c_int, [_vp, _ip, _ip, _dp, _dp]),

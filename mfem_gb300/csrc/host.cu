@@ -50,6 +50,7 @@ void set_error(const char* what, cudaError_t e) {
   } while (0)
 
 std::once_flag g_configured;
+constexpr int kMaxCallSteps = MFEM_BATCH_MAX_STEPS;  // timesteps of one mfem_gpu_batch_step_n call
 
 size_t align_up(size_t v, size_t a) { return (v + a - 1) / a * a; }
 
@@ -477,6 +478,10 @@ struct mfem_scene {
   mfem_batch* solo = nullptr;
   int nnzb = 0;
   bool pins_driven = false;  // pins set by the caller for the next step
+  // mfem_gpu_batch_step_n: the pins after each BC step of a call (grown on
+  // demand; 3 npin doubles per step) and its pinned host staging
+  double* d_pin_traj = nullptr;
+  size_t pin_traj_cap = 0;  // steps it holds
   // device checkpoint (mfem_gpu_scene_checkpoint): raw copies of the state
   char* ckpt = nullptr;
   int ckpt_head = 0;
@@ -491,6 +496,14 @@ struct mfem_batch {
   char* dmem = nullptr;
   Tile* d_tiles[TB_COUNT] = {nullptr, nullptr, nullptr, nullptr};
   int ntiles[TB_COUNT] = {0, 0, 0, 0};
+  // the tables the kernels are launched over: the full ones, or during a
+  // multi-step call the tiles of the scenes still stepping (compacted into
+  // d_tiles_c as scenes finish), with each scene's tile range
+  Tile* cur_tiles[TB_COUNT] = {nullptr, nullptr, nullptr, nullptr};
+  int cur_ntiles[TB_COUNT] = {0, 0, 0, 0};
+  Tile* d_tiles_c[TB_COUNT] = {nullptr, nullptr, nullptr, nullptr};
+  std::vector<Tile> h_tiles[TB_COUNT];
+  std::vector<int> full_first, full_count;  // scene x TB_COUNT
   SceneDev* d_sds = nullptr;
   std::vector<SceneDev> h_sds;
   double* d_partials = nullptr;
@@ -517,6 +530,17 @@ struct mfem_batch {
   // register-budget variants of K1, K5, K6 chosen by the autotuner
   int var_elem = 0, var_local = 0, var_ls = 0;
   std::string tune_report = "{\"source\": \"default\"}";
+  // mfem_gpu_batch_step_n: per scene and step the device time it was done
+  // (kMaxCallSteps per scene, then the call's start), and the ticked form's
+  // graph of one tick (captured on first use, dropped when a kernel shape or
+  // variant changes)
+  unsigned long long* d_step_ns = nullptr;
+  cudaGraphExec_t tick_graph = nullptr;
+  cudaGraphExec_t tick_graph_c = nullptr;  // the same over compacted tables
+  // PCG iterations in one tick: 16 measured best between the 64-scene mix's
+  // total time (8 iterations: 8.6 s for 100 steps, 16: 8.0 s, 32: 7.7 s) and
+  // the per-step latency of its light scenes
+  int tick_pcg = 16;
   int minres = 0;  // every scene uses "minres-indefinite-block"
   int fem = 0;     // every scene uses the standard-FEM variable
   int jacobi = 1;  // no scene uses the 3x3 block-Jacobi preconditioner
@@ -573,8 +597,8 @@ void harvest_timers(mfem_batch* b) {
 Launch make_launch(mfem_batch* b, int table) {
   Launch L;
   L.stream = b->stream;
-  L.tiles = b->d_tiles[table];
-  L.ntiles = b->ntiles[table];
+  L.tiles = b->cur_tiles[table];
+  L.ntiles = b->cur_ntiles[table];
   L.sds = b->d_sds;
   L.partials = b->d_partials;
   L.pstride = b->pstride;
@@ -764,14 +788,10 @@ int sync_counters(mfem_batch* b) {
   return MFEM_OK;
 }
 
-// Moves the pinned vertices by one BC step on the host and uploads them
-// (Meshes::update_bcs, meshes.cpp:156-167).
-int bc_step_upload(mfem_scene* s, cudaStream_t st) {
+// Moves the pinned vertices by one BC step on the host
+// (Meshes::update_bcs, meshes.cpp:156-167); true if any moved.
+bool bc_advance(mfem_scene* s) {
   HostMesh& M = s->M;
-  if (s->pins_driven) {  // the caller already uploaded this step's pins
-    s->pins_driven = false;
-    return MFEM_OK;
-  }
   bool moved = false;
   const double dt = s->h;
   for (int p = 0; p < M.npin; ++p) {
@@ -806,8 +826,17 @@ int bc_step_upload(mfem_scene* s, cudaStream_t st) {
         break;
     }
   }
-  if (moved && M.npin > 0)
-    CUDA_OR(cudaMemcpyAsync(s->d_pin_pos, s->pin_pos.data(), 3 * sizeof(double) * M.npin,
+  return moved;
+}
+
+// One BC step of the pins, uploaded for the step's end.
+int bc_step_upload(mfem_scene* s, cudaStream_t st) {
+  if (s->pins_driven) {  // the caller already uploaded this step's pins
+    s->pins_driven = false;
+    return MFEM_OK;
+  }
+  if (bc_advance(s) && s->M.npin > 0)
+    CUDA_OR(cudaMemcpyAsync(s->d_pin_pos, s->pin_pos.data(), 3 * sizeof(double) * s->M.npin,
                             cudaMemcpyHostToDevice, st),
             MFEM_ERR_CUDA);
   return MFEM_OK;
@@ -1062,6 +1091,304 @@ int batch_step_impl(mfem_batch* b, mfem_step_stats* stats) {
       st.device_ms = ms;
     }
     if (sc.status == MFEM_ERR_NONFINITE) worst = MFEM_ERR_NONFINITE;
+  }
+  return worst;
+}
+
+int upload_sds(mfem_batch* b);
+
+// One tick of the ticked multi-step form as a CUDA graph over the current
+// tables: every kernel of a Newton iteration once, each acting on the
+// scenes in its phase, with tick_pcg PCG iterations and one line-search
+// trial.
+int capture_tick_graph(mfem_batch* b, cudaGraphExec_t* out) {
+  Launch Lel = make_launch(b, TB_ELEM);
+  Lel.variant = b->var_elem;
+  const Launch Lev = make_launch(b, TB_EV);
+  Launch Llo = Lev, Lls = Lev;
+  Llo.variant = b->var_local;
+  Lls.variant = b->var_ls;
+  const Launch Lcg = make_launch(b, TB_CG);
+  cudaGraph_t g = nullptr;
+  CUDA_OR(cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal), MFEM_ERR_CUDA);
+  launch_elem_update(Lel, nullptr);
+  launch_assemble(make_launch(b, TB_ROW));
+  launch_cgf_init(Lcg);
+  for (int k = 0; k < b->tick_pcg; ++k) launch_cgf_iter(Lcg, b->cgf_shape);
+  launch_local_solve(Llo);
+  launch_ls_energy(Lls);
+  launch_apply(Lev);
+  launch_step_turn(Lev);
+  const cudaError_t ec = cudaStreamEndCapture(b->stream, &g);
+  if (ec != cudaSuccess) {
+    if (g) cudaGraphDestroy(g);
+    CUDA_OR(ec, MFEM_ERR_CUDA);
+  }
+  const cudaError_t ei = cudaGraphInstantiate(out, g, 0);
+  cudaGraphDestroy(g);
+  CUDA_OR(ei, MFEM_ERR_CUDA);
+  return MFEM_OK;
+}
+
+// The kernels' tables become the tiles of the scenes with active[i] set
+// (each scene's tiles stay contiguous, so its ticket groups and partials are
+// unchanged); the others get no tiles.  The stream must be idle.
+int compact_tables(mfem_batch* b, const std::vector<char>& active) {
+  const int n = (int)b->scenes.size();
+  for (int tb = 0; tb < TB_COUNT; ++tb) {
+    std::vector<Tile> t;
+    for (int i = 0; i < n; ++i) {
+      const int f = b->full_first[(size_t)i * TB_COUNT + tb], c = b->full_count[(size_t)i * TB_COUNT + tb];
+      b->h_sds[i].tile_first[tb] = (int)t.size();
+      b->h_sds[i].tile_count[tb] = active[i] ? c : 0;
+      if (active[i]) t.insert(t.end(), b->h_tiles[tb].begin() + f, b->h_tiles[tb].begin() + f + c);
+    }
+    if (!t.empty())
+      CUDA_OR(cudaMemcpyAsync(b->d_tiles_c[tb], t.data(), sizeof(Tile) * t.size(), cudaMemcpyHostToDevice,
+                              b->stream),
+              MFEM_ERR_CUDA);
+    b->cur_tiles[tb] = b->d_tiles_c[tb];
+    b->cur_ntiles[tb] = (int)t.size();
+  }
+  int rc = upload_sds(b);
+  if (rc) return rc;
+  if (b->tick_graph_c) cudaGraphExecDestroy(b->tick_graph_c);
+  b->tick_graph_c = nullptr;
+  return capture_tick_graph(b, &b->tick_graph_c);
+}
+
+// The full tables again.
+int restore_tables(mfem_batch* b) {
+  const int n = (int)b->scenes.size();
+  for (int tb = 0; tb < TB_COUNT; ++tb) {
+    b->cur_tiles[tb] = b->d_tiles[tb];
+    b->cur_ntiles[tb] = b->ntiles[tb];
+    for (int i = 0; i < n; ++i) {
+      b->h_sds[i].tile_first[tb] = b->full_first[(size_t)i * TB_COUNT + tb];
+      b->h_sds[i].tile_count[tb] = b->full_count[(size_t)i * TB_COUNT + tb];
+    }
+  }
+  if (b->tick_graph_c) cudaGraphExecDestroy(b->tick_graph_c);
+  b->tick_graph_c = nullptr;
+  return upload_sds(b);
+}
+
+// Several timesteps per scene in one call, each scene at its own pace
+// (mfem_gpu_batch_step_n).  A round is one Newton iteration of every scene
+// that still has steps to take: K1, assembly, the linear solve, the local
+// solve, the line search, the update; then k_step_turn turns over every
+// scene whose Newton loop ended in the round, so that it starts its next
+// timestep in the next round instead of waiting for the batch's slowest
+// scene.  The arithmetic of each scene is that of n calls of
+// mfem_gpu_batch_step (the same kernels and device functions).
+int batch_step_n_impl(mfem_batch* b, int steps, mfem_step_stats* stats, double* step_done_ms) {
+  std::call_once(g_configured, configure_kernels);
+  const int n = (int)b->scenes.size();
+  int rc;
+  // pins after each BC step of the call, for scenes whose pins move
+  for (int i = 0; i < n; ++i) {
+    mfem_scene* s = b->scenes[i];
+    const int np = s->M.npin;
+    const bool scripted = np > 0 && (s->pins_driven || s->M.bc_type == MFEM_BC_STRETCH ||
+                                     s->M.bc_type == MFEM_BC_COMPRESS || s->M.bc_type == MFEM_BC_TWIST ||
+                                     s->M.bc_type == MFEM_BC_BEND);
+    b->h_sds[i].pin_traj = nullptr;
+    if (!scripted) continue;
+    if (s->pin_traj_cap < (size_t)steps) {
+      if (s->d_pin_traj) cudaFree(s->d_pin_traj);
+      s->d_pin_traj = nullptr;
+      s->pin_traj_cap = 0;
+      CUDA_OR(cudaMalloc(&s->d_pin_traj, sizeof(double) * 3 * (size_t)np * steps), MFEM_ERR_OOM);
+      s->pin_traj_cap = (size_t)steps;
+    }
+    std::vector<double> traj(3 * (size_t)np * steps);
+    for (int j = 0; j < steps; ++j) {
+      if (j == 0 && s->pins_driven) s->pins_driven = false;  // the caller's pins for the first step
+      else bc_advance(s);
+      std::memcpy(&traj[3 * (size_t)np * j], s->pin_pos.data(), sizeof(double) * 3 * np);
+    }
+    CUDA_OR(cudaMemcpyAsync(s->d_pin_traj, traj.data(), sizeof(double) * traj.size(), cudaMemcpyHostToDevice,
+                            b->stream),
+            MFEM_ERR_CUDA);
+    // the pins after the call, as the plain form leaves them for later steps
+    CUDA_OR(cudaMemcpyAsync(s->d_pin_pos, s->pin_pos.data(), sizeof(double) * 3 * np, cudaMemcpyHostToDevice,
+                            b->stream),
+            MFEM_ERR_CUDA);
+    b->h_sds[i].pin_traj = s->d_pin_traj;
+  }
+  if ((rc = upload_sds(b))) return rc;  // synchronises: the host trajectories may go
+  // the ticked form needs every kernel of a Newton iteration to be gated by
+  // the scene's phase (the single-reduction PCG and the reduced system) and
+  // every scene to have rows to assemble and solve
+  bool ticked = b->pcg_kernel == MFEM_PCG_KERNEL_FUSED && !b->minres;
+  for (mfem_scene* s : b->scenes)
+    if (s->M.nf == 0) ticked = false;
+  unsigned long long* t_start = b->d_step_ns + (size_t)n * kMaxCallSteps;
+  CUDA_OR(cudaEventRecord(b->ev0, b->stream), MFEM_ERR_CUDA);
+  launch_stamp(t_start, b->stream);
+  Launch Lev = make_launch(b, TB_EV);
+  { KTimer t(b, MFEM_K_SCALARS); launch_scalars_begin_n(Lev, n, steps, ticked ? 1 : 0); }
+  { KTimer t(b, MFEM_K_STEP_BEGIN); launch_step_begin(Lev); }
+  if (ticked) {
+    // One tick: every kernel of a Newton iteration once, each acting on the
+    // scenes in its phase, with tick_pcg PCG iterations and one line-search
+    // trial; a scene goes as far through its iteration as the tick takes it
+    // and never waits for another scene.  The host reads the batch's
+    // counters after every few ticks, one check behind.
+    if (!b->tick_graph && (rc = capture_tick_graph(b, &b->tick_graph))) return rc;
+    constexpr int kTicksPerCheck = 4;
+    const long max_ticks = (long)steps * (b->max_newton + 2) * ((b->max_cg + 17) / b->tick_pcg + b->max_ls + 4);
+    long ticks = 0;
+    int nchunk = 0;
+    bool finished = false;
+    int table_scenes = n;  // scenes in the tables the ticks run over
+    cudaGraphExec_t tick = b->tick_graph;
+    while (ticks < max_ticks) {
+      for (int r = 0; r < kTicksPerCheck; ++r, ++ticks) {
+        const cudaError_t e = cudaGraphLaunch(tick, b->stream);
+        if (e != cudaSuccess) {
+          if (tick != b->tick_graph) restore_tables(b);
+          CUDA_OR(e, MFEM_ERR_CUDA);
+        }
+      }
+      const int slot = nchunk & 1;
+      CUDA_OR(cudaMemcpyAsync(&b->h_ctr_pipe[slot], b->d_ctr, sizeof(BatchCounters), cudaMemcpyDeviceToHost,
+                              b->stream),
+              MFEM_ERR_CUDA);
+      CUDA_OR(cudaEventRecord(b->ev_pipe[slot], b->stream), MFEM_ERR_CUDA);
+      if (nchunk > 0) {
+        CUDA_OR(cudaEventSynchronize(b->ev_pipe[slot ^ 1]), MFEM_ERR_CUDA);
+        const BatchCounters& c = b->h_ctr_pipe[slot ^ 1];
+        if (c.error) {
+          if (tick != b->tick_graph) restore_tables(b);
+          return MFEM_ERR_TIMEOUT;
+        }
+        if (c.newton_active == 0) {
+          finished = true;
+          break;
+        }
+        // half the scenes in the tables have finished: launch over the
+        // tiles of those still stepping from now on
+        if (table_scenes >= 4 && c.newton_active <= table_scenes / 2) {
+          CUDA_OR(cudaStreamSynchronize(b->stream), MFEM_ERR_CUDA);
+          for (int i = 0; i < n; ++i)
+            CUDA_OR(cudaMemcpyAsync(&b->h_sc[i], b->scenes[i]->d_sc, sizeof(SceneScalars),
+                                    cudaMemcpyDeviceToHost, b->stream),
+                    MFEM_ERR_CUDA);
+          CUDA_OR(cudaStreamSynchronize(b->stream), MFEM_ERR_CUDA);
+          std::vector<char> active(n);
+          int na = 0;
+          for (int i = 0; i < n; ++i) na += (active[i] = b->h_sc[i].newton_active ? 1 : 0);
+          if (na == 0) {
+            finished = true;
+            break;
+          }
+          if ((rc = compact_tables(b, active))) {
+            restore_tables(b);
+            return rc;
+          }
+          tick = b->tick_graph_c;
+          table_scenes = na;
+          nchunk = 0;
+          continue;
+        }
+      }
+      ++nchunk;
+    }
+    if (tick != b->tick_graph && (rc = restore_tables(b))) return rc;
+    if (!finished) {
+      if ((rc = sync_counters(b))) return rc;
+      if (b->h_ctr->error) return MFEM_ERR_TIMEOUT;
+    }
+  } else {
+    // rounds: one Newton iteration of every scene that still has steps to
+    // take; every step of a scene ends within max_newton + 2 rounds
+    const long max_rounds = (long)steps * (b->max_newton + 2);
+    for (long round = 0; round < max_rounds; ++round) {
+      b->newton_index = 0;  // scenes sit at different Newton iterations: one shared PCG hint
+      {
+        KTimer t(b, MFEM_K_ELEM_UPDATE);
+        Launch l = make_launch(b, TB_ELEM);
+        l.variant = b->var_elem;
+        launch_elem_update(l, nullptr);
+      }
+      { KTimer t(b, MFEM_K_ASSEMBLE); launch_assemble(make_launch(b, TB_ROW)); }
+      if (b->minres) {
+        if ((rc = run_minres(b, Lev))) return rc;
+      } else if ((rc = run_pcg(b, make_launch(b, TB_CG)))) {
+        return rc;
+      }
+      {
+        KTimer t(b, MFEM_K_LOCAL_SOLVE);
+        Launch l = Lev;
+        l.variant = b->var_local;
+        launch_local_solve(l);
+      }
+      for (int l = 0; l < b->max_ls; ++l) {
+        {
+          KTimer t(b, MFEM_K_LS_ENERGY);
+          Launch le = Lev;
+          le.variant = b->var_ls;
+          launch_ls_energy(le);
+        }
+        if ((rc = sync_counters(b))) return rc;
+        if (b->h_ctr->ls_active == 0) break;
+      }
+      { KTimer t(b, MFEM_K_APPLY); launch_apply(Lev); }
+      { KTimer t(b, MFEM_K_STEP_END); launch_step_turn(Lev); }
+      if ((rc = sync_counters(b))) return rc;
+      if (b->h_ctr->error) return MFEM_ERR_TIMEOUT;
+      if (b->h_ctr->newton_active == 0) break;
+    }
+  }
+  CUDA_OR(cudaEventRecord(b->ev1, b->stream), MFEM_ERR_CUDA);
+  for (int i = 0; i < n; ++i)
+    CUDA_OR(cudaMemcpyAsync(&b->h_sc[i], b->scenes[i]->d_sc, sizeof(SceneScalars), cudaMemcpyDeviceToHost,
+                            b->stream),
+            MFEM_ERR_CUDA);
+  std::vector<unsigned long long> sns((size_t)n * kMaxCallSteps + 1);
+  CUDA_OR(cudaMemcpyAsync(sns.data(), b->d_step_ns, sizeof(unsigned long long) * sns.size(),
+                          cudaMemcpyDeviceToHost, b->stream),
+          MFEM_ERR_CUDA);
+  CUDA_OR(cudaStreamSynchronize(b->stream), MFEM_ERR_CUDA);
+  CUDA_OR(cudaGetLastError(), MFEM_ERR_CUDA);
+  harvest_timers(b);
+  float ms = 0;
+  cudaEventElapsedTime(&ms, b->ev0, b->ev1);
+  const unsigned long long t0 = sns[(size_t)n * kMaxCallSteps];
+  int worst = MFEM_OK;
+  for (int i = 0; i < n; ++i) {
+    const SceneScalars& sc = b->h_sc[i];
+    const int done = sc.steps_done;
+    if (stats) {
+      mfem_step_stats& st = stats[i];
+      // a scene retired by a failed step reports that step's status; one
+      // cut off by the call's bound reports what it finished plus the step
+      // in progress
+      const bool retired = done < steps && (sc.acc_status == MFEM_ERR_NONFINITE ||
+                                            sc.acc_status == MFEM_ERR_PROCRUSTES);
+      const bool cut = done < steps && !retired;
+      st.status = cut ? MFEM_ERR_TIMEOUT : sc.acc_status;
+      st.newton_iterations = sc.acc_newton + (cut ? sc.newton_iter : 0);
+      st.cg_iterations = sc.acc_cg + (cut ? sc.cg_total : 0);
+      st.ls_iterations = sc.acc_ls + (cut ? sc.ls_total : 0);
+      st.energy = sc.E;
+      st.energy_residual = sc.eres;
+      st.decrement = sc.decrement;
+      st.alpha = sc.alpha_ls;
+      st.residual0 = sc.rhs_norm0;
+      st.residual = sc.rhs_norm;
+      st.cg_error = sc.cg_err;
+      st.device_ms = ms;
+    }
+    if (step_done_ms)
+      for (int j = 0; j < steps; ++j) {
+        const unsigned long long t = sns[(size_t)i * kMaxCallSteps + j];
+        step_done_ms[(size_t)i * steps + j] = (j < done && t >= t0) ? double(t - t0) * 1e-6 : -1.0;
+      }
+    if (sc.acc_status == MFEM_ERR_NONFINITE) worst = MFEM_ERR_NONFINITE;
+    if (done < steps && sc.acc_status != MFEM_ERR_NONFINITE && sc.acc_status != MFEM_ERR_PROCRUSTES)
+      worst = MFEM_ERR_TIMEOUT;
   }
   return worst;
 }
@@ -1466,17 +1793,36 @@ int batch_build(mfem_scene* const* scenes, int n, mfem_batch** out) {
   }
   Arena A;
   auto lay = [&](Arena& a) {
-    for (int tb = 0; tb < TB_COUNT; ++tb) b->d_tiles[tb] = a.take<Tile>(std::max<size_t>(tabs[tb].size(), 1));
+    for (int tb = 0; tb < TB_COUNT; ++tb) {
+      b->d_tiles[tb] = a.take<Tile>(std::max<size_t>(tabs[tb].size(), 1));
+      b->d_tiles_c[tb] = a.take<Tile>(std::max<size_t>(tabs[tb].size(), 1));
+    }
     b->d_sds = a.take<SceneDev>(n);
     b->d_partials = a.take<double>(maxt * kNumPartials);
     b->pstride = (int)maxt;
     b->d_ctr = a.take<BatchCounters>(1);
+    b->d_step_ns = a.take<unsigned long long>((size_t)n * kMaxCallSteps + 1);
   };
   lay(A);
   CUDA_OR(cudaMalloc(&b->dmem, A.used), MFEM_ERR_OOM);
   Arena B;
   B.base = b->dmem;
   lay(B);
+  b->full_first.resize((size_t)n * TB_COUNT);
+  b->full_count.resize((size_t)n * TB_COUNT);
+  for (int tb = 0; tb < TB_COUNT; ++tb) {
+    b->cur_tiles[tb] = b->d_tiles[tb];
+    b->cur_ntiles[tb] = b->ntiles[tb];
+    b->h_tiles[tb] = tabs[tb];
+    for (int i = 0; i < n; ++i) {
+      b->full_first[(size_t)i * TB_COUNT + tb] = b->h_sds[i].tile_first[tb];
+      b->full_count[(size_t)i * TB_COUNT + tb] = b->h_sds[i].tile_count[tb];
+    }
+  }
+  for (int i = 0; i < n; ++i) {
+    b->h_sds[i].step_ns = b->d_step_ns + (size_t)i * kMaxCallSteps;
+    b->h_sds[i].pin_traj = nullptr;
+  }
   CUDA_OR(cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking), MFEM_ERR_CUDA);
   CUDA_OR(cudaEventCreate(&b->ev0), MFEM_ERR_CUDA);
   CUDA_OR(cudaEventCreate(&b->ev1), MFEM_ERR_CUDA);
@@ -1510,6 +1856,8 @@ void batch_free(mfem_batch* b) {
     if (b->ev_pipe[k]) cudaEventDestroy(b->ev_pipe[k]);
   if (b->h_sc) cudaFreeHost(b->h_sc);
   for (cudaEvent_t e : b->ev_pool) cudaEventDestroy(e);
+  if (b->tick_graph) cudaGraphExecDestroy(b->tick_graph);
+  if (b->tick_graph_c) cudaGraphExecDestroy(b->tick_graph_c);
   if (b->ev0) cudaEventDestroy(b->ev0);
   if (b->ev1) cudaEventDestroy(b->ev1);
   if (b->stream) cudaStreamDestroy(b->stream);
@@ -1882,6 +2230,7 @@ int mfem_gpu_scene_destroy(mfem_scene* scene) {
   batch_free(scene->solo);
   if (scene->dmem) cudaFree(scene->dmem);
   if (scene->ckpt) cudaFree(scene->ckpt);
+  if (scene->d_pin_traj) cudaFree(scene->d_pin_traj);
   delete scene;
   return MFEM_OK;
 }
@@ -2206,10 +2555,13 @@ int mfem_gpu_batch_set_pcg_shape(mfem_batch* b, int32_t stages, int32_t keep, in
       b->cgf_shape.pdl == sh.pdl)
     return MFEM_OK;
   b->cgf_shape = sh;
-  if (b->cg_graph) {  // captured with the old shape
+  if (b->cg_graph || b->tick_graph) {  // captured with the old shape
     CUDA_OR(cudaStreamSynchronize(b->stream), MFEM_ERR_CUDA);
-    cudaGraphExecDestroy(b->cg_graph);
+    if (b->cg_graph) cudaGraphExecDestroy(b->cg_graph);
+    if (b->tick_graph) cudaGraphExecDestroy(b->tick_graph);
+  if (b->tick_graph_c) cudaGraphExecDestroy(b->tick_graph_c);
     b->cg_graph = nullptr;
+    b->tick_graph = nullptr;
   }
   return MFEM_OK;
 }
@@ -2231,6 +2583,11 @@ int mfem_gpu_batch_set_variants(mfem_batch* b, int32_t elem_update, int32_t loca
   b->var_elem = elem_update;
   b->var_local = local_solve;
   b->var_ls = ls_energy;
+  if (b->tick_graph) {  // captured with the old variants
+    CUDA_OR(cudaStreamSynchronize(b->stream), MFEM_ERR_CUDA);
+    cudaGraphExecDestroy(b->tick_graph);
+    b->tick_graph = nullptr;
+  }
   return MFEM_OK;
 }
 
@@ -2269,6 +2626,11 @@ int mfem_gpu_batch_destroy(mfem_batch* batch) {
   if (!batch) return MFEM_ERR_INVALID;
   batch_free(batch);
   return MFEM_OK;
+}
+
+int mfem_gpu_batch_step_n(mfem_batch* batch, int32_t steps, mfem_step_stats* stats, double* step_done_ms) {
+  if (!batch || steps < 1 || steps > MFEM_BATCH_MAX_STEPS) return MFEM_ERR_INVALID;
+  return batch_step_n_impl(batch, steps, stats, step_done_ms);
 }
 
 int mfem_gpu_batch_step(mfem_batch* batch, mfem_step_stats* stats) {

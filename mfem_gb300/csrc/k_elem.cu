@@ -259,7 +259,7 @@ __global__ void __launch_bounds__(kElemTile, MB)
   constexpr int kRhsWord = rec_rhs_offset(RB) / 4;
   const Tile t = tiles[blockIdx.x];
   const SceneDev& sd = sds[t.scene];
-  if (!sd.sc->newton_active) return;
+  if (!sd.sc->newton_active || not_my_phase(sd.sc, kPhNewton)) return;
   const int e = t.begin + threadIdx.x;
   const Real h2 = Ext<Real>::r(sd.h2, sd.h2x);
   if (e < t.end) {
@@ -421,7 +421,7 @@ __global__ void __launch_bounds__(kElemTile)
   constexpr int kRhsWord = rec_rhs_offset(RB) / 4;
   const Tile t = tiles[blockIdx.x];
   const SceneDev& sd = sds[t.scene];
-  if (!sd.sc->newton_active) return;
+  if (!sd.sc->newton_active || not_my_phase(sd.sc, kPhNewton)) return;
   const int e = t.begin + threadIdx.x;
   const Real h2 = Ext<Real>::r(sd.h2, sd.h2x);
   if (e < t.end) {
@@ -537,7 +537,7 @@ __global__ void __launch_bounds__(kElemTile, MB) k_local_solve(const Tile* tiles
   const Tile t = tiles[tix];
   const SceneDev& sd = sds[t.scene];
   SceneScalars* sc = sd.sc;
-  if (!sc->newton_active) return;
+  if (!sc->newton_active || not_my_phase(sc, kPhLocal)) return;
   const Real h2 = Ext<Real>::r(sd.h2, sd.h2x);
   const Real* cgx = static_cast<const Real*>(sd.cg_x);
   E sums[2] = {E(0), E(0)};
@@ -666,9 +666,11 @@ __global__ void __launch_bounds__(kElemTile, MB) k_local_solve(const Tile* tiles
       sc->ls_ok = 0;
       if (sd.max_ls > 0) {
         sc->ls_active = 1;
+        sc->nph = kPhLs;
         atomicAdd(&ctrs->ls_active, 1);
       } else {
         sc->ls_active = 0;
+        sc->nph = kPhApply;
       }
     }
   }
@@ -756,6 +758,7 @@ __global__ void __launch_bounds__(kElemTile, MB) k_ls_energy(const Tile* tiles, 
       if (isfinite(fx) && isfinite(noise) && fx < sc->fx0 + noise) {
         sc->ls_active = 0;
         sc->ls_ok = 1;
+        sc->nph = kPhApply;
         atomicSub(&ctrs->ls_active, 1);
       } else {
         sc->alpha_ls *= 0.5;
@@ -764,6 +767,7 @@ __global__ void __launch_bounds__(kElemTile, MB) k_ls_energy(const Tile* tiles, 
         if (sc->ls_iter >= sd.max_ls) {
           sc->ls_active = 0;
           sc->ls_ok = 0;
+          sc->nph = kPhApply;
           atomicSub(&ctrs->ls_active, 1);
         }
       }
@@ -781,7 +785,7 @@ __global__ void __launch_bounds__(kElemTile) k_apply(const Tile* tiles, const Sc
   const Tile t = tiles[tix];
   const SceneDev& sd = sds[t.scene];
   SceneScalars* sc = sd.sc;
-  if (!sc->newton_active) return;
+  if (!sc->newton_active || not_my_phase(sc, kPhApply)) return;
   const int idx = t.begin + threadIdx.x;
   if (sc->ls_ok && idx < t.end) {
     const E alpha = E(sc->alpha_ls_f);
@@ -813,26 +817,19 @@ __global__ void __launch_bounds__(kElemTile) k_apply(const Tile* tiles, const Sc
       // with a residual tolerance set, the mixed path stops on the residual.
       const bool eres_ok = (!sd.fp64 && sd.res_tol > 0) ? true : sc->eres > 1e-12;
       const bool go = sc->newton_iter < sd.max_newton && sc->decrement > sd.newton_tol && eres_ok;
-      if (!go) {
-        sc->newton_active = 0;
-        atomicSub(&ctrs->newton_active, 1);
-      }
+      if (!go) end_newton_loop(sc, ctrs);
+      else sc->nph = kPhNewton;
     }
   }
 }
 
 // ------------------------------------------------------------ BDF steps ---
-// x_tilde + h^2 f, BDF<I>::x_tilde (BDF.cpp:6-9) and Displacement::gradient's
-// target (displacement.cpp:63-73).
+// x_tilde + h^2 f of vertex a from the BDF ring at `head`, BDF<I>::x_tilde
+// (BDF.cpp:6-9) and Displacement::gradient's target (displacement.cpp:63-73).
 template <typename Real>
-__global__ void __launch_bounds__(kElemTile) k_step_begin(const Tile* tiles, const SceneDev* sds) {
+__device__ __forceinline__ void vertex_step_begin(const SceneDev& sd, int a, int head) {
   using E = typename Ext<Real>::T;
-  const Tile t = tiles[blockIdx.x];
-  const SceneDev& sd = sds[t.scene];
-  if (t.kind == 0) return;
-  const int a = t.begin + threadIdx.x;
-  if (a >= t.end) return;
-  const int I = sd.bdf_order, head = sd.sc->hist_head;
+  const int I = sd.bdf_order;
   const size_t n3 = 3 * (size_t)sd.nv;
   const E dt = E(sd.dt), h2 = E(sd.h2);
 #pragma unroll
@@ -848,11 +845,44 @@ __global__ void __launch_bounds__(kElemTile) k_step_begin(const Tile* tiles, con
   }
 }
 
+// Vertex a at the end of a step: a pin moves to its post-BC-step position
+// (from `pins`), BDF<I>::update (BDF.cpp:11-21) into ring slot nhead.
+template <typename Real>
+__device__ __forceinline__ void vertex_step_end(const SceneDev& sd, int a, int head, int nhead,
+                                                const double* pins) {
+  using E = typename Ext<Real>::T;
+  const int I = sd.bdf_order;
+  const int f = sd.free_map[a];
+  const size_t n3 = 3 * (size_t)sd.nv;
+  const E dt = E(sd.dt);
+#pragma unroll
+  for (int c = 0; c < 3; ++c) {
+    const size_t k = 3 * (size_t)a + c;
+    const E xv = (f < 0) ? E(pins[3 * (-1 - f) + c]) : Ext<Real>::ld(sd.x, k);
+    E wx = E(0);
+    for (int i = 0; i < I; ++i)
+      wx = wx + E(sd.bdf_alpha[i]) * Ext<Real>::ld(sd.xhist, (size_t)((head + i) % I) * n3 + k);
+    const E vnew = (xv - wx) / dt;
+    Ext<Real>::st(sd.x, k, xv);
+    Ext<Real>::st(sd.xhist, (size_t)nhead * n3 + k, xv);
+    Ext<Real>::st(sd.vhist, (size_t)nhead * n3 + k, vnew);
+  }
+}
+
+template <typename Real>
+__global__ void __launch_bounds__(kElemTile) k_step_begin(const Tile* tiles, const SceneDev* sds) {
+  const Tile t = tiles[blockIdx.x];
+  const SceneDev& sd = sds[t.scene];
+  if (t.kind == 0) return;
+  const int a = t.begin + threadIdx.x;
+  if (a >= t.end) return;
+  vertex_step_begin<Real>(sd, a, sd.sc->hist_head);
+}
+
 // Pins move to their post-BC-step positions, BDF<I>::update (BDF.cpp:11-21),
 // lambda = 0 (MixedStretch::post_solve, mixed_stretch.cpp:306-309).
 template <typename Real>
 __global__ void __launch_bounds__(kElemTile) k_step_end(const Tile* tiles, const SceneDev* sds) {
-  using E = typename Ext<Real>::T;
   const int tix = blockIdx.x;
   const Tile t = tiles[tix];
   const SceneDev& sd = sds[t.scene];
@@ -866,26 +896,80 @@ __global__ void __launch_bounds__(kElemTile) k_step_end(const Tile* tiles, const
 #pragma unroll
       for (int i = 0; i < 6; ++i) la[(size_t)i * sd.ntp + idx] = Real(0);
     } else {
-      const int a = idx;
-      const int f = sd.free_map[a];
-      const size_t n3 = 3 * (size_t)sd.nv;
-      const E dt = E(sd.dt);
-#pragma unroll
-      for (int c = 0; c < 3; ++c) {
-        const size_t k = 3 * (size_t)a + c;
-        const E xv = (f < 0) ? E(sd.pin_pos[3 * (-1 - f) + c]) : Ext<Real>::ld(sd.x, k);
-        E wx = E(0);
-        for (int i = 0; i < I; ++i)
-          wx = wx + E(sd.bdf_alpha[i]) * Ext<Real>::ld(sd.xhist, (size_t)((head + i) % I) * n3 + k);
-        const E vnew = (xv - wx) / dt;
-        Ext<Real>::st(sd.x, k, xv);
-        Ext<Real>::st(sd.xhist, (size_t)nhead * n3 + k, xv);
-        Ext<Real>::st(sd.vhist, (size_t)nhead * n3 + k, vnew);
-      }
+      vertex_step_end<Real>(sd, idx, head, nhead, sd.pin_pos);
     }
   }
   if (last_tile(sd, TB_EV, tix)) {
     if (threadIdx.x == 0) sc->hist_head = nhead;
+  }
+}
+
+// A step's status as the host reports it: non-finite first, then a failed
+// rotation solve, then the step's own status, then the PCG's.
+__device__ __forceinline__ int step_status(const SceneScalars* sc) {
+  if (sc->status == 4) return 4;
+  if (sc->procrustes_fail) return 7;
+  if (sc->status) return sc->status;
+  return sc->cg_status;
+}
+__device__ __forceinline__ int status_rank(int st) { return st == 4 ? 3 : st == 7 ? 2 : st ? 1 : 0; }
+
+// Several timesteps per call (mfem_gpu_batch_step_n): a scene whose Newton
+// loop has ended turns over here.  Its step ends as k_step_end
+// ends it (the pins from the step's slot of the precomputed trajectory);
+// unless that was its last step, the next one begins as k_step_begin begins
+// it, its per-step state is reset and it joins the next round's launches
+// while other scenes are still in their Newton loops.  The per-vertex work
+// is the same device code as the two kernels'.  A step that ends
+// non-finite or with a singular rotation solve retires the scene.
+template <typename Real>
+__global__ void __launch_bounds__(kElemTile) k_step_turn(const Tile* tiles, const SceneDev* sds,
+                                                         BatchCounters* ctrs) {
+  const int tix = blockIdx.x;
+  const Tile t = tiles[tix];
+  const SceneDev& sd = sds[t.scene];
+  SceneScalars* sc = sd.sc;
+  if (!sc->turn) return;
+  const int idx = t.begin + threadIdx.x;
+  const int I = sd.bdf_order, head = sc->hist_head;
+  const int nhead = (head + I - 1) % I;
+  const int done = sc->steps_done;
+  // a step that ended non-finite or with a singular rotation solve retires
+  // the scene: its state cannot give a meaningful next step
+  const bool failed = status_rank(step_status(sc)) >= 2;
+  const bool last = failed || done + 1 >= sc->steps_target;
+  if (idx < t.end) {
+    if (t.kind == 0) {
+      Real* la = static_cast<Real*>(sd.la);
+#pragma unroll
+      for (int i = 0; i < 6; ++i) la[(size_t)i * sd.ntp + idx] = Real(0);
+    } else {
+      const double* pins = sd.pin_traj ? sd.pin_traj + 3 * (size_t)sd.npin * done : sd.pin_pos;
+      vertex_step_end<Real>(sd, idx, head, nhead, pins);
+      if (!last) vertex_step_begin<Real>(sd, idx, nhead);
+    }
+  }
+  if (last_tile(sd, TB_EV, tix)) {
+    if (threadIdx.x == 0) {
+      sc->hist_head = nhead;
+      const int st = step_status(sc);
+      if (status_rank(st) > status_rank(sc->acc_status)) sc->acc_status = st;
+      sc->acc_newton += sc->newton_iter;
+      sc->acc_cg += sc->cg_total;
+      sc->acc_ls += sc->ls_total;
+      if (sd.step_ns) {
+        unsigned long long t;
+        asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+        sd.step_ns[done] = t;
+      }
+      sc->steps_done = done + 1;
+      sc->turn = 0;
+      if (last) {
+        atomicSub(&ctrs->newton_active, 1);  // the scene's last step: its stats stay
+      } else {
+        reset_step_scalars(sc);  // newton_active = 1: in the next round
+      }
+    }
   }
 }
 
@@ -997,5 +1081,6 @@ void launch_apply(const Launch& L) {
 }
 void launch_step_begin(const Launch& L) { MFEM_LAUNCH_EV(k_step_begin, L.tiles, L.sds); }
 void launch_step_end(const Launch& L) { MFEM_LAUNCH_EV(k_step_end, L.tiles, L.sds); }
+void launch_step_turn(const Launch& L) { MFEM_LAUNCH_EV(k_step_turn, L.tiles, L.sds, L.counters); }
 
 }  // namespace mfem_gpu

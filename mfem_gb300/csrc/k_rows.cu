@@ -171,7 +171,7 @@ __global__ void __launch_bounds__(256) k_assemble(const Tile* tiles, const Scene
   const Tile t = tiles[tix];
   const SceneDev& sd = sds[t.scene];
   SceneScalars* sc = sd.sc;
-  if (!sc->newton_active) return;
+  if (!sc->newton_active || not_my_phase(sc, kPhNewton)) return;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   typename Ext<Real>::T rn2 = typename Ext<Real>::T(0);
   for (int rr = warp; rr < kRowTile; rr += 8) {
@@ -342,16 +342,13 @@ __global__ void __launch_bounds__(256) k_assemble(const Tile* tiles, const Scene
       if (sd.res_tol > 0 && ((sc->newton_iter > 0 && rn <= sd.res_tol * sc->rhs_norm0) ||
                              rn <= sd.res_tol * sd.load_norm)) {
         sc->converged_by_residual = 1;
-        sc->newton_active = 0;
-        atomicSub(&ctrs->newton_active, 1);
+        end_newton_loop(sc, ctrs);
       }
       if (!(s == s) || isinf(s)) {
         sc->status = 4;  // MFEM_ERR_NONFINITE
-        if (sc->newton_active) {
-          sc->newton_active = 0;
-          atomicSub(&ctrs->newton_active, 1);
-        }
+        if (sc->newton_active) end_newton_loop(sc, ctrs);
       }
+      if (sc->newton_active) sc->nph = kPhPcgInit;
     }
   }
 }
@@ -391,7 +388,7 @@ __global__ void __launch_bounds__(kCgThreads) k_cg_init(const Tile* tiles, const
   const Tile t = tiles[tix];
   const SceneDev& sd = sds[t.scene];
   SceneScalars* sc = sd.sc;
-  if (!sc->newton_active) return;
+  if (!sc->newton_active || not_my_phase(sc, kPhPcgInit)) return;
   using E = typename Ext<Real>::T;
   E dots[2] = {E(0), E(0)};  // r.r, r.z
   const int row = t.begin + threadIdx.x;
@@ -426,11 +423,13 @@ __global__ void __launch_bounds__(kCgThreads) k_cg_init(const Tile* tiles, const
       sc->cg_err = 0.0;
       if (rrs == 0.0) {
         sc->cg_active = 0;
+        sc->nph = kPhLocal;
       } else {
         const double thr = fmax(sd.cg_tol * sd.cg_tol * rrs, DBL_MIN);
         sc->cg_threshold = thr;
         if (rrs < thr || sd.max_cg <= 0) {
           sc->cg_active = 0;
+          sc->nph = kPhLocal;
           sc->cg_err = 1.0;
         } else {
           sc->cg_active = 1;
@@ -590,6 +589,7 @@ __device__ __forceinline__ void cg_update_tile(int tix, const Tile* tiles, const
       if (stop) {
         sc->cg_total = ldv<kCo>(&sc->cg_total) + ldv<kCo>(&sc->cg_iter);
         sc->cg_active = 0;
+        sc->nph = kPhLocal;
         atomicSub(&ctrs->cg_active, 1);
       }
     }
@@ -659,6 +659,7 @@ __device__ __forceinline__ void cg_replace_tile(int tix, const Tile* tiles, cons
         sc->cg_total = ldv<kCo>(&sc->cg_total) + done;
         sc->cg_status = 0;
         sc->cg_active = 0;
+        sc->nph = kPhLocal;
         atomicSub(&ctrs->cg_active, 1);
       } else {
         const double b2 = Fin<float>::div(rzs, ldv<kCo>(&sc->rz_prev));
@@ -760,13 +761,16 @@ __device__ __forceinline__ void cgf_finish(const SceneDev& sd, BatchCounters* ct
         sc->cg_threshold = thr;
         if (rr == 0.0) {
           sc->cg_active = 0;
+          sc->nph = kPhLocal;
         } else if (rr < thr || sd.max_cg <= 0) {
           sc->cg_active = 0;
+          sc->nph = kPhLocal;
           sc->cg_err = 1.0;
         } else {
           sc->cg_active = 1;
           atomicAdd(&ctrs->cg_active, 1);
         }
+        sc->nph = sc->cg_active ? kPhPcg : kPhLocal;
         const double a0 = Fin<Real>::div(g, d);
         sc->cgf_gamma[0] = g;
         sc->alpha = a0;
@@ -802,6 +806,7 @@ __device__ __forceinline__ void cgf_finish(const SceneDev& sd, BatchCounters* ct
         if (stop) {
           sc->cg_total += sc->cg_iter;
           sc->cg_active = 0;
+          sc->nph = kPhLocal;
           atomicSub(&ctrs->cg_active, 1);
         }
       }
@@ -846,6 +851,7 @@ __device__ __forceinline__ void cgf_verify_step(const SceneDev& sd, BatchCounter
   if (ph == 3 || *(volatile int*)&ctrs->error) {
     sc->cg_total += sc->cg_iter;
     sc->cg_active = 0;
+    sc->nph = kPhLocal;
     atomicSub(&ctrs->cg_active, 1);
     return;
   }
@@ -1028,7 +1034,7 @@ __device__ __forceinline__ void cgf_tile(int tix, const Tile* tiles, const Scene
   const Tile t = tiles[tix];
   const SceneDev& sd = sds[t.scene];
   SceneScalars* sc = sd.sc;
-  if (kInit ? !sc->newton_active : !sc->cg_active) return;
+  if (kInit ? (!sc->newton_active || not_my_phase(sc, kPhPcgInit)) : !sc->cg_active) return;
   if constexpr (!kInit && sizeof(Real) == 4) {
     if (const int ph = sc->cgf_phase) {
       cgf_verify_tile<kScaled>(ph, tix, tiles, sds, partials, pstride, ctrs);
@@ -1522,31 +1528,20 @@ __global__ void __launch_bounds__(kCgThreads, sizeof(Real) == 4 ? 6 : 4) k_cg_so
   }
 }
 
-__global__ void k_scalars_begin(const SceneDev* sds, int n, BatchCounters* ctrs) {
+// steps: the call's timesteps per scene (0: the plain one-step form);
+// ticked: the kernels gate on the scenes' phases.
+__global__ void k_scalars_begin(const SceneDev* sds, int n, BatchCounters* ctrs, int steps, int ticked) {
   for (int i = threadIdx.x; i < n; i += blockDim.x) {
     SceneScalars* sc = sds[i].sc;
-    sc->newton_active = 1;
-    sc->newton_iter = 0;
-    sc->converged_by_residual = 0;
-    sc->status = 0;
-    sc->E = 0;
-    sc->E_prev = 0;
-    sc->eres = 0;
-    sc->decrement = 0;
-    sc->rhs_norm0 = 0;
-    sc->rhs_norm = 0;
-    sc->cg_active = 0;
-    sc->cg_iter = 0;
-    sc->cg_total = 0;
-    sc->cg_status = 0;
-    sc->cg_err = 0;
-    sc->ls_active = 0;
-    sc->ls_iter = 0;
-    sc->ls_ok = 0;
-    sc->ls_total = 0;
-    sc->alpha_ls = 1.0;
-    sc->alpha_ls_f = 1.0f;
-    sc->procrustes_fail = 0;
+    reset_step_scalars(sc);
+    sc->steps_target = steps;
+    sc->steps_done = 0;
+    sc->turn = 0;
+    sc->acc_newton = 0;
+    sc->acc_cg = 0;
+    sc->acc_ls = 0;
+    sc->acc_status = 0;
+    sc->ticked = ticked;
   }
   if (threadIdx.x == 0) {
     ctrs->newton_active = n;
@@ -1691,7 +1686,17 @@ cudaError_t launch_cg_solve(const Launch& L, int grid, int max_iters) {
 }
 
 void launch_scalars_begin(const Launch& L, int nscenes) {
-  k_scalars_begin<<<1, 128, 0, L.stream>>>(L.sds, nscenes, L.counters);
+  k_scalars_begin<<<1, 128, 0, L.stream>>>(L.sds, nscenes, L.counters, 0, 0);
 }
+void launch_scalars_begin_n(const Launch& L, int nscenes, int steps, int ticked) {
+  k_scalars_begin<<<1, 128, 0, L.stream>>>(L.sds, nscenes, L.counters, steps, ticked);
+}
+
+__global__ void k_stamp(unsigned long long* ns) {
+  unsigned long long t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  *ns = t;
+}
+void launch_stamp(unsigned long long* ns, cudaStream_t st) { k_stamp<<<1, 1, 0, st>>>(ns); }
 
 }  // namespace mfem_gpu

@@ -100,6 +100,16 @@ struct SceneScalars {
   double mr_beta, mr_beta_one, mr_alpha, mr_c, mr_c_old, mr_s, mr_s_old, mr_eta;
   double mr_r1, mr_r2, mr_r3, mr_coef, mr_resid2, mr_thr2;
   int mr_pending, mr_slot;
+  // several timesteps in one call (mfem_gpu_batch_step_n): the scene's own
+  // count of steps (0: one step, the plain form), the steps it finished, a
+  // flag raised by the Newton loop's end until the step is turned over, and
+  // the statistics of its finished steps
+  int steps_target, steps_done, turn;
+  int acc_newton, acc_cg, acc_ls, acc_status;
+  // the ticked multi-step form: every kernel acts only on the scenes in its
+  // phase of the Newton iteration (nph, kPh* in reduce.cuh), so that a scene
+  // never waits for another scene's PCG or line search
+  int ticked, nph;
 };
 
 // Counters of a batch: scenes still active in each loop.
@@ -210,6 +220,11 @@ struct SceneDev {
   // tiles of this scene in each table
   int tile_first[TB_COUNT];
   int tile_count[TB_COUNT];
+  // mfem_gpu_batch_step_n: pinned positions after each of the call's BC
+  // steps (3 npin per step; null when the pins do not move) and, per step,
+  // the Newton round of the call in which the scene finished it
+  const double* pin_traj;
+  unsigned long long* step_ns;  // global-timer ns at which each step was done
   int gmax;                // ticket groups per table (capacity of gctr rows)
   unsigned int* gctr;      // TB_COUNT x gmax first-level ticket counters
   SceneScalars* sc;
@@ -249,12 +264,21 @@ void launch_ls_energy(const Launch& L);                        // K6          (T
 void launch_apply(const Launch& L);                            // x,s update  (TB_EV)
 void launch_step_begin(const Launch& L);                       // x_tilde     (TB_EV)
 void launch_step_end(const Launch& L);                         // BDF, la = 0 (TB_EV)
+// Several timesteps in one call: the turnover of every scene whose Newton
+// loop has ended (step end, and the next step's begin unless it was its
+// last), recording the time the step was done (TB_EV).
+void launch_step_turn(const Launch& L);
 // Row kernels (k_rows.cu)
 void launch_assemble(const Launch& L);  // K2 + K3 (TB_ROW)
 void launch_cg_init(const Launch& L);   // r = b, z, rz  (TB_CG)
 void launch_cg_spmv(const Launch& L);   // Ap, pAp, alpha (TB_CG)
 void launch_cg_update(const Launch& L); // x, r, z, beta  (TB_CG)
 void launch_scalars_begin(const Launch& L, int nscenes);        // reset Newton state
+// The same for a call of `steps` timesteps per scene (steps_target);
+// ticked: every kernel gated by the scene's phase.
+void launch_scalars_begin_n(const Launch& L, int nscenes, int steps, int ticked);
+// The device's global timer (ns) into *ns.
+void launch_stamp(unsigned long long* ns, cudaStream_t st);
 // The whole PCG in one cooperative launch of `grid` co-resident blocks.
 cudaError_t launch_cg_solve(const Launch& L, int grid, int max_iters);
 void launch_cg_replace(const Launch& L);  // r = b - A x in df64 (mixed path)

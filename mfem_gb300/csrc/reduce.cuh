@@ -282,4 +282,50 @@ __device__ __forceinline__ bool last_tile(const SceneDev& sd, int table, int tix
   return s_last != 0;
 }
 
+// Phases of a Newton iteration in the ticked multi-step form: K1 and the
+// assembly, the PCG's init, its iterations, the local solve, the line
+// search, the update.  The kernels' finalizers move a scene along them in
+// every form; only a ticked scene's kernels check them.
+enum : int { kPhNewton = 0, kPhPcgInit = 1, kPhPcg = 2, kPhLocal = 3, kPhLs = 4, kPhApply = 5 };
+__device__ __forceinline__ bool not_my_phase(const SceneScalars* sc, int ph) { return sc->ticked && sc->nph != ph; }
+
+// Ends a scene's Newton loop for this timestep (thread 0 of its last tile).
+// In the one-step form the batch counts one scene fewer; in the multi-step
+// form (steps_target > 0) the scene is flagged for k_step_turn, which
+// retires it only after its last step.
+__device__ __forceinline__ void end_newton_loop(SceneScalars* sc, BatchCounters* ctrs) {
+  sc->newton_active = 0;
+  if (sc->steps_target > 0) sc->turn = 1;
+  else atomicSub(&ctrs->newton_active, 1);
+}
+
+// The per-step Newton, PCG and line-search state of a scene at the start of
+// a timestep.
+__device__ __forceinline__ void reset_step_scalars(SceneScalars* sc) {
+  sc->newton_active = 1;
+  sc->newton_iter = 0;
+  sc->converged_by_residual = 0;
+  sc->status = 0;
+  sc->E = 0;
+  sc->E_prev = 0;
+  sc->eres = 0;
+  sc->decrement = 0;
+  sc->rhs_norm0 = 0;
+  sc->rhs_norm = 0;
+  sc->cg_active = 0;
+  sc->cg_iter = 0;
+  sc->cg_total = 0;
+  sc->cg_status = 0;
+  sc->cg_err = 0;
+  sc->ls_active = 0;
+  sc->ls_iter = 0;
+  sc->ls_ok = 0;
+  sc->ls_total = 0;
+  sc->alpha_ls = 1.0;
+  sc->alpha_ls_f = 1.0f;
+  sc->procrustes_fail = 0;
+  sc->nph = kPhNewton;
+}
+
+
 }  // namespace mfem_gpu

@@ -236,4 +236,15 @@ class Batch:
         rc = load().mfem_gpu_batch_step(self._h, self._stats)
         if rc != abi.OK and (raise_on_error or rc in (abi.ERR_CUDA, abi.ERR_TIMEOUT, abi.ERR_INVALID)):
             check(rc, "batch_step")
-        return list(self._stats)
+        return [abi.StepStats.from_buffer_copy(st) for st in self._stats]
+
+    def step_n(self, steps, raise_on_error=True):
+        """`steps` timesteps of every scene, each scene at its own pace
+        (mfem_gpu_batch_step_n).  Returns (stats per scene, summed over its
+        steps; step_done_ms: scenes x steps device times from the call's
+        start at which each step was done)."""
+        done = np.zeros((len(self.scenes), max(int(steps), 1)))
+        rc = load().mfem_gpu_batch_step_n(self._h, int(steps), self._stats, done.ctypes.data_as(_dp))
+        if rc != abi.OK and (raise_on_error or rc in (abi.ERR_CUDA, abi.ERR_TIMEOUT, abi.ERR_INVALID)):
+            check(rc, "batch_step_n")
+        return [abi.StepStats.from_buffer_copy(st) for st in self._stats], done
