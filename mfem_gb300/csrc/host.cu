@@ -925,8 +925,12 @@ int run_pcg(mfem_batch* b, const Launch& Lcg) {
   const bool fused = b->pcg_kernel == MFEM_PCG_KERNEL_FUSED;
   {
     KTimer t(b, MFEM_K_CG_INIT);
-    if (fused) launch_cgf_init(Lcg);
-    else launch_cg_init(Lcg);
+    if (fused) {
+      launch_cgf_scale(Lcg);  // mixed path only
+      launch_cgf_init(Lcg);
+    } else {
+      launch_cg_init(Lcg);
+    }
   }
   if (b->pcg_kernel == MFEM_PCG_KERNEL_PERSISTENT) {
     cudaError_t e;
@@ -1113,6 +1117,7 @@ int capture_tick_graph(mfem_batch* b, cudaGraphExec_t* out) {
   CUDA_OR(cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal), MFEM_ERR_CUDA);
   launch_elem_update(Lel, nullptr);
   launch_assemble(make_launch(b, TB_ROW));
+  launch_cgf_scale(Lcg);
   launch_cgf_init(Lcg);
   for (int k = 0; k < b->tick_pcg; ++k) launch_cgf_iter(Lcg, b->cgf_shape);
   launch_local_solve(Llo);

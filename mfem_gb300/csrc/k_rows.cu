@@ -941,7 +941,7 @@ __device__ __noinline__ void cgf_verify_tile(int ph, int tix, const Tile* tiles,
       float bv[3], r[3], z[3];
       ld3<false>(static_cast<const float*>(sd.rhs) + k4, bv);
 #pragma unroll
-      for (int c = 0; c < 3; ++c) r[c] = Ext<float>::to_real(df64(bv[c]) - acc[c]);
+      for (int c = 0; c < 3; ++c) r[c] = Ext<float>::to_real(df64(ldexpf(bv[c], sc->cg_scale_exp)) - acc[c]);
       apply_prec<float>(sd, row, r, z);
       st3(r_cur + k4, kScaled ? z : r);  // the scaled form keeps r~ = M^-1 r (= u)
       if (!kScaled) st3(u + k4, z);
@@ -1003,13 +1003,16 @@ __device__ __noinline__ void cgf_verify_tile(int ph, int tix, const Tile* tiles,
         dots[4] = dots[4] + exact_prod(po[c], san[c]);
       }
     } else {
-      // the solution: x_e + x in x_e, and rounded to FP32 in x for its readers
+      // the solution: x_e + x in x_e, and rounded to FP32 in x for its
+      // readers, scaled back by 2^-cg_scale_exp
       X3 xe = xe_load<false>(sd.cg_xe, row);
       float xf[3];
       ld3<false>(x + k4, xf);
+      const int ue = -sc->cg_scale_exp;
 #pragma unroll
       for (int c = 0; c < 3; ++c) {
         xe.v[c] = xe.v[c] + df64(xf[c]);
+        xe.v[c] = df64(ldexpf(xe.v[c].hi, ue), ldexpf(xe.v[c].lo, ue));
         xf[c] = Ext<float>::to_real(xe.v[c]);
       }
       xe_store(sd.cg_xe, row, xe);
@@ -1064,6 +1067,10 @@ __device__ __forceinline__ void cgf_tile(int tix, const Tile* tiles, const Scene
     if (kScaled) ld3<false>(static_cast<const Real*>(sd.dinv) + k4, dv);
     if (kInit) {
       ld3<false>(r_old + k4, rn);
+      if constexpr (sizeof(Real) == 4) {
+#pragma unroll
+        for (int c = 0; c < 3; ++c) rn[c] = ldexpf(rn[c], sc->cg_scale_exp);
+      }
       apply_prec<Real>(sd, row, rn, un);
       const Real zero[3] = {Real(0), Real(0), Real(0)};
       st3(x + k4, zero);
@@ -1121,6 +1128,10 @@ __device__ __forceinline__ void cgf_tile(int tix, const Tile* tiles, const Scene
       if (kInit) {
         Real bc[3];
         ld3_keep(r_old + c4, bc, pol_k);
+        if constexpr (sizeof(Real) == 4) {
+#pragma unroll
+          for (int c = 0; c < 3; ++c) bc[c] = ldexpf(bc[c], sc->cg_scale_exp);
+        }
         apply_prec<Real>(sd, col, bc, uc);
       } else {
         Real rc[3], wc[3], spc[3], sc_[3], rnc[3];
@@ -1153,6 +1164,35 @@ __device__ __forceinline__ void cgf_tile(int tix, const Tile* tiles, const Scene
     }
   }
   cgf_finish<Real, kInit>(sd, ctrs, dots, partials, pstride, tix, it);
+}
+
+// Mixed path: the power of two 2^k with max |2^k b_i| in [0.5, 1), taken
+// from the entries' largest magnitude (no squares, so nothing underflows on
+// the way); the PCG then runs on 2^k b.  Scaling by a power of two is exact,
+// so for right-hand sides well inside FP32's range the iterates are those of
+// the unscaled solve, scaled.
+__global__ void __launch_bounds__(kCgThreads) k_cgf_scale(const Tile* tiles, const SceneDev* sds,
+                                                         double* partials, int pstride, BatchCounters* ctrs) {
+  const Tile t = tiles[blockIdx.x];
+  const SceneDev& sd = sds[t.scene];
+  SceneScalars* sc = sd.sc;
+  if (!sc->newton_active || not_my_phase(sc, kPhPcgInit)) return;
+  float m[1] = {0.f};
+  const int row = t.begin + threadIdx.x;
+  if (row < t.end) {
+    float bv[3];
+    ld3<false>(static_cast<const float*>(sd.rhs) + 4 * (size_t)row, bv);
+    m[0] = fmaxf(fabsf(bv[0]), fmaxf(fabsf(bv[1]), fabsf(bv[2])));
+  }
+  tile_partials<df64, float, 0, 1>(nullptr, m, partials, pstride, 0, blockIdx.x);
+  if (last_tile(sd, TB_CG, blockIdx.x)) {
+    const float mx = scene_max<float>(partials, pstride, 0, sd.tile_first[TB_CG], sd.tile_count[TB_CG]);
+    if (threadIdx.x == 0) {
+      int e = 0;
+      if (mx > 0.f && isfinite(mx)) frexpf(mx, &e);
+      sc->cg_scale_exp = -e;
+    }
+  }
 }
 
 // kScaled: every scene of the batch uses the Jacobi preconditioner.
@@ -1589,6 +1629,10 @@ void launch_cg_replace(const Launch& L) {
   } while (0)
 
 void launch_cgf_init(const Launch& L) { MFEM_LAUNCH_CGF(k_cgf_init); }
+void launch_cgf_scale(const Launch& L) {
+  if (L.ntiles == 0 || L.fp64) return;
+  k_cgf_scale<<<L.ntiles, kCgThreads, 0, L.stream>>>(L.tiles, L.sds, L.partials, L.pstride, L.counters);
+}
 
 namespace {
 template <typename Real, bool kScaled, int S, int kKeep, int U, bool kPdl>

@@ -80,6 +80,11 @@ struct SceneScalars {
   // 1: r = b - A (x_e + x) exactly; 2: fold x into x_e, w = A u and the
   // inner products of the true residual; 3: write the rounded solution)
   int cgf_phase, cgf_rounds;  // verifications that failed in this solve
+  // mixed path: the single-reduction PCG solves for 2^cg_scale_exp b (a
+  // power of two from max |b_i|, so that the float-float inner products of
+  // tiny or huge right-hand sides stay inside FP32's exponent range); the
+  // solution is scaled back when it is written
+  int cg_scale_exp, cg_pad;
   // line search (linesearch.h:80-129 with c = 0, p = 0.5)
   int ls_active, ls_iter, ls_ok, ls_total;
   double fx0, alpha_ls, E_trial;
@@ -299,6 +304,8 @@ struct CgfShape {
             // slots' copies) overlapping the previous iteration's tail
 };
 void launch_cgf_init(const Launch& L);
+// Mixed path, before launch_cgf_init: the power-of-two scale of b.
+void launch_cgf_scale(const Launch& L);
 void launch_cgf_iter(const Launch& L, const CgfShape& sh);
 int cg_solve_blocks_per_sm(int fp64);
 // Two-block cooperative launch whose grid barrier has a missing arrival.

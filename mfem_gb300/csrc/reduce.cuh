@@ -325,6 +325,7 @@ __device__ __forceinline__ void reset_step_scalars(SceneScalars* sc) {
   sc->alpha_ls_f = 1.0f;
   sc->procrustes_fail = 0;
   sc->nph = kPhNewton;
+  sc->cg_scale_exp = 0;
 }
 
 

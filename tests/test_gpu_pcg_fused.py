@@ -82,3 +82,37 @@ def test_fused_shape_is_validated(gpu_lib):
         with pytest.raises(MfemError):
             gpu.set_pcg_shape(bh, *bad)
     sc.close()
+
+
+@pytest.mark.parametrize("b2", [1e-20, 1e-32, 1e-38, 1e-42])
+def test_fused_mixed_tiny_rhs_stays_in_range(gpu_lib, b2):
+    """Right-hand sides whose per-entry squares fall below FP32's normal
+    range (the float-float inner products' exponent range): the mixed path
+    solves for 2^k b with 2^k from max |b_i|, so the verified stop still
+    meets the tolerance, with the unscaled solve's iteration count."""
+    tol = 1e-6
+    sc = gpu.Scene(cube(16, iterative_solver_tolerance=tol, max_iterative_solver_iters=5000))
+    sc.step()
+    rp, col, val, rhs = sc.get_system()
+    _, it0, _ = sc.pcg(rhs)
+    b = rhs * (np.sqrt(b2) / np.linalg.norm(rhs))
+    dx, it, err = sc.pcg(b)
+    assert np.isfinite(dx).all() and err < tol, (it, err)
+    true = np.linalg.norm(b - bsr_mul(rp, col, val, dx)) / np.linalg.norm(b)
+    assert true <= 1.01 * tol, true
+    assert abs(it - it0) <= max(3, it0 // 20), (it, it0)
+    sc.close()
+
+
+@pytest.mark.parametrize("p", [-40, 40])
+def test_fused_mixed_power_of_two_scaling_is_exact(gpu_lib, p):
+    """Scaling b by a power of two scales the solution by it, bitwise (2^p
+    keeps every entry of b, and of the solution's float pairs, a normal
+    FP32 number, so the scaling itself is exact)."""
+    sc = gpu.Scene(cube(16, iterative_solver_tolerance=1e-6, max_iterative_solver_iters=5000))
+    sc.step()
+    rp, col, val, rhs = sc.get_system()
+    dx0, it0, _ = sc.pcg(rhs)
+    dx1, it1, _ = sc.pcg(rhs * 2.0 ** p)
+    assert it1 == it0 and np.array_equal(dx1, dx0 * 2.0 ** p)
+    sc.close()
