@@ -263,10 +263,11 @@ int mfem_gpu_kernel_name(int kernel, char* name, int name_len);
 
 /* ---- kernel shapes (no counterpart in the reference) ---------------------
  * Shape of the batch's fused PCG iteration: stages = 0 streams the matrix
- * through registers; 2..4 stage each warp's ELL slots through that many
+ * through registers; 2..4 or 8 stage each warp's ELL slots through that many
  * shared-memory buffers filled by bulk copies; keep = 1 marks half of the
  * matrix's L2 lines evict-last, 0 all evict-first; unroll = 2 (with
- * stages = 4) puts two slots' gathers in flight together, unroll = 1 one;
+ * stages = 4) puts two slots' gathers in flight together, unroll = 4
+ * (with stages = 8) four, for systems too small to fill the GPU; unroll = 1 one;
  * pdl = 1 (staged shapes only) launches each iteration as a programmatic
  * dependent of the previous one.  FP64 batches use stages <= 2 and
  * unroll 1.  Every shape computes the same bits; the autotuner picks one

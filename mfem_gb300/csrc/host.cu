@@ -1550,7 +1550,7 @@ int pick(const std::vector<float>& t) {
 std::vector<CgfShape> cgf_candidates(int fp64) {
   if (fp64) return {CgfShape{0, 0, 1, 0}, CgfShape{2, 0, 1, 0}, CgfShape{2, 0, 1, 1}};
   return {CgfShape{2, 0, 1, 1}, CgfShape{0, 0, 1, 0}, CgfShape{2, 0, 1, 0}, CgfShape{3, 0, 1, 1},
-          CgfShape{2, 1, 1, 1}, CgfShape{4, 0, 2, 1}};
+          CgfShape{2, 1, 1, 1}, CgfShape{4, 0, 2, 1}, CgfShape{8, 0, 4, 1}};
 }
 
 std::string shape_str(const CgfShape& c) {
@@ -2550,8 +2550,9 @@ int mfem_gpu_batch_set_profiling(mfem_batch* b, int enable) {
 }
 
 int mfem_gpu_batch_set_pcg_shape(mfem_batch* b, int32_t stages, int32_t keep, int32_t unroll, int32_t pdl) {
-  if (!b || stages < 0 || stages > 4 || stages == 1 || keep < 0 || keep > 1 || unroll < 1 || unroll > 2 ||
-      (unroll == 2 && stages != 4) || pdl < 0 || pdl > 1 || (pdl && stages == 0))
+  if (!b || stages < 0 || (stages > 4 && stages != 8) || stages == 1 || keep < 0 || keep > 1 || unroll < 1 ||
+      (unroll != 1 && unroll != 2 && unroll != 4) || (unroll == 2 && stages != 4) || (unroll == 4 && stages != 8) ||
+      (stages == 8 && unroll != 4) || pdl < 0 || pdl > 1 || (pdl && stages == 0))
     return MFEM_ERR_INVALID;
   if (b->fp64 && stages > 2) stages = 2;
   if (b->fp64) unroll = 1;

@@ -1476,10 +1476,13 @@ __device__ __forceinline__ void cgf_staged_tile(int tix, const Tile* tiles, cons
 
 // Resident blocks per SM: six (40 registers) in FP32 where the stages fit
 // six blocks' shared memory, five with four stages (41 KB a block), four
-// (64 registers) when two slots' gathers are in flight together.
+// (64 registers) when two slots' gathers are in flight together, two (82 KB
+// of stages) with eight stages and four slots in flight: the shape for
+// systems too small to fill the GPU, where each row's chain of slots, not
+// the bandwidth, sets the iteration's time.
 template <typename Real, int S, int U>
 constexpr int cgf_staged_min_blocks() {
-  return sizeof(Real) == 4 ? (U > 1 ? 4 : (S >= 4 ? 5 : 6)) : 4;
+  return sizeof(Real) == 4 ? (U >= 4 ? 2 : (U > 1 ? 4 : (S >= 4 ? 5 : 6))) : 4;
 }
 template <typename Real, bool kScaled, int S, int kKeep, int U, bool kPdl>
 __global__ void __launch_bounds__(kCgThreads, cgf_staged_min_blocks<Real, S, U>()) k_cgf_iter_staged(
@@ -1638,6 +1641,11 @@ namespace {
 template <typename Real, bool kScaled, int S, int kKeep, int U, bool kPdl>
 void launch_staged(const Launch& L) {
   const size_t smem = cgf_staged_smem_bytes<Real, S>(kCgThreads / 32);
+  if (smem > 48 * 1024) {  // above the default dynamic limit: opt in once
+    static const cudaError_t opt = cudaFuncSetAttribute(k_cgf_iter_staged<Real, kScaled, S, kKeep, U, kPdl>,
+                                                        cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    (void)opt;
+  }
   if constexpr (kPdl) {
     // the launch may start while the previous kernel of the stream runs; the
     // kernel waits for it (griddepcontrol.wait) before reading its results
@@ -1661,7 +1669,8 @@ void launch_staged(const Launch& L) {
 template <typename Real, bool kScaled, int kKeep, bool kPdl>
 void launch_staged_s(const Launch& L, int stages, int unroll) {
   if constexpr (sizeof(Real) == 4) {
-    if (unroll > 1) launch_staged<Real, kScaled, 4, kKeep, 2, kPdl>(L);
+    if (unroll >= 4) launch_staged<Real, kScaled, 8, kKeep, 4, kPdl>(L);
+    else if (unroll > 1) launch_staged<Real, kScaled, 4, kKeep, 2, kPdl>(L);
     else if (stages == 2) launch_staged<Real, kScaled, 2, kKeep, 1, kPdl>(L);
     else if (stages == 3) launch_staged<Real, kScaled, 3, kKeep, 1, kPdl>(L);
     else launch_staged<Real, kScaled, 4, kKeep, 1, kPdl>(L);

@@ -289,12 +289,13 @@ cudaError_t launch_cg_solve(const Launch& L, int grid, int max_iters);
 void launch_cg_replace(const Launch& L);  // r = b - A x in df64 (mixed path)
 // Single-reduction PCG: init (r0, u0, w0 = A u0) and one launch per iteration.
 // The iteration's shape: stages = 0 streams the matrix through registers;
-// stages = 2..4 stages each warp's ELL slots through a ring of that many
+// stages = 2..4 (or 8) stages each warp's ELL slots through a ring of that many
 // shared-memory buffers filled by bulk copies (the FP64 path uses 2);
 // keep = 1 marks half of the matrix lines evict-last in L2 (0: all
 // evict-first); unroll = 2 puts two slots' gathers in flight together
-// (four stages, four resident blocks of 64 registers; FP32 only).  Every
-// shape computes the same bits.
+// (four stages, four resident blocks of 64 registers; FP32 only), unroll =
+// 4 four (eight stages, two resident blocks).  Every shape computes the
+// same bits.
 struct CgfShape {
   int stages;
   int keep;

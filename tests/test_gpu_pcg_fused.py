@@ -54,7 +54,7 @@ def test_fused_shapes_compute_the_same_bits(gpu_lib, prec):
     sc.step()
     s0 = sc.get_state()
     shapes = [(0, 0, 1, 0), (2, 0, 1, 0), (3, 0, 1, 0), (4, 0, 1, 0), (2, 1, 1, 0), (4, 1, 1, 0),
-              (4, 0, 2, 0), (4, 1, 2, 0), (2, 0, 1, 1), (4, 0, 2, 1), (3, 1, 1, 1)]
+              (4, 0, 2, 0), (4, 1, 2, 0), (2, 0, 1, 1), (4, 0, 2, 1), (3, 1, 1, 1), (8, 0, 4, 0), (8, 0, 4, 1)]
     fp64 = prec == abi.PRECISION_FP64
     ref = None
     for shape in shapes:
@@ -78,7 +78,7 @@ def test_fused_shape_is_validated(gpu_lib):
     bh = sc.solo_batch_handle()
     from mfem_gb300._lib import MfemError
     for bad in ((1, 0, 1, 0), (5, 0, 1, 0), (-1, 0, 1, 0), (2, 2, 1, 0), (2, 0, 2, 0), (4, 0, 3, 0),
-                (4, 0, 0, 0), (0, 0, 1, 1), (2, 0, 1, 2)):
+                (4, 0, 0, 0), (0, 0, 1, 1), (2, 0, 1, 2), (8, 0, 1, 0), (8, 0, 2, 0), (4, 0, 4, 0), (6, 0, 1, 0)):
         with pytest.raises(MfemError):
             gpu.set_pcg_shape(bh, *bad)
     sc.close()
