@@ -74,6 +74,8 @@ def parse():
                     help="skip the batched-vs-plain measurement on the 64-scene mix")
     ap.add_argument("--mix-plain-steps", type=int, default=100,
                     help="timesteps per scene of the plain (one scene at a time) 64-scene mix")
+    ap.add_argument("--mix-lanes", type=int, default=4,
+                    help="batches the 64-scene mix is split into for the side-by-side (lanes) form")
     ap.add_argument("--mix-steps", type=int, default=100,
                     help="timesteps per scene of the batched 64-scene mix (its stated 100)")
     ap.add_argument("--no-error", action="store_true",
@@ -636,6 +638,16 @@ def run_batch_mix(args, gpu, abi, configs):
     stats, done = batch.step_n(steps, raise_on_error=False)
     batched_ms = stats[0].device_ms
     batch.close()
+    # the same 100 timesteps from the same state with the scenes in lanes:
+    # balanced batches stepped side by side on their own streams
+    restore()
+    lanes = gpu.Lanes(scenes, lanes=args.mix_lanes)
+    t_l = time.perf_counter()
+    lstats, ldone = lanes.step_n(steps, raise_on_error=False)
+    lanes_s = time.perf_counter() - t_l
+    lanes_ms = max(st.device_ms for st in lstats)
+    lanes.close()
+    lanes_steps = int((ldone >= 0).sum())
     for s in scenes:
         s.close()
     taken = done >= 0
@@ -686,6 +698,11 @@ def run_batch_mix(args, gpu, abi, configs):
                         "slowest_scenes": [{"scene": int(i), "tets": specs[i].n_tets, "done_ms": float(finish[i]),
                                             "newton": int(stats[i].newton_iterations),
                                             "cg": int(stats[i].cg_iterations)} for i in slowest]},
+            "batched_lanes": {"value": lanes_steps / (lanes_ms / 1e3), "unit": UNIT, "steps": steps,
+                              "lanes": len(lanes.parts), "scene_steps": lanes_steps,
+                              "ms_total": lanes_ms, "wall_s": lanes_s,
+                              "form": "mfem_gpu_batches_step_n: tets-balanced batches side by side, each on its "
+                                      "own stream (the lane of the smallest scenes at the highest priority)"},
             "batched_3": {"value": b3, "unit": UNIT, "steps": short},
             "lockstep": {"value": lockstep, "unit": UNIT, "steps": short,
                          "ms_per_batch_step": float(np.mean(ls_ms))},
@@ -694,7 +711,9 @@ def run_batch_mix(args, gpu, abi, configs):
                       "slowest_scene_ms": float(max(scene_ms)), "slowest_scene": int(np.argmax(scene_ms)),
                       "ratio_bound_sum_over_slowest": float(sum(scene_ms) / max(max(scene_ms), 1e-9))},
             "plain_3": {"value": plain_3, "unit": UNIT, "steps_per_scene": short, "scene_steps": p3_n},
-            "batched_vs_plain": batched / plain, "batched_3_vs_plain_3": b3 / plain_3,
+            "batched_vs_plain": batched / plain,
+            "batched_lanes_vs_plain": (lanes_steps / (lanes_ms / 1e3)) / plain,
+            "batched_3_vs_plain_3": b3 / plain_3,
             "lockstep_vs_plain_3": lockstep / plain_3}
 
 
@@ -746,7 +765,7 @@ def run_served(args):
     served_dev_s = sum(ms for _, _, ms in srv.ticks) / 1e3
     line = {"metric": METRIC, "value": summ["timesteps_per_s"], "unit": UNIT, "n_gpus": ws,
             "steps": args.c5_steps, "warmup": 0, "higher_is_better": True, "scaling": "strong",
-            "vs_baseline": None, "dtype": "f32+f64" if args.precision == "mixed" else "f64",
+            "vs_baseline": None, "dtype": "f32+df64" if args.precision == "mixed" else "f64",
             "data": "synthetic",
             "config": {"workload": f"served_stream_c5_{args.c5_duration:g}s_{args.c5_steps}steps",
                        "arrival_rate_per_s": 20.0, "tets_range": [1e3, 5e5],

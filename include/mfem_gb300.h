@@ -235,6 +235,17 @@ int mfem_gpu_batch_step(mfem_batch* batch, mfem_step_stats* stats);
 #define MFEM_BATCH_MAX_STEPS 1024
 int mfem_gpu_batch_step_n(mfem_batch* batch, int32_t steps, mfem_step_stats* stats,
                           double* step_done_ms);
+/* mfem_gpu_batch_step_n for several batches at once (no counterpart in the
+ * reference): each batch on its own stream, driven by its own host thread,
+ * so that the GPU runs the batches' launches side by side -- a latency-bound
+ * small scene then waits only for the launches of its own batch.  The
+ * batches must be distinct and on the calling thread's device (no scene in
+ * two of them).  stats and step_done_ms are laid out batch after batch, each
+ * batch's scenes in its order; step_done_ms is measured from each batch's
+ * own start.  Returns the first failure in batch order (MFEM_ERR_NONFINITE
+ * only if nothing else failed). */
+int mfem_gpu_batches_step_n(mfem_batch* const* batches, int32_t nbatch, int32_t steps,
+                            mfem_step_stats* stats, double* step_done_ms);
 
 /* Prescribed positions of the pinned vertices for the next step (3*n_pinned
  * doubles in the order of mfem_gpu_scene_pinned), replacing the scripted
@@ -257,6 +268,11 @@ enum {
 };
 int mfem_gpu_scene_solo_batch(mfem_scene* scene, mfem_batch** batch);
 int mfem_gpu_batch_set_profiling(mfem_batch* batch, int enable);
+/* Scheduling priority of the batch's stream against other batches' streams
+ * on the device (no counterpart in the reference): 0 the default, 1, 2, ...
+ * higher (clamped to the device's range).  Waits for the batch's work in
+ * flight. */
+int mfem_gpu_batch_set_priority(mfem_batch* batch, int32_t priority);
 int mfem_gpu_batch_kernel_stats(mfem_batch* batch, int kernel, double* total_ms,
                                 int64_t* launches);
 int mfem_gpu_kernel_name(int kernel, char* name, int name_len);
@@ -287,6 +303,12 @@ int mfem_gpu_batch_get_pcg_shape(mfem_batch* batch, int32_t* stages, int32_t* ke
  * MFEM_GB300_TUNE_CACHE names the cache file.  MFEM_ERR_CAPACITY if len is
  * too small. */
 int mfem_gpu_batch_tune_report(mfem_batch* batch, char* buf, int32_t len);
+/* The autotuner's mode for batches created from now on, process-wide (no
+ * counterpart in the reference): 0 built-in defaults, 1 time on a cache
+ * miss, 2 always time, -1 back to MFEM_GB300_TUNE.  A serving loop that
+ * creates batches as requests come and go sets 0 (or relies on a warm
+ * cache) so that no batch creation pays for timing runs. */
+int mfem_gpu_set_tuning(int32_t mode);
 /* Sets the register-budget variants of K1 (0..1; FP64 and the standard-FEM
  * variable have only 0), K5 (0..2) and K6 (0..1) by hand, overriding the
  * autotuner; 0 is the built-in default.  Every variant computes the same

@@ -41,6 +41,7 @@ SIGNATURES = {
     "mfem_gpu_batch_destroy": (C.c_int, [_vp]),
     "mfem_gpu_batch_step": (C.c_int, [_vp, _vp]),
     "mfem_gpu_batch_step_n": (C.c_int, [_vp, C.c_int32, _vp, _dp]),
+    "mfem_gpu_batches_step_n": (C.c_int, [C.POINTER(_vp), C.c_int32, C.c_int32, _vp, _dp]),
     "mfem_gpu_scene_elem_update": (C.c_int, [_vp, _dp, C.c_double] + [_dp] * 8),
     "mfem_gpu_scene_bcsr_sizes": (C.c_int, [_vp, _ip, _ip]),
     "mfem_gpu_scene_get_system": (C.c_int, [_vp, _ip, _ip, _dp, _dp]),
@@ -49,6 +50,8 @@ SIGNATURES = {
     "mfem_gpu_scene_set_pins": (C.c_int, [_vp, _dp]),
     "mfem_gpu_scene_solo_batch": (C.c_int, [_vp, C.POINTER(_vp)]),
     "mfem_gpu_batch_set_profiling": (C.c_int, [_vp, C.c_int]),
+    "mfem_gpu_batch_set_priority": (C.c_int, [_vp, C.c_int32]),
+    "mfem_gpu_set_tuning": (C.c_int, [C.c_int32]),
     "mfem_gpu_batch_kernel_stats": (C.c_int, [_vp, C.c_int, _dp, C.POINTER(C.c_int64)]),
     "mfem_gpu_batch_set_pcg_shape": (C.c_int, [_vp, C.c_int32, C.c_int32, C.c_int32, C.c_int32]),
     "mfem_gpu_batch_get_pcg_shape": (C.c_int, [_vp] + [C.POINTER(C.c_int32)] * 4),

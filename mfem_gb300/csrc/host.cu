@@ -22,6 +22,7 @@
 #include <map>
 #include <memory>
 #include <mutex>
+#include <thread>
 #include <sys/stat.h>
 #include <new>
 #include <string>
@@ -1429,7 +1430,11 @@ std::mutex g_tune_mu;
 std::map<std::string, std::string> g_tune_mem;
 bool g_tune_loaded = false;
 
+std::atomic<int> g_tune_override{-1};  // mfem_gpu_set_tuning; -1: the environment decides
+
 int tune_mode() {
+  const int o = g_tune_override.load();
+  if (o >= 0) return o;
   const char* v = std::getenv("MFEM_GB300_TUNE");
   if (!v) return 1;
   if (!std::strcmp(v, "0") || !std::strcmp(v, "off")) return 0;
@@ -2549,6 +2554,25 @@ int mfem_gpu_batch_set_profiling(mfem_batch* b, int enable) {
   return MFEM_OK;
 }
 
+int mfem_gpu_set_tuning(int32_t mode) {
+  if (mode < -1 || mode > 2) return MFEM_ERR_INVALID;
+  g_tune_override.store(mode);
+  return MFEM_OK;
+}
+
+int mfem_gpu_batch_set_priority(mfem_batch* b, int32_t priority) {
+  if (!b) return MFEM_ERR_INVALID;
+  int least = 0, greatest = 0;  // CUDA: numerically lower is the higher priority
+  CUDA_OR(cudaDeviceGetStreamPriorityRange(&least, &greatest), MFEM_ERR_CUDA);
+  const int p = std::max(greatest, std::min(least, least - (int)priority));
+  cudaStream_t st = nullptr;
+  CUDA_OR(cudaStreamCreateWithPriority(&st, cudaStreamNonBlocking, p), MFEM_ERR_CUDA);
+  CUDA_OR(cudaStreamSynchronize(b->stream), MFEM_ERR_CUDA);
+  cudaStreamDestroy(b->stream);
+  b->stream = st;
+  return MFEM_OK;
+}
+
 int mfem_gpu_batch_set_pcg_shape(mfem_batch* b, int32_t stages, int32_t keep, int32_t unroll, int32_t pdl) {
   if (!b || stages < 0 || (stages > 4 && stages != 8) || stages == 1 || keep < 0 || keep > 1 || unroll < 1 ||
       (unroll != 1 && unroll != 2 && unroll != 4) || (unroll == 2 && stages != 4) || (unroll == 4 && stages != 8) ||
@@ -2642,6 +2666,42 @@ int mfem_gpu_batch_step_n(mfem_batch* batch, int32_t steps, mfem_step_stats* sta
 int mfem_gpu_batch_step(mfem_batch* batch, mfem_step_stats* stats) {
   if (!batch) return MFEM_ERR_INVALID;
   return batch_step_impl(batch, stats);
+}
+
+int mfem_gpu_batches_step_n(mfem_batch* const* batches, int32_t nbatch, int32_t steps, mfem_step_stats* stats,
+                            double* step_done_ms) {
+  if (!batches || nbatch < 1 || steps < 1 || steps > MFEM_BATCH_MAX_STEPS) return MFEM_ERR_INVALID;
+  std::vector<size_t> first(nbatch + 1, 0);
+  for (int k = 0; k < nbatch; ++k) {
+    if (!batches[k]) return MFEM_ERR_INVALID;
+    for (int j = 0; j < k; ++j)
+      if (batches[j] == batches[k]) return MFEM_ERR_INVALID;
+    first[k + 1] = first[k] + batches[k]->scenes.size();
+  }
+  int dev = 0;
+  CUDA_OR(cudaGetDevice(&dev), MFEM_ERR_CUDA);
+  // one host thread per batch, each driving its batch's stream; the GPU
+  // runs the batches' launches side by side
+  std::vector<int> rc(nbatch, MFEM_OK);
+  std::vector<std::thread> th;
+  th.reserve(nbatch);
+  for (int k = 0; k < nbatch; ++k)
+    th.emplace_back([&, k]() {
+      if (cudaSetDevice(dev) != cudaSuccess) {
+        rc[k] = MFEM_ERR_CUDA;
+        return;
+      }
+      rc[k] = batch_step_n_impl(batches[k], steps, stats ? stats + first[k] : nullptr,
+                                step_done_ms ? step_done_ms + first[k] * (size_t)steps : nullptr);
+    });
+  for (std::thread& t : th) t.join();
+  // the first failure of the call in batch order; a retired scene's
+  // non-finite status as the single-batch call reports it
+  for (int k = 0; k < nbatch; ++k)
+    if (rc[k] != MFEM_OK && rc[k] != MFEM_ERR_NONFINITE) return rc[k];
+  for (int k = 0; k < nbatch; ++k)
+    if (rc[k] != MFEM_OK) return rc[k];
+  return MFEM_OK;
 }
 
 int mfem_gpu_scene_elem_update(mfem_scene* s, const double* x, double h, double* R, double* S,

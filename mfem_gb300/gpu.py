@@ -248,3 +248,78 @@ class Batch:
         if rc != abi.OK and (raise_on_error or rc in (abi.ERR_CUDA, abi.ERR_TIMEOUT, abi.ERR_INVALID)):
             check(rc, "batch_step_n")
         return [abi.StepStats.from_buffer_copy(st) for st in self._stats], done
+
+
+def set_tuning(mode):
+    """Autotuner mode for batches created from now on (mfem_gpu_set_tuning:
+    0 defaults, 1 time on a cache miss, 2 always, -1 the environment's)."""
+    check(load().mfem_gpu_set_tuning(int(mode)), "set_tuning")
+
+
+def set_priority(batch_handle, priority):
+    """Stream priority of a batch against other batches (0 default, higher
+    runs first; mfem_gpu_batch_set_priority)."""
+    check(load().mfem_gpu_batch_set_priority(batch_handle, int(priority)), "set_priority")
+
+
+def lane_partition(weights, lanes):
+    """Indices per lane: longest-processing-time first by weight (a scene's
+    tets), each to the least-loaded lane; empty lanes dropped."""
+    out = [[] for _ in range(max(1, int(lanes)))]
+    load_ = [0.0] * len(out)
+    for i in sorted(range(len(weights)), key=lambda i: (-float(weights[i]), i)):
+        k = min(range(len(out)), key=lambda j: (load_[j], j))
+        out[k].append(i)
+        load_[k] += float(weights[i])
+    return [sorted(l) for l in out if l]
+
+
+class Lanes:
+    """Scenes split into `lanes` batches (balanced by tets) that step side by
+    side, each on its own stream and host thread (mfem_gpu_batches_step_n):
+    a latency-bound small scene waits only for its own batch's launches.
+    The lane of the smallest scenes on average runs at the highest stream
+    priority.  A scene's arithmetic does not depend on its batch, so every
+    result is the one of the same scene in a single batch of the same PCG
+    form."""
+
+    def __init__(self, scenes, lanes=4):
+        self.scenes = list(scenes)
+        self.parts = lane_partition([s.n_tets for s in self.scenes], lanes)
+        self.batches = [Batch([self.scenes[i] for i in p]) for p in self.parts]
+        mean = [np.mean([self.scenes[i].n_tets for i in p]) for p in self.parts]
+        for r, k in enumerate(np.argsort(mean)):
+            set_priority(self.batches[k].handle, max(0, len(self.parts) - 1 - r))
+        self._order = [i for p in self.parts for i in p]
+        self._stats = (abi.StepStats * len(self.scenes))()
+
+    def close(self):
+        for b in self.batches:
+            b.close()
+        self.batches = []
+
+    def step(self, raise_on_error=True):
+        """One timestep of every scene (each lane one mfem_gpu_batch_step)."""
+        out = [None] * len(self.scenes)
+        for p, b in zip(self.parts, self.batches):
+            for i, st in zip(p, b.step(raise_on_error=raise_on_error)):
+                out[i] = st
+        return out
+
+    def step_n(self, steps, raise_on_error=True):
+        """`steps` timesteps of every scene, each at its own pace, the lanes
+        concurrently; (stats per scene in the scenes' order, step_done_ms
+        scenes x steps from each lane's start)."""
+        n = len(self.scenes)
+        done = np.zeros((n, max(int(steps), 1)))
+        arr = (C.c_void_p * len(self.batches))(*[b.handle.value for b in self.batches])
+        rc = load().mfem_gpu_batches_step_n(arr, len(self.batches), int(steps), self._stats,
+                                             done.ctypes.data_as(_dp))
+        if rc != abi.OK and (raise_on_error or rc in (abi.ERR_CUDA, abi.ERR_TIMEOUT, abi.ERR_INVALID)):
+            check(rc, "batches_step_n")
+        stats = [None] * n
+        out_done = np.zeros_like(done)
+        for pos, i in enumerate(self._order):
+            stats[i] = abi.StepStats.from_buffer_copy(self._stats[pos])
+            out_done[i] = done[pos]
+        return stats, out_done

@@ -6,10 +6,17 @@ admits them in arrival order while their device footprint
 instance's state resident (positions, velocities, stretch variables,
 rotations, BDF history and solver state live in the scene's device arena),
 and at every tick steps ALL admitted instances together: one batch, one
-launch per kernel phase for all of them (mfem_gpu_batch_step).  An instance
-that has taken its timesteps leaves the batch, its memory is freed and the
-next queued request takes its place at the next tick, so requests that
-arrive while others are on the GPU join them there.
+launch per kernel phase for all of them.  A tick takes up to
+`steps_per_tick` timesteps of every instance with each instance at its own
+pace (mfem_gpu_batch_step_n: an instance whose Newton loop ends starts its
+next timestep at once instead of waiting for the slowest one), bounded by
+the fewest timesteps any member still owes; with steps_per_tick = 1 every
+tick is one mfem_gpu_batch_step.  An instance that has taken its timesteps
+leaves the batch, its memory is freed and the next queued request takes its
+place at the next tick, so requests that arrive while others are on the GPU
+join them there.  Batches are created with the autotuner off
+(mfem_gpu_set_tuning(0)) unless `tune` is set, so that membership changes
+do not pay for timing runs.
 
 Scenes are built on a worker thread (the host mesh build and the arena
 upload), overlapping the GPU ticks.  A scene's arithmetic does not depend on
@@ -68,10 +75,16 @@ class Server:
     keep_state    which final state arrays to return ("x", "v", "s", "R")
     escalate      continue a mixed-precision scene in FP64 after a failed
                   line search
+    steps_per_tick  timesteps a tick may take per instance (each at its own
+                  pace); a failed step rolls back the instance's whole tick
+    tune          let batch creation run the autotuner's timings
     """
 
-    def __init__(self, budget_bytes, keep_state=("x",), max_scenes=4096, escalate=True):
+    def __init__(self, budget_bytes, keep_state=("x",), max_scenes=4096, escalate=True, steps_per_tick=1,
+                 tune=False):
         self.budget = int(budget_bytes)
+        self.steps_per_tick = max(1, int(steps_per_tick))
+        self.tune = bool(tune)
         self.keep = tuple(keep_state)
         self.max_scenes = max_scenes
         self.escalate = escalate
@@ -122,6 +135,9 @@ class Server:
         stepper = cf.ThreadPoolExecutor(max_workers=2)
         t0 = time.perf_counter()
         now = lambda: time.perf_counter() - t0
+        set_tuning = getattr(gpu, "set_tuning", None)
+        if set_tuning is not None and not self.tune:
+            set_tuning(0)
 
         def close_batches():
             for b, _ in groups.values():
@@ -166,27 +182,40 @@ class Server:
                 # stream (the library's calls on distinct batches are
                 # thread-safe and release the interpreter lock)
                 order = sorted(by_prec)
-                futs = [stepper.submit(groups[p][0].step, raise_on_error=False) for p in order]
+
+                def tick(p):
+                    b, members = groups[p]
+                    k = min([self.steps_per_tick] + [active[m][0].steps - active[m][0].steps_done
+                                                     for m in members])
+                    if k > 1:
+                        return b.step_n(k, raise_on_error=False)
+                    return b.step(raise_on_error=False), None
+
+                futs = [stepper.submit(tick, p) for p in order]
                 results, tick_ms = [], 0.0
                 for p, f in zip(order, futs):
-                    stats = f.result()
+                    stats, done = f.result()
                     tick_ms = max(tick_ms, stats[0].device_ms)
-                    results += [(k, st, stats[0].device_ms) for k, st in zip(groups[p][1], stats)]
+                    for j, (k, st) in enumerate(zip(groups[p][1], stats)):
+                        if done is None:
+                            ms = [stats[0].device_ms]
+                        else:   # the device time of each timestep the scene took in the tick
+                            d = done[j][done[j] >= 0]
+                            ms = list(np.diff(np.concatenate([[0.0], d])))
+                        results.append((k, st, ms))
                 self.ticks.append((now(), len(active), tick_ms))
                 finished, escalate = [], []
-                for k, st, batch_ms in results:
+                for k, st, ms in results:
                     r, sc = active[k]
-                    r.steps_done += 1
-                    r.step_ms.append(batch_ms)
-                    r.newton.append(st.newton_iterations)
-                    r.cg.append(st.cg_iterations)
                     if (self.escalate and sc.spec.precision == abi.PRECISION_MIXED
                             and st.status in (abi.ERR_LS_FAILED, abi.ERR_NONFINITE, abi.ERR_PROCRUSTES)):
-                        # undo the step: the FP64 scene takes it again
-                        r.steps_done -= 1
-                        del r.step_ms[-1], r.newton[-1], r.cg[-1]
+                        # undo the tick: the FP64 scene takes its steps again
                         escalate.append(k)
                         continue
+                    r.steps_done += len(ms)
+                    r.step_ms += ms
+                    r.newton.append(st.newton_iterations)
+                    r.cg.append(st.cg_iterations)
                     if st.status not in (abi.OK, abi.ERR_CG_MAXITER, abi.ERR_LS_FAILED):
                         r.status = st.status
                     # a scene whose state is no longer finite leaves with its status
@@ -213,6 +242,8 @@ class Server:
                     r.footprint, r.escalated_at = fp, r.steps_done
                     active[k] = (r, sc64)
         finally:
+            if set_tuning is not None and not self.tune:
+                set_tuning(-1)
             close_batches()
             for r, sc in active.values():
                 sc.close()

@@ -60,7 +60,7 @@ def _rank(rank, port, q):
     ws, r, _, pg = bench.dist_setup()
     weights = [5, 1, 4, 4, 2, 7, 3]           # tets x steps of seven requests
     mine = server.shard(weights, ws, r)
-    srv = server.Server(budget_bytes=100)
+    srv = server.Server(budget_bytes=100, steps_per_tick=1)
     for i in mine:
         srv.submit(SimpleNamespace(bytes=10, precision=abi.PRECISION_MIXED), weights[i])
     out = srv.run(realtime=False)

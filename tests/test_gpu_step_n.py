@@ -95,3 +95,25 @@ def test_step_n_validates_its_count(gpu_lib):
         with pytest.raises(MfemError):
             b.step_n(bad)
     b.close()
+
+
+def test_lanes_equal_one_batch(gpu_lib):
+    """The scenes split into lanes (batches stepped side by side on their own
+    streams, mfem_gpu_batches_step_n) take the same steps, bitwise, as in a
+    single batch of the same PCG form."""
+    specs = mix_specs(abi.PRECISION_MIXED)
+    a = [gpu.Scene(s) for s in specs]
+    b = [gpu.Scene(s) for s in specs]
+    one = gpu.Batch(a)
+    lanes = gpu.Lanes(b, lanes=3)
+    assert len(lanes.batches) == 3 and sorted(i for p in lanes.parts for i in p) == list(range(len(specs)))
+    s1, d1 = one.step_n(4, raise_on_error=False)
+    s2, d2 = lanes.step_n(4, raise_on_error=False)
+    for i in range(len(specs)):
+        assert (s1[i].newton_iterations, s1[i].cg_iterations, s1[i].status) == \
+            (s2[i].newton_iterations, s2[i].cg_iterations, s2[i].status), i
+        assert ((d1[i] >= 0) == (d2[i] >= 0)).all()
+    for (xa, sa), (xb, sb) in zip(state(a), state(b)):
+        assert np.array_equal(xa, xb) and np.array_equal(sa, sb)
+    lanes.close()
+    one.close()

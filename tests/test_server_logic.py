@@ -81,6 +81,17 @@ class _FakeGpu:
                     out.append(_Stats(s.spec.fail if fail else abi.OK))
                 return out
 
+            def step_n(self, k, raise_on_error=True):
+                # k steps per scene; a scene's status is the worst of its steps
+                worst = [abi.OK] * len(scenes)
+                done = np.zeros((len(scenes), k))
+                for j in range(k):
+                    for i, st in enumerate(self.step()):
+                        if st.status != abi.OK:
+                            worst[i] = st.status
+                        done[i, j] = j + 1.0
+                return [_Stats(w) for w in worst], done
+
             def close(self):
                 pass
         return B()
@@ -89,7 +100,7 @@ class _FakeGpu:
 def test_admission_by_budget_and_leaving_batches(monkeypatch):
     fake = _FakeGpu()
     monkeypatch.setattr(server, "gpu", fake)
-    srv = server.Server(budget_bytes=100)
+    srv = server.Server(budget_bytes=100, steps_per_tick=1)
     specs = [_spec("a", 60), _spec("b", 30), _spec("c", 50), _spec("d", 10)]
     steps = [3, 1, 2, 2]
     for sp, n in zip(specs, steps):
@@ -110,7 +121,7 @@ def test_admission_by_budget_and_leaving_batches(monkeypatch):
 def test_failed_line_search_continues_in_fp64(monkeypatch):
     fake = _FakeGpu()
     monkeypatch.setattr(server, "gpu", fake)
-    srv = server.Server(budget_bytes=200)
+    srv = server.Server(budget_bytes=200, steps_per_tick=1)
     srv.submit(_spec("soft", 40, ls_fail_at=2), 5)
     srv.submit(_spec("stiff", 40), 4)
     srv.submit(_spec("last", 40, ls_fail_at=3), 3)   # fails on its final step
@@ -135,7 +146,7 @@ def test_failed_line_search_continues_in_fp64(monkeypatch):
 def test_escalation_off_keeps_mixed(monkeypatch):
     fake = _FakeGpu()
     monkeypatch.setattr(server, "gpu", fake)
-    srv = server.Server(budget_bytes=200, escalate=False)
+    srv = server.Server(budget_bytes=200, escalate=False, steps_per_tick=1)
     srv.submit(_spec("soft", 40, ls_fail_at=2), 4)
     (r,) = srv.run(realtime=False)
     assert r.escalated_at is None and r.steps_done == 4
@@ -175,3 +186,32 @@ def test_shard_is_balanced_and_deterministic():
     loads = [sum(w[i] for i in p) for p in parts]
     assert max(loads) - min(loads) <= max(w)
     assert parts == [server.shard(w, 3, r) for r in range(3)]
+
+
+def test_lane_partition_balances_by_weight():
+    from mfem_gb300 import gpu
+    w = [100, 5, 60, 40, 35, 30, 1, 9]
+    parts = gpu.lane_partition(w, 3)
+    assert sorted(i for p in parts for i in p) == list(range(len(w)))
+    loads = [sum(w[i] for i in p) for p in parts]
+    assert max(loads) - min(loads) <= max(w)
+    assert parts == gpu.lane_partition(w, 3)
+    assert gpu.lane_partition([3, 2], 5) == [[0], [1]]
+
+
+def test_multi_step_ticks_roll_back_the_whole_tick(monkeypatch):
+    """Ticks of several timesteps (each scene at its own pace): a tick never
+    takes a scene past its own count, and a failed step rolls the scene back
+    to the tick's start, from where the FP64 scene takes the tick again."""
+    fake = _FakeGpu()
+    monkeypatch.setattr(server, "gpu", fake)
+    srv = server.Server(budget_bytes=200, steps_per_tick=4)
+    srv.submit(_spec("soft", 40, ls_fail_at=6), 9)
+    srv.submit(_spec("stiff", 40), 10)
+    out = srv.run(realtime=False)
+    soft, stiff = out
+    # ticks of min(4, what the members still owe): 4, 4, then 1 for soft
+    assert soft.escalated_at == 4 and soft.steps_done == 9 and soft.result["x"][0, 0] == 9
+    assert stiff.escalated_at is None and stiff.steps_done == 10 and stiff.result["x"][0, 0] == 10
+    assert len(soft.step_ms) == 9 and len(stiff.step_ms) == 10
+    assert not fake.live
