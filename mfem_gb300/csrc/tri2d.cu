@@ -27,7 +27,10 @@
 //   t2_norm     one block: |rhs|^2
 //   t2_pcg      ONE thread block for the whole PCG solve: every reduction a
 //               fixed-order tree in shared memory, __syncthreads between the
-//               phases, no grid-wide waits; one launch per solve
+//               phases, no grid-wide waits; one launch per solve.  Sheets
+//               with more free rows than the block has threads run
+//               t2_pcg_grid instead: the same iteration over co-resident
+//               blocks with bounded grid barriers, also one launch per solve
 //   t2_local    one thread per triangle: lambda and ds
 //   t2_energy   one thread per triangle and vertex: the three energy parts
 //   t2_esum     one block: the fixed-order sums (and max|dx|, max|ds|)
@@ -106,6 +109,9 @@ struct T2 {
   double* r;     // PCG vectors, 2 nf
   double* p;
   double* q;
+  double* p2;     // the grid PCG's second direction buffer (p of iteration k in p or p2 by parity)
+  double* part;   // the grid PCG's block partials: 2 x kT2MaxGrid
+  unsigned int* bar;  // the grid PCG's barrier: arrivals, generation, error flag
   double* epart;  // 2 nt + nv energy parts
   double* scal;   // SC_COUNT device scalars
   int* status;    // worst status the kernels saw
@@ -514,6 +520,204 @@ __global__ void __launch_bounds__(kBlock) t2_pcg(T2 d, int max_iter, double tol)
   }
 }
 
+// ----------------------------------------------------- grid PCG ---
+// The same Jacobi-PCG iteration over many blocks for sheets too large for
+// one (the FP64 work of a 10^4-triangle sheet on one SM at GB300's FP64
+// rate sets ~40 us per iteration).  One cooperative launch of G blocks of
+// kGridThreads, each owning a contiguous range of free rows; a reduction is
+// each block's fixed-order partial, a bounded grid barrier, and the G
+// partials summed in the same fixed order by every block (so every block
+// takes the same branches).  Two barriers per iteration: the direction
+// p_k = D^-1 r_k + beta_k p_{k-1} of a neighbouring row is formed where the
+// product gathers it (the same expression the row's owner evaluates), so
+// no barrier is needed between the update of p and the next product; p_k
+// alternates between p and p2.  Every wait is bounded (kT2BarrierNs or
+// kT2BarrierPolls): when one runs out the kernel flags MFEM_ERR_TIMEOUT in
+// the scene's status and every block leaves at its next barrier.
+constexpr int kGridThreads = 256;
+constexpr int kT2MaxGrid = 1024;
+constexpr unsigned long long kT2BarrierNs = 2000000000ull;
+constexpr unsigned int kT2BarrierPolls = 1u << 26;
+
+__device__ __forceinline__ unsigned long long t2_ns() {
+  unsigned long long t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+
+// bar[0] arrivals, bar[1] generation, bar[2] error.  False: leave the kernel.
+__device__ bool t2_grid_sync(const T2& d) {
+  __shared__ int ok_s;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    volatile unsigned int* gen = d.bar + 1;
+    volatile unsigned int* err = d.bar + 2;
+    int ok = *err == 0u;
+    if (ok) {
+      const unsigned int g = *gen;
+      __threadfence();
+      if (atomicAdd(d.bar, 1u) + 1u == gridDim.x) {
+        d.bar[0] = 0u;
+        __threadfence();
+        atomicAdd(d.bar + 1, 1u);
+      } else {
+        const unsigned long long t0 = t2_ns();
+        unsigned int polls = 0;
+        while (*gen == g) {
+          if (*err) {
+            ok = 0;
+            break;
+          }
+          if (++polls >= kT2BarrierPolls || ((polls & 255u) == 0 && t2_ns() - t0 > kT2BarrierNs)) {
+            atomicExch(d.bar + 2, 1u);
+            atomicExch(d.status, MFEM_ERR_TIMEOUT);
+            ok = 0;
+            break;
+          }
+          __nanosleep(32);
+        }
+      }
+      __threadfence();
+    }
+    ok_s = ok;
+  }
+  __syncthreads();
+  return ok_s != 0;
+}
+
+// Fixed-order tree sum over the block (kGridThreads values).
+__device__ double t2_block_sum256(double v, double* sh) {
+  const int t = threadIdx.x;
+  sh[t] = v;
+  __syncthreads();
+  for (int w = kGridThreads / 2; w > 0; w >>= 1) {
+    if (t < w) sh[t] += sh[t + w];
+    __syncthreads();
+  }
+  const double out = sh[0];
+  __syncthreads();
+  return out;
+}
+
+// The NQ block partials of this block into part[q * kT2MaxGrid + block].
+template <int NQ> __device__ void t2_put_partials(const T2& d, const double (&v)[NQ], double* sh) {
+#pragma unroll
+  for (int q = 0; q < NQ; ++q) {
+    const double s = t2_block_sum256(v[q], sh);
+    if (threadIdx.x == 0) d.part[q * kT2MaxGrid + blockIdx.x] = s;
+  }
+}
+
+// The sum of the G partials of quantity q, in the same order in every
+// block (lane l sums entries l, l + 32, ... ; then a shuffle tree).
+__device__ double t2_total(const T2& d, int q, double* sh) {
+  __shared__ double tot_s;
+  if (threadIdx.x < 32) {
+    double a = 0.0;
+    for (int i = threadIdx.x; i < (int)gridDim.x; i += 32) a += __ldcg(d.part + q * kT2MaxGrid + i);
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) a += __shfl_down_sync(0xffffffffu, a, off);
+    if (threadIdx.x == 0) tot_s = a;
+  }
+  __syncthreads();
+  const double out = tot_s;
+  __syncthreads();
+  return out;
+}
+
+__global__ void __launch_bounds__(kGridThreads) t2_pcg_grid(T2 d, int max_iter, double tol) {
+  __shared__ double sh[kGridThreads];
+  const int G = gridDim.x;
+  const int per = (d.nf + G - 1) / G;
+  const int r0 = min(d.nf, (int)blockIdx.x * per), r1 = min(d.nf, r0 + per);
+  const int t = threadIdx.x;
+  // r = b, dx = 0; |b|^2
+  double v1[1] = {0.0};
+  for (int i = 2 * r0 + t; i < 2 * r1; i += kGridThreads) {
+    const double ri = d.rhs[i];
+    d.dx[i] = 0.0;
+    d.r[i] = ri;
+    v1[0] += ri * ri;
+  }
+  t2_put_partials<1>(d, v1, sh);
+  if (!t2_grid_sync(d)) return;
+  const double b2 = t2_total(d, 0, sh);
+  const double thr = fmax(tol * tol * b2, DBL_MIN);
+  if (b2 == 0.0 || b2 < thr) {  // Eigen's test before the first iteration: no iteration
+    if (blockIdx.x == 0 && t == 0) {
+      d.scal[SC_CG_IT] = 0;
+      d.scal[SC_CG_RN2] = b2;
+      d.scal[SC_CG_B2] = b2;
+    }
+    return;
+  }
+  // (r, D^-1 r) of r_0: absNew; p_0 = D^-1 r_0 formed where it is read
+  v1[0] = 0.0;
+  for (int i = 2 * r0 + t; i < 2 * r1; i += kGridThreads) v1[0] += d.r[i] * (d.dinv[i] * d.r[i]);
+  t2_put_partials<1>(d, v1, sh);
+  if (!t2_grid_sync(d)) return;
+  double absNew = t2_total(d, 0, sh);
+  double beta = 0.0, rn2 = b2;
+  int it = 0;
+  while (it < max_iter) {
+    const double* pold = (it & 1) ? d.p : d.p2;  // p_{k-1} (unused when k = 0)
+    double* pnew = (it & 1) ? d.p2 : d.p;        // p_k
+    // q = A p_k over the block's rows, p_k of each column formed on the
+    // fly; the block's own rows' p_k stored for the next iteration and dx
+    v1[0] = 0.0;
+    for (int rr = r0 + t; rr < r1; rr += kGridThreads) {
+      double y0 = 0, y1 = 0;
+      for (int qq = d.b_ptr[rr]; qq < d.b_ptr[rr + 1]; ++qq) {
+        const double* a = d.A + 4 * size_t(qq);
+        const int c = d.b_col[qq];
+        const double rc0 = __ldcg(d.r + 2 * c), rc1 = __ldcg(d.r + 2 * c + 1);
+        double p0 = d.dinv[2 * c] * rc0, p1 = d.dinv[2 * c + 1] * rc1;
+        if (it > 0) {
+          p0 += beta * __ldcg(pold + 2 * c);
+          p1 += beta * __ldcg(pold + 2 * c + 1);
+        }
+        y0 += a[0] * p0 + a[1] * p1;
+        y1 += a[2] * p0 + a[3] * p1;
+      }
+      double pr0 = d.dinv[2 * rr] * __ldcg(d.r + 2 * rr), pr1 = d.dinv[2 * rr + 1] * __ldcg(d.r + 2 * rr + 1);
+      if (it > 0) {
+        pr0 += beta * __ldcg(pold + 2 * rr);
+        pr1 += beta * __ldcg(pold + 2 * rr + 1);
+      }
+      pnew[2 * rr] = pr0;
+      pnew[2 * rr + 1] = pr1;
+      d.q[2 * rr] = y0;
+      d.q[2 * rr + 1] = y1;
+      v1[0] += pr0 * y0 + pr1 * y1;
+    }
+    t2_put_partials<1>(d, v1, sh);
+    if (!t2_grid_sync(d)) return;
+    const double alpha = absNew / t2_total(d, 0, sh);
+    // dx += alpha p, r -= alpha q over the block's rows; |r|^2 and (r, D^-1 r)
+    double v2[2] = {0.0, 0.0};
+    for (int i = 2 * r0 + t; i < 2 * r1; i += kGridThreads) {
+      d.dx[i] += alpha * pnew[i];
+      const double ri = d.r[i] - alpha * d.q[i];
+      d.r[i] = ri;
+      v2[0] += ri * ri;
+      v2[1] += ri * (d.dinv[i] * ri);
+    }
+    t2_put_partials<2>(d, v2, sh);
+    if (!t2_grid_sync(d)) return;
+    rn2 = t2_total(d, 0, sh);
+    if (rn2 < thr) break;
+    const double absOld = absNew;
+    absNew = t2_total(d, 1, sh);
+    beta = absNew / absOld;
+    ++it;
+  }
+  if (blockIdx.x == 0 && t == 0) {
+    d.scal[SC_CG_IT] = it;
+    d.scal[SC_CG_RN2] = rn2;
+    d.scal[SC_CG_B2] = b2;
+  }
+}
+
 // MixedStretch::solve (mixed_stretch.cpp:243-259): Jdx = -vol Jloc dx,
 // lambda = -gl + Htil dSdF^T Jdx, ds = -H^-1 (Sym lambda + g).
 __global__ void __launch_bounds__(kThreads) t2_local(T2 d) {
@@ -679,6 +883,8 @@ struct mfem_tri2d {
   struct Pending { int kernel, a, b; };
   std::vector<Pending> ev_pending;
   size_t ev_used = 0;
+  // blocks of the grid PCG (t2_pcg_grid), 0: the one-block t2_pcg
+  int pcg_grid = 0;
   // configuration
   int bdf = 1, max_newton = 5, ls_iters = 20, cg_iters = 500;
   double h = 0.0333, cg_tol = 1e-4, newton_tol = 1e-10, res_tol = 0, load_norm = 0;
@@ -939,9 +1145,23 @@ int t2_step(mfem_tri2d& sc, mfem_step_stats* out) {
     st.residual = rn;
     if (sc.res_tol > 0 && ((i > 0 && rn <= sc.res_tol * st.residual0) || rn <= sc.res_tol * sc.load_norm))
       break;
-    if (sc.nf > 0)
+    if (sc.nf > 0 && sc.pcg_grid > 0) {
+      // a fresh barrier (arrivals, generation, error) for the cooperative launch
+      T2_CUDA(cudaMemsetAsync(sc.d.bar, 0, 4 * sizeof(unsigned int), sc.stream));
+      cudaError_t e = cudaSuccess;
+      launch(sc, MFEM_T2_K_PCG, [&] {
+        T2 dd = sc.d;
+        int mi = sc.cg_iters;
+        double tl = sc.cg_tol;
+        void* args[] = {&dd, &mi, &tl};
+        e = cudaLaunchCooperativeKernel((const void*)t2_pcg_grid, dim3(sc.pcg_grid), dim3(kGridThreads), args, 0,
+                                        sc.stream);
+      });
+      T2_CUDA(e);
+    } else if (sc.nf > 0) {
       launch(sc, MFEM_T2_K_PCG,
              [&] { t2_pcg<<<1, kBlock, 0, sc.stream>>>(sc.d, sc.cg_iters, sc.cg_tol); });
+    }
     launch(sc, MFEM_T2_K_LOCAL, [&] { t2_local<<<grid_of(sc.nt), kThreads, 0, sc.stream>>>(sc.d); });
     if (launch_status() != MFEM_OK) return MFEM_ERR_CUDA;
     if (t2_energy_at(sc, 0.0, 1, scal) != MFEM_OK) return MFEM_ERR_CUDA;
@@ -1229,6 +1449,8 @@ int mfem_gpu_tri2d_create(const mfem_tri2d_desc* dsc, mfem_tri2d** out) {
                o_dinv = L.take<double>(2 * size_t(std::max(nf, 1))),
                o_r = L.take<double>(2 * size_t(std::max(nf, 1))), o_p = L.take<double>(2 * size_t(std::max(nf, 1))),
                o_q = L.take<double>(2 * size_t(std::max(nf, 1))),
+               o_p2 = L.take<double>(2 * size_t(std::max(nf, 1))), o_part = L.take<double>(2 * kT2MaxGrid),
+               o_bar = L.take<unsigned int>(4),
                o_ep = L.take<double>(2 * size_t(nt) + nv), o_scal = L.take<double>(SC_COUNT),
                o_st = L.take<int>(4), o_xh = L.take<double>(2 * size_t(nv) * sc->bdf),
                o_vh = L.take<double>(2 * size_t(nv) * sc->bdf), o_xs = L.take<double>(2 * size_t(nv));
@@ -1243,6 +1465,16 @@ int mfem_gpu_tri2d_create(const mfem_tri2d_desc* dsc, mfem_tri2d** out) {
   }
   char* base = sc->dev;
   if (cudaMemsetAsync(base, 0, total, sc->stream) != cudaSuccess) return MFEM_ERR_CUDA;
+  // sheets with more free rows than the one-block PCG can carry (one row a
+  // thread) iterate over co-resident blocks of at least 64 rows each
+  if (nf > kBlock) {
+    int dev = 0, sms = 0, per_sm = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess ||
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess ||
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, t2_pcg_grid, kGridThreads, 0) != cudaSuccess)
+      return MFEM_ERR_CUDA;
+    sc->pcg_grid = std::max(1, std::min({per_sm * sms, (nf + 63) / 64, kT2MaxGrid}));
+  }
   T2& d = sc->d;
   d.nv = nv;
   d.nt = nt;
@@ -1291,6 +1523,9 @@ int mfem_gpu_tri2d_create(const mfem_tri2d_desc* dsc, mfem_tri2d** out) {
   d.r = dp(o_r);
   d.p = dp(o_p);
   d.q = dp(o_q);
+  d.p2 = dp(o_p2);
+  d.part = dp(o_part);
+  d.bar = reinterpret_cast<unsigned int*>(base + o_bar);
   d.epart = dp(o_ep);
   d.scal = dp(o_scal);
   d.status = ip(o_st);

@@ -180,3 +180,26 @@ def test_scene_json_2d_runs_on_gpu_like_the_oracle(gpu_lib, tmp_path):
     xo, xg = o.get_state()["x"], g.get_state()["x"]
     assert np.abs(xg - xo).max() < 1e-8 * _bbox(xo)
     g.close()
+
+
+@pytest.mark.gpu
+def test_large_sheet_grid_pcg_matches_oracle_and_is_reproducible(gpu_lib):
+    """A sheet with more free rows (about 1070) than the one-block PCG takes
+    (1024): the PCG runs over co-resident blocks (t2_pcg_grid, two grid
+    barriers an iteration) and still follows the oracle within 1e-8 of the
+    bounding-box diagonal, with equal Newton counts, and reruns bitwise."""
+    from mfem_gb300.tri2d import Tri2dScene
+    sp = spec2(64, 16, spacing=1.0 / 64, max_iterative_solver_iters=5000)
+    so, sg, g = _run_pair(sp, 3)
+    assert g.n_free > 1024
+    assert np.abs(sg["x"] - so["x"]).max() < 1e-8 * _bbox(so["x"])
+    assert np.abs(so["x"] - sp.V_rest).max() > 1e-4 * _bbox(so["x"])   # it moved
+    g.close()
+    out = []
+    for _ in range(2):
+        h = Tri2dScene(sp)
+        for _ in range(2):
+            h.step()
+        out.append(h.get_state()["x"])
+        h.close()
+    assert np.array_equal(out[0], out[1])
