@@ -62,6 +62,10 @@ def parse():
     ap.add_argument("--c5-duration", type=float, default=5.0,
                     help="seconds of Poisson arrivals (lambda = 20/s) in the served stream")
     ap.add_argument("--c5-steps", type=int, default=20, help="timesteps per served request")
+    ap.add_argument("--c5-lanes", type=int, default=4,
+                    help="independent serving loops (each its own batches, stream and thread)")
+    ap.add_argument("--c5-steps-per-tick", type=int, default=1,
+                    help="timesteps a serving tick may take per instance")
     ap.add_argument("--size", type=int, default=60, help="cubes per axis for c2")
     ap.add_argument("--precision", default="mixed", choices=["mixed", "fp64"])
     ap.add_argument("--solver", default="eigen-pcg-diag",
@@ -467,6 +471,7 @@ def run_ours(args):
     sampler = ClockSampler(local)
     sampler.start()
     ms, stats = [], []
+    k_before = gpu.kernel_stats(batch_h)
     t0 = time.perf_counter()
     for _ in range(args.steps):
         st = scene.step()
@@ -474,6 +479,10 @@ def run_ours(args):
         stats.append(st.as_dict())
     wall = time.perf_counter() - t0
     clocks = sampler.stop()
+    k_after = gpu.kernel_stats(batch_h)
+    # the library's launches in the timed region, by kernel (counted on the
+    # host; the device-driven PCG loop's launches as its bodies report them)
+    timed_launches = {k: int(k_after[k][1] - k_before[k][1]) for k in k_after if k_after[k][1] > k_before[k][1]}
     dev_s = sum(ms) / 1000.0
     dev_s_max = allmax(pg, dev_s)
     value = ws * args.steps / dev_s_max
@@ -542,7 +551,7 @@ def run_ours(args):
             per_kernel[k] = {"ms": round(kms, 3), "launches": kn,
                              "share": round(kms / max(prof_s * 1e3, 1e-9), 4),
                              "GBps": round(b / (kms / kn / 1e3) / 1e9, 1) if (b and kms > 0) else None}
-    launches = int(sum(n for (_, n) in kstats.values()))
+    launches = int(sum(timed_launches.values()))
 
     newton = float(np.mean([s["newton_iterations"] for s in stats]))
     cgits = float(np.mean([s["cg_iterations"] for s in stats]))
@@ -566,6 +575,7 @@ def run_ours(args):
         "newton_iterations_per_step": newton, "cg_iterations_per_step": cgits,
         "residual_rel_last": stats[-1]["residual"] / max(stats[-1]["residual0"], 1e-300),
         "clocks": clocks, "e2e": e2e, "roofline": roof, "gpu_launches": launches,
+        "gpu_launches_by_kernel": timed_launches,
         "profiled_replay_ms_per_step": 1000.0 * prof_s / args.steps,
         "kernels": per_kernel,
         "pcg_shape": pcg_shape,
@@ -736,7 +746,7 @@ def run_served(args):
         sp.pcg_kernel = kern
     # N GPUs: the requests are dealt out by work (tets x timesteps), no exchange
     mine = server.shard([sp.n_tets * n for _, sp, n in stream], ws, rank)
-    srv = server.Server(budget_bytes=150e9)
+    srv = server.Server(budget_bytes=150e9, lanes=args.c5_lanes, steps_per_tick=args.c5_steps_per_tick)
     for i in mine:
         t, sp, n = stream[i]
         srv.submit(sp, n, arrival=t)
@@ -769,7 +779,8 @@ def run_served(args):
             "data": "synthetic",
             "config": {"workload": f"served_stream_c5_{args.c5_duration:g}s_{args.c5_steps}steps",
                        "arrival_rate_per_s": 20.0, "tets_range": [1e3, 5e5],
-                       "budget_bytes": 150e9, "pcg_kernel": args.pcg_kernel},
+                       "budget_bytes": 150e9, "pcg_kernel": args.pcg_kernel,
+                       "lanes": args.c5_lanes, "steps_per_tick": args.c5_steps_per_tick},
             "served": summ,
             "plain": {"value": plain, "unit": UNIT, "wall_value": plain_n / plain_wall,
                       "sample": f"all timesteps of the first {len(sample)} requests, one scene at a time "
@@ -915,7 +926,9 @@ def run_tri2d(args):
                 "algorithmic_bytes_per_launch": abytes, "avg_launch_us": 1e3 * dom_ms / dom_n,
                 "peak_source": f"{peak_src} (MEASURED_PEAKS.json hbm_gbs)",
                 "note": (f"{cg_per_launch:.1f} PCG iterations per launch; the sheet's system "
-                         "sits in L2, one thread block runs the solve")
+                         "sits in L2; " + ("one thread block runs the solve" if sc.n_free <= 1024 else
+                                            "co-resident blocks with grid barriers run the solve "
+                                            "(t2_pcg_grid)"))
                         if dom == "t2_pcg" else None}
     sc.close()
     newton = float(np.mean([t["newton_iterations"] for t in stats]))

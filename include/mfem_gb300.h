@@ -264,7 +264,8 @@ enum {
   MFEM_K_CG_UPDATE = 4, MFEM_K_LOCAL_SOLVE = 5, MFEM_K_LS_ENERGY = 6, MFEM_K_APPLY = 7,
   MFEM_K_STEP_BEGIN = 8, MFEM_K_STEP_END = 9, MFEM_K_SCALARS = 10, MFEM_K_CG_SOLVE = 11,
   MFEM_K_CGF_ITER = 12, MFEM_K_CG_REPLACE = 13, MFEM_K_MR_INIT = 14, MFEM_K_MR_ELEM = 15,
-  MFEM_K_MR_VERT = 16, MFEM_K_MR_UPDATE = 17, MFEM_K_MR_EXPORT = 18, MFEM_K_COUNT = 19
+  MFEM_K_MR_VERT = 16, MFEM_K_MR_UPDATE = 17, MFEM_K_MR_EXPORT = 18, MFEM_K_CG_LOOP = 19,
+  MFEM_K_COUNT = 20
 };
 int mfem_gpu_scene_solo_batch(mfem_scene* scene, mfem_batch** batch);
 int mfem_gpu_batch_set_profiling(mfem_batch* batch, int enable);

@@ -512,6 +512,16 @@ struct mfem_batch {
   BatchCounters* h_ctr = nullptr;   // pinned
   BatchCounters* h_ctr_pipe = nullptr;  // pinned, 2 slots: PCG chunk checks in flight
   cudaGraphExec_t cg_graph = nullptr;   // one chunk of PCG iterations, captured once
+  // the whole PCG loop as one graph: a WHILE node around a chunk of
+  // iterations and the loop's condition kernel (the device decides when
+  // the solve has ended; no host round trip per chunk); cg_loop_len
+  // iterations a body; loop_pending: a solve whose bodies the host has not
+  // yet counted (read with the next counter sync)
+  cudaGraphExec_t cg_loop = nullptr;
+  bool cg_loop_on = true;
+  bool loop_pending = false;
+  int cg_loop_len = 8;
+  bool loop_fused = true;
   cudaEvent_t ev_pipe[2] = {nullptr, nullptr};
   SceneScalars* h_sc = nullptr;     // pinned, one per scene
   int max_newton = 0, max_ls = 0, max_cg = 0;
@@ -786,6 +796,19 @@ int sync_counters(mfem_batch* b) {
   CUDA_OR(cudaMemcpyAsync(b->h_ctr, b->d_ctr, sizeof(BatchCounters), cudaMemcpyDeviceToHost, b->stream),
           MFEM_ERR_CUDA);
   CUDA_OR(cudaStreamSynchronize(b->stream), MFEM_ERR_CUDA);
+  if (b->loop_pending) {
+    // a device-driven PCG loop has finished: its launches into the counts
+    const int64_t bodies = b->h_ctr->cg_bodies;
+    b->k_launches[MFEM_K_CG_LOOP] += 1 + bodies;  // k_cg_enter and one k_cg_continue a body
+    if (b->loop_fused) {
+      b->k_launches[MFEM_K_CGF_ITER] += bodies * b->cg_loop_len;
+    } else {
+      b->k_launches[MFEM_K_CG_SPMV] += bodies * b->cg_loop_len;
+      b->k_launches[MFEM_K_CG_UPDATE] += bodies * b->cg_loop_len;
+      if (!b->fp64) b->k_launches[MFEM_K_CG_REPLACE] += bodies;
+    }
+    b->loop_pending = false;
+  }
   return MFEM_OK;
 }
 
@@ -884,8 +907,86 @@ int capture_cg_graph(mfem_batch* b, const Launch& Lcg, bool fused, cudaGraphExec
   return MFEM_OK;
 }
 
+// The whole PCG loop of a batch as one CUDA graph: k_cg_enter sets the
+// condition of a WHILE node whose body is one chunk of iterations (as
+// capture_cg_graph) followed by k_cg_continue, which sets it again from the
+// batch's counters.  A solve ends within one chunk of its last iteration,
+// with no host round trip.
+int capture_cg_loop(mfem_batch* b, const Launch& Lcg, bool fused, cudaGraphExec_t* out) {
+  const int len = fused ? 8 : kCgReplace;
+  const int max_launch = b->max_cg + (fused && !b->fp64 ? 9 : 0);
+  const int max_bodies = (max_launch + len - 1) / len + 1;
+  cudaGraph_t g = nullptr;
+  CUDA_OR(cudaGraphCreate(&g, 0), MFEM_ERR_CUDA);
+  auto fail = [&](cudaError_t e) {
+    cudaGraphDestroy(g);
+    set_error("PCG loop graph", e);
+    return MFEM_ERR_CUDA;
+  };
+  cudaGraphConditionalHandle h;
+  cudaError_t e = cudaGraphConditionalHandleCreate(&h, g, 0u, cudaGraphCondAssignDefault);
+  if (e != cudaSuccess) return fail(e);
+  // the loop is entered only if a scene's solve is active (a Newton pass
+  // that met the residual test at assembly runs no body)
+  if ((e = cudaStreamBeginCaptureToGraph(b->stream, g, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal)) !=
+      cudaSuccess)
+    return fail(e);
+  launch_cg_enter(Lcg, h);
+  {
+    cudaGraph_t cap = g;
+    if ((e = cudaStreamEndCapture(b->stream, &cap)) != cudaSuccess) return fail(e);
+  }
+  cudaGraphNode_t enter = nullptr;
+  size_t nn = 1;
+  if ((e = cudaGraphGetNodes(g, &enter, &nn)) != cudaSuccess || nn != 1) return fail(e);
+  cudaGraphNodeParams np = {};
+  np.type = cudaGraphNodeTypeConditional;
+  np.conditional.handle = h;
+  np.conditional.type = cudaGraphCondTypeWhile;
+  np.conditional.size = 1;
+  cudaGraphNode_t node = nullptr;
+  if ((e = cudaGraphAddNode(&node, g, &enter, nullptr, 1, &np)) != cudaSuccess) return fail(e);
+  cudaGraph_t body = np.conditional.phGraph_out[0];
+  if ((e = cudaStreamBeginCaptureToGraph(b->stream, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal)) !=
+      cudaSuccess)
+    return fail(e);
+  for (int k = 0; k < len; ++k) {
+    if (fused) {
+      launch_cgf_iter(Lcg, b->cgf_shape);
+    } else {
+      launch_cg_spmv(Lcg);
+      launch_cg_update(Lcg);
+      if (!b->fp64 && k + 1 == kCgReplace) launch_cg_replace(Lcg);
+    }
+  }
+  launch_cg_continue(Lcg, h, max_bodies);
+  cudaGraph_t cap = body;
+  e = cudaStreamEndCapture(b->stream, &cap);
+  if (e != cudaSuccess) return fail(e);
+  e = cudaGraphInstantiate(out, g, 0);
+  cudaGraphDestroy(g);
+  CUDA_OR(e, MFEM_ERR_CUDA);
+  b->cg_loop_len = len;
+  b->loop_fused = fused;
+  return MFEM_OK;
+}
+
 int run_pcg_graph(mfem_batch* b, const Launch& Lcg, bool fused) {
   const int len = fused ? 8 : kCgReplace;
+  if (b->cg_loop_on && !b->cg_loop) {
+    if (capture_cg_loop(b, Lcg, fused, &b->cg_loop) != MFEM_OK) {
+      // conditional nodes unavailable: chunks with host checks instead
+      cudaGetLastError();
+      b->cg_loop = nullptr;
+      b->cg_loop_on = false;
+    }
+  }
+  if (b->cg_loop) {
+    CUDA_OR(cudaMemsetAsync(&b->d_ctr->cg_bodies, 0, sizeof(int), b->stream), MFEM_ERR_CUDA);
+    CUDA_OR(cudaGraphLaunch(b->cg_loop, b->stream), MFEM_ERR_CUDA);
+    b->loop_pending = true;
+    return MFEM_OK;
+  }
   if (!b->cg_graph) {
     const int rc = capture_cg_graph(b, Lcg, fused, &b->cg_graph);
     if (rc) return rc;
@@ -1778,6 +1879,9 @@ int batch_build(mfem_scene* const* scenes, int n, mfem_batch** out) {
   // the batch's size class
   b->cgf_shape = b->fp64 ? CgfShape{0, 0, 1, 0} : CgfShape{2, 0, 1, 1};
   b->pcg_kernel = scenes[0]->cfg.pcg_kernel;
+  // MFEM_GB300_CG_LOOP=0: the PCG loop as chunks with host checks instead
+  // of the device-driven WHILE graph
+  if (const char* e = std::getenv("MFEM_GB300_CG_LOOP")) b->cg_loop_on = std::atoi(e) != 0;
   b->minres = scenes[0]->dev.minres;
   b->fem = scenes[0]->dev.fem;
   b->jacobi = 1;
@@ -1862,6 +1966,7 @@ void batch_free(mfem_batch* b) {
   if (b->h_ctr) cudaFreeHost(b->h_ctr);
   if (b->h_ctr_pipe) cudaFreeHost(b->h_ctr_pipe);
   if (b->cg_graph) cudaGraphExecDestroy(b->cg_graph);
+  if (b->cg_loop) cudaGraphExecDestroy(b->cg_loop);
   for (int k = 0; k < 2; ++k)
     if (b->ev_pipe[k]) cudaEventDestroy(b->ev_pipe[k]);
   if (b->h_sc) cudaFreeHost(b->h_sc);
@@ -2460,7 +2565,10 @@ int mfem_gpu_scene_rollback(mfem_scene* s) {
   state_sizes(s, &bx, &bslot, &bs, &bq);
   const size_t I = s->cfg.bdf_order;
   cudaStream_t st = s->solo->stream;
-  CUDA_OR(cudaDeviceSynchronize(), MFEM_ERR_CUDA);
+  // the scene's batches return only when their streams are idle; the copies
+  // go on the scene's own stream (no device-wide wait: another thread may be
+  // capturing a graph on its batch's stream meanwhile)
+  CUDA_OR(cudaStreamSynchronize(st), MFEM_ERR_CUDA);
   const char* d = s->ckpt;
   CUDA_OR(cudaMemcpyAsync(s->dev.x, d, bx, cudaMemcpyDeviceToDevice, st), MFEM_ERR_CUDA);
   d += bx;
@@ -2585,13 +2693,16 @@ int mfem_gpu_batch_set_pcg_shape(mfem_batch* b, int32_t stages, int32_t keep, in
       b->cgf_shape.pdl == sh.pdl)
     return MFEM_OK;
   b->cgf_shape = sh;
-  if (b->cg_graph || b->tick_graph) {  // captured with the old shape
+  if (b->cg_graph || b->cg_loop || b->tick_graph || b->tick_graph_c) {  // captured with the old shape
     CUDA_OR(cudaStreamSynchronize(b->stream), MFEM_ERR_CUDA);
     if (b->cg_graph) cudaGraphExecDestroy(b->cg_graph);
+    if (b->cg_loop) cudaGraphExecDestroy(b->cg_loop);
     if (b->tick_graph) cudaGraphExecDestroy(b->tick_graph);
-  if (b->tick_graph_c) cudaGraphExecDestroy(b->tick_graph_c);
+    if (b->tick_graph_c) cudaGraphExecDestroy(b->tick_graph_c);
     b->cg_graph = nullptr;
+    b->cg_loop = nullptr;
     b->tick_graph = nullptr;
+    b->tick_graph_c = nullptr;
   }
   return MFEM_OK;
 }
@@ -2640,7 +2751,7 @@ int mfem_gpu_kernel_name(int kernel, char* name, int name_len) {
       "k_elem_update", "k_assemble", "k_cg_init", "k_cg_spmv", "k_cg_update", "k_local_solve",
       "k_ls_energy", "k_apply", "k_step_begin", "k_step_end", "k_scalars_begin",
       "k_cg_solve", "k_cgf_iter", "k_cg_replace", "k_mr_init", "k_mr_elem", "k_mr_vert",
-      "k_mr_update", "k_mr_export"};
+      "k_mr_update", "k_mr_export", "k_cg_loop"};
   if (kernel < 0 || kernel >= MFEM_K_COUNT || !name || name_len <= 0) return MFEM_ERR_INVALID;
   strncpy(name, names[kernel], name_len - 1);
   name[name_len - 1] = 0;

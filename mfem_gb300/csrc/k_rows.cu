@@ -1631,6 +1631,25 @@ void launch_cg_replace(const Launch& L) {
     }                                                                                        \
   } while (0)
 
+__global__ void k_cg_continue(BatchCounters* ctrs, cudaGraphConditionalHandle h, int max_bodies) {
+  const int n = ++ctrs->cg_bodies;
+  const bool more = *(volatile int*)&ctrs->cg_active > 0 && *(volatile int*)&ctrs->error == 0 && n < max_bodies;
+  cudaGraphSetConditional(h, more ? 1u : 0u);
+}
+
+void launch_cg_continue(const Launch& L, cudaGraphConditionalHandle h, int max_bodies) {
+  k_cg_continue<<<1, 1, 0, L.stream>>>(L.counters, h, max_bodies);
+}
+
+__global__ void k_cg_enter(BatchCounters* ctrs, cudaGraphConditionalHandle h) {
+  const bool go = *(volatile int*)&ctrs->cg_active > 0 && *(volatile int*)&ctrs->error == 0;
+  cudaGraphSetConditional(h, go ? 1u : 0u);
+}
+
+void launch_cg_enter(const Launch& L, cudaGraphConditionalHandle h) {
+  k_cg_enter<<<1, 1, 0, L.stream>>>(L.counters, h);
+}
+
 void launch_cgf_init(const Launch& L) { MFEM_LAUNCH_CGF(k_cgf_init); }
 void launch_cgf_scale(const Launch& L) {
   if (L.ntiles == 0 || L.fp64) return;

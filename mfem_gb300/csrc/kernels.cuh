@@ -125,7 +125,8 @@ struct BatchCounters {
   int error;                // a bounded wait of the persistent PCG ran out
   unsigned int bar_count;   // grid barrier of the persistent PCG: arrivals
   unsigned int bar_gen;     //   and generation
-  int pad[2];
+  int cg_bodies;            // bodies of the device-driven PCG loop run in this solve
+  int pad;
 };
 
 // One scene as the kernels see it (pointers into the scene's arena).
@@ -308,6 +309,14 @@ void launch_cgf_init(const Launch& L);
 // Mixed path, before launch_cgf_init: the power-of-two scale of b.
 void launch_cgf_scale(const Launch& L);
 void launch_cgf_iter(const Launch& L, const CgfShape& sh);
+// The condition of the device-driven PCG loop (a WHILE node of a CUDA
+// graph whose body is a chunk of iterations): another body while a scene of
+// the batch is still iterating, no wait has run out and fewer than
+// max_bodies bodies have run (counted in ctrs->cg_bodies).
+void launch_cg_continue(const Launch& L, cudaGraphConditionalHandle h, int max_bodies);
+// The loop's entry: its condition from the batch's counters, before the
+// first body.
+void launch_cg_enter(const Launch& L, cudaGraphConditionalHandle h);
 int cg_solve_blocks_per_sm(int fp64);
 // Two-block cooperative launch whose grid barrier has a missing arrival.
 cudaError_t launch_barrier_selftest(BatchCounters* ctrs, cudaStream_t st);

@@ -158,7 +158,7 @@ class Scene:
 KERNELS = ["k_elem_update", "k_assemble", "k_cg_init", "k_cg_spmv", "k_cg_update",
            "k_local_solve", "k_ls_energy", "k_apply", "k_step_begin", "k_step_end",
            "k_scalars_begin", "k_cg_solve", "k_cgf_iter", "k_cg_replace", "k_mr_init", "k_mr_elem",
-           "k_mr_vert", "k_mr_update", "k_mr_export"]
+           "k_mr_vert", "k_mr_update", "k_mr_export", "k_cg_loop"]
 
 
 def set_profiling(batch_handle, enable=True):

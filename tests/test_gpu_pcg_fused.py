@@ -116,3 +116,38 @@ def test_fused_mixed_power_of_two_scaling_is_exact(gpu_lib, p):
     dx1, it1, _ = sc.pcg(rhs * 2.0 ** p)
     assert it1 == it0 and np.array_equal(dx1, dx0 * 2.0 ** p)
     sc.close()
+
+
+@pytest.mark.parametrize("kern", [abi.PCG_KERNEL_FUSED, abi.PCG_KERNEL_SPLIT])
+@pytest.mark.parametrize("prec", [abi.PRECISION_MIXED, abi.PRECISION_FP64])
+def test_device_driven_pcg_loop_equals_host_checked(gpu_lib, monkeypatch, kern, prec):
+    """The PCG loop as one graph (a WHILE node whose condition the device
+    sets after each chunk of iterations) takes the same steps, bitwise, as
+    the chunks the host checks one behind, and launches at most one chunk
+    beyond the iterations of each solve."""
+    sp = configs.cube_c2(n=14, precision=prec, pcg_kernel=kern)
+    monkeypatch.setenv("MFEM_GB300_CG_LOOP", "0")
+    host = gpu.Scene(sp)
+    monkeypatch.delenv("MFEM_GB300_CG_LOOP")
+    dev = gpu.Scene(sp)
+    name = "k_cgf_iter" if kern == abi.PCG_KERNEL_FUSED else "k_cg_spmv"
+    chunk = 8 if kern == abi.PCG_KERNEL_FUSED else 25
+    l0 = gpu.kernel_stats(dev.solo_batch_handle())[name][1]
+    cg = solves = 0
+    for _ in range(3):
+        a, b = host.step(), dev.step()
+        assert (a.status, a.newton_iterations, a.cg_iterations) == (b.status, b.newton_iterations, b.cg_iterations)
+        cg += b.cg_iterations
+        solves += b.newton_iterations
+    assert np.array_equal(host.positions(), dev.positions())
+    launched = gpu.kernel_stats(dev.solo_batch_handle())[name][1] - l0
+    # per solve: the iteration that meets the tolerance (not counted, as in
+    # Eigen), the rest of its chunk, and in the mixed fused form up to 9
+    # launches of its verified stop; a Newton pass whose residual test is
+    # met at assembly enters no chunk
+    extra = 9 if (kern == abi.PCG_KERNEL_FUSED and prec == abi.PRECISION_MIXED) else 0
+    assert cg <= launched <= cg + solves * (chunk + 1 + extra), (launched, cg, solves)
+    loop = gpu.kernel_stats(dev.solo_batch_handle())["k_cg_loop"][1]
+    assert loop > 0 and gpu.kernel_stats(host.solo_batch_handle())["k_cg_loop"][1] == 0
+    host.close()
+    dev.close()

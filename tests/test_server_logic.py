@@ -215,3 +215,34 @@ def test_multi_step_ticks_roll_back_the_whole_tick(monkeypatch):
     assert stiff.escalated_at is None and stiff.steps_done == 10 and stiff.result["x"][0, 0] == 10
     assert len(soft.step_ms) == 9 and len(stiff.step_ms) == 10
     assert not fake.live
+
+
+def test_lanes_serve_every_request_in_its_own_loop(monkeypatch):
+    """lanes > 1: requests dealt out by work to independent loops (own
+    batches, own thread, budget / lanes each); every request still takes
+    exactly its timesteps, escalation still works, nothing leaks."""
+    fake = _FakeGpu()
+    monkeypatch.setattr(server, "gpu", fake)
+    srv = server.Server(budget_bytes=200, lanes=2)
+    reqs = [("a", 40, 3, None), ("b", 30, 5, None), ("c", 20, 2, 1), ("d", 40, 4, None), ("e", 10, 6, None)]
+    for name, nb, n, fail in reqs:
+        srv.submit(_spec(name, nb, ls_fail_at=fail), n)
+    out = srv.run(realtime=False)
+    for r, (_, _, n, fail) in zip(out, reqs):
+        assert r.steps_done == n and r.result["x"][0, 0] == n
+        assert (r.escalated_at is not None) == (fail is not None)
+    assert not fake.live
+    # the greedy deal by footprint x timesteps: a(120) b(150) c(40) d(160) e(60)
+    # -> lane 0 a, c, e; lane 1 b, d; no batch mixes the two lanes' requests
+    lanes = [{"a", "c", "e"}, {"b", "d"}]
+    for _, b in fake.batches:
+        assert any(set(b) <= lane for lane in lanes), b
+    assert len(srv.ticks) > 0
+    try:
+        server.Server(budget_bytes=100, lanes=4).submit(_spec("big", 30), 1)
+        srv2 = server.Server(budget_bytes=100, lanes=4)
+        srv2.submit(_spec("big", 30), 1)
+        srv2.run(realtime=False)
+    except ValueError:
+        return
+    raise AssertionError("a request over a lane's budget was accepted")
