@@ -62,9 +62,9 @@ def parse():
     ap.add_argument("--c5-duration", type=float, default=5.0,
                     help="seconds of Poisson arrivals (lambda = 20/s) in the served stream")
     ap.add_argument("--c5-steps", type=int, default=20, help="timesteps per served request")
-    ap.add_argument("--c5-lanes", type=int, default=4,
+    ap.add_argument("--c5-lanes", type=int, default=8,
                     help="independent serving loops (each its own batches, stream and thread)")
-    ap.add_argument("--c5-steps-per-tick", type=int, default=1,
+    ap.add_argument("--c5-steps-per-tick", type=int, default=4,
                     help="timesteps a serving tick may take per instance")
     ap.add_argument("--size", type=int, default=60, help="cubes per axis for c2")
     ap.add_argument("--precision", default="mixed", choices=["mixed", "fp64"])
@@ -574,6 +574,11 @@ def run_ours(args):
         "wall_ms_per_step": 1000.0 * wall / args.steps,
         "newton_iterations_per_step": newton, "cg_iterations_per_step": cgits,
         "residual_rel_last": stats[-1]["residual"] / max(stats[-1]["residual0"], 1e-300),
+        # the last linear solve of each timed step against its tolerance (a
+        # solver that stops on its iteration limit shows here)
+        "linear_solve_rel_residual": [float(st["cg_error"]) for st in stats],
+        "linear_solve_converged_steps": int(sum(1 for st in stats
+                                                if st["cg_error"] <= spec.iterative_solver_tolerance)),
         "clocks": clocks, "e2e": e2e, "roofline": roof, "gpu_launches": launches,
         "gpu_launches_by_kernel": timed_launches,
         "profiled_replay_ms_per_step": 1000.0 * prof_s / args.steps,

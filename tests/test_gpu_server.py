@@ -59,3 +59,28 @@ def test_soft_scene_escalates_to_fp64_and_stays_finite(gpu_lib):
     assert r.steps_done == 20 and r.status in (abi.OK, abi.ERR_CG_MAXITER)
     x = r.result["x"]
     assert np.isfinite(x).all() and x[:, 1].min() > -0.3
+
+
+@pytest.mark.gpu
+def test_served_in_lanes_with_multi_step_ticks_equals_alone(gpu_lib):
+    """Two lanes (independent loops, batches and streams in two threads) and
+    ticks of up to three timesteps per instance: every result is still the
+    request served alone, bitwise."""
+    from mfem_gb300 import gpu, server
+    reqs = [((5, 3, 2), 2e5, 0, 4), ((3, 4, 4), 4e5, 1, 5), ((7, 2, 3), 1e5, 2, 3),
+            ((4, 4, 4), 3e5, 0, 6), ((6, 3, 3), 2.5e5, 1, 2)]
+    specs = [_spec(d, E, ax, abi.PRECISION_MIXED) for d, E, ax, _ in reqs]
+    alone = []
+    for sp, (_, _, _, n) in zip(specs, reqs):
+        s = gpu.Scene(sp)
+        for _ in range(n):
+            s.step()
+        alone.append(s.get_state()["x"])
+        s.close()
+    srv = server.Server(budget_bytes=int(1e9), lanes=2, steps_per_tick=3)
+    for sp, (_, _, _, n) in zip(specs, reqs):
+        srv.submit(sp, n, arrival=0.0)
+    out = srv.run(realtime=False)
+    for r, ref, (_, _, _, n) in zip(out, alone, reqs):
+        assert r.steps_done == n and len(r.step_ms) == n
+        assert np.array_equal(r.result["x"], ref)
