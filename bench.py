@@ -67,7 +67,8 @@ def parse():
     ap.add_argument("--c5-steps-per-tick", type=int, default=4,
                     help="timesteps a serving tick may take per instance")
     ap.add_argument("--size", type=int, default=60, help="cubes per axis for c2")
-    ap.add_argument("--precision", default="mixed", choices=["mixed", "fp64"])
+    ap.add_argument("--precision", default=None, choices=["mixed", "fp64"],
+                    help="default: fp64 for c1 (the beam is stated FP64 throughout), mixed otherwise")
     ap.add_argument("--solver", default="eigen-pcg-diag",
                     choices=["eigen-pcg-diag", "gpu-pcg-block", "minres-indefinite-block"])
     ap.add_argument("--formulation", default="mixed-stretch", choices=["mixed-stretch", "stretch"],
@@ -96,7 +97,10 @@ def parse():
     ap.add_argument("--cpu-threads", type=int, default=0)
     ap.add_argument("--pcg-kernel", default="auto", choices=["persistent", "split", "fused", "auto"],
                     help="auto: the batch picks fused or split by its PCG tile count")
-    return ap.parse_args()
+    args = ap.parse_args()
+    if args.precision is None:
+        args.precision = "fp64" if args.config == "c1" else "mixed"
+    return args
 
 
 # ----------------------------------------------------------------- ranks --
@@ -512,6 +516,10 @@ def run_ours(args):
                "newton_iterations_per_step": float(np.mean([t.newton_iterations for t in e2e_stats])),
                "cg_iterations_per_step": float(np.mean([t.cg_iterations for t in e2e_stats])),
                "host_buffers": "pinned (cudaHostAlloc through torch.pin_memory)"}
+        if spec.bc_type not in (abi.BC_NULL, abi.BC_HANG, abi.BC_HANGENDS) and len(pins):
+            e2e["note"] = ("the caller drives the pins: each step uploads their starting positions, which "
+                           "replaces the scripted boundary motion the timed value follows, so the two "
+                           "figures step different problems")
 
     # ---- per-kernel CUDA events: a replay of the same steps from the same
     # state with an event pair around every launch (the events slow the
