@@ -29,8 +29,9 @@
 //               fixed-order tree in shared memory, __syncthreads between the
 //               phases, no grid-wide waits; one launch per solve.  Sheets
 //               with more free rows than the block has threads run
-//               t2_pcg_grid instead: the same iteration over co-resident
-//               blocks with bounded grid barriers, also one launch per solve
+//               t2_pcg_grid instead: the single-reduction form of the same
+//               iteration over co-resident blocks, one bounded grid barrier
+//               an iteration, also one launch per solve
 //   t2_local    one thread per triangle: lambda and ds
 //   t2_energy   one thread per triangle and vertex: the three energy parts
 //   t2_esum     one block: the fixed-order sums (and max|dx|, max|ds|)
@@ -109,8 +110,8 @@ struct T2 {
   double* r;     // PCG vectors, 2 nf
   double* p;
   double* q;
-  double* p2;     // the grid PCG's second direction buffer (p of iteration k in p or p2 by parity)
-  double* part;   // the grid PCG's block partials: 2 x kT2MaxGrid
+  double* sr;     // the grid PCG's r, w, s by iteration parity: 6 x 2 nf (r0 r1 w0 w1 s0 s1)
+  double* part;   // the grid PCG's block partials: 3 x kT2MaxGrid
   unsigned int* bar;  // the grid PCG's barrier: arrivals, generation, error flag
   double* epart;  // 2 nt + nv energy parts
   double* scal;   // SC_COUNT device scalars
@@ -521,19 +522,24 @@ __global__ void __launch_bounds__(kBlock) t2_pcg(T2 d, int max_iter, double tol)
 }
 
 // ----------------------------------------------------- grid PCG ---
-// The same Jacobi-PCG iteration over many blocks for sheets too large for
-// one (the FP64 work of a 10^4-triangle sheet on one SM at GB300's FP64
-// rate sets ~40 us per iteration).  One cooperative launch of G blocks of
-// kGridThreads, each owning a contiguous range of free rows; a reduction is
-// each block's fixed-order partial, a bounded grid barrier, and the G
-// partials summed in the same fixed order by every block (so every block
-// takes the same branches).  Two barriers per iteration: the direction
-// p_k = D^-1 r_k + beta_k p_{k-1} of a neighbouring row is formed where the
-// product gathers it (the same expression the row's owner evaluates), so
-// no barrier is needed between the update of p and the next product; p_k
-// alternates between p and p2.  Every wait is bounded (kT2BarrierNs or
-// kT2BarrierPolls): when one runs out the kernel flags MFEM_ERR_TIMEOUT in
-// the scene's status and every block leaves at its next barrier.
+// The Jacobi-PCG over many blocks for sheets too large for one (the FP64
+// work of a 10^4-triangle sheet on one SM at GB300's FP64 rate sets ~40 us
+// per iteration).  One cooperative launch of G blocks of kGridThreads, each
+// owning a contiguous range of free rows; a reduction is each block's
+// fixed-order partial, a bounded grid barrier, and the G partials summed in
+// the same fixed order by every block (so every block takes the same
+// branches).  The iteration is the single-reduction form of the same PCG
+// (Chronopoulos & Gear 1989; equal to Eigen's iteration in exact
+// arithmetic): with u = D^-1 r, w = A u, s = A p, each iteration needs one
+// reduction of (r, u), (w, u) and |r|^2 -- one grid barrier.  A
+// neighbouring row's u_{k+1} = D^-1 (r_k - a_k (w_k + b_k s_{k-1})) is
+// formed where the product gathers it, with the expression its owner
+// evaluates (t2_next), so r, w, s alternate between two buffers by the
+// iteration's parity and no barrier separates the updates from the product.
+// Eigen's stop: |r|^2 < max(tol^2 |b|^2, DBL_MIN), the iteration that meets
+// it not counted.  Every wait is bounded (kT2BarrierNs or kT2BarrierPolls):
+// when one runs out the kernel flags MFEM_ERR_TIMEOUT in the scene's status
+// and every block leaves at its next barrier.
 constexpr int kGridThreads = 256;
 constexpr int kT2MaxGrid = 1024;
 constexpr unsigned long long kT2BarrierNs = 2000000000ull;
@@ -585,44 +591,61 @@ __device__ bool t2_grid_sync(const T2& d) {
   return ok_s != 0;
 }
 
-// Fixed-order tree sum over the block (kGridThreads values).
-__device__ double t2_block_sum256(double v, double* sh) {
-  const int t = threadIdx.x;
-  sh[t] = v;
-  __syncthreads();
-  for (int w = kGridThreads / 2; w > 0; w >>= 1) {
-    if (t < w) sh[t] += sh[t + w];
-    __syncthreads();
-  }
-  const double out = sh[0];
-  __syncthreads();
-  return out;
-}
-
-// The NQ block partials of this block into part[q * kT2MaxGrid + block].
+// The NQ block partials of this block into part[q * kT2MaxGrid + block]:
+// a shuffle tree in each warp, then warp 0 combines the warps' sums, in a
+// fixed order (one barrier).
 template <int NQ> __device__ void t2_put_partials(const T2& d, const double (&v)[NQ], double* sh) {
+  constexpr int kWarps = kGridThreads / 32;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  double x[NQ];
 #pragma unroll
   for (int q = 0; q < NQ; ++q) {
-    const double s = t2_block_sum256(v[q], sh);
-    if (threadIdx.x == 0) d.part[q * kT2MaxGrid + blockIdx.x] = s;
+    x[q] = v[q];
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) x[q] += __shfl_down_sync(0xffffffffu, x[q], off);
   }
+  if (lane == 0)
+#pragma unroll
+    for (int q = 0; q < NQ; ++q) sh[q * kWarps + warp] = x[q];
+  __syncthreads();
+  if (warp == 0) {
+#pragma unroll
+    for (int q = 0; q < NQ; ++q) {
+      double y = lane < kWarps ? sh[q * kWarps + lane] : 0.0;
+#pragma unroll
+      for (int off = 16; off > 0; off >>= 1) y += __shfl_down_sync(0xffffffffu, y, off);
+      if (lane == 0) d.part[q * kT2MaxGrid + blockIdx.x] = y;
+    }
+  }
+  __syncthreads();  // sh is free again
 }
 
-// The sum of the G partials of quantity q, in the same order in every
-// block (lane l sums entries l, l + 32, ... ; then a shuffle tree).
-__device__ double t2_total(const T2& d, int q, double* sh) {
-  __shared__ double tot_s;
+// The sums of the G partials of quantities 0..NQ-1, in the same order in
+// every block (lane l sums entries l, l + 32, ... ; then a shuffle tree).
+template <int NQ> __device__ void t2_totals(const T2& d, double (&out)[NQ], double* sh) {
   if (threadIdx.x < 32) {
-    double a = 0.0;
-    for (int i = threadIdx.x; i < (int)gridDim.x; i += 32) a += __ldcg(d.part + q * kT2MaxGrid + i);
 #pragma unroll
-    for (int off = 16; off > 0; off >>= 1) a += __shfl_down_sync(0xffffffffu, a, off);
-    if (threadIdx.x == 0) tot_s = a;
+    for (int q = 0; q < NQ; ++q) {
+      double a = 0.0;
+      for (int i = threadIdx.x; i < (int)gridDim.x; i += 32) a += __ldcg(d.part + q * kT2MaxGrid + i);
+#pragma unroll
+      for (int off = 16; off > 0; off >>= 1) a += __shfl_down_sync(0xffffffffu, a, off);
+      if (threadIdx.x == 0) sh[q] = a;
+    }
   }
   __syncthreads();
-  const double out = tot_s;
+#pragma unroll
+  for (int q = 0; q < NQ; ++q) out[q] = sh[q];
   __syncthreads();
-  return out;
+}
+
+// s_k, r_{k+1} and u_{k+1} of one dof from r_k, w_k, s_{k-1} (wherever a
+// row's values are formed: the same operations in the same order).
+__device__ __forceinline__ void t2_next(double r, double w, double sp, double di, double a, double b,
+                                        double& s, double& rn, double& u) {
+  s = fma(b, sp, w);
+  rn = fma(-a, s, r);
+  u = di * rn;
 }
 
 __global__ void __launch_bounds__(kGridThreads) t2_pcg_grid(T2 d, int max_iter, double tol) {
@@ -631,17 +654,43 @@ __global__ void __launch_bounds__(kGridThreads) t2_pcg_grid(T2 d, int max_iter, 
   const int per = (d.nf + G - 1) / G;
   const int r0 = min(d.nf, (int)blockIdx.x * per), r1 = min(d.nf, r0 + per);
   const int t = threadIdx.x;
-  // r = b, dx = 0; |b|^2
-  double v1[1] = {0.0};
-  for (int i = 2 * r0 + t; i < 2 * r1; i += kGridThreads) {
-    const double ri = d.rhs[i];
-    d.dx[i] = 0.0;
-    d.r[i] = ri;
-    v1[0] += ri * ri;
+  const size_t n2 = 2 * (size_t)d.nf;
+  double* R[2] = {d.sr, d.sr + n2};
+  double* W[2] = {d.sr + 2 * n2, d.sr + 3 * n2};
+  double* S[2] = {d.sr + 4 * n2, d.sr + 5 * n2};
+  // iteration -1: r_0 = b, s_{-1} = 0, p_{-1} = 0, dx = 0; w_0 = A u_0 with
+  // u_0 = D^-1 b (formed where gathered); (r_0, u_0), (w_0, u_0), |b|^2
+  double v3[3] = {0.0, 0.0, 0.0};
+  for (int rr = r0 + t; rr < r1; rr += kGridThreads) {
+    double y0 = 0, y1 = 0;
+    for (int qq = d.b_ptr[rr]; qq < d.b_ptr[rr + 1]; ++qq) {
+      const double* a = d.A + 4 * size_t(qq);
+      const int c = d.b_col[qq];
+      const double u0 = d.dinv[2 * c] * d.rhs[2 * c], u1 = d.dinv[2 * c + 1] * d.rhs[2 * c + 1];
+      y0 += a[0] * u0 + a[1] * u1;
+      y1 += a[2] * u0 + a[3] * u1;
+    }
+    const double y[2] = {y0, y1};
+#pragma unroll
+    for (int k = 0; k < 2; ++k) {
+      const size_t i = 2 * (size_t)rr + k;
+      const double b = d.rhs[i], u = d.dinv[i] * b;
+      R[0][i] = b;
+      W[0][i] = y[k];
+      S[1][i] = 0.0;  // s_{-1}
+      d.p[i] = 0.0;
+      d.dx[i] = 0.0;
+      v3[0] += b * u;
+      v3[1] += y[k] * u;
+      v3[2] += b * b;
+    }
   }
-  t2_put_partials<1>(d, v1, sh);
+  t2_put_partials<3>(d, v3, sh);
   if (!t2_grid_sync(d)) return;
-  const double b2 = t2_total(d, 0, sh);
+  double tot[3];
+  t2_totals<3>(d, tot, sh);
+  double g = tot[0];
+  const double dl = tot[1], b2 = tot[2];
   const double thr = fmax(tol * tol * b2, DBL_MIN);
   if (b2 == 0.0 || b2 < thr) {  // Eigen's test before the first iteration: no iteration
     if (blockIdx.x == 0 && t == 0) {
@@ -651,64 +700,60 @@ __global__ void __launch_bounds__(kGridThreads) t2_pcg_grid(T2 d, int max_iter, 
     }
     return;
   }
-  // (r, D^-1 r) of r_0: absNew; p_0 = D^-1 r_0 formed where it is read
-  v1[0] = 0.0;
-  for (int i = 2 * r0 + t; i < 2 * r1; i += kGridThreads) v1[0] += d.r[i] * (d.dinv[i] * d.r[i]);
-  t2_put_partials<1>(d, v1, sh);
-  if (!t2_grid_sync(d)) return;
-  double absNew = t2_total(d, 0, sh);
-  double beta = 0.0, rn2 = b2;
+  double a = g / dl, bt = 0.0, rn2 = b2;
   int it = 0;
   while (it < max_iter) {
-    const double* pold = (it & 1) ? d.p : d.p2;  // p_{k-1} (unused when k = 0)
-    double* pnew = (it & 1) ? d.p2 : d.p;        // p_k
-    // q = A p_k over the block's rows, p_k of each column formed on the
-    // fly; the block's own rows' p_k stored for the next iteration and dx
-    v1[0] = 0.0;
+    const int c0 = it & 1, c1 = c0 ^ 1;
+    const double* r_o = R[c0];
+    const double* w_o = W[c0];
+    const double* s_p = S[c1];  // s_{k-1}
+    double* r_n = R[c1];
+    double* w_n = W[c1];
+    double* s_n = S[c0];  // s_k
+    v3[0] = v3[1] = v3[2] = 0.0;
     for (int rr = r0 + t; rr < r1; rr += kGridThreads) {
+      // w_{k+1} = A u_{k+1}, each column's u_{k+1} formed from its r, w, s
       double y0 = 0, y1 = 0;
+#pragma unroll 4
       for (int qq = d.b_ptr[rr]; qq < d.b_ptr[rr + 1]; ++qq) {
-        const double* a = d.A + 4 * size_t(qq);
+        const double* am = d.A + 4 * size_t(qq);
         const int c = d.b_col[qq];
-        const double rc0 = __ldcg(d.r + 2 * c), rc1 = __ldcg(d.r + 2 * c + 1);
-        double p0 = d.dinv[2 * c] * rc0, p1 = d.dinv[2 * c + 1] * rc1;
-        if (it > 0) {
-          p0 += beta * __ldcg(pold + 2 * c);
-          p1 += beta * __ldcg(pold + 2 * c + 1);
-        }
-        y0 += a[0] * p0 + a[1] * p1;
-        y1 += a[2] * p0 + a[3] * p1;
+        double sc0, rc0, u0, sc1, rc1, u1;
+        t2_next(__ldcg(r_o + 2 * c), __ldcg(w_o + 2 * c), __ldcg(s_p + 2 * c), d.dinv[2 * c], a, bt, sc0, rc0, u0);
+        t2_next(__ldcg(r_o + 2 * c + 1), __ldcg(w_o + 2 * c + 1), __ldcg(s_p + 2 * c + 1), d.dinv[2 * c + 1], a,
+                bt, sc1, rc1, u1);
+        y0 += am[0] * u0 + am[1] * u1;
+        y1 += am[2] * u0 + am[3] * u1;
       }
-      double pr0 = d.dinv[2 * rr] * __ldcg(d.r + 2 * rr), pr1 = d.dinv[2 * rr + 1] * __ldcg(d.r + 2 * rr + 1);
-      if (it > 0) {
-        pr0 += beta * __ldcg(pold + 2 * rr);
-        pr1 += beta * __ldcg(pold + 2 * rr + 1);
+      const double y[2] = {y0, y1};
+#pragma unroll
+      for (int k = 0; k < 2; ++k) {
+        const size_t i = 2 * (size_t)rr + k;
+        const double r = __ldcg(r_o + i), w = __ldcg(w_o + i), sp = __ldcg(s_p + i);
+        double sv, rn, un;
+        t2_next(r, w, sp, d.dinv[i], a, bt, sv, rn, un);
+        // p_k = u_k + b p_{k-1} with u_k = D^-1 r_k; x += a p_k
+        const double pk = fma(bt, d.p[i], d.dinv[i] * r);
+        d.p[i] = pk;
+        d.dx[i] = fma(a, pk, d.dx[i]);
+        s_n[i] = sv;
+        r_n[i] = rn;
+        w_n[i] = y[k];
+        v3[0] += rn * un;
+        v3[1] += y[k] * un;
+        v3[2] += rn * rn;
       }
-      pnew[2 * rr] = pr0;
-      pnew[2 * rr + 1] = pr1;
-      d.q[2 * rr] = y0;
-      d.q[2 * rr + 1] = y1;
-      v1[0] += pr0 * y0 + pr1 * y1;
     }
-    t2_put_partials<1>(d, v1, sh);
+    t2_put_partials<3>(d, v3, sh);
     if (!t2_grid_sync(d)) return;
-    const double alpha = absNew / t2_total(d, 0, sh);
-    // dx += alpha p, r -= alpha q over the block's rows; |r|^2 and (r, D^-1 r)
-    double v2[2] = {0.0, 0.0};
-    for (int i = 2 * r0 + t; i < 2 * r1; i += kGridThreads) {
-      d.dx[i] += alpha * pnew[i];
-      const double ri = d.r[i] - alpha * d.q[i];
-      d.r[i] = ri;
-      v2[0] += ri * ri;
-      v2[1] += ri * (d.dinv[i] * ri);
-    }
-    t2_put_partials<2>(d, v2, sh);
-    if (!t2_grid_sync(d)) return;
-    rn2 = t2_total(d, 0, sh);
+    t2_totals<3>(d, tot, sh);
+    const double gn = tot[0], dn = tot[1];
+    rn2 = tot[2];
     if (rn2 < thr) break;
-    const double absOld = absNew;
-    absNew = t2_total(d, 1, sh);
-    beta = absNew / absOld;
+    const double bn = gn / g;
+    a = gn / (dn - bn * gn / a);
+    bt = bn;
+    g = gn;
     ++it;
   }
   if (blockIdx.x == 0 && t == 0) {
@@ -1449,7 +1494,7 @@ int mfem_gpu_tri2d_create(const mfem_tri2d_desc* dsc, mfem_tri2d** out) {
                o_dinv = L.take<double>(2 * size_t(std::max(nf, 1))),
                o_r = L.take<double>(2 * size_t(std::max(nf, 1))), o_p = L.take<double>(2 * size_t(std::max(nf, 1))),
                o_q = L.take<double>(2 * size_t(std::max(nf, 1))),
-               o_p2 = L.take<double>(2 * size_t(std::max(nf, 1))), o_part = L.take<double>(2 * kT2MaxGrid),
+               o_sr = L.take<double>(12 * size_t(std::max(nf, 1))), o_part = L.take<double>(3 * kT2MaxGrid),
                o_bar = L.take<unsigned int>(4),
                o_ep = L.take<double>(2 * size_t(nt) + nv), o_scal = L.take<double>(SC_COUNT),
                o_st = L.take<int>(4), o_xh = L.take<double>(2 * size_t(nv) * sc->bdf),
@@ -1523,7 +1568,7 @@ int mfem_gpu_tri2d_create(const mfem_tri2d_desc* dsc, mfem_tri2d** out) {
   d.r = dp(o_r);
   d.p = dp(o_p);
   d.q = dp(o_q);
-  d.p2 = dp(o_p2);
+  d.sr = dp(o_sr);
   d.part = dp(o_part);
   d.bar = reinterpret_cast<unsigned int*>(base + o_bar);
   d.epart = dp(o_ep);
