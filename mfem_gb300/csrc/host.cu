@@ -2783,12 +2783,17 @@ int mfem_gpu_batches_step_n(mfem_batch* const* batches, int32_t nbatch, int32_t 
                             double* step_done_ms) {
   if (!batches || nbatch < 1 || steps < 1 || steps > MFEM_BATCH_MAX_STEPS) return MFEM_ERR_INVALID;
   std::vector<size_t> first(nbatch + 1, 0);
+  std::vector<const mfem_scene*> seen;
   for (int k = 0; k < nbatch; ++k) {
     if (!batches[k]) return MFEM_ERR_INVALID;
     for (int j = 0; j < k; ++j)
       if (batches[j] == batches[k]) return MFEM_ERR_INVALID;
     first[k + 1] = first[k] + batches[k]->scenes.size();
+    seen.insert(seen.end(), batches[k]->scenes.begin(), batches[k]->scenes.end());
   }
+  // a scene in two of the batches would be stepped by two threads at once
+  std::sort(seen.begin(), seen.end());
+  if (std::adjacent_find(seen.begin(), seen.end()) != seen.end()) return MFEM_ERR_INVALID;
   int dev = 0;
   CUDA_OR(cudaGetDevice(&dev), MFEM_ERR_CUDA);
   // one host thread per batch, each driving its batch's stream; the GPU

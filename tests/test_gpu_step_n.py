@@ -115,5 +115,15 @@ def test_lanes_equal_one_batch(gpu_lib):
         assert ((d1[i] >= 0) == (d2[i] >= 0)).all()
     for (xa, sa), (xb, sb) in zip(state(a), state(b)):
         assert np.array_equal(xa, xb) and np.array_equal(sa, sb)
+    # a batch twice, or a scene in two of the batches, is refused
+    from mfem_gb300._lib import load
+    import ctypes as C
+    h = lanes.batches[0].handle.value
+    arr = (C.c_void_p * 2)(h, h)
+    assert load().mfem_gpu_batches_step_n(arr, 2, 1, None, None) == abi.ERR_INVALID
+    extra = gpu.Batch([b[lanes.parts[0][0]]])
+    arr = (C.c_void_p * 2)(h, extra.handle.value)
+    assert load().mfem_gpu_batches_step_n(arr, 2, 1, None, None) == abi.ERR_INVALID
+    extra.close()
     lanes.close()
     one.close()
