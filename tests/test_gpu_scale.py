@@ -2,7 +2,7 @@
 element work, float-float reductions) against the all-FP64 GPU path and,
 where the oracle finishes in seconds, against the FP64 oracle.
 
-Bounds (the benchmark spec's): converged positions within 1e-6 of the
+Bounds (those the workloads state): converged positions within 1e-6 of the
 bounding-box diagonal; per-element quantities at the same state within
 1e-5 relative (norm-wise over the scene).  Measured on a GB300: C3 mixed
 vs FP64 1e-7 of the diagonal over six steps, C2 2e-9, the C4 mix 1.5e-9;
