@@ -46,13 +46,17 @@ __device__ __forceinline__ df64 two_prod(float a, float b) {
   return df64(p, e);
 }
 
+// Addition: one TwoSum of the high parts with the low parts folded into
+// its error term, then renormalised (Dekker's add2; the "sloppy" addition
+// of Hida, Li and Bailey).  Its error is below about 2^-47 (|a| + |b|):
+// relative to the operands, not to the result, which is as much as either
+// operand's own representation error allows anyway -- the residual chains
+// and dot products this type carries are bounded that way (S - s, b - A x,
+// sums of products).  11 FP32 instructions instead of the 20 of the
+// two-TwoSum form that is accurate relative to the result.
 __device__ __forceinline__ df64 operator+(df64 a, df64 b) {
-  df64 s = two_sum(a.hi, b.hi);
-  df64 t = two_sum(a.lo, b.lo);
-  s.lo = __fadd_rn(s.lo, t.hi);
-  s = fast_two_sum(s.hi, s.lo);
-  s.lo = __fadd_rn(s.lo, t.lo);
-  return fast_two_sum(s.hi, s.lo);
+  const df64 s = two_sum(a.hi, b.hi);
+  return fast_two_sum(s.hi, __fadd_rn(s.lo, __fadd_rn(a.lo, b.lo)));
 }
 __device__ __forceinline__ df64 operator-(df64 a) { return df64(-a.hi, -a.lo); }
 __device__ __forceinline__ df64 operator-(df64 a, df64 b) { return a + (-b); }

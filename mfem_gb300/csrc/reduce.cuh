@@ -72,15 +72,9 @@ template <> struct Slot<float> {
   __device__ static float sget(const double* p) { return *reinterpret_cast<const float*>(p); }
 };
 
-// Addition in the reduction trees.  df64: one TwoSum of the high parts with
-// the low parts folded in (about 2^-48 relative per addition, the accuracy
-// of the representation) instead of the two-TwoSum form -- half the FP32
-// instructions on the critical path of every block's tail.
-__device__ __forceinline__ df64 radd(df64 a, df64 b) {
-  df64 s = two_sum(a.hi, b.hi);
-  s.lo = __fadd_rn(s.lo, __fadd_rn(a.lo, b.lo));
-  return fast_two_sum(s.hi, s.lo);
-}
+// Addition in the reduction trees (df64: the one-TwoSum addition of
+// df64.cuh, about 2^-47 of the operands per addition).
+__device__ __forceinline__ df64 radd(df64 a, df64 b) { return a + b; }
 __device__ __forceinline__ double radd(double a, double b) { return a + b; }
 
 // Reduces the per-warp values red[w][q] (w < nw <= 32) in warp 0 with a
