@@ -95,6 +95,27 @@ template <typename T> MI void quat_to_rot(const T q_in[4], T* R) {
   R[5] = s * (y * z + w * x);
   R[8] = T(1) - s * (x * x + y * y);
 }
+// The rotation of a float quaternion in float-float: the ten products of its
+// components are exact (TwoProduct), so only the normalisation 2 / |q|^2 and
+// the combinations round -- the same entries as quat_to_rot on the
+// float-float quaternion, without its products of zero low parts.
+MI void quat_to_rot_df(const float q[4], df64* R) {
+  const float w = q[0], x = q[1], y = q[2], z = q[3];
+  const df64 ww = two_prod(w, w), xx = two_prod(x, x), yy = two_prod(y, y), zz = two_prod(z, z);
+  const df64 xy = two_prod(x, y), xz = two_prod(x, z), yz = two_prod(y, z);
+  const df64 wx = two_prod(w, x), wy = two_prod(w, y), wz = two_prod(w, z);
+  const df64 n = ww + xx + yy + zz;
+  const df64 s = n.hi > 0.f ? df64(2.f) / n : df64(0.f);
+  R[0] = df64(1.f) - s * (yy + zz);
+  R[3] = s * (xy - wz);
+  R[6] = s * (xz + wy);
+  R[1] = s * (xy + wz);
+  R[4] = df64(1.f) - s * (xx + zz);
+  R[7] = s * (yz - wx);
+  R[2] = s * (xz - wy);
+  R[5] = s * (yz + wx);
+  R[8] = df64(1.f) - s * (xx + yy);
+}
 template <typename T> MI void rot_to_quat(const T* R, T q[4]) {
   T t = R[0] + R[4] + R[8];
   if (t > T(0)) {
@@ -897,6 +918,38 @@ template <typename T> MI void polish_rotation(T* R, const T* F) {
   mul33(dR, R, tmp);
 #pragma unroll
   for (int i = 0; i < 9; ++i) R[i] = tmp[i];
+}
+
+// The same polish for the mixed path's float-float rotation.  Only the
+// gradient g (the axial part of Y = R F^T, |g| ~ 1e-7 after the FP32
+// Procrustes solve: a difference of O(1) entries) needs float-float.  The
+// Hessian (O(1)), the 3x3 solve for omega and the increment
+// dR R - R = (K + K^2/2) R, whose entries are ~|omega|, are taken in FP32:
+// their rounding, about 6e-8 of ~1e-7, sits at the float-float resolution of
+// R.  The increment is then added to R in float-float.
+MI void polish_rotation(df64* R, const df64* F) {
+  // Y(i, j) = sum_k R(i, k) F(j, k); off-diagonal entries in float-float
+  auto y = [&](int i, int j) { return R[i] * F[j] + R[i + 3] * F[j + 3] + R[i + 6] * F[j + 6]; };
+  const df64 g0 = y(2, 1) - y(1, 2), g1 = y(0, 2) - y(2, 0), g2 = y(1, 0) - y(0, 1);
+  float Rh[9], Fh[9], Yf[9];
+#pragma unroll
+  for (int i = 0; i < 9; ++i) {
+    Rh[i] = R[i].hi;
+    Fh[i] = F[i].hi;
+  }
+  mulABt(Rh, Fh, Yf);
+  float g[3] = {g0.hi, g1.hi, g2.hi}, h[6], gy[3], om[3];
+  procrustes_gH(Yf, gy, h);
+  if (!solve_sym3(h, g, om)) return;
+  // K = [omega]x with omega = -H^-1 g; M = K + K^2 / 2
+  const float K[9] = {0.f, -om[2], om[1], om[2], 0.f, -om[0], -om[1], om[0], 0.f};
+  float M[9], D[9];
+  mul33(K, K, M);
+#pragma unroll
+  for (int i = 0; i < 9; ++i) M[i] = K[i] + 0.5f * M[i];
+  mul33(M, Rh, D);
+#pragma unroll
+  for (int i = 0; i < 9; ++i) R[i] = R[i] + df64(D[i]);
 }
 
 // ---------------------------------------------------- compensated sums ---

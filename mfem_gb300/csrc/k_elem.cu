@@ -123,12 +123,11 @@ __device__ __forceinline__ void load_quat(const SceneDev& sd, int e, Real* R) {
 template <typename Real>
 __device__ __forceinline__ void quat_rot_ext(const Real qq[4], const Real* R, typename Ext<Real>::T* RE) {
   using E = typename Ext<Real>::T;
-  if (Prec<Real>::kFP64) {
+  if constexpr (Prec<Real>::kFP64) {
 #pragma unroll
     for (int i = 0; i < 9; ++i) RE[i] = E(R[i]);
   } else {
-    E qe[4] = {E(qq[0]), E(qq[1]), E(qq[2]), E(qq[3])};
-    quat_to_rot(qe, RE);
+    quat_to_rot_df(qq, RE);
   }
 }
 
