@@ -192,6 +192,26 @@ template <typename T> MI bool solve_sym3(const T h[6], const T b[3], T x[3]) {
   return true;
 }
 
+// The same solve in float-float: an FP32 solve and one correction from the
+// float-float residual b - h x0 (one step of iterative refinement).  With
+// h = tr(S) I - S (condition number the ratio of the largest to the
+// smallest sum of two principal stretches) the error after it is about the
+// square of FP32's, below the float-float resolution of what it feeds.
+MI bool solve_sym3(const df64 h[6], const df64 b[3], df64 x[3]) {
+  const float hf[6] = {h[0].hi, h[1].hi, h[2].hi, h[3].hi, h[4].hi, h[5].hi};
+  const float bf[3] = {b[0].hi, b[1].hi, b[2].hi};
+  float x0[3], dx[3];
+  if (!solve_sym3(hf, bf, x0)) return false;
+  const df64 r[3] = {b[0] - (h[0] * df64(x0[0]) + h[3] * df64(x0[1]) + h[4] * df64(x0[2])),
+                     b[1] - (h[3] * df64(x0[0]) + h[1] * df64(x0[1]) + h[5] * df64(x0[2])),
+                     b[2] - (h[4] * df64(x0[0]) + h[5] * df64(x0[1]) + h[2] * df64(x0[2]))};
+  const float rf[3] = {r[0].hi, r[1].hi, r[2].hi};
+  solve_sym3(hf, rf, dx);
+#pragma unroll
+  for (int i = 0; i < 3; ++i) x[i] = two_sum(x0[i], dx[i]);
+  return true;
+}
+
 // Gradient g_k = -tr(cp_k Y) and Hessian H_kl = -tr(cp_kl Y) of the
 // Procrustes energy (newton_procrustes.h:128,136-138), written out:
 // g is the axial part of Y and H = tr(sym Y) I - sym Y.

@@ -295,12 +295,28 @@ __global__ void __launch_bounds__(kElemTile, MB)
       const E h2E = Ext<Real>::c(sd.h2, sd.h2x);
 #pragma unroll
       for (int i = 0; i < 6; ++i) dE[i] = SE[i] - sE[i];
+      if constexpr (Prec<Real>::kFP64) {
 #pragma unroll
-      for (int i = 0; i < 6; ++i) {
-        E acc = h2E * gE[i];
+        for (int i = 0; i < 6; ++i) {
+          E acc = h2E * gE[i];
 #pragma unroll
-        for (int j = 0; j < 6; ++j) acc = acc + E(H[i + 6 * j]) * dE[j];
-        qE[i] = acc;
+          for (int j = 0; j < 6; ++j) acc = acc + E(H[i + 6 * j]) * dE[j];
+          qE[i] = acc;
+        }
+      } else {
+        // H (S - s) in FP32: its rounding is relative to |S - s|, which
+        // vanishes as the Newton iteration converges, so it cannot floor
+        // the residual; h^2 psi'(s), an O(stress) term, stays float-float.
+        Real d32[6];
+#pragma unroll
+        for (int j = 0; j < 6; ++j) d32[j] = Real(Ext<Real>::to_real(dE[j]));
+#pragma unroll
+        for (int i = 0; i < 6; ++i) {
+          Real hd = 0;
+#pragma unroll
+          for (int j = 0; j < 6; ++j) hd += H[i + 6 * j] * d32[j];
+          qE[i] = h2E * gE[i] + E(hd);
+        }
       }
 #pragma unroll
       for (int i = 0; i < 12; ++i) dphE[i] = E(dph[i]);
