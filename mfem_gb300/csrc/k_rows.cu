@@ -154,7 +154,8 @@ __device__ __forceinline__ void xe_store(void* base, int row, const X3& x) {
 }
 
 constexpr int kAsmWindow = 64;  // block slots per warp accumulated in shared memory per pass
-constexpr int kAsmUnroll = 4;   // incidences whose record entries are in flight together
+constexpr int kAsmUnroll = 8;   // incidences whose record entries are in flight together
+static_assert(kAsmUnroll == 8, "the 4 entries past 32 of 8 incidences fill one warp");
 
 template <typename Real>
 __global__ void __launch_bounds__(256) k_assemble(const Tile* tiles, const SceneDev* sds,
@@ -192,8 +193,11 @@ __global__ void __launch_bounds__(256) k_assemble(const Tile* tiles, const Scene
       for (int c = 0; c < 3; ++c)
         acc[c] = acc[c] - m * (Ext<Real>::ld(sd.x, 3 * (size_t)b + c) - Ext<Real>::ld(sd.xt, 3 * (size_t)b + c));
     }
+    // the row's first 32 incidences, one a lane: the RHS shares and the
+    // block pass below read them from registers
+    const int2 inc0 = ib + lane < ie ? sd.inc[ib + lane] : make_int2(0, 0);
     for (int k = ib + lane; k < ie; k += 32) {
-      const int2 ic = sd.inc[k];
+      const int2 ic = k < ib + 32 ? inc0 : sd.inc[k];
       const void* rp = sd.rec + (size_t)ic.x * rec_bytes(RB) + rec_rhs_offset(RB);
 #pragma unroll
       for (int c = 0; c < 3; ++c) acc[c] = acc[c] + Ext<Real>::ld(rp, 3 * (ic.y & 3) + c);
@@ -232,41 +236,48 @@ __global__ void __launch_bounds__(256) k_assemble(const Tile* tiles, const Scene
       // first (independent gathers in flight together), then added in
       // incidence order with the warp synchronised between incidences, so
       // every entry still sums its contributions in element order.
-      for (int k0 = ib; k0 < ie; k0 += kAsmUnroll) {
-        Real av[kAsmUnroll][2];
-        int sv[kAsmUnroll][2];
-#pragma unroll
-        for (int u = 0; u < kAsmUnroll; ++u) {
-#pragma unroll
-          for (int pass = 0; pass < 2; ++pass) {
-            sv[u][pass] = -1;
-            av[u][pass] = Real(0);
-          }
-          if (k0 + u < ie) {
-            const int2 ic = sd.inc[k0 + u];
-            const int i = ic.y & 3;
-            const Real* rp = reinterpret_cast<const Real*>(sd.rec + (size_t)ic.x * rec_bytes(RB));
-#pragma unroll
-            for (int pass = 0; pass < 2; ++pass) {
-              const int l = lane + 32 * pass;
-              if (l < 36) {
-                const int j = l / 9, ent = l - 9 * j;
-                const int slot = (ic.y >> (2 + 7 * j)) & 127;
-                const int sl = slot - w0;
-                if (slot != 127 && sl >= 0 && sl < wn) {
-                  sv[u][pass] = 9 * sl + ent;
-                  av[u][pass] = rp[offtab[i][j][ent]];
-                }
+      for (int c0 = ib; c0 < ie; c0 += 32) {
+        const int cn = min(32, ie - c0);
+        const int2 my = c0 == ib ? inc0 : (lane < cn ? sd.inc[c0 + lane] : make_int2(0, 0));
+        for (int k0 = 0; k0 < cn; k0 += kAsmUnroll) {
+          // entry l < 32 of incidence k0 + u in lane l; entries 32..35 of
+          // incidence k0 + lane / 4 in lane (lane % 4) + 32
+          Real av[kAsmUnroll], aw = Real(0);
+          int sv[kAsmUnroll], sw = -1;
+          {
+            const int uw = lane >> 2, lw = 32 + (lane & 3);
+            const int2 icw = make_int2(__shfl_sync(0xffffffffu, my.x, (k0 + uw) & 31),
+                                       __shfl_sync(0xffffffffu, my.y, (k0 + uw) & 31));
+            if (k0 + uw < cn) {
+              const int i = icw.y & 3, j = lw / 9, ent = lw - 9 * j;
+              const int slot = (icw.y >> (2 + 7 * j)) & 127, sl = slot - w0;
+              if (slot != 127 && sl >= 0 && sl < wn) {
+                sw = 9 * sl + ent;
+                aw = reinterpret_cast<const Real*>(sd.rec + (size_t)icw.x * rec_bytes(RB))[offtab[i][j][ent]];
               }
             }
           }
-        }
 #pragma unroll
-        for (int u = 0; u < kAsmUnroll; ++u) {
+          for (int u = 0; u < kAsmUnroll; ++u) {
+            sv[u] = -1;
+            av[u] = Real(0);
+            const int2 ic = make_int2(__shfl_sync(0xffffffffu, my.x, (k0 + u) & 31),
+                                      __shfl_sync(0xffffffffu, my.y, (k0 + u) & 31));
+            if (k0 + u < cn) {
+              const int i = ic.y & 3, j = lane / 9, ent = lane - 9 * j;
+              const int slot = (ic.y >> (2 + 7 * j)) & 127, sl = slot - w0;
+              if (slot != 127 && sl >= 0 && sl < wn) {
+                sv[u] = 9 * sl + ent;
+                av[u] = reinterpret_cast<const Real*>(sd.rec + (size_t)ic.x * rec_bytes(RB))[offtab[i][j][ent]];
+              }
+            }
+          }
 #pragma unroll
-          for (int pass = 0; pass < 2; ++pass)
-            if (sv[u][pass] >= 0) acc_w[sv[u][pass]] += av[u][pass];
-          __syncwarp();
+          for (int u = 0; u < kAsmUnroll; ++u) {
+            if (sv[u] >= 0) acc_w[sv[u]] += av[u];
+            if ((lane >> 2) == u && sw >= 0) acc_w[sw] += aw;
+            __syncwarp();
+          }
         }
       }
       for (int o = lane; o < 9 * wn; o += 32) {
