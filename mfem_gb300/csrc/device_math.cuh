@@ -375,15 +375,16 @@ template <typename T> struct MatCoef {
 
 template <typename T> MI void invariants(const T* s, T& Q, T& J, T& t, T dJ[6]) {
   Q = s[0] * s[0] + s[1] * s[1] + s[2] * s[2] + T(2) * (s[3] * s[3] + s[4] * s[4] + s[5] * s[5]);
-  J = s[0] * s[1] * s[2] + T(2) * s[3] * s[4] * s[5] - s[0] * s[5] * s[5] - s[1] * s[4] * s[4] -
-      s[2] * s[3] * s[3];
   t = s[0] + s[1] + s[2];
-  dJ[0] = s[1] * s[2] - s[5] * s[5];
+  const T c0 = s[1] * s[2] - s[5] * s[5], c3 = s[4] * s[5] - s[2] * s[3], c4 = s[3] * s[5] - s[1] * s[4];
+  dJ[0] = c0;
   dJ[1] = s[0] * s[2] - s[4] * s[4];
   dJ[2] = s[0] * s[1] - s[3] * s[3];
-  dJ[3] = T(2) * (s[4] * s[5] - s[2] * s[3]);
-  dJ[4] = T(2) * (s[3] * s[5] - s[1] * s[4]);
+  dJ[3] = T(2) * c3;
+  dJ[4] = T(2) * c4;
   dJ[5] = T(2) * (s[3] * s[4] - s[0] * s[5]);
+  // det S by cofactors of its first row
+  J = s[0] * c0 + s[3] * c3 + s[4] * c4;
 }
 
 template <typename T>
@@ -500,7 +501,9 @@ MI bool material_grad_hess(int type, T mu, T la, const T* s, T g[6], T H[36]) {
 }
 
 // In-place lower Cholesky of the symmetric 6x6 H (column-major, lower part
-// used); succeeds only if every pivot exceeds `floor_`.
+// used); succeeds only if every pivot exceeds `floor_`.  In FP32, where it
+// only tests definiteness, the diagonal is left holding 1/L_jj (one rsqrt
+// instead of a square root and a division).
 template <typename T> MI bool cholesky6(T* A, T floor_) {
   bool ok = true;
 #pragma unroll
@@ -509,9 +512,15 @@ template <typename T> MI bool cholesky6(T* A, T floor_) {
 #pragma unroll
     for (int k = 0; k < j; ++k) d -= A[j + 6 * k] * A[j + 6 * k];
     ok = ok && (d > floor_);
-    T ljj = Prec<T>::sqrt_(d > floor_ ? d : floor_);
-    A[j + 6 * j] = ljj;
-    T inv = T(1) / ljj;
+    T inv;
+    if constexpr (Prec<T>::kFP64) {
+      const T ljj = Prec<T>::sqrt_(d > floor_ ? d : floor_);
+      A[j + 6 * j] = ljj;
+      inv = T(1) / ljj;
+    } else {
+      inv = Prec<T>::rsqrt_(d > floor_ ? d : floor_);
+      A[j + 6 * j] = inv;
+    }
 #pragma unroll
     for (int i = j + 1; i < 6; ++i) {
       T v = A[i + 6 * j];
@@ -909,10 +918,13 @@ MI bool element_force(const T* R, const T s6[6], const T q[6], const T dph[12], 
   T P[9];
   mul33(R, D, P);
 #pragma unroll
-  for (int a = 0; a < 4; ++a)
+  for (int a = 1; a < 4; ++a)
 #pragma unroll
     for (int r = 0; r < 3; ++r)
       f[3 * a + r] = -vol * (P[r] * dph[3 * a] + P[r + 3] * dph[3 * a + 1] + P[r + 6] * dph[3 * a + 2]);
+  // dphi_0 = -(dphi_1 + dphi_2 + dphi_3)
+#pragma unroll
+  for (int r = 0; r < 3; ++r) f[r] = -(f[3 + r] + f[6 + r] + f[9 + r]);
   return ok;
 }
 

@@ -369,9 +369,11 @@ __global__ void __launch_bounds__(kElemTile, MB)
 #pragma unroll
         for (int j = i; j < 6; ++j, ++k) Ho[(size_t)k * sd.ntp + e] = H[i + 6 * j];
     }
-    // ---- upper 3x3 blocks of Aloc = vol * B^T H B  (mixed_stretch.cpp:174-175)
+    // ---- upper 3x3 blocks of Aloc = vol * B^T H B  (mixed_stretch.cpp:174-175);
+    // with B_0 = -(B_1 + B_2 + B_3), block (0, 0) is -sum_b (0, b)
+    Real A00[6] = {Real(0), Real(0), Real(0), Real(0), Real(0), Real(0)};
 #pragma unroll
-    for (int b = 0; b < 4; ++b) {
+    for (int b = 1; b < 4; ++b) {
       Real HB[18];
 #pragma unroll
       for (int i = 0; i < 6; ++i)
@@ -395,6 +397,7 @@ __global__ void __launch_bounds__(kElemTile, MB)
             for (int i = 0; i < 6; ++i) acc += B[12 * i + 3 * a + l] * HB[3 * i + m];
             const int k = base + (a == b ? sym_idx(l, m) : 3 * l + m);
             const Real v = in.vol * acc;
+            if (a == 0 && m >= l) A00[sym_idx(l, m)] -= v;
             put_word(out, k * (RB / 4), v);
             if (DBG) {
               const size_t Ei = e;
@@ -404,6 +407,18 @@ __global__ void __launch_bounds__(kElemTile, MB)
           }
       }
     }
+#pragma unroll
+    for (int l = 0; l < 3; ++l)
+#pragma unroll
+      for (int m = l; m < 3; ++m) {
+        const Real v = A00[sym_idx(l, m)];
+        put_word(out, sym_idx(l, m) * (RB / 4), v);
+        if (DBG) {
+          const size_t Ei = e;
+          dbg.Aloc[144 * Ei + l + 12 * m] = double(v);
+          dbg.Aloc[144 * Ei + m + 12 * l] = double(v);
+        }
+      }
   }
   __syncthreads();
   // contiguous store of the tile's records as 32-bit words

@@ -157,6 +157,43 @@ constexpr int kAsmWindow = 64;  // block slots per warp accumulated in shared me
 constexpr int kAsmUnroll = 8;   // incidences whose record entries are in flight together
 static_assert(kAsmUnroll == 8, "the 4 entries past 32 of 8 incidences fill one warp");
 
+// Jacobi or block-Jacobi inverse of a free row from its diagonal block D
+// (row-major 3x3; zero where the row has no diagonal block).
+template <typename Real>
+__device__ __forceinline__ void write_row_precond(const SceneDev& sd, int row, const Real* D) {
+  Real* dinv = static_cast<Real*>(sd.dinv);
+  if (sd.block_jacobi) {
+    // inverse of the 3x3 diagonal block (row-major)
+    Real c00 = D[4] * D[8] - D[5] * D[7], c01 = D[5] * D[6] - D[3] * D[8],
+         c02 = D[3] * D[7] - D[4] * D[6];
+    Real det = D[0] * c00 + D[1] * c01 + D[2] * c02;
+    if (det != Real(0)) {
+      Real id = Real(1) / det;
+      dinv[9 * row + 0] = c00 * id;
+      dinv[9 * row + 1] = (D[2] * D[7] - D[1] * D[8]) * id;
+      dinv[9 * row + 2] = (D[1] * D[5] - D[2] * D[4]) * id;
+      dinv[9 * row + 3] = c01 * id;
+      dinv[9 * row + 4] = (D[0] * D[8] - D[2] * D[6]) * id;
+      dinv[9 * row + 5] = (D[2] * D[3] - D[0] * D[5]) * id;
+      dinv[9 * row + 6] = c02 * id;
+      dinv[9 * row + 7] = (D[1] * D[6] - D[0] * D[7]) * id;
+      dinv[9 * row + 8] = (D[0] * D[4] - D[1] * D[3]) * id;
+    } else {
+#pragma unroll
+      for (int k = 0; k < 9; ++k) dinv[9 * row + k] = (k % 4 == 0) ? Real(1) : Real(0);
+    }
+  } else {
+    // DiagonalPreconditioner: 1/a_ii, or 1 where a_ii == 0
+    Real dj[3];
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+      const Real d = D[4 * c];
+      dj[c] = d != Real(0) ? Real(1) / d : Real(1);
+    }
+    st3(dinv + 4 * (size_t)row, dj);
+  }
+}
+
 template <typename Real>
 __global__ void __launch_bounds__(256) k_assemble(const Tile* tiles, const SceneDev* sds,
                                                             double* partials, int pstride,
@@ -228,6 +265,13 @@ __global__ void __launch_bounds__(256) k_assemble(const Tile* tiles, const Scene
     Real* val = static_cast<Real*>(sd.ell);
     const Real* bm = static_cast<const Real*>(sd.b_mass) + rb;
     Real* acc_w = acc_s[warp];
+    // the diagonal block's slot (the row's own column)
+    int qd = -1;
+    for (int q0 = 0; q0 < nb; q0 += 32) {
+      const bool hit = (q0 + lane < nb) && sd.b_col[rb + q0 + lane] == row;
+      const unsigned bal = __ballot_sync(0xffffffffu, hit);
+      if (bal && qd < 0) qd = q0 + __ffs(bal) - 1;
+    }
     for (int w0 = 0; w0 < nb; w0 += kAsmWindow) {
       const int wn = min(kAsmWindow, nb - w0);
       for (int o = lane; o < 9 * wn; o += 32) acc_w[o] = Real(0);
@@ -285,6 +329,14 @@ __global__ void __launch_bounds__(256) k_assemble(const Tile* tiles, const Scene
         val[ell_entry(soff, w0 + q, rs, ent)] =
             acc_w[o] + ((ent == 0 || ent == 4 || ent == 8) ? bm[w0 + q] : Real(0));
       }
+      if (lane == 0 && qd >= w0 && qd < w0 + wn) {
+        // the diagonal block as written above, from shared memory
+        Real D[9];
+#pragma unroll
+        for (int k = 0; k < 9; ++k)
+          D[k] = acc_w[9 * (qd - w0) + k] + ((k == 0 || k == 4 || k == 8) ? bm[qd] : Real(0));
+        write_row_precond(sd, row, D);
+      }
       __syncwarp();
     }
     // padding blocks of the slice beyond this row's length are zero
@@ -292,48 +344,10 @@ __global__ void __launch_bounds__(256) k_assemble(const Tile* tiles, const Scene
       const int q = nb + o / 9, ent = o % 9;
       val[ell_entry(soff, q, rs, ent)] = Real(0);
     }
-    // ---- preconditioner from the diagonal block
-    int qd = -1;
-    for (int q0 = 0; q0 < nb; q0 += 32) {
-      const bool hit = (q0 + lane < nb) && sd.b_col[rb + q0 + lane] == row;
-      const unsigned bal = __ballot_sync(0xffffffffu, hit);
-      if (bal && qd < 0) qd = q0 + __ffs(bal) - 1;
-    }
-    if (lane == 0) {
-      Real* dinv = static_cast<Real*>(sd.dinv);
-      Real D[9];
-#pragma unroll
-      for (int k = 0; k < 9; ++k) D[k] = (qd >= 0) ? val[ell_entry(soff, qd, rs, k)] : Real(0);
-      if (sd.block_jacobi) {
-        // inverse of the 3x3 diagonal block (row-major)
-        Real c00 = D[4] * D[8] - D[5] * D[7], c01 = D[5] * D[6] - D[3] * D[8],
-             c02 = D[3] * D[7] - D[4] * D[6];
-        Real det = D[0] * c00 + D[1] * c01 + D[2] * c02;
-        if (det != Real(0)) {
-          Real id = Real(1) / det;
-          dinv[9 * row + 0] = c00 * id;
-          dinv[9 * row + 1] = (D[2] * D[7] - D[1] * D[8]) * id;
-          dinv[9 * row + 2] = (D[1] * D[5] - D[2] * D[4]) * id;
-          dinv[9 * row + 3] = c01 * id;
-          dinv[9 * row + 4] = (D[0] * D[8] - D[2] * D[6]) * id;
-          dinv[9 * row + 5] = (D[2] * D[3] - D[0] * D[5]) * id;
-          dinv[9 * row + 6] = c02 * id;
-          dinv[9 * row + 7] = (D[1] * D[6] - D[0] * D[7]) * id;
-          dinv[9 * row + 8] = (D[0] * D[4] - D[1] * D[3]) * id;
-        } else {
-#pragma unroll
-          for (int k = 0; k < 9; ++k) dinv[9 * row + k] = (k % 4 == 0) ? Real(1) : Real(0);
-        }
-      } else {
-        // DiagonalPreconditioner: 1/a_ii, or 1 where a_ii == 0
-        Real dj[3];
-#pragma unroll
-        for (int c = 0; c < 3; ++c) {
-          const Real d = D[4 * c];
-          dj[c] = d != Real(0) ? Real(1) / d : Real(1);
-        }
-        st3(dinv + 4 * (size_t)row, dj);
-      }
+    // ---- preconditioner of a row without a diagonal block
+    if (lane == 0 && qd < 0) {
+      const Real Z[9] = {Real(0), Real(0), Real(0), Real(0), Real(0), Real(0), Real(0), Real(0), Real(0)};
+      write_row_precond(sd, row, Z);
     }
   }
   }

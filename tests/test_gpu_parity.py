@@ -55,10 +55,12 @@ def test_elem_update_parity(gpu_lib, prec):
     for k in ("dSdF", "g", "H", "Aloc", "gl"):
         assert rel(eg[k], eo[k]) < (1e-6 if tight else 1e-5), k
     # Hinv is ill-conditioned where the psd projection clamps eigenvalues to
-    # 1e-6 h^2; check it as an inverse instead of entry by entry.
+    # 1e-6 h^2; its error is about cond(H) times that of H (rounding 1e-16 in
+    # FP64, 1e-7 in FP32), so it is checked on elements whose condition
+    # number keeps that below the bound.
     H = eo["H"].reshape(-1, 6, 6)
-    well = np.linalg.cond(H) < 1e6
-    assert well.any()
+    well = np.linalg.cond(H) < (1e6 if tight else 1e3)
+    assert well.sum() > len(H) // 2
     assert rel(eg["Hinv"][well], eo["Hinv"][well]) < (1e-6 if tight else 1e-4)
 
 
