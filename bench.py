@@ -691,7 +691,7 @@ def run_batch_mix(args, gpu, abi, configs):
             s.step()
         own = 0.0
         for k in range(plain_steps):
-            st = s.step()
+            st = s.step(raise_on_error=False)
             plain_ms += st.device_ms
             own += st.device_ms
             plain_n += 1

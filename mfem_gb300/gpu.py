@@ -77,10 +77,14 @@ class Scene:
         check(load().mfem_gpu_scene_solo_batch(self._h, C.byref(h)), "solo_batch")
         return h
 
-    def step(self):
+    def step(self, raise_on_error=True):
+        """One timestep; its stats (.status says how it ended).  With
+        raise_on_error=False a numerical failure (non-finite state, singular
+        rotation Hessian, ...) is left to the caller; a CUDA error, a timed
+        out wait or an invalid call still raises."""
         st = abi.StepStats()
         rc = load().mfem_gpu_scene_step(self._h, C.byref(st))
-        if rc not in (abi.OK,):
+        if rc != abi.OK and (raise_on_error or rc in (abi.ERR_CUDA, abi.ERR_TIMEOUT, abi.ERR_INVALID)):
             check(rc, "scene_step")
         return st
 
