@@ -48,6 +48,9 @@ template <> struct Prec<df64> {
 
 #define MI __device__ __forceinline__
 
+// acc + a b; float-float has its own one-pass form (df64.cuh).
+template <typename T> MI T madd(T acc, T a, T b) { return acc + a * b; }
+
 // ---------------------------------------------------------------- 3x3 ----
 template <typename T> MI T tr_AB(const T* A, const T* B) {  // tr(A*B)
   T s = 0;
@@ -62,21 +65,21 @@ template <typename T> MI void mul33(const T* A, const T* B, T* C) {  // C = A*B
   for (int i = 0; i < 3; ++i)
 #pragma unroll
     for (int j = 0; j < 3; ++j)
-      C[i + 3 * j] = A[i] * B[3 * j] + A[i + 3] * B[1 + 3 * j] + A[i + 6] * B[2 + 3 * j];
+      C[i + 3 * j] = madd(madd(A[i] * B[3 * j], A[i + 3], B[1 + 3 * j]), A[i + 6], B[2 + 3 * j]);
 }
 template <typename T> MI void mulAtB(const T* A, const T* B, T* C) {  // C = A^T*B
 #pragma unroll
   for (int i = 0; i < 3; ++i)
 #pragma unroll
     for (int j = 0; j < 3; ++j)
-      C[i + 3 * j] = A[3 * i] * B[3 * j] + A[1 + 3 * i] * B[1 + 3 * j] + A[2 + 3 * i] * B[2 + 3 * j];
+      C[i + 3 * j] = madd(madd(A[3 * i] * B[3 * j], A[1 + 3 * i], B[1 + 3 * j]), A[2 + 3 * i], B[2 + 3 * j]);
 }
 template <typename T> MI void mulABt(const T* A, const T* B, T* C) {  // C = A*B^T
 #pragma unroll
   for (int i = 0; i < 3; ++i)
 #pragma unroll
     for (int j = 0; j < 3; ++j)
-      C[i + 3 * j] = A[i] * B[j] + A[i + 3] * B[j + 3] + A[i + 6] * B[j + 6];
+      C[i + 3 * j] = madd(madd(A[i] * B[j], A[i + 3], B[j + 3]), A[i + 6], B[j + 6]);
 }
 
 // Rotation <-> unit quaternion (w, x, y, z).  Rotations are stored as
@@ -374,17 +377,19 @@ template <typename T> struct MatCoef {
 };
 
 template <typename T> MI void invariants(const T* s, T& Q, T& J, T& t, T dJ[6]) {
-  Q = s[0] * s[0] + s[1] * s[1] + s[2] * s[2] + T(2) * (s[3] * s[3] + s[4] * s[4] + s[5] * s[5]);
+  Q = madd(madd(s[0] * s[0], s[1], s[1]), s[2], s[2]) +
+      T(2) * madd(madd(s[3] * s[3], s[4], s[4]), s[5], s[5]);
   t = s[0] + s[1] + s[2];
-  const T c0 = s[1] * s[2] - s[5] * s[5], c3 = s[4] * s[5] - s[2] * s[3], c4 = s[3] * s[5] - s[1] * s[4];
+  const T c0 = madd(s[1] * s[2], -s[5], s[5]), c3 = madd(s[4] * s[5], -s[2], s[3]),
+          c4 = madd(s[3] * s[5], -s[1], s[4]);
   dJ[0] = c0;
-  dJ[1] = s[0] * s[2] - s[4] * s[4];
-  dJ[2] = s[0] * s[1] - s[3] * s[3];
+  dJ[1] = madd(s[0] * s[2], -s[4], s[4]);
+  dJ[2] = madd(s[0] * s[1], -s[3], s[3]);
   dJ[3] = T(2) * c3;
   dJ[4] = T(2) * c4;
-  dJ[5] = T(2) * (s[3] * s[4] - s[0] * s[5]);
+  dJ[5] = T(2) * madd(s[3] * s[4], -s[0], s[5]);
   // det S by cofactors of its first row
-  J = s[0] * c0 + s[3] * c3 + s[4] * c4;
+  J = madd(madd(s[0] * c0, s[3], c3), s[4], c4);
 }
 
 template <typename T>
@@ -458,7 +463,7 @@ template <typename T> MI void material_grad(int type, T mu, T la, const T* s, T 
   MatCoef<T> c = material_coef<T>(type, mu, la, Q, J, t, false);
 #pragma unroll
   for (int i = 0; i < 6; ++i)
-    g[i] = c.A1 * T(2) * (i < 3 ? T(1) : T(2)) * s[i] + c.B1 * dJ[i] + (i < 3 ? c.C1 : T(0));
+    g[i] = madd(c.A1 * T(2) * (i < 3 ? T(1) : T(2)) * s[i], c.B1, dJ[i]) + (i < 3 ? c.C1 : T(0));
 }
 
 // Gradient and (unfixed) Hessian of psi on the 6-vector; H full 6x6 column-major.
@@ -921,7 +926,7 @@ MI bool element_force(const T* R, const T s6[6], const T q[6], const T dph[12], 
   for (int a = 1; a < 4; ++a)
 #pragma unroll
     for (int r = 0; r < 3; ++r)
-      f[3 * a + r] = -vol * (P[r] * dph[3 * a] + P[r + 3] * dph[3 * a + 1] + P[r + 6] * dph[3 * a + 2]);
+      f[3 * a + r] = -vol * madd(madd(P[r] * dph[3 * a], P[r + 3], dph[3 * a + 1]), P[r + 6], dph[3 * a + 2]);
   // dphi_0 = -(dphi_1 + dphi_2 + dphi_3)
 #pragma unroll
   for (int r = 0; r < 3; ++r) f[r] = -(f[3 + r] + f[6 + r] + f[9 + r]);
@@ -961,7 +966,7 @@ template <typename T> MI void polish_rotation(T* R, const T* F) {
 // R.  The increment is then added to R in float-float.
 MI void polish_rotation(df64* R, const df64* F) {
   // Y(i, j) = sum_k R(i, k) F(j, k); off-diagonal entries in float-float
-  auto y = [&](int i, int j) { return R[i] * F[j] + R[i + 3] * F[j + 3] + R[i + 6] * F[j + 6]; };
+  auto y = [&](int i, int j) { return madd(madd(R[i] * F[j], R[i + 3], F[j + 3]), R[i + 6], F[j + 6]); };
   const df64 g0 = y(2, 1) - y(1, 2), g1 = y(0, 2) - y(2, 0), g2 = y(1, 0) - y(0, 1);
   float Rh[9], Fh[9], Yf[9];
 #pragma unroll

@@ -93,7 +93,7 @@ __device__ __forceinline__ void deformation_gradients(const SceneDev& sd, const 
 #pragma unroll
     for (int r = 0; r < 3; ++r) {
       if (FE) {
-        const E f = ed[r] * E(in.dp[c]) + ed[3 + r] * E(in.dp[3 + c]) + ed[6 + r] * E(in.dp[6 + c]);
+        const E f = madd(madd(ed[r] * E(in.dp[c]), ed[3 + r], in.dp[3 + c]), ed[6 + r], in.dp[6 + c]);
         FE[r + 3 * c] = f;
         F[r + 3 * c] = Real(Ext<Real>::to_real(f));
       } else {
