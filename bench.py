@@ -687,10 +687,13 @@ def run_batch_mix(args, gpu, abi, configs):
     scene_ms = []
     for sp in specs:
         s = gpu.Scene(sp)
+        retired = False
         for _ in range(warm):
-            s.step()
+            if s.step(raise_on_error=False).status in (abi.ERR_NONFINITE, abi.ERR_PROCRUSTES):
+                retired = True
+                break
         own = 0.0
-        for k in range(plain_steps):
+        for k in range(0 if retired else plain_steps):
             st = s.step(raise_on_error=False)
             plain_ms += st.device_ms
             own += st.device_ms
