@@ -10,7 +10,9 @@
 //   k_cg_*       Eigen::ConjugateGradient<.., Lower|Upper, DiagonalPreconditioner>
 //                with zero initial guess (eigen_iterative_solver.h:20-29):
 //                stop when |r|^2 < tol^2 |b|^2, at most max_iterative_solver_iters.
-//                Vectors are Real; every inner product is accumulated in FP64.
+//                Vectors are Real; every inner product is accumulated in the
+//                path's high precision (double, or float-float in the mixed
+//                path).
 #include <cfloat>
 
 #include "device_math.cuh"
