@@ -67,3 +67,32 @@ def test_standard_fem_refusals(gpu_lib):
     assert _footprint_status(gpu_lib, s)[0] == abi.ERR_UNSUPPORTED
     s = configs.beam_c1(linear_solver=abi.SOLVER_MINRES_ID, **fem)
     assert _footprint_status(gpu_lib, s)[0] == abi.ERR_UNSUPPORTED
+
+
+@pytest.mark.parametrize("rc", [abi.ERR_NONFINITE, abi.ERR_PROCRUSTES])
+def test_scene_step_returns_numerical_failures_on_request(gpu_lib, monkeypatch, rc):
+    """Scene.step(raise_on_error=False) hands a numerical failure back as the
+    step's status (the batched forms retire such a scene); by default it
+    raises.  A CUDA error, a timed-out wait or an invalid call raises either
+    way.  The library's step entry point is faked: this is host logic."""
+    from mfem_gb300 import gpu
+    from mfem_gb300._lib import MfemError
+
+    class FakeLib:
+        def __init__(self, code):
+            self.code = code
+
+        def mfem_gpu_scene_step(self, handle, stats_ref):
+            stats_ref._obj.status = self.code
+            return self.code
+
+    sc = gpu.Scene.__new__(gpu.Scene)
+    sc._h = None
+    monkeypatch.setattr(gpu, "load", lambda: FakeLib(rc))
+    assert sc.step(raise_on_error=False).status == rc
+    with pytest.raises(MfemError):
+        sc.step()
+    for hard in (abi.ERR_CUDA, abi.ERR_TIMEOUT, abi.ERR_INVALID):
+        monkeypatch.setattr(gpu, "load", lambda hard=hard: FakeLib(hard))
+        with pytest.raises(MfemError):
+            sc.step(raise_on_error=False)
